@@ -1,0 +1,414 @@
+// DNC5 residual and fused residual + JVP kernels for sm_103a.
+//
+// Reference: srcfv/prepro/flux_num_dnc5.f90 (primal), the Tapenade tangent
+// srcfv/tangent/flux_num_dnc5_d.f90 (S = DK<K> here).
+//
+// GB300 note: the stencil is bound by the FP64 pipe, not by HBM, so every
+// cell primitive, cell gradient and face flux is computed exactly once and
+// parked in HBM scratch (L2-resident for the grid sizes of interest); the
+// memory traffic this costs is far below the bandwidth roof.
+#include "dnc5.cuh"
+#include "residual.h"
+
+namespace bcg {
+
+// ---------------------------------------------------------------------------
+// pass 1: primitives on every padded cell (phys/Primitives.F, phys/viscosity.F)
+template <class S>
+__global__ void __launch_bounds__(256) k_prim(Ext e, Coef c, State<S> w, Scratch<S> pr) {
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= e.np) return;
+  const size_t n = e.np;
+  const S ro = w(q), ru = w(q + n), rv = w(q + 2 * n), rw = w(q + 3 * n), re = w(q + 4 * n);
+  const S rom1 = 1.0 / ro;
+  const S u = ru * rom1, v = rv * rom1, ww = rw * rom1;
+  const S ec = 0.5 * (u * u + v * v + ww * ww);
+  const S eloc = (re - ec * ro) * rom1;
+  const S t = eloc * c.cvm1;
+  const S p = c.gam1 * ro * eloc;
+  const S htot = (re + p) * rom1;
+  pr.st(F_U, q, u); pr.st(F_V, q, v); pr.st(F_W, q, ww); pr.st(F_T, q, t); pr.st(F_P, q, p);
+  pr.st(F_F2, q, ru * u + p); pr.st(F_F3, q, ru * v); pr.st(F_F4, q, ru * ww); pr.st(F_F5, q, ru * htot);
+  pr.st(F_G2, q, rv * u); pr.st(F_G3, q, rv * v + p); pr.st(F_G4, q, rv * ww); pr.st(F_G5, q, rv * htot);
+  pr.st(F_MU, q, c.betas / (t + c.s_suth) * sqrt_t(t) * t);
+}
+
+// ---------------------------------------------------------------------------
+// pass 2: 4th-order cell gradients of u and v on interior cells
+// (rhs/gradop_5pi.F, gradop_5pj.F, gradient.F)
+template <class S>
+__global__ void __launch_bounds__(256) k_grad(Ext e, Coef c, Scratch<S> pr, Scratch<S> gr, const double* __restrict__ nx,
+                                              const double* __restrict__ ny, const double* __restrict__ vol) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= e.im * e.jm) return;
+  const int i = 1 + t % e.im, j = 1 + t / e.im;
+  const size_t q = e.cidx(i, j);
+  const int di = 1, dj = e.ni;
+  auto g4 = [&](int f, int s) {
+    return c.b1 * (pr.ld(f, q + s) - pr.ld(f, q - s)) + c.b2 * (pr.ld(f, q + 2 * s) - pr.ld(f, q - 2 * s));
+  };
+  const S gui = g4(F_U, di), gvi = g4(F_V, di), guj = g4(F_U, dj), gvj = g4(F_V, dj);
+  const size_t nn = e.nn();
+  const int a = e.nidx(i, j);
+  const double volm1 = 1.0 / __ldg(vol + q);
+  const double dxm1 = 0.5 * (__ldg(nx + a) + __ldg(nx + a + 1)) * volm1;
+  const double dxm2 = 0.5 * (__ldg(nx + nn + a) + __ldg(nx + nn + a + e.ni + 1)) * volm1;
+  const double dym1 = 0.5 * (__ldg(ny + a) + __ldg(ny + a + 1)) * volm1;
+  const double dym2 = 0.5 * (__ldg(ny + nn + a) + __ldg(ny + nn + a + e.ni + 1)) * volm1;
+  gr.st(G_UX, q, dxm1 * gui + dxm2 * guj);
+  gr.st(G_VX, q, dxm1 * gvi + dxm2 * gvj);
+  gr.st(G_UY, q, dym1 * gui + dym2 * guj);
+  gr.st(G_VY, q, dym1 * gvi + dym2 * gvj);
+}
+
+// ---------------------------------------------------------------------------
+// pass 3: face fluxes
+template <class S>
+struct FaceCtx {
+  Ext e;
+  Coef c;
+  State<S> w;
+  Scratch<S> pr, gr;
+  const double* __restrict__ nx;
+  const double* __restrict__ ny;
+  const double* __restrict__ vol;
+  const double* __restrict__ volf;
+
+  BCG_HD S W(int i, int j, int v) const { return w((size_t)e.cidx(i, j) + (size_t)(v - 1) * e.np); }
+  BCG_HD S P(int f, int i, int j) const { return pr.ld(f, e.cidx(i, j)); }
+  // Euler flux components f(.,.,v), g(.,.,v) with f1 = rho u, g1 = rho v
+  BCG_HD S Fl(int v, int i, int j) const { return v == 1 ? W(i, j, 2) : P(F_F2 + v - 2, i, j); }
+  BCG_HD S Gl(int v, int i, int j) const { return v == 1 ? W(i, j, 3) : P(F_G2 + v - 2, i, j); }
+  BCG_HD double NX(int i, int j, int d) const { return __ldg(nx + (size_t)(d - 1) * e.nn() + e.nidx(i, j)); }
+  BCG_HD double NY(int i, int j, int d) const { return __ldg(ny + (size_t)(d - 1) * e.nn() + e.nidx(i, j)); }
+  BCG_HD double VOL(int i, int j) const { return __ldg(vol + e.cidx(i, j)); }
+  BCG_HD double VOLF(int i, int j, int d) const { return __ldg(volf + (size_t)(d - 1) * e.np + e.cidx(i, j)); }
+  // gradients, with the ghost lines the faces need (rhs/gradveloingh.F)
+  BCG_HD S G(int f, int i, int j) const {
+    if (i == 0) return 2.0 * gr.ld(f, e.cidx(1, j)) - gr.ld(f, e.cidx(2, j));
+    if (i == e.im + 1) return 2.0 * gr.ld(f, e.cidx(e.im, j)) - gr.ld(f, e.cidx(e.im - 1, j));
+    if (j == e.jm + 1) return 2.0 * gr.ld(f, e.cidx(i, e.jm)) - gr.ld(f, e.cidx(i, e.jm - 1));
+    return gr.ld(f, e.cidx(i, j));
+  }
+  BCG_HD static S q4(const S& a, const S& b, const S& cc, const S& d) { return -a + 9.0 * b + 9.0 * cc - d; }
+
+  BCG_HD void visc_fluxes(const S& mmu, const S& lambda, const S& uu, const S& vv, const S& ww, const S& ux,
+                          const S& uy, const S& vx, const S& vy, const S& wx, const S& wy, const S& tx, const S& ty,
+                          S fv[4], S gv[4]) const {
+    const double TWOTHIRD = 2.0 / 3.0;
+    fv[0] = TWOTHIRD * mmu * (2.0 * ux - vy);
+    fv[1] = mmu * (uy + vx);
+    fv[2] = mmu * (wx);
+    fv[3] = (lambda * tx + uu * fv[0] + vv * fv[1] + ww * fv[2]);
+    gv[0] = mmu * (uy + vx);
+    gv[1] = TWOTHIRD * mmu * (-ux + 2.0 * vy);
+    gv[2] = mmu * (wy);
+    gv[3] = lambda * ty + uu * gv[0] + vv * gv[1] + ww * gv[2];
+  }
+
+  // viscous flux through i-face (i,j): o4 (rhs/flux_visqueux_o4_i.F) or o2
+  BCG_HD void visc_i(int i, int j, bool o2, S fv[4], S gv[4]) const {
+    const double volm1 = VOLF(i, j, 1);
+    const double nxN = 0.5 * (NX(i + 1, j, 1) + NX(i, j, 1)), nxS = -(0.5 * (NX(i - 1, j, 1) + NX(i, j, 1)));
+    const double nxO = 0.5 * (NX(i - 1, j + 1, 2) + NX(i, j + 1, 2)), nxE = -(0.5 * (NX(i - 1, j, 2) + NX(i, j, 2)));
+    const double nyN = 0.5 * (NY(i + 1, j, 1) + NY(i, j, 1)), nyS = -(0.5 * (NY(i - 1, j, 1) + NY(i, j, 1)));
+    const double nyO = 0.5 * (NY(i - 1, j + 1, 2) + NY(i, j + 1, 2)), nyE = -(0.5 * (NY(i - 1, j, 2) + NY(i, j, 2)));
+    S gx[4], gy[4];
+    const int fl[4] = {F_U, F_V, F_W, F_T};
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int f = fl[a];
+      S vN, vS, vE, vO;
+      if (!o2) {
+        const double T24 = 1.0 / 24.0, cc = c.ccross;
+        vN = T24 * (-P(f, i + 1, j) + 26.0 * P(f, i, j) - P(f, i - 1, j));
+        vS = T24 * (-P(f, i, j) + 26.0 * P(f, i - 1, j) - P(f, i - 2, j));
+        const S r0 = q4(P(f, i - 2, j - 2), P(f, i - 1, j - 2), P(f, i, j - 2), P(f, i + 1, j - 2));
+        const S r1 = q4(P(f, i - 2, j - 1), P(f, i - 1, j - 1), P(f, i, j - 1), P(f, i + 1, j - 1));
+        const S r2 = q4(P(f, i - 2, j), P(f, i - 1, j), P(f, i, j), P(f, i + 1, j));
+        const S r3 = q4(P(f, i - 2, j + 1), P(f, i - 1, j + 1), P(f, i, j + 1), P(f, i + 1, j + 1));
+        const S r4 = q4(P(f, i - 2, j + 2), P(f, i - 1, j + 2), P(f, i, j + 2), P(f, i + 1, j + 2));
+        vE = cc * (-r0 + 7.0 * r1 + 7.0 * r2 - r3);
+        vO = cc * (-r1 + 7.0 * r2 + 7.0 * r3 - r4);
+      } else {
+        vN = P(f, i, j);
+        vS = P(f, i - 1, j);
+        vE = 0.25 * (P(f, i, j) + P(f, i, j - 1) + P(f, i - 1, j) + P(f, i - 1, j - 1));
+        vO = 0.25 * (P(f, i, j) + P(f, i, j + 1) + P(f, i - 1, j) + P(f, i - 1, j + 1));
+      }
+      gx[a] = (vN * nxN + vS * nxS + vO * nxO + vE * nxE) * volm1;
+      gy[a] = (vN * nyN + vS * nyS + vO * nyO + vE * nyE) * volm1;
+    }
+    S uu, vv, ww, mmu, lambda;
+    if (!o2) {
+      uu = 0.0625 * q4(P(F_U, i - 2, j), P(F_U, i - 1, j), P(F_U, i, j), P(F_U, i + 1, j));
+      vv = 0.0625 * q4(P(F_V, i - 2, j), P(F_V, i - 1, j), P(F_V, i, j), P(F_V, i + 1, j));
+      ww = 0.0625 * q4(P(F_W, i - 2, j), P(F_W, i - 1, j), P(F_W, i, j), P(F_W, i + 1, j));
+      mmu = 0.0625 * q4(P(F_MU, i - 2, j), P(F_MU, i - 1, j), P(F_MU, i, j), P(F_MU, i + 1, j));
+      lambda = mmu * c.cpprandtl;
+    } else {
+      uu = 0.5 * (P(F_U, i, j) + P(F_U, i - 1, j));
+      vv = 0.5 * (P(F_V, i, j) + P(F_V, i - 1, j));
+      ww = 0.5 * (P(F_W, i, j) + P(F_W, i - 1, j));
+      mmu = 0.5 * (P(F_MU, i, j) + P(F_MU, i - 1, j));
+      lambda = 0.5 * (P(F_MU, i, j) + P(F_MU, i - 1, j)) * c.cpprandtl;
+    }
+    visc_fluxes(mmu, lambda, uu, vv, ww, gx[0], gy[0], gx[1], gy[1], gx[2], gy[2], gx[3], gy[3], fv, gv);
+  }
+
+  // viscous flux through j-face (i,j): o4 (rhs/flux_visqueux_o4_j.F) or o2
+  BCG_HD void visc_j(int i, int j, bool o2, S fv[4], S gv[4]) const {
+    const double volm1 = VOLF(i, j, 2);
+    const double nxN = 0.5 * (NX(i + 1, j - 1, 1) + NX(i + 1, j, 1)), nxS = -(0.5 * (NX(i, j - 1, 1) + NX(i, j, 1)));
+    const double nxO = 0.5 * (NX(i, j + 1, 2) + NX(i, j, 2)), nxE = -(0.5 * (NX(i, j - 1, 2) + NX(i, j, 2)));
+    const double nyN = 0.5 * (NY(i + 1, j - 1, 1) + NY(i + 1, j, 1)), nyS = -(0.5 * (NY(i, j - 1, 1) + NY(i, j, 1)));
+    const double nyO = 0.5 * (NY(i, j + 1, 2) + NY(i, j, 2)), nyE = -(0.5 * (NY(i, j - 1, 2) + NY(i, j, 2)));
+    S gx[4], gy[4];
+    const int fl[4] = {F_U, F_V, F_W, F_T};
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int f = fl[a];
+      S vN, vS, vE, vO;
+      if (!o2) {
+        const double T24 = 1.0 / 24.0, cc = c.ccross;
+        const S k0 = q4(P(f, i - 2, j - 2), P(f, i - 2, j - 1), P(f, i - 2, j), P(f, i - 2, j + 1));
+        const S k1 = q4(P(f, i - 1, j - 2), P(f, i - 1, j - 1), P(f, i - 1, j), P(f, i - 1, j + 1));
+        const S k2 = q4(P(f, i, j - 2), P(f, i, j - 1), P(f, i, j), P(f, i, j + 1));
+        const S k3 = q4(P(f, i + 1, j - 2), P(f, i + 1, j - 1), P(f, i + 1, j), P(f, i + 1, j + 1));
+        const S k4 = q4(P(f, i + 2, j - 2), P(f, i + 2, j - 1), P(f, i + 2, j), P(f, i + 2, j + 1));
+        vN = cc * (-k1 + 7.0 * k2 + 7.0 * k3 - k4);
+        vS = cc * (-k0 + 7.0 * k1 + 7.0 * k2 - k3);
+        vE = T24 * (-P(f, i, j) + 26.0 * P(f, i, j - 1) - P(f, i, j - 2));
+        vO = T24 * (-P(f, i, j + 1) + 26.0 * P(f, i, j) - P(f, i, j - 1));
+      } else {
+        vN = 0.25 * (P(f, i, j) + P(f, i + 1, j) + P(f, i, j - 1) + P(f, i + 1, j - 1));
+        vS = 0.25 * (P(f, i, j) + P(f, i - 1, j) + P(f, i, j - 1) + P(f, i - 1, j - 1));
+        vO = P(f, i, j);
+        vE = P(f, i, j - 1);
+      }
+      gx[a] = (vN * nxN + vS * nxS + vO * nxO + vE * nxE) * volm1;
+      gy[a] = (vN * nyN + vS * nyS + vO * nyO + vE * nyE) * volm1;
+    }
+    S uu, vv, ww, mmu, lambda;
+    if (!o2) {
+      uu = 0.0625 * q4(P(F_U, i, j - 2), P(F_U, i, j - 1), P(F_U, i, j), P(F_U, i, j + 1));
+      vv = 0.0625 * q4(P(F_V, i, j - 2), P(F_V, i, j - 1), P(F_V, i, j), P(F_V, i, j + 1));
+      ww = 0.0625 * q4(P(F_W, i, j - 2), P(F_W, i, j - 1), P(F_W, i, j), P(F_W, i, j + 1));
+      mmu = 0.0625 * q4(P(F_MU, i, j - 2), P(F_MU, i, j - 1), P(F_MU, i, j), P(F_MU, i, j + 1));
+      lambda = mmu * c.cpprandtl;
+    } else {
+      uu = 0.5 * (P(F_U, i, j) + P(F_U, i, j - 1));
+      vv = 0.5 * (P(F_V, i, j) + P(F_V, i, j - 1));
+      ww = 0.5 * (P(F_W, i, j) + P(F_W, i, j - 1));
+      mmu = 0.5 * (P(F_MU, i, j) + P(F_MU, i, j - 1));
+      lambda = 0.5 * (P(F_MU, i, j) + P(F_MU, i, j - 1)) * c.cpprandtl;
+    }
+    visc_fluxes(mmu, lambda, uu, vv, ww, gx[0], gy[0], gx[1], gy[1], gx[2], gy[2], gx[3], gy[3], fv, gv);
+  }
+
+  // spectral radius, Ducros/pressure sensor and dissipation through the face
+  // between cells L and R (rhs/spectralradius_i.F, ducrosfordnc_i.F,
+  // dissipation_ducros_i.F); LL/RR extend the pressure stencil.
+  BCG_HD void dissipation(int iL, int jL, int iR, int jR, int iLL, int jLL, int iRR, int jRR, double fnx, double fny,
+                          const S pred[5], S diss[5]) const {
+    const S rhomr = W(iR, jR, 1), ur = W(iR, jR, 2) / rhomr, vr = W(iR, jR, 3) / rhomr;
+    const S c2r = c.c2fac * P(F_T, iR, jR);
+    const S rhoml = W(iL, jL, 1), ul = W(iL, jL, 2) / rhoml, vl = W(iL, jL, 3) / rhoml;
+    const S c2l = c.c2fac * P(F_T, iL, jL);
+    const S r = sqrt_t(rhomr / rhoml);
+    const S rr = 1.0 / (1.0 + r);
+    const S omrr = 1.0 - rr;
+    const S u = ul * rr + ur * omrr, v = vl * rr + vr * omrr;
+    const S c2x = c2l * rr + c2r * omrr;
+    const double nx2 = fnx * fnx + fny * fny;
+    const S rspec = fabs_t(fnx * u + fny * v) + sqrt_t(c2x * nx2);
+    S eps2 = Planes<S>::c(0.0), eps4 = Planes<S>::c(0.0 < c.k4 ? c.k4 : 0.0);
+    if (c.k2 != 0.0) {
+      // with k2 = 0 the sensor is multiplied by zero: skipped (the reference
+      // value 0*coef is exactly 0 for the finite coef of a physical state)
+      const S pL = P(F_P, iL, jL), pR = P(F_P, iR, jR), pLL = P(F_P, iLL, jLL), pRR = P(F_P, iRR, jRR);
+      const S ks1 = fabs_t(pL - 2.0 * pR + pRR) / fabs_t(pL + 2.0 * pR + pRR);
+      const S ks2 = fabs_t(pLL - 2.0 * pL + pR) / fabs_t(pLL + 2.0 * pL + pR);
+      S divu = G(G_UX, iR, jR) + G(G_VY, iR, jR);
+      S divu2 = divu * divu;
+      S vo = G(G_VX, iR, jR) - G(G_UY, iR, jR);
+      S vort2 = vo * vo;
+      const S ducros1 = divu2 / (divu2 + vort2 + 1e-15);
+      const S dxm1 = 0.5 * (1.0 - tanh_t(2.5 + 10.0 * VOL(iR, jR) / (sqrt_t(c2r * nx2) + 1e-15) * divu));
+      divu = G(G_UX, iL, jL) + G(G_VY, iL, jL);
+      divu2 = divu * divu;
+      vo = G(G_VX, iL, jL) - G(G_UY, iL, jL);
+      vort2 = vo * vo;
+      const S ducros2 = divu2 / (divu2 + vort2 + 1e-15);
+      const S dxm2 = 0.5 * (1.0 - tanh_t(2.5 + 10.0 * VOL(iL, jL) / (sqrt_t(c2l * nx2) + 1e-15) * divu));
+      const S coef = fmax_t(ks1, ks2) * fmax_t(ducros1, ducros2) * fmax_t(dxm1, dxm2);
+      eps2 = c.k2 * coef;
+      eps4 = fmax_t(Planes<S>::c(0.0), c.k4 - eps2 * 12.0);
+    }
+#pragma unroll
+    for (int v5 = 1; v5 <= 5; ++v5) {
+      const S diff = 0.5 * (W(iR, jR, v5) - W(iL, jL, v5));
+      diss[v5 - 1] = rspec * (eps2 * diff + eps4 * pred[v5 - 1]);
+    }
+  }
+
+  BCG_HD void assemble(double snx, double sny, const S fx[5], const S diss[5], const S fv[4], const S gv[4], S h[5]) const {
+    const double sn = sqrt(snx * snx + sny * sny);
+    const double invsn = 1.0 / sn;
+    const double nxl = snx * invsn, nyl = sny * invsn;
+    h[0] = fx[0] - diss[0];
+#pragma unroll
+    for (int v5 = 2; v5 <= 5; ++v5) h[v5 - 1] = fx[v5 - 1] - diss[v5 - 1] - (fv[v5 - 2] * nxl + gv[v5 - 2] * nyl) * sn;
+  }
+
+  // i-face (i,j), between cells (i-1,j) and (i,j)
+  BCG_HD void iface(int i, int j, S h[5]) const {
+    S fx[5], pred[5], diss[5], fv[4], gv[4];
+    const double fnx = NX(i, j, 1), fny = NY(i, j, 1);
+#pragma unroll
+    for (int v5 = 1; v5 <= 5; ++v5) {
+      fx[v5 - 1] = (c.c1 * (Fl(v5, i, j) + Fl(v5, i - 1, j)) + c.c2 * (Fl(v5, i + 1, j) + Fl(v5, i - 2, j)) +
+                    c.c3 * (Fl(v5, i + 2, j) + Fl(v5, i - 3, j))) * fnx +
+                   (c.c1 * (Gl(v5, i, j) + Gl(v5, i - 1, j)) + c.c2 * (Gl(v5, i + 1, j) + Gl(v5, i - 2, j)) +
+                    c.c3 * (Gl(v5, i + 2, j) + Gl(v5, i - 3, j))) * fny;
+      pred[v5 - 1] = -(c.d3 * W(i - 3, j, v5)) + c.d2 * W(i - 2, j, v5) - c.d1 * W(i - 1, j, v5) +
+                     c.d1 * W(i, j, v5) - c.d2 * W(i + 1, j, v5) + c.d3 * W(i + 2, j, v5);
+    }
+    visc_i(i, j, j <= 2, fv, gv);
+    dissipation(i - 1, j, i, j, i - 2, j, i + 1, j, fnx, fny, pred, diss);
+    assemble(fnx, fny, fx, diss, fv, gv, h);
+  }
+
+  // j-face (i,j), between cells (i,j-1) and (i,j); j >= 2
+  BCG_HD void jface(int i, int j, S h[5]) const {
+    S fx[5], pred[5], diss[5], fv[4], gv[4];
+    const double fnx = NX(i, j, 2), fny = NY(i, j, 2);
+#pragma unroll
+    for (int v5 = 1; v5 <= 5; ++v5) {
+      if (j >= 4) {
+        fx[v5 - 1] = (c.c1 * (Fl(v5, i, j) + Fl(v5, i, j - 1)) + c.c2 * (Fl(v5, i, j + 1) + Fl(v5, i, j - 2)) +
+                      c.c3 * (Fl(v5, i, j + 2) + Fl(v5, i, j - 3))) * fnx +
+                     (c.c1 * (Gl(v5, i, j) + Gl(v5, i, j - 1)) + c.c2 * (Gl(v5, i, j + 1) + Gl(v5, i, j - 2)) +
+                      c.c3 * (Gl(v5, i, j + 2) + Gl(v5, i, j - 3))) * fny;
+      } else {
+        const double* cw = (j == 3) ? c.c5 : c.c3w;  // rhs/nearbndfluxes5demi_7p.F, 3demi
+        fx[v5 - 1] = (cw[0] * Fl(v5, i, 1) + cw[1] * Fl(v5, i, 2) + cw[2] * Fl(v5, i, 3) + cw[3] * Fl(v5, i, 4) +
+                      cw[4] * Fl(v5, i, 5)) * fnx +
+                     (cw[0] * Gl(v5, i, 1) + cw[1] * Gl(v5, i, 2) + cw[2] * Gl(v5, i, 3) + cw[3] * Gl(v5, i, 4) +
+                      cw[4] * Gl(v5, i, 5)) * fny;
+      }
+      pred[v5 - 1] = -(c.d3 * W(i, j - 3, v5)) + c.d2 * W(i, j - 2, v5) - c.d1 * W(i, j - 1, v5) +
+                     c.d1 * W(i, j, v5) - c.d2 * W(i, j + 1, v5) + c.d3 * W(i, j + 2, v5);
+    }
+    visc_j(i, j, j == 2, fv, gv);
+    dissipation(i, j - 1, i, j, i, j - 2, i, j + 1, fnx, fny, pred, diss);
+    assemble(fnx, fny, fx, diss, fv, gv, h);
+  }
+
+  // adiabatic no-slip wall face j = 1 (rhs/fluxwall.F)
+  BCG_HD void wallface(int i, S h[5]) const {
+    const int j = 1;
+    const S pw = c.ct0 * P(F_P, i, j) + c.ct1 * P(F_P, i, j + 1);
+    const S mmu = P(F_MU, i, j);
+    const double nx2 = NX(i, j, 2), ny2 = NY(i, j, 2), vf = VOLF(i, j, 2);
+    const S ux = 2.0 * P(F_U, i, j) * nx2 * vf, vx = 2.0 * P(F_V, i, j) * nx2 * vf, wx = 2.0 * P(F_W, i, j) * nx2 * vf;
+    const S uy = 2.0 * P(F_U, i, j) * ny2 * vf, vy = 2.0 * P(F_V, i, j) * ny2 * vf, wy = 2.0 * P(F_W, i, j) * ny2 * vf;
+    const double TWOTHIRD = 2.0 / 3.0;
+    const S fvrou = TWOTHIRD * mmu * (2.0 * ux - vy), fvrov = mmu * (uy + vx), fvrow = mmu * (wx);
+    const S gvrou = mmu * (uy + vx), gvrov = TWOTHIRD * mmu * (-ux + 2.0 * vy), gvrow = mmu * (wy);
+    h[0] = Planes<S>::c(0.0);
+    h[1] = pw * nx2 - (fvrou * nx2 + gvrou * ny2);
+    h[2] = pw * ny2 - (fvrov * nx2 + gvrov * ny2);
+    h[3] = -(fvrow * nx2 + gvrow * ny2);
+    h[4] = Planes<S>::c(0.0);
+  }
+};
+
+// thread per node (i,j), i in [1, im+1], j in [1, jm+1]: the i-face (j <= jm)
+// and the j-face (i <= im) of the node.  hn holds 10 fields (5 i-face, 5
+// j-face) on the (im+1) x (jm+1) node set.
+template <class S>
+__global__ void __launch_bounds__(128) k_faces(FaceCtx<S> fc, Scratch<S> hn) {
+  const Ext& e = fc.e;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nI = e.im + 1;
+  if (t >= nI * (e.jm + 1)) return;
+  const int i = 1 + t % nI, j = 1 + t / nI;
+  S h[5];
+  if (j <= e.jm) {
+    fc.iface(i, j, h);
+#pragma unroll
+    for (int v5 = 0; v5 < 5; ++v5) hn.st(v5, t, h[v5]);
+  }
+  if (i <= e.im) {
+    if (j == 1) fc.wallface(i, h); else fc.jface(i, j, h);
+#pragma unroll
+    for (int v5 = 0; v5 < 5; ++v5) hn.st(5 + v5, t, h[v5]);
+  }
+}
+
+// balance (rhs/balance.F): residu = -(h1(i+1)-h1(i)) - (h2(j+1)-h2(j))
+template <class S>
+__global__ void __launch_bounds__(256) k_balance(Ext e, Scratch<S> hn, double* __restrict__ res, double* __restrict__ resd,
+                                                 size_t dstride) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= e.im * e.jm) return;
+  const int i = 1 + t % e.im, j = 1 + t / e.im;
+  const int nI = e.im + 1;
+  const int a = (i - 1) + (j - 1) * nI;
+  const size_t q = e.cidx(i, j);
+  constexpr int K = NDir<S>::value;
+#pragma unroll
+  for (int v5 = 0; v5 < 5; ++v5) {
+    const S r = -(hn.ld(v5, a + 1) - hn.ld(v5, a)) - (hn.ld(5 + v5, a + nI) - hn.ld(5 + v5, a));
+    if constexpr (K == 0) {
+      if (res) res[q + (size_t)v5 * e.np] = r;
+    } else {
+      if (res) res[q + (size_t)v5 * e.np] = r.v;
+#pragma unroll
+      for (int k = 0; k < K; ++k) resd[(size_t)k * dstride + q + (size_t)v5 * e.np] = r.d[k];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+template <class S>
+static cudaError_t run_residual_t(const ResidualArgs& a, cudaStream_t st) {
+  const Ext e = make_ext(a.im, a.jm, a.gh);
+  const Coef c = make_coef(a.phys);
+  constexpr int NP = NDir<S>::value + 1;
+  const size_t nn = (size_t)(a.im + 1) * (a.jm + 1);
+  Scratch<S> pr{a.scratch, e.np};
+  Scratch<S> gr{a.scratch + (size_t)F_NPRIM * NP * e.np, e.np};
+  Scratch<S> hn{a.scratch + (size_t)(F_NPRIM + G_NGRAD) * NP * e.np, nn};
+  State<S> w;
+  if constexpr (NP == 1) w = State<S>{a.w};
+  else w = State<S>{a.w, a.wd, a.dstride};
+  const int B = 256;
+  k_prim<S><<<(unsigned)((e.np + B - 1) / B), B, 0, st>>>(e, c, w, pr);
+  if (c.k2 != 0.0)
+    k_grad<S><<<(unsigned)((a.im * a.jm + B - 1) / B), B, 0, st>>>(e, c, pr, gr, a.nx, a.ny, a.vol);
+  FaceCtx<S> fc{e, c, w, pr, gr, a.nx, a.ny, a.vol, a.volf};
+  const int BF = 128;
+  k_faces<S><<<(unsigned)((nn + BF - 1) / BF), BF, 0, st>>>(fc, hn);
+  k_balance<S><<<(unsigned)((a.im * a.jm + B - 1) / B), B, 0, st>>>(e, hn, a.res, a.resd, a.dstride);
+  return cudaGetLastError();
+}
+
+size_t residual_scratch_doubles(int im, int jm, int gh, int ndir) {
+  const Ext e = make_ext(im, jm, gh);
+  const size_t nn = (size_t)(im + 1) * (jm + 1);
+  return (size_t)(ndir + 1) * ((size_t)(F_NPRIM + G_NGRAD) * e.np + 10 * nn);
+}
+
+cudaError_t run_residual(const ResidualArgs& a, cudaStream_t st) {
+  switch (a.ndir) {
+    case 0: return run_residual_t<double>(a, st);
+    case 1: return run_residual_t<DK<1>>(a, st);
+    case 2: return run_residual_t<DK<2>>(a, st);
+    case 4: return run_residual_t<DK<4>>(a, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace bcg

@@ -1,0 +1,28 @@
+// Launch interface of the DNC5 residual / fused residual + JVP kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include "dnc5.cuh"
+
+namespace bcg {
+
+struct ResidualArgs {
+  int im, jm, gh;
+  int ndir;              // 0: residual only; K: residual + K tangent directions
+  Phys phys;
+  const double* w;       // (ni, nj, 5)
+  const double* wd;      // K stacked (ni, nj, 5) tangent states, stride dstride
+  size_t dstride;        // doubles between tangent directions (>= 5*ni*nj)
+  const double* nx;      // (ni+1, nj+1, 2)
+  const double* ny;
+  const double* vol;     // (ni, nj)
+  const double* volf;    // (ni, nj, 2)
+  double* res;           // (ni, nj, 5), interior written; may be null when ndir > 0
+  double* resd;          // K stacked (ni, nj, 5), interior written
+  double* scratch;       // residual_scratch_doubles(im, jm, gh, ndir) doubles
+};
+
+size_t residual_scratch_doubles(int im, int jm, int gh, int ndir);
+cudaError_t run_residual(const ResidualArgs& a, cudaStream_t st);
+
+}  // namespace bcg

@@ -1,0 +1,18 @@
+"""Drop-in for the reference's srcfv.f_sch (residual routines).
+
+flux_num_dnc5_2d: srcfv/rhs/flux_num_dnc5.F90:7-8.
+"""
+from .._f2py import arr, call, dims_from_cell
+
+
+def flux_num_dnc5_2d(residu, w, x0, y0, nx, ny, xc, yc, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref, tref,
+                     s_suth, k2, k4, im=None, jm=None):
+    """Residual R(w) of the 5th-order DNC (FE-MUSCL) scheme; writes the
+    interior of `residu` in place (not divided by the cell volume)."""
+    gh = int(gh)
+    if im is None or jm is None:
+        im, jm = dims_from_cell(w, gh)
+    residu = arr(residu, "residu", inout=True)
+    w, nx, ny, vol, volf = (arr(a, n) for a, n in ((w, "w"), (nx, "nx"), (ny, "ny"), (vol, "vol"), (volf, "volf")))
+    call("bcg_flux_num_dnc5_2d", residu, w, None, None, nx, ny, None, None, vol, volf, gh, cp, cv, prandtl, gam, rgaz,
+         cs, muref, tref, s_suth, k2, k4, int(im), int(jm))

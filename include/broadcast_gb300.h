@@ -1,0 +1,142 @@
+/* broadcast_gb300.h - C ABI of libbroadcast_gb300.so, the GB300 (sm_103a)
+ * implementation of BROADCAST's DNC5 residual / tangent / boundary /
+ * colored-Jacobian hot path.
+ *
+ * Each entry point replaces one f2py-wrapped Fortran routine of the reference
+ * and keeps its name (prefixed bcg_) and argument order; the reference routine
+ * it replaces is cited on each declaration.  Conventions:
+ *
+ *  - Arrays are double precision, Fortran (column-major) order, with the
+ *    caller's ghost-padded extents: cell arrays (im+2gh, jm+2gh[, nv]), face
+ *    and node arrays (im+2gh+1, jm+2gh+1[, 2]).  Outputs are written in place,
+ *    as with the reference's intent(inout) arguments.
+ *  - An array may be a host pointer or a CUDA device pointer.  Host arrays
+ *    are copied to the device and back around the call, which has completed
+ *    when it returns.  When every array is a device pointer the work is queued
+ *    on the library stream (bcg_set_stream) and the call returns at once.
+ *  - interf/prr/prd are the reference's Fortran (2,2) integer arrays in
+ *    column-major order {imin, imax, jmin, jmax}; loc is one of "Ilo", "Ihi",
+ *    "Jlo", "Jhi" (3 characters, no terminator needed).  These small index
+ *    arrays are always host pointers.
+ *  - Every function returns 0 on success or a negative code: -1 bad arguments,
+ *    -2 CUDA failure, -3 device allocation failure, -4 no CUDA device.
+ *    bcg_last_error_string() describes the last failure of the calling thread.
+ *  - Trailing dimension arguments that f2py infers from array shapes (lm, em,
+ *    nbentry) are explicit here.
+ *  - Calls are serialised on one library stream per process; two host threads
+ *    must not call the library at the same time.
+ */
+#ifndef BROADCAST_GB300_H
+#define BROADCAST_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- runtime --------------------------------------------------------------- */
+int bcg_abi_version(void);
+int bcg_set_stream(void* cuda_stream);      /* NULL selects the legacy default stream */
+void* bcg_get_stream(void);
+int bcg_synchronize(void);
+const char* bcg_last_error_string(void);
+size_t bcg_residual_scratch_bytes(int im, int jm, int gh, int ndir);
+
+/* ---- residual, tangent ------------------------------------------------------ */
+/* srcfv/rhs/flux_num_dnc5.F90:7-8 (flux_num_dnc5_2d).  x0, y0, xc, yc are
+ * accepted for signature compatibility and unused, as in the reference. */
+int bcg_flux_num_dnc5_2d(double* residu, const double* w, const double* x0, const double* y0, const double* nx,
+                         const double* ny, const double* xc, const double* yc, const double* vol, const double* volf,
+                         int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs,
+                         double muref, double tref, double s_suth, double k2, double k4, int im, int jm);
+
+/* srcfv/tangent/flux_num_dnc5_d.f90:15-17 (FLUX_NUM_DNC5_2D_D): residu and
+ * residud = dR/dw . wd */
+int bcg_flux_num_dnc5_2d_d(double* residu, double* residud, const double* w, const double* wd, const double* x0,
+                           const double* y0, const double* nx, const double* ny, const double* xc, const double* yc,
+                           const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
+                           double gam, double rgaz, double cs, double muref, double tref, double s_suth, double k2,
+                           double k4, int im, int jm);
+
+/* Batched form of FLUX_NUM_DNC5_2D_D (no reference counterpart beyond the
+ * routine it batches): nd tangent states stacked in wd, nd outputs in residud,
+ * one primal evaluation per group of up to 4 directions. */
+int bcg_flux_num_dnc5_2d_dn(double* residu, double* residud, const double* w, const double* wd, int nd,
+                            const double* x0, const double* y0, const double* nx, const double* ny, const double* xc,
+                            const double* yc, const double* vol, const double* volf, int gh, double cp, double cv,
+                            double prandtl, double gam, double rgaz, double cs, double muref, double tref,
+                            double s_suth, double k2, double k4, int im, int jm);
+
+/* ---- boundary conditions ---------------------------------------------------- */
+/* srcfv/borders/bc_wall_viscous.F90:2 ; tangent/bc_wall_viscous_d.f90:11 */
+int bcg_bc_wall_viscous_adia_2d(double* w, const char* loc, double gam, const int* interf, int gh, int im, int jm);
+int bcg_bc_wall_viscous_adia_2d_d(double* w, double* wd, const char* loc, double gam, const int* interf, int gh,
+                                  int im, int jm);
+/* srcfv/borders/bc_no_reflexion.F90:8 ; tangent/bc_no_reflexion_d.f90:16 (wbd is (lm,5)) */
+int bcg_bc_no_reflexion_2d(double* w, const double* wbd, const char* loc, const int* interf, const double* nx,
+                           const double* ny, double gam, int gh, int im, int jm, int lm);
+int bcg_bc_no_reflexion_2d_d(double* w, double* wd, const double* wbd, const char* loc, const int* interf,
+                             const double* nx, const double* ny, double gam, int gh, int im, int jm, int lm);
+/* srcfv/borders/bc_supandsubinlet.F90:2 ; tangent/bc_supandsubinlet_d.f90:11 (field is (lm,gh,5)) */
+int bcg_bc_supandsubinlet_2d(double* w, const char* loc, const int* interf, const double* field, const double* nx,
+                             const double* ny, double gam, int im, int jm, int lm, int gh);
+int bcg_bc_supandsubinlet_2d_d(double* w, double* wd, const char* loc, const int* interf, const double* field,
+                               const double* nx, const double* ny, double gam, int im, int jm, int lm, int gh);
+/* srcfv/borders/bc_extrapolate.F90:39 ; tangent/bc_extrapolateo2_d.f90:18 (em variables) */
+int bcg_bc_extrapolate_o2_2d(double* w, const char* loc, const int* interf, int im, int jm, int gh, int em);
+int bcg_bc_extrapolate_o2_2d_d(double* w, double* wd, const char* loc, const int* interf, int im, int jm, int gh,
+                               int em);
+/* srcfv/borders/jn_match.F90:3 ; tangent/jn_match_2d_d.f90:11 */
+int bcg_jn_match_2d(double* wr, const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, int imr, int jmr,
+                    const double* wd, const int* prd, int gh1d, int gh2d, int gh3d, int gh4d, int imd, int jmd,
+                    const int* tr, int em);
+int bcg_jn_match_2d_d(double* wr, double* wrd, const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, int imr,
+                      int jmr, const double* wd, const double* wdd, const int* prd, int gh1d, int gh2d, int gh3d,
+                      int gh4d, int imd, int jmd, const int* tr, int em);
+/* srcfv/borders/jn_match_geom.F90:7 (tr(1) = +-1 only) */
+int bcg_jn_match_geom_2d(double* wr, const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, int imr, int jmr,
+                         const double* wd, const int* prd, int gh1d, int gh2d, int gh3d, int gh4d, int imd, int jmd,
+                         const int* tr);
+
+/* ---- colored Jacobian assembly (misc/ComputeJacobian.f90) -------------------- */
+/* :357 testvector ; :1075 testvector_partial */
+int bcg_testvector(double* wd, int m, int l, int k, int gh, int im, int jm);
+int bcg_testvector_partial(double* wd, int m, int l, int k, int gh, int im, int jm, int istart, int iend, int jstart,
+                           int jend);
+/* :292 computejacobianfromjv ; :503 _relaxed ; :847 _relaxed_withjn ; :929 _withjn ;
+ * :1095 _relaxed_withjnandcheck ; :708 computejacobianfromdz.  jac/ia/ja hold
+ * nbentry entries; only the 5*im*jm slots of the given seed are written. */
+int bcg_computejacobianfromjv(double* jac, int* ia, int* ja, const double* resd, int m, int l, int k, int gh, int im,
+                              int jm, long long nbentry);
+int bcg_computejacobianfromjv_relaxed(double* jac, int* ia, int* ja, const double* resd, int m, int l, int k, int gh,
+                                      int im, int jm, long long nbentry, const double* coefdiag);
+int bcg_computejacobianfromjv_relaxed_withjn(double* jac, int* ia, int* ja, const double* resd, int m, int l, int k,
+                                             int gh, int im, int jm, long long nbentry, const double* coefdiag);
+int bcg_computejacobianfromjv_withjn(double* jac, int* ia, int* ja, const double* resd, int m, int l, int k, int gh,
+                                     int im, int jm, long long nbentry);
+int bcg_computejacobianfromjv_relaxed_withjnandcheck(double* jac, int* ia, int* ja, const double* resd, int m, int l,
+                                                     int k, int gh, int im, int jm, long long nbentry,
+                                                     const double* coefdiag, double mini, int n);
+int bcg_computejacobianfromdz(double* jac, int* ia, int* ja, const double* dz, int m, int l, int k, int gh, int im,
+                              int jm, long long nbentry);
+
+/* ---- norms (srcfv/norm.F90) ---------------------------------------------------- */
+/* :2 compute_norml2 ; :34 compute_norml2inf ; :79 compute_maxnorm (5-vectors) */
+int bcg_compute_norml2(double* norm, double* nmoy, const double* rhs, int im, int jm, int gh);
+int bcg_compute_norml2inf(double* norm, double* ninf, const double* rhs, int im, int jm, int gh);
+int bcg_compute_maxnorm(double* norm, int* imax, int* jmax, const double* rhs, int im, int jm, int gh);
+
+/* ---- one-time pre-processing (host) ------------------------------------------- */
+/* srcfv/geom/computegeom.F90:3 */
+int bcg_computegeom_2d(double* x0, double* y0, double* nx, double* ny, double* xc, double* yc, double* vol,
+                       double* volf, int im, int jm, int gh);
+/* set_bnd.f90:1 (field is (jm,gh,5), wbd is (im+gh,5)) */
+int bcg_set_bndbl_2d(const double* w, double* field, double* wbd, int im, int jm, int gh);
+/* initialisation.f90:2 */
+int bcg_initblfv(double muinf, const double* xc, const double* yc, double* w, double* field, int im, int gh, int jm);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BROADCAST_GB300_H */

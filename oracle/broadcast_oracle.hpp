@@ -1,0 +1,1029 @@
+// Test infrastructure only: CPU oracle for the BROADCAST DNC5 hot path.
+//
+// A plain restatement of the reference Fortran, templated on the scalar type
+// of the state so that one source gives
+//   T = double      : the primal routines,
+//   T = Dual<N>     : their exact forward derivatives (what Tapenade's
+//                     srcfv/tangent/*_d.f90 computes, up to rounding),
+//   T = OpCount     : the algorithmic floating-point operation count.
+// Arithmetic is written in the same evaluation order as the Fortran text so
+// that the double instantiation, compiled without contraction
+// (-ffp-contract=off), reproduces the reference bit for bit.
+//
+// Only tests, the smoke check and the CPU-baseline leg of the benchmark use
+// this code.  The shipped library never links it.
+//
+// Arrays follow the reference's f2py layout: Fortran (column-major) order,
+// cell arrays indexed (1-gh:im+gh, 1-gh:jm+gh[, nv]), node/face arrays
+// (1-gh:im+gh+1, 1-gh:jm+gh+1[, nv]).
+#pragma once
+#include <cstddef>
+#include <cstring>
+#include <vector>
+#include <cmath>
+#include "dual.hpp"
+
+namespace orc {
+
+// Fortran-indexed view of a column-major array with lower bounds (lo, lo).
+template <class T>
+struct FArr {
+  T* p;
+  int ni, nj, lo;
+  FArr(T* p_, int ni_, int nj_, int lo_) : p(p_), ni(ni_), nj(nj_), lo(lo_) {}
+  inline T& operator()(int i, int j, int v = 1) const {
+    return p[(size_t)(i - lo) + (size_t)(j - lo) * ni + (size_t)(v - 1) * ni * nj];
+  }
+};
+
+struct Consts {
+  double cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4;
+};
+
+// ===========================================================================
+// Residual: srcfv/prepro/flux_num_dnc5.f90 (flattened srcfv/rhs/flux_num_dnc5.F90)
+// ===========================================================================
+template <class T>
+struct Dnc5 {
+  int im, jm, gh;
+  Consts k;
+  // coefficients (flux_num_dnc5.f90:69-122, 938-950)
+  double HALF = 0.5, ONE = 1.0, ZERO = 0.0, TWO = 2.0, TWOTHIRD = 2.0 / 3.0, FOURTH = 0.25;
+  double TWELFTH = 0.25 / 3.0, TWENTYFOURTH = 1.0 / 24.0, ccross, cpprandtl, cvm1, betas;
+  double b1, b2, c1, c2, c3, d1, d2, d3;
+  double c5d0, c5d1, c5d2, c5d3, c5d4, c3d0, c3d1, c3d2, c3d3, c3d4, ct0, ct1;
+
+  FArr<const T> w;
+  FArr<const double> nx, ny, vol, volf;
+  std::vector<T> velx_, vely_, velz_, tloc_, p_, mu_, f_, g_, gradu_, gradv_, hn_;
+  FArr<T> velx, vely, velz, tloc, p, mu, f, g, gradu, gradv;
+  int nni, nnj;  // node extents
+
+  Dnc5(const T* w_, const double* nx_, const double* ny_, const double* vol_, const double* volf_,
+       int gh_, const Consts& c, int im_, int jm_)
+      : im(im_), jm(jm_), gh(gh_), k(c),
+        w(w_, im_ + 2 * gh_, jm_ + 2 * gh_, 1 - gh_),
+        nx(nx_, im_ + 2 * gh_ + 1, jm_ + 2 * gh_ + 1, 1 - gh_),
+        ny(ny_, im_ + 2 * gh_ + 1, jm_ + 2 * gh_ + 1, 1 - gh_),
+        vol(vol_, im_ + 2 * gh_, jm_ + 2 * gh_, 1 - gh_),
+        volf(volf_, im_ + 2 * gh_, jm_ + 2 * gh_, 1 - gh_),
+        velx(nullptr, 0, 0, 0), vely(nullptr, 0, 0, 0), velz(nullptr, 0, 0, 0), tloc(nullptr, 0, 0, 0),
+        p(nullptr, 0, 0, 0), mu(nullptr, 0, 0, 0), f(nullptr, 0, 0, 0), g(nullptr, 0, 0, 0),
+        gradu(nullptr, 0, 0, 0), gradv(nullptr, 0, 0, 0) {
+    const int ni = im + 2 * gh, nj = jm + 2 * gh, lo = 1 - gh;
+    nni = ni + 1; nnj = nj + 1;
+    const size_t np = (size_t)ni * nj;
+    velx_.assign(np, T(0.0)); vely_.assign(np, T(0.0)); velz_.assign(np, T(0.0));
+    tloc_.assign(np, T(0.0)); p_.assign(np, T(0.0)); mu_.assign(np, T(0.0));
+    f_.assign(np * 5, T(0.0)); g_.assign(np * 5, T(0.0));
+    gradu_.assign(np * 2, T(0.0)); gradv_.assign(np * 2, T(0.0));
+    hn_.assign((size_t)nni * nnj * 10, T(0.0));
+    velx = FArr<T>(velx_.data(), ni, nj, lo); vely = FArr<T>(vely_.data(), ni, nj, lo);
+    velz = FArr<T>(velz_.data(), ni, nj, lo); tloc = FArr<T>(tloc_.data(), ni, nj, lo);
+    p = FArr<T>(p_.data(), ni, nj, lo); mu = FArr<T>(mu_.data(), ni, nj, lo);
+    f = FArr<T>(f_.data(), ni, nj, lo); g = FArr<T>(g_.data(), ni, nj, lo);
+    gradu = FArr<T>(gradu_.data(), ni, nj, lo); gradv = FArr<T>(gradv_.data(), ni, nj, lo);
+    cpprandtl = k.cp / k.prandtl;
+    cvm1 = ONE / k.cv;
+    ccross = TWELFTH * 0.0625;
+    double denom = 1.0 / 12.0;
+    b1 = 8.0 * denom; b2 = -denom;
+    denom = 1.0 / 60.0;
+    c1 = 37.0 * denom; c2 = -8.0 * denom; c3 = denom;
+    d1 = 10.0 * denom; d2 = 5.0 * denom; d3 = denom;
+    betas = k.muref * (k.tref + k.cs) / (std::sqrt(k.tref) * k.tref);
+    // near-wall off-centred coefficients (rhs/coefnearbnd_7p.F)
+    c5d0 = -3.0 * denom; c5d1 = 27.0 * denom; c5d2 = 47.0 * denom; c5d3 = -13.0 * denom; c5d4 = 2.0 * denom;
+    c3d0 = 12.0 * denom; c3d1 = 77.0 * denom; c3d2 = -43.0 * denom; c3d3 = 17.0 * denom; c3d4 = -3.0 * denom;
+    ct0 = 1.125; ct1 = -0.125;
+  }
+
+  inline T& hn(int i, int j, int e, int d) {
+    return hn_[(size_t)(i - (1 - gh)) + (size_t)(j - (1 - gh)) * nni + (size_t)(e - 1) * nni * nnj +
+               (size_t)(d - 1) * nni * nnj * 5];
+  }
+
+  // flux_num_dnc5.f90:125-175 (phys/Primitives.F, phys/viscosity.F)
+  void primitives() {
+#pragma omp parallel for schedule(static)
+    for (int j = 1 - gh; j <= jm + gh; ++j)
+      for (int i = 1 - gh; i <= im + gh; ++i) {
+        const T ro = w(i, j, 1);
+        const T rom1 = ONE / ro;
+        velx(i, j) = w(i, j, 2) * rom1;
+        vely(i, j) = w(i, j, 3) * rom1;
+        velz(i, j) = w(i, j, 4) * rom1;
+        const T ec = HALF * (velx(i, j) * velx(i, j) + vely(i, j) * vely(i, j) + velz(i, j) * velz(i, j));
+        const T eloc = (w(i, j, 5) - ec * ro) * rom1;
+        tloc(i, j) = eloc * cvm1;
+        p(i, j) = (k.gam - ONE) * ro * eloc;
+        const T htot = (w(i, j, 5) + p(i, j)) * rom1;
+        f(i, j, 1) = w(i, j, 2);
+        f(i, j, 2) = w(i, j, 2) * velx(i, j) + p(i, j);
+        f(i, j, 3) = w(i, j, 2) * vely(i, j);
+        f(i, j, 4) = w(i, j, 2) * velz(i, j);
+        f(i, j, 5) = w(i, j, 2) * htot;
+        g(i, j, 1) = w(i, j, 3);
+        g(i, j, 2) = w(i, j, 3) * velx(i, j);
+        g(i, j, 3) = w(i, j, 3) * vely(i, j) + p(i, j);
+        g(i, j, 4) = w(i, j, 3) * velz(i, j);
+        g(i, j, 5) = w(i, j, 3) * htot;
+        mu(i, j) = betas / (tloc(i, j) + k.s_suth) * sqrt_t(tloc(i, j)) * tloc(i, j);
+      }
+  }
+
+  // flux_num_dnc5.f90:179-257 (rhs/gradop_5pi.F, gradop_5pj.F, gradient.F,
+  // gradveloingh.F).  Only the u and v gradients reach the residual (Ducros
+  // sensor); the w and mu gradients of the reference are dead code.
+  void gradients() {
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= jm; ++j)
+      for (int i = 1; i <= im; ++i) {
+        const T gui = (b1 * (velx(i + 1, j) - velx(i - 1, j)) + b2 * (velx(i + 2, j) - velx(i - 2, j)));
+        const T gvi = (b1 * (vely(i + 1, j) - vely(i - 1, j)) + b2 * (vely(i + 2, j) - vely(i - 2, j)));
+        const T guj = (b1 * (velx(i, j + 1) - velx(i, j - 1)) + b2 * (velx(i, j + 2) - velx(i, j - 2)));
+        const T gvj = (b1 * (vely(i, j + 1) - vely(i, j - 1)) + b2 * (vely(i, j + 2) - vely(i, j - 2)));
+        const double volm1 = ONE / vol(i, j);
+        const double dxm1 = HALF * (nx(i, j, 1) + nx(i + 1, j, 1)) * volm1;
+        const double dxm2 = HALF * (nx(i, j, 2) + nx(i, j + 1, 2)) * volm1;
+        const double dym1 = HALF * (ny(i, j, 1) + ny(i + 1, j, 1)) * volm1;
+        const double dym2 = HALF * (ny(i, j, 2) + ny(i, j + 1, 2)) * volm1;
+        gradu(i, j, 1) = dxm1 * gui + dxm2 * guj;
+        gradv(i, j, 1) = dxm1 * gvi + dxm2 * gvj;
+        gradu(i, j, 2) = dym1 * gui + dym2 * guj;
+        gradv(i, j, 2) = dym1 * gvi + dym2 * gvj;
+      }
+    // ghost extrapolation, twice, full-range slices as in gradveloingh.F
+    const int lo = 1 - gh;
+    for (int it = 1; it <= 2; ++it)
+      for (int h = 1; h <= gh; ++h) {
+        for (int c = 1; c <= 2; ++c)
+          for (int i = lo; i <= im + gh; ++i) {
+            gradu(i, 1 - h, c) = TWO * gradu(i, 2 - h, c) - gradu(i, 3 - h, c);
+          }
+        for (int c = 1; c <= 2; ++c)
+          for (int i = lo; i <= im + gh; ++i) gradv(i, 1 - h, c) = TWO * gradv(i, 2 - h, c) - gradv(i, 3 - h, c);
+        for (int c = 1; c <= 2; ++c)
+          for (int i = lo; i <= im + gh; ++i)
+            gradu(i, jm + h, c) = TWO * gradu(i, jm - 1 + h, c) - gradu(i, jm - 2 + h, c);
+        for (int c = 1; c <= 2; ++c)
+          for (int i = lo; i <= im + gh; ++i)
+            gradv(i, jm + h, c) = TWO * gradv(i, jm - 1 + h, c) - gradv(i, jm - 2 + h, c);
+        for (int c = 1; c <= 2; ++c)
+          for (int j = lo; j <= jm + gh; ++j) gradu(1 - h, j, c) = TWO * gradu(2 - h, j, c) - gradu(3 - h, j, c);
+        for (int c = 1; c <= 2; ++c)
+          for (int j = lo; j <= jm + gh; ++j) gradv(1 - h, j, c) = TWO * gradv(2 - h, j, c) - gradv(3 - h, j, c);
+        for (int c = 1; c <= 2; ++c)
+          for (int j = lo; j <= jm + gh; ++j)
+            gradu(im + h, j, c) = TWO * gradu(im - 1 + h, j, c) - gradu(im - 2 + h, j, c);
+        for (int c = 1; c <= 2; ++c)
+          for (int j = lo; j <= jm + gh; ++j)
+            gradv(im + h, j, c) = TWO * gradv(im - 1 + h, j, c) - gradv(im - 2 + h, j, c);
+      }
+  }
+
+  // 4-point interpolation row used by the cross terms (rhs/flux_visqueux_o4_i.F)
+  static inline T q4(const T& a, const T& b, const T& c, const T& d) { return -a + 9.0 * b + 9.0 * c - d; }
+
+  // --- i-face pieces -------------------------------------------------------
+  // Centred 6th-order Euler flux through i-face (i,j) (rhs/euler_o6_i.F)
+  void euler_i(int i, int j, T fx[5]) {
+    for (int e = 1; e <= 5; ++e)
+      fx[e - 1] = (c1 * (f(i, j, e) + f(i - 1, j, e)) + c2 * (f(i + 1, j, e) + f(i - 2, j, e)) +
+                   c3 * (f(i + 2, j, e) + f(i - 3, j, e))) * nx(i, j, 1) +
+                  (c1 * (g(i, j, e) + g(i - 1, j, e)) + c2 * (g(i + 1, j, e) + g(i - 2, j, e)) +
+                   c3 * (g(i + 2, j, e) + g(i - 3, j, e))) * ny(i, j, 1);
+  }
+  void euler_j(int i, int j, T fx[5]) {
+    for (int e = 1; e <= 5; ++e)
+      fx[e - 1] = (c1 * (f(i, j, e) + f(i, j - 1, e)) + c2 * (f(i, j + 1, e) + f(i, j - 2, e)) +
+                   c3 * (f(i, j + 2, e) + f(i, j - 3, e))) * nx(i, j, 2) +
+                  (c1 * (g(i, j, e) + g(i, j - 1, e)) + c2 * (g(i, j + 1, e) + g(i, j - 2, e)) +
+                   c3 * (g(i, j + 2, e) + g(i, j - 3, e))) * ny(i, j, 2);
+  }
+  // Off-centred near-wall j-flux from rows 1..5 (rhs/nearbndfluxes5demi_7p.F,
+  // nearbndfluxes3demi_7p.F)
+  void euler_j_wall(int i, int j, const double c[5], T fx[5]) {
+    for (int e = 1; e <= 5; ++e)
+      fx[e - 1] = (c[0] * f(i, 1, e) + c[1] * f(i, 2, e) + c[2] * f(i, 3, e) + c[3] * f(i, 4, e) +
+                   c[4] * f(i, 5, e)) * nx(i, j, 2) +
+                  (c[0] * g(i, 1, e) + c[1] * g(i, 2, e) + c[2] * g(i, 3, e) + c[3] * g(i, 4, e) +
+                   c[4] * g(i, 5, e)) * ny(i, j, 2);
+  }
+  // 7-point predictor (rhs/predictor_7p_i.F, predictor_7p_j.F)
+  void pred_i(int i, int j, T pr[5]) {
+    for (int e = 1; e <= 5; ++e)
+      pr[e - 1] = -(d3 * w(i - 3, j, e)) + d2 * w(i - 2, j, e) - d1 * w(i - 1, j, e) + d1 * w(i, j, e) -
+                  d2 * w(i + 1, j, e) + d3 * w(i + 2, j, e);
+  }
+  void pred_j(int i, int j, T pr[5]) {
+    for (int e = 1; e <= 5; ++e)
+      pr[e - 1] = -(d3 * w(i, j - 3, e)) + d2 * w(i, j - 2, e) - d1 * w(i, j - 1, e) + d1 * w(i, j, e) -
+                  d2 * w(i, j + 1, e) + d3 * w(i, j + 2, e);
+  }
+
+  // viscous fluxes from the face gradients (rhs/flux_visqueux_o4_i.F:80-103)
+  void visc_fluxes(const T& mmu, const T& lambda, const T& uu, const T& vv, const T& ww, const T& ux,
+                   const T& uy, const T& vx, const T& vy, const T& wx, const T& wy, const T& tx, const T& ty,
+                   T fv[4], T gv[4]) {
+    fv[0] = TWOTHIRD * mmu * (TWO * ux - vy);
+    fv[1] = mmu * (uy + vx);
+    fv[2] = mmu * (wx);
+    fv[3] = (lambda * tx + uu * fv[0] + vv * fv[1] + ww * fv[2]);
+    gv[0] = mmu * (uy + vx);
+    gv[1] = TWOTHIRD * mmu * (-ux + TWO * vy);
+    gv[2] = mmu * (wy);
+    gv[3] = lambda * ty + uu * gv[0] + vv * gv[1] + ww * gv[2];
+  }
+
+  // 4th-order viscous flux through i-face (rhs/flux_visqueux_o4_i.F)
+  void visc_i_o4(int i, int j, T fv[4], T gv[4]) {
+    const double volm1 = volf(i, j, 1);
+    const double nx_N = HALF * (nx(i + 1, j, 1) + nx(i, j, 1));
+    const double nx_S = -(HALF * (nx(i - 1, j, 1) + nx(i, j, 1)));
+    const double nx_O = HALF * (nx(i - 1, j + 1, 2) + nx(i, j + 1, 2));
+    const double nx_E = -(HALF * (nx(i - 1, j, 2) + nx(i, j, 2)));
+    const double ny_N = HALF * (ny(i + 1, j, 1) + ny(i, j, 1));
+    const double ny_S = -(HALF * (ny(i - 1, j, 1) + ny(i, j, 1)));
+    const double ny_O = HALF * (ny(i - 1, j + 1, 2) + ny(i, j + 1, 2));
+    const double ny_E = -(HALF * (ny(i - 1, j, 2) + ny(i, j, 2)));
+    auto grad = [&](FArr<T>& q, T& gx, T& gy) {
+      const T vN = TWENTYFOURTH * (-q(i + 1, j) + 26.0 * q(i, j) - q(i - 1, j));
+      const T vS = TWENTYFOURTH * (-q(i, j) + 26.0 * q(i - 1, j) - q(i - 2, j));
+      auto row = [&](int jj) { return q4(q(i - 2, jj), q(i - 1, jj), q(i, jj), q(i + 1, jj)); };
+      const T vE = ccross * (-row(j - 2) + 7.0 * row(j - 1) + 7.0 * row(j) - row(j + 1));
+      const T vO = ccross * (-row(j - 1) + 7.0 * row(j) + 7.0 * row(j + 1) - row(j + 2));
+      gx = (vN * nx_N + vS * nx_S + vO * nx_O + vE * nx_E) * volm1;
+      gy = (vN * ny_N + vS * ny_S + vO * ny_O + vE * ny_E) * volm1;
+    };
+    T ux, uy, vx, vy, wx, wy, tx, ty;
+    grad(velx, ux, uy); grad(vely, vx, vy); grad(velz, wx, wy); grad(tloc, tx, ty);
+    const T uu = 0.0625 * q4(velx(i - 2, j), velx(i - 1, j), velx(i, j), velx(i + 1, j));
+    const T vv = 0.0625 * q4(vely(i - 2, j), vely(i - 1, j), vely(i, j), vely(i + 1, j));
+    const T ww = 0.0625 * q4(velz(i - 2, j), velz(i - 1, j), velz(i, j), velz(i + 1, j));
+    const T mmu = 0.0625 * q4(mu(i - 2, j), mu(i - 1, j), mu(i, j), mu(i + 1, j));
+    const T lambda = mmu * cpprandtl;
+    visc_fluxes(mmu, lambda, uu, vv, ww, ux, uy, vx, vy, wx, wy, tx, ty, fv, gv);
+  }
+  // 2nd-order viscous flux through i-face (rhs/flux_visqueux_o2_i.F), rows 1-2
+  void visc_i_o2(int i, int j, T fv[4], T gv[4]) {
+    const double volm1 = volf(i, j, 1);
+    const double nx_N = HALF * (nx(i + 1, j, 1) + nx(i, j, 1));
+    const double nx_S = -(HALF * (nx(i - 1, j, 1) + nx(i, j, 1)));
+    const double nx_O = HALF * (nx(i - 1, j + 1, 2) + nx(i, j + 1, 2));
+    const double nx_E = -(HALF * (nx(i - 1, j, 2) + nx(i, j, 2)));
+    const double ny_N = HALF * (ny(i + 1, j, 1) + ny(i, j, 1));
+    const double ny_S = -(HALF * (ny(i - 1, j, 1) + ny(i, j, 1)));
+    const double ny_O = HALF * (ny(i - 1, j + 1, 2) + ny(i, j + 1, 2));
+    const double ny_E = -(HALF * (ny(i - 1, j, 2) + ny(i, j, 2)));
+    auto grad = [&](FArr<T>& q, T& gx, T& gy) {
+      const T vN = q(i, j);
+      const T vS = q(i - 1, j);
+      const T vE = FOURTH * (q(i, j) + q(i, j - 1) + q(i - 1, j) + q(i - 1, j - 1));
+      const T vO = FOURTH * (q(i, j) + q(i, j + 1) + q(i - 1, j) + q(i - 1, j + 1));
+      gx = (vN * nx_N + vS * nx_S + vO * nx_O + vE * nx_E) * volm1;
+      gy = (vN * ny_N + vS * ny_S + vO * ny_O + vE * ny_E) * volm1;
+    };
+    T ux, uy, vx, vy, wx, wy, tx, ty;
+    grad(velx, ux, uy); grad(vely, vx, vy); grad(velz, wx, wy); grad(tloc, tx, ty);
+    const T uu = HALF * (velx(i, j) + velx(i - 1, j));
+    const T vv = HALF * (vely(i, j) + vely(i - 1, j));
+    const T ww = HALF * (velz(i, j) + velz(i - 1, j));
+    const T mmu = HALF * (mu(i, j) + mu(i - 1, j));
+    const T lambda = HALF * (mu(i, j) + mu(i - 1, j)) * cpprandtl;
+    visc_fluxes(mmu, lambda, uu, vv, ww, ux, uy, vx, vy, wx, wy, tx, ty, fv, gv);
+  }
+  // 4th-order viscous flux through j-face (rhs/flux_visqueux_o4_j.F)
+  void visc_j_o4(int i, int j, T fv[4], T gv[4]) {
+    const double volm1 = volf(i, j, 2);
+    const double nx_N = HALF * (nx(i + 1, j - 1, 1) + nx(i + 1, j, 1));
+    const double nx_S = -(HALF * (nx(i, j - 1, 1) + nx(i, j, 1)));
+    const double nx_O = HALF * (nx(i, j + 1, 2) + nx(i, j, 2));
+    const double nx_E = -(HALF * (nx(i, j - 1, 2) + nx(i, j, 2)));
+    const double ny_N = HALF * (ny(i + 1, j - 1, 1) + ny(i + 1, j, 1));
+    const double ny_S = -(HALF * (ny(i, j - 1, 1) + ny(i, j, 1)));
+    const double ny_O = HALF * (ny(i, j + 1, 2) + ny(i, j, 2));
+    const double ny_E = -(HALF * (ny(i, j - 1, 2) + ny(i, j, 2)));
+    auto grad = [&](FArr<T>& q, T& gx, T& gy) {
+      auto col = [&](int ii) { return q4(q(ii, j - 2), q(ii, j - 1), q(ii, j), q(ii, j + 1)); };
+      const T vN = ccross * (-col(i - 1) + 7.0 * col(i) + 7.0 * col(i + 1) - col(i + 2));
+      const T vS = ccross * (-col(i - 2) + 7.0 * col(i - 1) + 7.0 * col(i) - col(i + 1));
+      const T vE = TWENTYFOURTH * (-q(i, j) + 26.0 * q(i, j - 1) - q(i, j - 2));
+      const T vO = TWENTYFOURTH * (-q(i, j + 1) + 26.0 * q(i, j) - q(i, j - 1));
+      gx = (vN * nx_N + vS * nx_S + vO * nx_O + vE * nx_E) * volm1;
+      gy = (vN * ny_N + vS * ny_S + vO * ny_O + vE * ny_E) * volm1;
+    };
+    T ux, uy, vx, vy, wx, wy, tx, ty;
+    grad(velx, ux, uy); grad(vely, vx, vy); grad(velz, wx, wy); grad(tloc, tx, ty);
+    const T uu = 0.0625 * q4(velx(i, j - 2), velx(i, j - 1), velx(i, j), velx(i, j + 1));
+    const T vv = 0.0625 * q4(vely(i, j - 2), vely(i, j - 1), vely(i, j), vely(i, j + 1));
+    const T ww = 0.0625 * q4(velz(i, j - 2), velz(i, j - 1), velz(i, j), velz(i, j + 1));
+    const T mmu = 0.0625 * q4(mu(i, j - 2), mu(i, j - 1), mu(i, j), mu(i, j + 1));
+    const T lambda = mmu * cpprandtl;
+    visc_fluxes(mmu, lambda, uu, vv, ww, ux, uy, vx, vy, wx, wy, tx, ty, fv, gv);
+  }
+  // 2nd-order viscous flux through j-face (rhs/flux_visqueux_o2_j.F), row 2
+  void visc_j_o2(int i, int j, T fv[4], T gv[4]) {
+    const double volm1 = volf(i, j, 2);
+    const double nx_N = HALF * (nx(i + 1, j - 1, 1) + nx(i + 1, j, 1));
+    const double nx_S = -(HALF * (nx(i, j - 1, 1) + nx(i, j, 1)));
+    const double nx_O = HALF * (nx(i, j + 1, 2) + nx(i, j, 2));
+    const double nx_E = -(HALF * (nx(i, j - 1, 2) + nx(i, j, 2)));
+    const double ny_N = HALF * (ny(i + 1, j - 1, 1) + ny(i + 1, j, 1));
+    const double ny_S = -(HALF * (ny(i, j - 1, 1) + ny(i, j, 1)));
+    const double ny_O = HALF * (ny(i, j + 1, 2) + ny(i, j, 2));
+    const double ny_E = -(HALF * (ny(i, j - 1, 2) + ny(i, j, 2)));
+    auto grad = [&](FArr<T>& q, T& gx, T& gy) {
+      const T vN = FOURTH * (q(i, j) + q(i + 1, j) + q(i, j - 1) + q(i + 1, j - 1));
+      const T vS = FOURTH * (q(i, j) + q(i - 1, j) + q(i, j - 1) + q(i - 1, j - 1));
+      const T vO = q(i, j);
+      const T vE = q(i, j - 1);
+      gx = (vN * nx_N + vS * nx_S + vO * nx_O + vE * nx_E) * volm1;
+      gy = (vN * ny_N + vS * ny_S + vO * ny_O + vE * ny_E) * volm1;
+    };
+    T ux, uy, vx, vy, wx, wy, tx, ty;
+    grad(velx, ux, uy); grad(vely, vx, vy); grad(velz, wx, wy); grad(tloc, tx, ty);
+    const T uu = HALF * (velx(i, j) + velx(i, j - 1));
+    const T vv = HALF * (vely(i, j) + vely(i, j - 1));
+    const T ww = HALF * (velz(i, j) + velz(i, j - 1));
+    const T mmu = HALF * (mu(i, j) + mu(i, j - 1));
+    const T lambda = HALF * (mu(i, j) + mu(i, j - 1)) * cpprandtl;
+    visc_fluxes(mmu, lambda, uu, vv, ww, ux, uy, vx, vy, wx, wy, tx, ty, fv, gv);
+  }
+
+  // Spectral radius, sensor and dissipation through the face between cell L
+  // and cell R (rhs/spectralradius_i.F, ducrosfordnc_i.F, dissipation_ducros_i.F).
+  void dissipation(int iL, int jL, int iR, int jR, int iLL, int jLL, int iRR, int jRR, double fnx, double fny,
+                   const T pr[5], T diss[5]) {
+    const T rhomr = w(iR, jR, 1);
+    const T ur = w(iR, jR, 2) / rhomr;
+    const T vr = w(iR, jR, 3) / rhomr;
+    const T c2r = k.gam * k.rgaz * tloc(iR, jR);
+    const T rhoml = w(iL, jL, 1);
+    const T ul = w(iL, jL, 2) / rhoml;
+    const T vl = w(iL, jL, 3) / rhoml;
+    const T c2l = k.gam * k.rgaz * tloc(iL, jL);
+    const T r = sqrt_t(rhomr / rhoml);
+    const T rr = ONE / (ONE + r);
+    const T omrr = ONE - rr;
+    const T u = ul * rr + ur * omrr;
+    const T v = vl * rr + vr * omrr;
+    const T c2x = c2l * rr + c2r * omrr;
+    const double nx2 = fnx * fnx + fny * fny;
+    const T ab = fabs_t(fnx * u + fny * v);
+    const T sq = sqrt_t(c2x * nx2);
+    const T rspec = ab + sq;
+    if (k.k2 == 0.0) {
+      // eps2 = k2*coef = 0 and eps4 = max(0, k4) exactly for the finite coef
+      // of a physical state, so the sensor does not change the result.
+      const T eps4 = fmax_t(T(ZERO), T(k.k4));
+      for (int e = 1; e <= 5; ++e) diss[e - 1] = rspec * (eps4 * pr[e - 1]);
+      return;
+    }
+    // pressure sensor on the three-point stencils (L-1, L, R) and (LL, L, R)
+    const T ks1 = fabs_t(p(iL, jL) - TWO * p(iR, jR) + p(iRR, jRR)) / fabs_t(p(iL, jL) + TWO * p(iR, jR) + p(iRR, jRR));
+    const T ks2 = fabs_t(p(iLL, jLL) - TWO * p(iL, jL) + p(iR, jR)) / fabs_t(p(iLL, jLL) + TWO * p(iL, jL) + p(iR, jR));
+    T divu = (gradu(iR, jR, 1) + gradv(iR, jR, 2));
+    T divu2 = divu * divu;
+    T vort2 = (gradv(iR, jR, 1) - gradu(iR, jR, 2)) * (gradv(iR, jR, 1) - gradu(iR, jR, 2));
+    const T ducros1 = divu2 / (divu2 + vort2 + 1e-15);
+    const T dxm1 = HALF * (ONE - tanh_t(2.5 + 10.0 * vol(iR, jR) / (sqrt_t(c2r * nx2) + 1e-15) * divu));
+    divu = (gradu(iL, jL, 1) + gradv(iL, jL, 2));
+    divu2 = divu * divu;
+    vort2 = (gradv(iL, jL, 1) - gradu(iL, jL, 2)) * (gradv(iL, jL, 1) - gradu(iL, jL, 2));
+    const T ducros2 = divu2 / (divu2 + vort2 + 1e-15);
+    const T dxm2 = HALF * (ONE - tanh_t(2.5 + 10.0 * vol(iL, jL) / (sqrt_t(c2l * nx2) + 1e-15) * divu));
+    const T coef = fmax_t(ks1, ks2) * fmax_t(ducros1, ducros2) * fmax_t(dxm1, dxm2);
+    const T eps2 = k.k2 * coef;
+    const T eps4 = fmax_t(T(ZERO), k.k4 - eps2 * 12.0);
+    for (int e = 1; e <= 5; ++e) {
+      const T diff = HALF * (w(iR, jR, e) - w(iL, jL, e));
+      diss[e - 1] = rspec * (eps2 * diff + eps4 * pr[e - 1]);
+    }
+  }
+
+  // rhs/fluxnumassembly_i.F, fluxnumassembly_j.F
+  void assemble(int i, int j, int dir, const T fx[5], const T diss[5], const T fv[4], const T gv[4]) {
+    const double sc1 = nx(i, j, dir), sc2 = ny(i, j, dir);
+    const double sn = std::sqrt(sc1 * sc1 + sc2 * sc2);
+    const double invsn = ONE / sn;
+    const double nxloc = sc1 * invsn, nyloc = sc2 * invsn;
+    hn(i, j, 1, dir) = fx[0] - diss[0];
+    for (int e = 2; e <= 5; ++e)
+      hn(i, j, e, dir) = fx[e - 1] - diss[e - 1] - (fv[e - 2] * nxloc + gv[e - 2] * nyloc) * sn;
+  }
+
+  // i-face (i,j): between cells (i-1,j) and (i,j)
+  void iface(int i, int j, bool o2) {
+    T fx[5], pr[5], diss[5], fv[4], gv[4];
+    euler_i(i, j, fx);
+    pred_i(i, j, pr);
+    if (o2) visc_i_o2(i, j, fv, gv); else visc_i_o4(i, j, fv, gv);
+    dissipation(i - 1, j, i, j, i - 2, j, i + 1, j, nx(i, j, 1), ny(i, j, 1), pr, diss);
+    assemble(i, j, 1, fx, diss, fv, gv);
+  }
+  // j-face (i,j): between cells (i,j-1) and (i,j).  euler: 0 centred, 5 or 3
+  // off-centred near-wall formula.
+  void jface(int i, int j, int euler, bool o2) {
+    T fx[5], pr[5], diss[5], fv[4], gv[4];
+    if (euler == 0) euler_j(i, j, fx);
+    else {
+      const double c5[5] = {c5d0, c5d1, c5d2, c5d3, c5d4};
+      const double c3[5] = {c3d0, c3d1, c3d2, c3d3, c3d4};
+      euler_j_wall(i, j, euler == 5 ? c5 : c3, fx);
+    }
+    pred_j(i, j, pr);
+    if (o2) visc_j_o2(i, j, fv, gv); else visc_j_o4(i, j, fv, gv);
+    dissipation(i, j - 1, i, j, i, j - 2, i, j + 1, nx(i, j, 2), ny(i, j, 2), pr, diss);
+    assemble(i, j, 2, fx, diss, fv, gv);
+  }
+  // adiabatic no-slip wall face j=1 (rhs/fluxwall.F)
+  void wallface(int i, int j) {
+    const T pw = ct0 * p(i, j) + ct1 * p(i, j + 1);
+    const T fxrov2 = pw;
+    const T mmu = mu(i, j);
+    const double nx2 = nx(i, j, 2), ny2 = ny(i, j, 2), vf = volf(i, j, 2);
+    const T ux = TWO * velx(i, j) * nx2 * vf;
+    const T vx = TWO * vely(i, j) * nx2 * vf;
+    const T wx = TWO * velz(i, j) * nx2 * vf;
+    const T uy = TWO * velx(i, j) * ny2 * vf;
+    const T vy = TWO * vely(i, j) * ny2 * vf;
+    const T wy = TWO * velz(i, j) * ny2 * vf;
+    const T fvrou2 = TWOTHIRD * mmu * (TWO * ux - vy);
+    const T fvrov2 = mmu * (uy + vx);
+    const T fvrow2 = mmu * (wx);
+    const T gvrou2 = mmu * (uy + vx);
+    const T gvrov2 = TWOTHIRD * mmu * (-ux + TWO * vy);
+    const T gvrow2 = mmu * (wy);
+    hn(i, j, 1, 2) = T(ZERO);
+    hn(i, j, 2, 2) = fxrov2 * nx2 - (fvrou2 * nx2 + gvrou2 * ny2);
+    hn(i, j, 3, 2) = fxrov2 * ny2 - (fvrov2 * nx2 + gvrov2 * ny2);
+    hn(i, j, 4, 2) = -(fvrow2 * nx2 + gvrow2 * ny2);
+    hn(i, j, 5, 2) = T(ZERO);
+  }
+
+  void run(T* residu_) {
+    primitives();
+    gradients();
+#pragma omp parallel for schedule(static)
+    for (int j = 4; j <= jm + 1; ++j)
+      for (int i = 1; i <= im + 1; ++i) { iface(i, j, false); jface(i, j, 0, false); }
+    for (int i = 1; i <= im + 1; ++i) { iface(i, 3, false); jface(i, 3, 5, false); }
+    for (int i = 1; i <= im + 1; ++i) { iface(i, 2, true); jface(i, 2, 3, true); }
+    for (int i = 1; i <= im + 1; ++i) { iface(i, 1, true); wallface(i, 1); }
+    FArr<T> res(residu_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= jm; ++j)
+      for (int i = 1; i <= im; ++i)
+        for (int e = 1; e <= 5; ++e)
+          res(i, j, e) = -(hn(i + 1, j, e, 1) - hn(i, j, e, 1)) - (hn(i, j + 1, e, 2) - hn(i, j, e, 2));
+  }
+};
+
+template <class T>
+void flux_num_dnc5_2d(T* residu, const T* w, const double* nx, const double* ny, const double* vol,
+                      const double* volf, int gh, const Consts& c, int im, int jm) {
+  Dnc5<T> s(w, nx, ny, vol, volf, gh, c, im, jm);
+  s.run(residu);
+}
+
+// ===========================================================================
+// Boundary conditions (srcfv/borders/*.F90 with init_2d.F)
+// interf is the Fortran (2,2) array in column-major order:
+//   interf = {imin, imax, jmin, jmax}
+// loc is one of "Ilo", "Ihi", "Jlo", "Jhi".
+// ===========================================================================
+struct Side {
+  int kdir = 0, i0 = 0, j0 = 0, high = 0, lmin = 1, lmax = 0, imin, jmin, imax, jmax;
+  bool ok = true;
+  Side(const char* loc, const int* interf) {
+    imin = interf[0]; imax = interf[1]; jmin = interf[2]; jmax = interf[3];
+    if (!std::strncmp(loc, "Ilo", 3)) { kdir = 1; i0 = 1; lmax = jmax - jmin + 1; }
+    else if (!std::strncmp(loc, "Ihi", 3)) { kdir = 1; i0 = -1; lmax = jmax - jmin + 1; high = 1; }
+    else if (!std::strncmp(loc, "Jlo", 3)) { kdir = 2; j0 = 1; lmax = imax - imin + 1; }
+    else if (!std::strncmp(loc, "Jhi", 3)) { kdir = 2; j0 = -1; lmax = imax - imin + 1; high = 1; }
+    else ok = false;
+  }
+  int li(int l) const { return imin + (l - lmin) * j0 * j0; }
+  int lj(int l) const { return jmin + (l - lmin) * i0 * i0; }
+};
+
+// bc_wall_viscous_adia_2d (borders/bc_wall_viscous.F90:2-99)
+template <class T>
+void bc_wall_viscous_adia_2d(T* w_, const char* loc, double gam, const int* interf, int gh, int im, int jm) {
+  FArr<T> w(w_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  Side s(loc, interf);
+  const double gam1 = gam - 1.0, gami = 1.0 / gam, ct0 = 1.125, ct1 = -0.125, THIRD = 1.0 / 3.0, FOUR = 4.0,
+               HALF = 0.5, ONE = 1.0;
+  const int i0 = s.i0, j0 = s.j0;
+  for (int l = s.lmin; l <= s.lmax; ++l) {
+    const int i = s.li(l), j = s.lj(l);
+    const T roe = w(i, j, 1);
+    T roem1 = ONE / roe;
+    const T ue = w(i, j, 2) * roem1, ve = w(i, j, 3) * roem1, we = w(i, j, 4) * roem1;
+    const T ve2 = ue * ue + ve * ve;
+    const T pe = gam1 * (w(i, j, 5) - HALF * roe * ve2);
+    const T roe1 = w(i + i0, j + j0, 1);
+    const T roe1m1 = ONE / roe1;
+    const T ue1 = w(i + i0, j + j0, 2) * roe1m1, ve1 = w(i + i0, j + j0, 3) * roe1m1;
+    const T ve21 = ue1 * ue1 + ve1 * ve1;
+    const T pe1 = gam1 * (w(i + i0, j + j0, 5) - HALF * roe1 * ve21);
+    const T pw = ct0 * pe + ct1 * pe1;
+    const T pi = THIRD * (FOUR * pw - pe);
+    T roi = pow_t(pi / pe * pow_t(roe, gam), gami);
+    T ui = -ue, vi = -ve, wi = -we;
+    T roiei = pi / gam1 + HALF * roi * (ui * ui + vi * vi);
+    for (int de = 1; de <= gh; ++de) {
+      w(i - de * i0, j - de * j0, 1) = roi;
+      w(i - de * i0, j - de * j0, 2) = roi * ui;
+      w(i - de * i0, j - de * j0, 3) = roi * vi;
+      w(i - de * i0, j - de * j0, 4) = roi * wi;
+      w(i - de * i0, j - de * j0, 5) = roiei;
+      roi = w(i + de * i0, j + de * j0, 1);
+      roem1 = ONE / roi;
+      const T a = w(i + de * i0, j + de * j0, 2) * roem1;
+      const T b = w(i + de * i0, j + de * j0, 3) * roem1;
+      const T c = w(i + de * i0, j + de * j0, 4) * roem1;
+      roiei = w(i + de * i0, j + de * j0, 5);
+      ui = -a; vi = -b; wi = -c;
+    }
+  }
+}
+
+// bc_no_reflexion_2d (borders/bc_no_reflexion.F90:8-152); wbd is (lm,5)
+template <class T>
+void bc_no_reflexion_2d(T* w_, const double* wbd_, int lm, const char* loc, const int* interf, const double* nx_,
+                        const double* ny_, double gam, int gh, int im, int jm) {
+  FArr<T> w(w_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  FArr<const double> nx(nx_, im + 2 * gh + 1, jm + 2 * gh + 1, 1 - gh), ny(ny_, im + 2 * gh + 1, jm + 2 * gh + 1, 1 - gh);
+  auto wbd = [&](int l, int v) { return wbd_[(size_t)(l - 1) + (size_t)(v - 1) * lm]; };
+  Side s(loc, interf);
+  const double ONE = 1.0, HALF = 0.5, TWO = 2.0, gam1 = gam - ONE;
+  const double sens = (double)(s.i0 + s.j0);
+  const int i1 = s.i0 * s.i0, j1 = s.j0 * s.j0, i0 = s.i0, j0 = s.j0;
+  for (int l = s.lmin; l <= s.lmax; ++l) {
+    const int i = s.imin + (l - s.lmin) * j1, j = s.jmin + (l - s.lmin) * i1;
+    const double nxloc = nx(i + s.high * i1, j + s.high * j1, s.kdir);
+    const double nyloc = ny(i + s.high * i1, j + s.high * j1, s.kdir);
+    const double nsum = std::sqrt(nxloc * nxloc + nyloc * nyloc);
+    const double nsumi = ONE / nsum;
+    const double nxnorm = nxloc * nsumi * sens, nynorm = nyloc * nsumi * sens;
+    const T ro0 = w(i, j, 1);
+    const T ro0m1 = ONE / ro0;
+    const T uu = w(i, j, 2) * ro0m1, vv = w(i, j, 3) * ro0m1, ww = w(i, j, 4) * ro0m1;
+    const T roe1 = w(i, j, 5) - HALF * ro0 * (uu * uu + vv * vv + ww * ww);
+    const T p0 = gam1 * (roe1);
+    const T roc0 = ro0 * sqrt_t(gam * p0 * ro0m1);
+    const T roc0m1 = ONE / roc0;
+    const T rovn0 = (w(i, j, 2) * nxnorm + w(i, j, 3) * nynorm);
+    const double epsm = HALF + fsign(HALF, roc0 - rovn0);
+    const double eps0 = HALF + fsign(HALF, -rovn0);
+    const double epsp = HALF + fsign(HALF, -roc0 - rovn0);
+    const double rod = wbd(l, 1);
+    const double rodm1 = ONE / rod;
+    const double ud = wbd(l, 2) * rodm1, vd = wbd(l, 3) * rodm1, wdi = wbd(l, 4) * rodm1;
+    const double pd = gam1 * (wbd(l, 5) - rod * HALF * (ud * ud + vd * vd + wdi * wdi));
+    const double vnd = (ud * nxnorm + vd * nynorm);
+    const double utd = ud - vnd * nxnorm, vtd = vd - vnd * nynorm;
+    const T ros = w(i, j, 1);
+    const T rosm1 = ONE / ros;
+    const T us = w(i, j, 2) * rosm1, vs = w(i, j, 3) * rosm1, ws = w(i, j, 4) * rosm1;
+    const T ps = gam1 * (w(i, j, 5) - ros * HALF * (us * us + vs * vs + ws * ws));
+    const T vns = (us * nxnorm + vs * nynorm);
+    const T uts = us - vns * nxnorm, vts = vs - vns * nynorm;
+    const T ut = eps0 * uts + (ONE - eps0) * utd;
+    const T vt = eps0 * vts + (ONE - eps0) * vtd;
+    const T wt = eps0 * ws + (ONE - eps0) * wdi;
+    const T am = epsm * (ps - roc0 * vns) + (ONE - epsm) * (pd - roc0 * vnd);
+    const T ap = epsp * (ps + roc0 * vns) + (ONE - epsp) * (pd + roc0 * vnd);
+    const T vn = (ap - am) * HALF * roc0m1;
+    const T pp = (ap + am) * HALF;
+    const T bs = (pp - ps) * ro0 * ro0 * roc0m1 * roc0m1 + ros;
+    const T b0 = (pp - pd) * ro0 * ro0 * roc0m1 * roc0m1 + rod;
+    T ro = eps0 * bs + (ONE - eps0) * b0;
+    const T rom1 = ONE / ro;
+    const T roe = pp / gam1;
+    T rou = ro * (ut + vn * nxnorm);
+    T rov = ro * (vt + vn * nynorm);
+    T row = ro * wt;
+    T roe2 = roe + HALF * rom1 * (rou * rou + rov * rov + row * row);
+    for (int de = 1; de <= gh; ++de) {
+      const int da = de - 1;
+      w(i - de * i0, j - de * j0, 1) = ro;
+      w(i - de * i0, j - de * j0, 2) = rou;
+      w(i - de * i0, j - de * j0, 3) = rov;
+      w(i - de * i0, j - de * j0, 4) = row;
+      w(i - de * i0, j - de * j0, 5) = roe2;
+      ro = TWO * ro - w(i - da * i0, j - da * j0, 1);
+      rou = TWO * rou - w(i - da * i0, j - da * j0, 2);
+      rov = TWO * rov - w(i - da * i0, j - da * j0, 3);
+      row = TWO * row - w(i - da * i0, j - da * j0, 4);
+      roe2 = TWO * roe2 - w(i - da * i0, j - da * j0, 5);
+    }
+  }
+}
+
+// bc_supandsubinlet_2d (borders/bc_supandsubinlet.F90:2-171); field is (lm,gh,5)
+template <class T>
+void bc_supandsubinlet_2d(T* w_, const char* loc, const int* interf, const double* field_, int lm,
+                          const double* nx_, const double* ny_, double gam, int im, int jm, int gh) {
+  FArr<T> w(w_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  FArr<const double> nx(nx_, im + 2 * gh + 1, jm + 2 * gh + 1, 1 - gh), ny(ny_, im + 2 * gh + 1, jm + 2 * gh + 1, 1 - gh);
+  auto field = [&](int a, int b, int v) { return field_[(size_t)(a - 1) + (size_t)(b - 1) * lm + (size_t)(v - 1) * lm * gh]; };
+  Side s(loc, interf);
+  const double HALF = 0.5, ONE = 1.0, gam1 = gam - ONE;
+  const int i0 = s.i0, j0 = s.j0;
+  for (int l = s.lmin; l <= s.lmax; ++l) {
+    const int i = s.li(l), j = s.lj(l);
+    const T wr1 = w(i, j, 1);
+    T rom1 = ONE / wr1;
+    const T wr2 = w(i, j, 2) * rom1, wr3 = w(i, j, 3) * rom1, wr4 = w(i, j, 4) * rom1;
+    const T pr = gam1 * (w(i, j, 5) - wr1 * (wr2 * wr2 + wr3 * wr3 + wr4 * wr4));
+    T hr = (w(i, j, 5) + pr) * rom1;
+    const double wl1 = field(j, i, 1);
+    const double rosm1_ = ONE / wl1;
+    const double wl2 = field(j, i, 2) * rosm1_, wl3 = field(j, i, 3) * rosm1_, wl4 = field(j, i, 4) * rosm1_;
+    const double pl = gam1 * (field(j, i, 5) - wl1 * (wl2 * wl2 + wl3 * wl3 + wl4 * wl4));
+    T hl = T((field(j, i, 5) + pl) * rosm1_);
+    T r = sqrt_t(wr1 / wl1);
+    T rr = sqrt_t(wr1 * wl1);
+    T oneonrplusone = ONE / (r + ONE);
+    T uu = (wr2 * r + wl2) * oneonrplusone;
+    T vv = (wr3 * r + wl3) * oneonrplusone;
+    T ww = (wr4 * r + wl4) * oneonrplusone;
+    T hh = (hr * r + hl) * oneonrplusone;
+    const T velo2 = uu * uu + vv * vv + ww;
+    T ee = HALF * velo2;
+    T sound2 = gam1 * (hh - ee);
+    const T mach = sqrt_t(velo2 / sound2);
+    const bool sub = (mach < ONE);
+    double nxnorm = 0.0, nynorm = 0.0, epsm = 0.0, eps0 = 0.0, epsp = 0.0;
+    if (sub) {
+      const double nxloc = nx(i, j, s.kdir), nyloc = ny(i, j, s.kdir);
+      const double nsum = ONE / std::sqrt(nxloc * nxloc + nyloc * nyloc);
+      nxnorm = nxloc * nsum; nynorm = nyloc * nsum;
+      const T roc0 = rr * sqrt_t(sound2);
+      const T rovn0 = rr * (uu * nxnorm + vv * nynorm);
+      epsm = HALF + fsign(HALF, roc0 - rovn0);
+      eps0 = HALF + fsign(HALF, -rovn0);
+      epsp = HALF + fsign(HALF, -roc0 - rovn0);
+    }
+    for (int de = 1; de <= gh; ++de) {
+      for (int v = 1; v <= 5; ++v) w(i - de * i0, j - de * j0, v) = T(field(l, de, v));
+      const int da = de - 1;
+      if (sub) {
+        const T rod = w(i - de * i0, j - de * j0, 1);
+        rom1 = ONE / rod;
+        const T ud = w(i - de * i0, j - de * j0, 2) * rom1;
+        const T vd = w(i - de * i0, j - de * j0, 3) * rom1;
+        const T wd = w(i - de * i0, j - de * j0, 4) * rom1;
+        const T pd = gam1 * (w(i - de * i0, j - de * j0, 5) - rod * HALF * (ud * ud + vd * vd + wd * wd));
+        const T vnd = (ud * nxnorm + vd * nynorm);
+        const T utd = ud - vnd * nxnorm, vtd = vd - vnd * nynorm;
+        hl = (w(i - de * i0, j - de * j0, 5) + pd) * rom1;
+        const T ros = w(i - da * i0, j - da * j0, 1);
+        const T rosm1 = ONE / ros;
+        const T us = w(i - da * i0, j - da * j0, 2) * rosm1;
+        const T vs = w(i - da * i0, j - da * j0, 3) * rosm1;
+        const T ws = w(i - da * i0, j - da * j0, 4) * rosm1;
+        const T ps = gam1 * (w(i - da * i0, j - da * j0, 5) - ros * HALF * (us * us + vs * vs + ws * ws));
+        const T vns = (us * nxnorm + vs * nynorm);
+        const T uts = us - vns * nxnorm, vts = vs - vns * nynorm;
+        hr = (w(i - da * i0, j - da * j0, 5) + ps) * rosm1;
+        r = sqrt_t(ros * rom1);
+        rr = sqrt_t(ros * rod);
+        oneonrplusone = ONE / (r + ONE);
+        uu = (us * r + ud) * oneonrplusone;
+        vv = (vs * r + vd) * oneonrplusone;
+        ww = (ws * r + wd) * oneonrplusone;
+        ee = HALF * (uu * uu + vv * vv + ww * ww);
+        hh = (hr * r + hl) * oneonrplusone;
+        sound2 = gam1 * (hh - ee);
+        const T roc0 = rr * sqrt_t(sound2);
+        const T roc0m1 = ONE / roc0;
+        const T ut = eps0 * uts + (ONE - eps0) * utd;
+        const T vt = eps0 * vts + (ONE - eps0) * vtd;
+        const T am = epsm * (ps - roc0 * vns) + (ONE - epsm) * (pd - roc0 * vnd);
+        const T ap = epsp * (ps + roc0 * vns) + (ONE - epsp) * (pd + roc0 * vnd);
+        const T vn = (ap - am) * HALF * roc0m1;
+        const T pp = (ap + am) * HALF;
+        const T bs = (pp - ps) * rr * rr * roc0m1 * roc0m1 + ros;
+        const T b0 = (pp - pd) * rr * rr * roc0m1 * roc0m1 + rod;
+        const T ro = eps0 * bs + (ONE - eps0) * b0;
+        const T roe = pp / gam1;
+        const T rou = ro * (ut + vn * nxnorm);
+        const T rov = ro * (vt + vn * nynorm);
+        const T row = T(field(j, de, 4));
+        w(i - de * i0, j - de * j0, 1) = ro;
+        w(i - de * i0, j - de * j0, 2) = rou;
+        w(i - de * i0, j - de * j0, 3) = rov;
+        w(i - de * i0, j - de * j0, 4) = row;
+        w(i - de * i0, j - de * j0, 5) = roe + HALF * (rou * rou + rov * rov + row * row) / ro;
+      }
+    }
+  }
+}
+
+// bc_extrapolate_o2_2d (borders/bc_extrapolate.F90:39-71)
+template <class T>
+void bc_extrapolate_o2_2d(T* w_, const char* loc, const int* interf, int im, int jm, int gh, int em) {
+  FArr<T> w(w_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  Side s(loc, interf);
+  const int i0 = s.i0, j0 = s.j0;
+  for (int l = s.lmin; l <= s.lmax; ++l) {
+    const int i = s.li(l), j = s.lj(l);
+    for (int de = 1; de <= gh; ++de) {
+      const int e1 = de - 1, e2 = de - 2;
+      for (int v = 1; v <= em; ++v)
+        w(i - i0 * de, j - j0 * de, v) = 2.0 * w(i - i0 * e1, j - j0 * e1, v) - w(i - i0 * e2, j - j0 * e2, v);
+    }
+  }
+}
+
+// jn_match_2d (borders/jn_match.F90:3-66): copy of a block of cells.  Arrays
+// are (1-gh1:im+gh2, 1-gh3:jm+gh4, em); prr/prd are Fortran (2,2) column-major
+// {imin, imax, jmin, jmax}; tr is (2).
+template <class T>
+void jn_match_2d(T* wr_, const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, int imr, int jmr, const T* wd_,
+                 const int* prd, int gh1d, int gh2d, int gh3d, int gh4d, int imd, int jmd, const int* tr, int em) {
+  const int nir = imr + gh1r + gh2r, njr = jmr + gh3r + gh4r;
+  const int nid = imd + gh1d + gh2d, njd = jmd + gh3d + gh4d;
+  auto WR = [&](int i, int j, int v) -> T& { return wr_[(size_t)(i - (1 - gh1r)) + (size_t)(j - (1 - gh3r)) * nir + (size_t)(v - 1) * nir * njr]; };
+  auto WD = [&](int i, int j, int v) -> const T& { return wd_[(size_t)(i - (1 - gh1d)) + (size_t)(j - (1 - gh3d)) * nid + (size_t)(v - 1) * nid * njd]; };
+  auto P = [](const int* a, int r, int c) { return a[(r - 1) + (c - 1) * 2]; };
+  const int istep = tr[0] >= 0 ? 1 : -1, jstep = tr[1] >= 0 ? 1 : -1;
+  const int idir = std::abs(tr[0]), jdir = std::abs(tr[1]);
+  int i1, i2, j1, j2;
+  if (istep == 1) { i1 = 1; i2 = P(prd, 2, idir) - P(prd, 1, idir) + 1; } else { i1 = P(prd, 2, idir) - P(prd, 1, idir) + 1; i2 = 1; }
+  if (jstep == 1) { j1 = 1; j2 = P(prd, 2, jdir) - P(prd, 1, jdir) + 1; } else { j1 = P(prd, 2, jdir) - P(prd, 1, jdir) + 1; j2 = 1; }
+  int idd = 1, jdd = 1;
+  for (int j = j1; jstep > 0 ? j <= j2 : j >= j2; j += jstep) {
+    for (int i = i1; istep > 0 ? i <= i2 : i >= i2; i += istep) {
+      const int ir = P(prr, 1, 1) + idd - 1, jr = P(prr, 1, 2) + jdd - 1;
+      const int id = P(prd, 1, idir) + i - 1, jd = P(prd, 1, jdir) + j - 1;
+      for (int v = 1; v <= em; ++v) WR(ir, jr, v) = WD(id, jd, v);
+      ++idd;
+    }
+    idd = 1; ++jdd;
+  }
+}
+
+// ===========================================================================
+// Geometry (srcfv/prepro/computegeom.f90), double only
+// ===========================================================================
+inline void computegeom_2d(double* x0_, double* y0_, double* nx_, double* ny_, double* xc_, double* yc_,
+                           double* vol_, double* volf_, int im, int jm, int gh) {
+  const int lo = 1 - gh, nni = im + 2 * gh + 1, nnj = jm + 2 * gh + 1, ni = im + 2 * gh, nj = jm + 2 * gh;
+  FArr<double> x0(x0_, nni, nnj, lo), y0(y0_, nni, nnj, lo), nx(nx_, nni, nnj, lo), ny(ny_, nni, nnj, lo);
+  FArr<double> xc(xc_, ni, nj, lo), yc(yc_, ni, nj, lo), vol(vol_, ni, nj, lo), volf(volf_, ni, nj, lo);
+  const double TWO = 2.0, HALF = 0.5, FOURTH = 0.25;
+  for (int g = 1; g <= gh; ++g)
+    for (int dummy = 1; dummy <= 2; ++dummy) {
+      for (int j = lo; j <= jm + gh + 1; ++j) x0(1 - g, j) = TWO * x0(2 - g, j) - x0(3 - g, j);
+      for (int j = lo; j <= jm + gh + 1; ++j) x0(im + 1 + g, j) = TWO * x0(im + g, j) - x0(im - 1 + g, j);
+      for (int i = lo; i <= im + gh + 1; ++i) x0(i, 1 - g) = TWO * x0(i, 2 - g) - x0(i, 3 - g);
+      for (int i = lo; i <= im + gh + 1; ++i) x0(i, jm + 1 + g) = TWO * x0(i, jm + g) - x0(i, jm - 1 + g);
+      for (int i = lo; i <= im + gh + 1; ++i) y0(i, 1 - g) = TWO * y0(i, 2 - g) - y0(i, 3 - g);
+      for (int i = lo; i <= im + gh + 1; ++i) y0(i, jm + 1 + g) = TWO * y0(i, jm + g) - y0(i, jm - 1 + g);
+      for (int j = lo; j <= jm + gh + 1; ++j) y0(1 - g, j) = TWO * y0(2 - g, j) - y0(3 - g, j);
+      for (int j = lo; j <= jm + gh + 1; ++j) y0(im + 1 + g, j) = TWO * y0(im + g, j) - y0(im - 1 + g, j);
+    }
+  for (int j = 1; j <= jm + 1; ++j)
+    for (int i = 1; i <= im + 1; ++i) {
+      xc(i, j) = FOURTH * (x0(i, j) + x0(i + 1, j) + x0(i, j + 1) + x0(i + 1, j + 1));
+      yc(i, j) = FOURTH * (y0(i, j) + y0(i + 1, j) + y0(i, j + 1) + y0(i + 1, j + 1));
+      const double xa = x0(i, j), ya = y0(i, j), xb = x0(i + 1, j), yb = y0(i + 1, j);
+      const double xc1 = x0(i, j + 1), yc1 = y0(i, j + 1), xd = x0(i + 1, j + 1), yd = y0(i + 1, j + 1);
+      const double abx = xb - xa, aby = yb - ya, acx = xc1 - xa, acy = yc1 - ya;
+      const double q1 = HALF * std::fabs(abx * acy - acx * aby);
+      const double dcx = xc1 - xd, dcy = yc1 - yd, dbx = xb - xd, dby = yb - yd;
+      const double q2 = HALF * std::fabs(dcx * dby - dbx * dcy);
+      vol(i, j) = q1 + q2;
+      nx(i, j, 1) = y0(i, j + 1) - y0(i, j);
+      ny(i, j, 1) = x0(i, j) - x0(i, j + 1);
+      nx(i, j, 2) = y0(i, j) - y0(i + 1, j);
+      ny(i, j, 2) = x0(i + 1, j) - x0(i, j);
+    }
+  for (int g = 1; g <= gh; ++g)
+    for (int dummy = 1; dummy <= 2; ++dummy) {
+      for (int j = lo; j <= jm + gh; ++j) xc(1 - g, j) = TWO * xc(2 - g, j) - xc(3 - g, j);
+      for (int j = lo; j <= jm + gh; ++j) xc(im + g, j) = TWO * xc(im - 1 + g, j) - xc(im - 2 + g, j);
+      for (int i = lo; i <= im + gh; ++i) xc(i, 1 - g) = TWO * xc(i, 2 - g) - xc(i, 3 - g);
+      for (int i = lo; i <= im + gh; ++i) xc(i, jm + g) = TWO * xc(i, jm - 1 + g) - xc(i, jm - 2 + g);
+      for (int j = lo; j <= jm + gh; ++j) yc(1 - g, j) = TWO * yc(2 - g, j) - yc(3 - g, j);
+      for (int j = lo; j <= jm + gh; ++j) yc(im + g, j) = TWO * yc(im - 1 + g, j) - yc(im - 2 + g, j);
+      for (int i = lo; i <= im + gh; ++i) yc(i, 1 - g) = TWO * yc(i, 2 - g) - yc(i, 3 - g);
+      for (int i = lo; i <= im + gh; ++i) yc(i, jm + g) = TWO * yc(i, jm - 1 + g) - yc(i, jm - 2 + g);
+      for (int j = 1; j <= jm; ++j) vol(1 - g, j) = TWO * vol(2 - g, j) - vol(3 - g, j);
+      for (int j = 1; j <= jm; ++j) vol(im + g, j) = TWO * vol(im - 1 + g, j) - vol(im - 2 + g, j);
+      for (int i = lo; i <= im + gh; ++i) vol(i, 1 - g) = TWO * vol(i, 2 - g) - vol(i, 3 - g);
+      for (int i = lo; i <= im + gh; ++i) vol(i, jm + g) = TWO * vol(i, jm - 1 + g) - vol(i, jm - 2 + g);
+      for (int c = 1; c <= 2; ++c)
+        for (int j = lo; j <= jm + gh + 1; ++j) nx(1 - g, j, c) = TWO * nx(2 - g, j, c) - nx(3 - g, j, c);
+      for (int c = 1; c <= 2; ++c)
+        for (int j = lo; j <= jm + gh + 1; ++j) ny(1 - g, j, c) = TWO * ny(2 - g, j, c) - ny(3 - g, j, c);
+      for (int c = 1; c <= 2; ++c)
+        for (int j = lo; j <= jm + gh + 1; ++j) nx(im + 1 + g, j, c) = TWO * nx(im + g, j, c) - nx(im - 1 + g, j, c);
+      for (int c = 1; c <= 2; ++c)
+        for (int j = lo; j <= jm + gh + 1; ++j) ny(im + 1 + g, j, c) = TWO * ny(im + g, j, c) - ny(im - 1 + g, j, c);
+      for (int c = 1; c <= 2; ++c)
+        for (int i = lo; i <= im + gh + 1; ++i) nx(i, 1 - g, c) = TWO * nx(i, 2 - g, c) - nx(i, 3 - g, c);
+      for (int c = 1; c <= 2; ++c)
+        for (int i = lo; i <= im + gh + 1; ++i) ny(i, 1 - g, c) = TWO * ny(i, 2 - g, c) - ny(i, 3 - g, c);
+      for (int c = 1; c <= 2; ++c)
+        for (int i = lo; i <= im + gh + 1; ++i) nx(i, 1 + jm + g, c) = TWO * nx(i, jm + g, c) - nx(i, g + jm - 1, c);
+      for (int c = 1; c <= 2; ++c)
+        for (int i = lo; i <= im + gh + 1; ++i) ny(i, 1 + jm + g, c) = TWO * ny(i, jm + g, c) - ny(i, g + jm - 1, c);
+    }
+  for (int j = 1; j <= jm + 1; ++j)
+    for (int i = 1; i <= im + 1; ++i) {
+      volf(i, j, 1) = TWO / (vol(i, j) + vol(i - 1, j));
+      volf(i, j, 2) = TWO / (vol(i, j) + vol(i, j - 1));
+    }
+}
+
+// ===========================================================================
+// Norms (srcfv/norm.F90)
+// ===========================================================================
+inline void compute_norml2(double* norm, double* nmoy, const double* rhs_, int im, int jm, int gh) {
+  FArr<const double> rhs(rhs_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  double s[5] = {0, 0, 0, 0, 0};
+  for (int j = 1; j <= jm; ++j)
+    for (int i = 1; i <= im; ++i)
+      for (int e = 1; e <= 5; ++e) s[e - 1] = s[e - 1] + rhs(i, j, e) * rhs(i, j, e);
+  for (int e = 0; e < 5; ++e) { norm[e] = std::sqrt(s[e]); nmoy[e] = norm[e] / (double)(im * jm); }
+}
+inline void compute_norml2inf(double* norm, double* ninf, const double* rhs_, int im, int jm, int gh) {
+  FArr<const double> rhs(rhs_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  double s[5] = {0, 0, 0, 0, 0}, t[5] = {0, 0, 0, 0, 0};
+  for (int j = 1; j <= jm; ++j)
+    for (int i = 1; i <= im; ++i)
+      for (int e = 1; e <= 5; ++e) {
+        s[e - 1] = s[e - 1] + rhs(i, j, e) * rhs(i, j, e);
+        t[e - 1] = t[e - 1] + std::pow(rhs(i, j, e), 10.0);
+      }
+  for (int e = 0; e < 5; ++e) { norm[e] = std::sqrt(s[e]); ninf[e] = std::pow(t[e], 0.1); }
+}
+inline void compute_maxnorm(double* norm, int* imax, int* jmax, const double* rhs_, int im, int jm, int gh) {
+  FArr<const double> rhs(rhs_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  for (int e = 0; e < 5; ++e) norm[e] = 0.0;
+  for (int j = 1; j <= jm; ++j)
+    for (int i = 1; i <= im; ++i)
+      for (int e = 0; e < 5; ++e) {
+        norm[e] = std::fabs(norm[e]);
+        if (std::fabs(rhs(i, j, e + 1)) > norm[e]) { norm[e] = rhs(i, j, e + 1); imax[e] = i; jmax[e] = j; }
+      }
+}
+
+// ===========================================================================
+// Colored Jacobian assembly indexing (misc/ComputeJacobian.f90)
+// ===========================================================================
+// testvector (ComputeJacobian.f90:357-374)
+inline void testvector(double* wd_, int m, int l, int k, int gh, int im, int jm) {
+  FArr<double> wd(wd_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  const int step = 1 + 2 * gh;
+  std::memset(wd_, 0, sizeof(double) * (size_t)(im + 2 * gh) * (jm + 2 * gh) * 5);
+  for (int j = k + 1; j <= jm; j += step)
+    for (int i = l + 1; i <= im; i += step) wd(i, j, m + 1) = 1.0;
+}
+// testvector_partial (ComputeJacobian.f90:1075-1092)
+inline void testvector_partial(double* wd_, int m, int l, int k, int gh, int im, int jm, int istart, int iend,
+                               int jstart, int jend) {
+  FArr<double> wd(wd_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  const int step = 1 + 2 * gh;
+  std::memset(wd_, 0, sizeof(double) * (size_t)(im + 2 * gh) * (jm + 2 * gh) * 5);
+  for (int j = jstart + k + 1; j <= jend + 1; j += step)
+    for (int i = istart + l + 1; i <= iend + 1; i += step) wd(i, j, m + 1) = 1.0;
+}
+
+// Variants of the COO fill.  mode selects the reference routine:
+enum JacMode {
+  JAC_PLAIN = 0,          // computejacobianfromjv            (:292-355)
+  JAC_RELAXED = 1,        // computejacobianfromjv_relaxed    (:503-570)
+  JAC_RELAXED_WITHJN = 2, // computejacobianfromjv_relaxed_withjn (:847-926)
+  JAC_WITHJN = 3,         // computejacobianfromjv_withjn     (:929-999)
+  JAC_DZ = 4,             // computejacobianfromdz            (:708-779)
+};
+inline void computejacobian(int mode, double* jac, int* ia, int* ja, const double* resd_, int m, int l, int k,
+                            int gh, int im, int jm, const double* coefdiag) {
+  FArr<const double> resd(resd_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  const int step = 1 + 2 * gh;
+  const bool jn = (mode == JAC_RELAXED_WITHJN || mode == JAC_WITHJN);
+  const bool relaxed = (mode == JAC_RELAXED || mode == JAC_RELAXED_WITHJN);
+  const int bad = jn ? 5 * im * jm - 2 : 5 * im * jm - 1;
+  for (int e = 1; e <= 5; ++e)
+    for (int j = 1; j <= jm; ++j)
+      for (int i = 1; i <= im; ++i) {
+        const long long cur = (long long)(i - 1) + (long long)(j - 1) * im + (long long)(e - 1) * im * jm +
+                              (long long)k * im * jm * 5 + (long long)l * im * jm * 5 * step +
+                              (long long)m * im * jm * 5 * step * step;
+        ia[cur] = e - 1 + (j - 1) * 5 + (i - 1) * jm * 5;
+        int valj, vali;
+        if (mode == JAC_DZ) {
+          if (k <= gh) valj = (j <= k + 1 + gh) ? k : (j - (k + 1) + gh) / step * step + k;
+          else valj = (j <= k - gh) ? jm + 1 : (j - (k + 1) + gh) / step * step + k;
+        } else {
+          valj = (j <= k + 1 + gh) ? k : (j - gh - (k + 1) + 2 * gh) / step * step + k;
+        }
+        if (valj >= jm) { ia[cur] = bad; ja[cur] = 0; jac[cur] = 0.0; continue; }
+        if (l <= gh) vali = (i <= l + 1 + gh) ? l : (i - (l + 1) + gh) / step * step + l;
+        else {
+          if (i <= l - gh) vali = jn ? im - 1 - 2 * gh + l : im + 1;
+          else vali = (i - (l + 1) + gh) / step * step + l;
+        }
+        if (vali >= im) {
+          if (jn && vali - im <= gh - 1) vali = l;
+          else { ia[cur] = bad; ja[cur] = 0; jac[cur] = 0.0; continue; }
+        }
+        ja[cur] = m + valj * 5 + vali * jm * 5;
+        const double r = resd(i, j, e);
+        if (mode == JAC_DZ) jac[cur] = r;
+        else if (relaxed && ia[cur] == ja[cur]) jac[cur] = coefdiag[(i - 1) + (size_t)(j - 1) * im] - r;
+        else jac[cur] = -r;
+      }
+}
+
+// computejacobianfromjv_relaxed_withjnandcheck (ComputeJacobian.f90:1095-1204)
+inline void computejacobian_withjnandcheck(double* jac, int* ia, int* ja, const double* resd_, int m, int l, int k,
+                                           int gh, int im, int jm, const double* coefdiag, double mini, int n) {
+  FArr<const double> resd(resd_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  const int step = 1 + 2 * gh;
+  const int bad = 5 * im * jm - 2;
+  for (int e = 1; e <= 5; ++e)
+    for (int j = 1; j <= jm; ++j)
+      for (int i = 1; i <= im; ++i) {
+        const long long cur = (long long)(i - 1) + (long long)(j - 1) * im + (long long)(e - 1) * im * jm +
+                              (long long)k * im * jm * 5 + (long long)l * im * jm * 5 * step +
+                              (long long)m * im * jm * 5 * step * step + (long long)n * im * jm * 5 * 5 * step * step;
+        ia[cur] = e - 1 + (j - 1) * 5 + (i - 1) * jm * 5;
+        const int valj = (j <= k + 1 + gh) ? k : (j - gh - (k + 1) + 2 * gh) / step * step + k;
+        if (valj >= jm) { ia[cur] = bad; ja[cur] = 0; jac[cur] = 0.0; continue; }
+        int vali;
+        if (l <= gh) vali = (i <= l + 1 + gh) ? l : (i - (l + 1) + gh) / step * step + l;
+        else vali = (i <= l - gh) ? l : (i - (l + 1) + gh) / step * step + l;
+        const double cd = coefdiag[(i - 1) + (size_t)(j - 1) * im];
+        const double r = resd(i, j, e);
+        auto setv = [&](int vi) {
+          ja[cur] = m + valj * 5 + vi * jm * 5;
+          jac[cur] = (ia[cur] == ja[cur]) ? cd - r : -r;
+        };
+        if (n == 0) {
+          if (vali >= im - 2 * gh) {
+            vali = l;
+            if (std::fabs(jac[cur]) < mini) setv(vali);
+            else { ia[cur] = bad; ja[cur] = 0; jac[cur] = 0.0; }
+          } else {
+            if (std::fabs(jac[cur]) < mini) setv(vali);
+          }
+        } else {
+          if (vali <= 2 * gh) {
+            vali = im - (im % step) + l;
+            if (vali > im - 1) vali = vali - step;
+            if (std::fabs(jac[cur]) < mini) setv(vali);
+          } else {
+            if (std::fabs(jac[cur]) < mini) setv(vali);
+            else { ia[cur] = bad; ja[cur] = 0; jac[cur] = 0.0; }
+          }
+        }
+      }
+}
+
+// ===========================================================================
+// Initial state helpers (initialisation.f90:2-58, set_bnd.f90:1-24)
+// ===========================================================================
+inline void initblfv(double muinf, const double* xc_, const double* yc_, double* w_, double* field_, int im, int gh,
+                     int jm) {
+  FArr<const double> xc(xc_, im + 2 * gh, jm + 2 * gh, 1 - gh), yc(yc_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  FArr<double> w(w_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  auto field = [&](int a, int b, int v) -> double& { return field_[(size_t)(a - 1) + (size_t)(b - 1) * jm + (size_t)(v - 1) * jm * gh]; };
+  const double ro = w(3, 3, 1), rou = w(3, 3, 2), roE = w(3, 3, 5);
+  const double ue = rou / ro, rou2 = 0.5 * rou * ue, xdeltam1 = std::sqrt(rou / muinf);
+  for (int j = 1; j <= jm + gh; ++j)
+    for (int i = 1 - gh; i <= im + gh; ++i) {
+      const double eta = yc(i, j) * xdeltam1 / std::sqrt(xc(i, j));
+      double ubl = (eta < 1.0) ? 2.0 * eta - 2.0 * eta * eta * eta + eta * eta * eta * eta : 1.0;
+      ubl = ubl * ue;
+      w(i, j, 2) = ro * ubl;
+      w(i, j, 5) = roE - rou2 + 0.5 * ro * ubl * ubl;
+    }
+  for (int i = 1 - gh; i <= im + gh; ++i) w(i, 0, 2) = -w(i, 1, 2);
+  for (int j = 1; j <= jm; ++j)
+    for (int i = 1 - gh; i <= 0; ++i) {
+      const double eta = yc(i, j) * xdeltam1 * std::sqrt(xc(i, j));
+      double ubl = (eta < 1.0) ? 2.0 * eta - 2.0 * eta * eta * eta + eta * eta * eta * eta : 1.0;
+      ubl = ubl * ue;
+      field(j, 1 - i, 2) = ro * ubl;
+      field(j, 1 - i, 5) = roE - rou2 + 0.5 * ro * ubl * ubl;
+    }
+}
+inline void set_bndbl_2d(const double* w_, double* field_, double* wbd_, int im, int jm, int gh) {
+  FArr<const double> w(w_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  for (int j = 1; j <= jm; ++j)
+    for (int d = 1; d <= gh; ++d)
+      for (int v = 1; v <= 5; ++v) field_[(size_t)(j - 1) + (size_t)(d - 1) * jm + (size_t)(v - 1) * jm * gh] = w(1 - d, j, v);
+  const int lm = im + gh;
+  for (int i = 1; i <= im + gh; ++i)
+    for (int v = 1; v <= 5; ++v) wbd_[(size_t)(i - 1) + (size_t)(v - 1) * lm] = w(i - gh, jm, v);
+}
+
+}  // namespace orc

@@ -1,0 +1,173 @@
+"""Parity of the CUDA path (libbroadcast_gb300.so through its f2py-style
+modules and the device operator API) against the CPU oracle.
+
+Tolerances (spec criteria): residual within 1e-12 of the face-flux
+magnitude (max-norm per variable); tangent outputs within 1e-11 of the same
+scale times the tangent magnitude; boundary fills within 1e-13 relative;
+integer index work bit-exact.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+RES_TOL = 1e-12
+JVP_TOL = 1e-11
+
+
+def _prepared(kind, im, jm, seed=None):
+    kw = {} if seed is None else {"seed": seed}
+    c = H.bl_case(im, jm, **kw) if kind == "bl" else H.cyl_case(im, jm, **kw)
+    H.oracle_bcs(c, c["w"])
+    return c
+
+
+def _args(c):
+    g, ph = c["grid"], c["phys"]
+    return (g["x0"], g["y0"], g["nx"], g["ny"], g["xc"], g["yc"], g["vol"], g["volf"], g["gh"], ph["cp"], ph["cv"],
+            ph["prandtl"], ph["gam"], ph["rgaz"], ph["cs"], ph["muref"], ph["tref"], ph["s_suth"], ph["k2"], ph["k4"])
+
+
+@pytest.mark.parametrize("kind,im,jm", [("bl", 40, 30), ("cyl", 28, 20), ("bl", 13, 9), ("cyl", 21, 7)])
+def test_residual_host_arrays(kind, im, jm):
+    from broadcast_gb300.srcfv import f_sch
+    c = _prepared(kind, im, jm)
+    ref = O.residual(c["grid"], c["phys"], c["w"])
+    res = np.full_like(c["w"], 7.0)
+    f_sch.flux_num_dnc5_2d(res, c["w"], *_args(c))
+    assert np.isfinite(H.interior(res)).all()
+    err = H.rel_err(res, ref, H.flux_scale(c, c["w"]))
+    assert err < RES_TOL, err
+    # ghosts of the output are left untouched, as in the reference
+    assert (res[:3] == 7.0).all() and (res[:, -3:] == 7.0).all()
+
+
+@pytest.mark.parametrize("kind,im,jm", [("bl", 400, 150), ("cyl", 256, 256)])
+def test_residual_full_size_device(kind, im, jm):
+    import torch
+    from broadcast_gb300.operator import Dnc5Operator, to_device, to_host
+    c = _prepared(kind, im, jm)
+    ref = O.residual(c["grid"], c["phys"], c["w"])
+    op = Dnc5Operator(c["grid"], c["phys"])
+    res = op.residual(to_device(c["w"]))
+    torch.cuda.synchronize()
+    err = H.rel_err(to_host(res), ref, H.flux_scale(c, c["w"]))
+    assert err < RES_TOL, err
+
+
+@pytest.mark.parametrize("kind,im,jm", [("bl", 40, 30), ("cyl", 28, 20)])
+def test_jvp_single_direction_host_arrays(kind, im, jm):
+    from broadcast_gb300.srcfv import f_lin
+    c = _prepared(kind, im, jm)
+    rng = np.random.default_rng(3)
+    wd = np.asfortranarray(rng.standard_normal(c["w"].shape))
+    r0, rd0 = O.jvp(c["grid"], c["phys"], c["w"], wd)
+    res, resd = np.zeros_like(c["w"]), np.zeros_like(c["w"])
+    f_lin.flux_num_dnc5_2d_d(res, resd, c["w"], wd, *_args(c))
+    sc = H.flux_scale(c, c["w"])
+    assert H.rel_err(res, r0, sc) < RES_TOL
+    tsc = np.abs(H.interior(rd0)).reshape(-1, 5).max(0)
+    assert H.rel_err(resd, rd0, tsc) < JVP_TOL
+
+
+@pytest.mark.parametrize("kind,im,jm,nd", [("bl", 40, 30, 7), ("cyl", 28, 20, 5), ("cyl", 256, 256, 4)])
+def test_jvp_batched_device(kind, im, jm, nd):
+    import torch
+    from broadcast_gb300.operator import Dnc5Operator, to_device, to_host
+    c = _prepared(kind, im, jm)
+    rng = np.random.default_rng(4)
+    wds = np.stack([np.asfortranarray(rng.standard_normal(c["w"].shape)) for _ in range(nd)])
+    r0, rd0 = O.jvp(c["grid"], c["phys"], c["w"], wds)
+    op = Dnc5Operator(c["grid"], c["phys"])
+    wd_dev = torch.stack([to_device(x) for x in wds])
+    res, resd = op.jvp(to_device(c["w"]), wd_dev)
+    torch.cuda.synchronize()
+    sc = H.flux_scale(c, c["w"])
+    assert H.rel_err(to_host(res), r0, sc) < RES_TOL
+    for k in range(nd):
+        tsc = np.abs(H.interior(rd0[k])).reshape(-1, 5).max(0)
+        assert H.rel_err(to_host(resd[k]), rd0[k], tsc) < JVP_TOL, k
+
+
+@pytest.mark.parametrize("kind", ["bl", "cyl"])
+def test_boundary_fills_match_oracle(kind):
+    c = H.bl_case(40, 30) if kind == "bl" else H.cyl_case(28, 20)
+    w0 = c["w"].copy(order="F")
+    # scramble the ghosts so that every ghost value must come from the fill
+    rng = np.random.default_rng(5)
+    g = w0.copy(order="F")
+    g[:3] += rng.uniform(0.1, 0.2, g[:3].shape)
+    g[-3:] += rng.uniform(0.1, 0.2, g[-3:].shape)
+    g[:, :3] += rng.uniform(0.1, 0.2, g[:, :3].shape)
+    g[:, -3:] += rng.uniform(0.1, 0.2, g[:, -3:].shape)
+    a, b = g.copy(order="F"), g.copy(order="F")
+    H.oracle_bcs(c, a)
+    H.lib_bcs(c, b)
+    # one scale for all variables: the state magnitude (momenta of a
+    # near-zero component still carry rounding of O(|w|) terms)
+    scale = np.abs(a).max()
+    assert np.abs(a - b).max() / scale < 1e-13
+    # tangent fills
+    wd = np.asfortranarray(rng.standard_normal(g.shape))
+    a, b, ad, bd = g.copy(order="F"), g.copy(order="F"), wd.copy(order="F"), wd.copy(order="F")
+    H.oracle_bcs(c, a, ad)
+    H.lib_bcs(c, b, bd)
+    assert np.abs(a - b).max() / scale < 1e-13
+    assert np.abs(ad - bd).max() / np.abs(ad).max() < 1e-12
+
+
+def test_norms_match_oracle():
+    from broadcast_gb300.srcfv import f_norm
+    c = _prepared("bl", 40, 30)
+    r = O.residual(c["grid"], c["phys"], c["w"])
+    a, b = f_norm.compute_norml2(r, 40, 30, 3)
+    ea, eb = O.norml2(r, 40, 30, 3)
+    assert np.allclose(a, ea, rtol=1e-13, atol=0) and np.allclose(b, eb, rtol=1e-13, atol=0)
+    a, b = f_norm.compute_norml2inf(r, 40, 30, 3)
+    ea, eb = O.norml2inf(r, 40, 30, 3)
+    assert np.allclose(a, ea, rtol=1e-13, atol=0) and np.allclose(b, eb, rtol=1e-12, atol=0)
+    a, i, j = f_norm.compute_maxnorm(r, 40, 30, 3)
+    ea, ei, ej = O.maxnorm(r, 40, 30, 3)
+    assert np.array_equal(a, ea) and np.array_equal(i, ei) and np.array_equal(j, ej)
+
+
+@pytest.mark.parametrize("mode", ["plain", "relaxed", "relaxed_withjn", "withjn", "dz"])
+def test_colored_indexing_bit_exact(mode):
+    from broadcast_gb300.misc import f_misc
+    im, jm, gh = 16, 11, 3
+    rng = np.random.default_rng(6)
+    resd = np.asfortranarray(rng.standard_normal((im + 6, jm + 6, 5)))
+    coef = np.asfortranarray(rng.standard_normal((im, jm)))
+    nb = im * jm * 49 * 25
+    codes = dict(plain=O.JAC_PLAIN, relaxed=O.JAC_RELAXED, relaxed_withjn=O.JAC_RELAXED_WITHJN, withjn=O.JAC_WITHJN,
+                 dz=O.JAC_DZ)
+    for (m, l, k) in [(0, 0, 0), (2, 5, 1), (4, 6, 6), (1, 3, 4)]:
+        ja_, ia_, jac_ = np.zeros(nb, np.int32), np.zeros(nb, np.int32), np.zeros(nb)
+        jb_, ib_, jbc_ = np.zeros(nb, np.int32), np.zeros(nb, np.int32), np.zeros(nb)
+        O.computejacobian(codes[mode], jac_, ia_, ja_, resd, m, l, k, gh, im, jm, coef if "relaxed" in mode else None)
+        if mode == "plain":
+            f_misc.computejacobianfromjv(jbc_, ib_, jb_, resd, m, l, k, gh)
+        elif mode == "relaxed":
+            f_misc.computejacobianfromjv_relaxed(jbc_, ib_, jb_, resd, m, l, k, gh, coef)
+        elif mode == "relaxed_withjn":
+            f_misc.computejacobianfromjv_relaxed_withjn(jbc_, ib_, jb_, resd, m, l, k, gh, coef)
+        elif mode == "withjn":
+            f_misc.computejacobianfromjv_withjn(jbc_, ib_, jb_, resd, m, l, k, gh)
+        else:
+            f_misc.computejacobianfromdz(jbc_, ib_, jb_, resd, m, l, k, gh)
+        assert np.array_equal(ia_, ib_) and np.array_equal(ja_, jb_) and np.array_equal(jac_, jbc_)
+
+
+def test_testvector_bit_exact():
+    from broadcast_gb300.misc import f_misc
+    im, jm, gh = 23, 17, 3
+    for (m, l, k) in [(0, 0, 0), (3, 6, 2), (4, 1, 6)]:
+        wd = np.full((im + 6, jm + 6, 5), 9.0, order="F")
+        f_misc.testvector(wd, m, l, k, gh)
+        assert np.array_equal(wd, O.testvector(m, l, k, gh, im, jm))
+        wd[:] = 9.0
+        f_misc.testvector_partial(wd, m, l, k, gh, im, jm, 2, 15, 0, 16)
+        assert np.array_equal(wd, O.testvector_partial(m, l, k, gh, im, jm, 2, 15, 0, 16))
