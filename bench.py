@@ -1,0 +1,411 @@
+"""Benchmark of the FP64 DNC5 residual + JVP hot path on GB300.
+
+Workload (the reference's second configuration): 2-D cylinder O-mesh,
+256 (azimuth, periodic) x 256 (radial) cells, outer radius 50 D, radial
+stretching 1.05, Mach 0.1, Re 47, seeded uniform-flow state plus 1e-3 noise,
+32 seeded Gaussian direction vectors.  One step = the residual R(w) and the 32
+Jacobian-vector products dR/dw . v_k, i.e. 256*256*32 cell evaluations of
+residual + JVP.  The metric is Mcells/s = interior cells x directions / s.
+
+  value : kernels only, inputs resident in HBM, L2 flushed between steps
+  e2e   : through the C ABI (bcg_flux_num_dnc5_2d_dn) with pinned host arrays,
+          host->device and device->host copies inside the timed region
+
+python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+Under torchrun each rank runs its own 32 directions (weak scaling); rank 0
+prints one JSON line.  --impl reference times the reference path's CPU
+restatement (the oracle port, OpenMP on all host cores) on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "FP64 residual+JVP Mcells/s"
+UNIT = "Mcells/s"
+IM, JM, NDIR, GROUP = 256, 256, 32, 4
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class LibOps:
+    """Host pre-processing through the library's host entry points."""
+
+    @staticmethod
+    def computegeom(*a):
+        from broadcast_gb300.srcfv import f_geom
+        f_geom.computegeom_2d(*a)
+
+    @staticmethod
+    def initblfv(muinf, xc, yc, w, field, im, gh, jm):
+        from broadcast_gb300 import f_init
+        f_init.initblfv(muinf, xc, yc, w, field, im, gh, jm)
+
+    @staticmethod
+    def set_bndbl(w, field, wbd, im, jm, gh):
+        from broadcast_gb300 import f_init
+        f_init.set_bndbl_2d(w, field, wbd, im, jm, gh)
+
+
+def cylinder_bcs(c, w, wd=None):
+    """Cylinder boundary sequence of handleBC.applyBC (order Jhi, Jlo, Ilo, Ihi)."""
+    from broadcast_gb300.srcfv import f_bnd, f_lin
+    g, ph, it = c["grid"], c["phys"], c["interf"]
+    im, jm, gh = g["im"], g["jm"], g["gh"]
+    if wd is None:
+        f_bnd.bc_no_reflexion_2d(w, c["wbd"], "Jhi", it["Jhi"], g["nx"], g["ny"], ph["gam"], gh, im, jm)
+        f_bnd.bc_wall_viscous_adia_2d(w, "Jlo", ph["gam"], it["Jlo"], gh, im, jm)
+    else:
+        f_lin.bc_no_reflexion_2d_d(w, wd, c["wbd"], "Jhi", it["Jhi"], g["nx"], g["ny"], ph["gam"], gh, im, jm)
+        f_lin.bc_wall_viscous_adia_2d_d(w, wd, "Jlo", ph["gam"], it["Jlo"], gh, im, jm)
+    for _ in range(2):
+        for a in ([w] if wd is None else [wd, w]):
+            f_bnd.jn_match_2d(a, it["prr1"], gh, gh, gh, gh, im, jm, a, it["prd2"], gh, gh, gh, gh, im, jm, it["tr"])
+            f_bnd.jn_match_2d(a, it["prr2"], gh, gh, gh, gh, im, jm, a, it["prd1"], gh, gh, gh, gh, im, jm, it["tr"])
+
+
+def build_workload():
+    from broadcast_gb300 import cases
+    c = cases.cyl_case(IM, JM, ops=LibOps)
+    cylinder_bcs(c, c["w"])
+    rng = np.random.default_rng(2)
+    wds = []
+    gh = cases.GH
+    for _ in range(NDIR):
+        wd = np.zeros_like(c["w"], order="F")
+        wd[gh:-gh, gh:-gh, :] = rng.standard_normal((IM, JM, 5))
+        wtmp = c["w"].copy(order="F")
+        cylinder_bcs(c, wtmp, wd)
+        wds.append(wd)
+    return c, wds
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(im, jm, gh, ndir):
+    """Compulsory HBM bytes of one residual + ndir-direction JVP evaluation:
+    w and the ndir tangent states (5 per padded cell each), vol and volf (3 per
+    padded cell), nx and ny (4 per padded node), residual and ndir tangent
+    outputs (5 per interior cell each)."""
+    np_ = (im + 2 * gh) * (jm + 2 * gh)
+    nn = (im + 2 * gh + 1) * (jm + 2 * gh + 1)
+    nc = im * jm
+    return 8 * ((5 + 5 * ndir + 3) * np_ + 4 * nn + 5 * (1 + ndir) * nc)
+
+
+def flop_counts(c):
+    from oracle import oracle as O
+    primal, tangent, _ = O.opcount(c["grid"], c["phys"], c["w"])
+    return primal, tangent
+
+
+def cpu_baseline(c, wds, seconds=12.0, threads=None):
+    """The oracle (C++ restatement of the reference Fortran) with OpenMP on the
+    host cores: residual + 1-direction JVP evaluations of the full grid,
+    repeated for about `seconds`."""
+    from oracle import oracle as O
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    O.lib(openmp=True)
+    import ctypes
+    lib = O.lib(openmp=True)
+    g, ph = c["grid"], c["phys"]
+    res = np.zeros_like(c["w"], order="F")
+    out = np.zeros_like(c["w"], order="F")
+    args = (O._p(g["nx"]), O._p(g["ny"]), O._p(g["vol"]), O._p(g["volf"]), g["gh"], *O._phys(ph), g["im"], g["jm"])
+    n, t0 = 0, time.perf_counter()
+    while True:
+        wd = wds[n % len(wds)]
+        lib.orc_flux_num_dnc5_2d_d(O._p(res), O._p(out), O._p(c["w"]), O._p(wd), 1, *args)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds and n >= 2:
+            break
+    cells = g["im"] * g["jm"] * n
+    return {"value": cells / el / 1e6, "unit": UNIT, "cores": threads or os.cpu_count(), "kind": "port",
+            "sample": "%d residual+JVP (1 direction) evaluations of the %dx%d cylinder grid, %.1f s" % (n, IM, JM, el)}
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    from broadcast_gb300 import cases
+
+    class OracleOps:
+        from oracle import oracle as _O
+        computegeom = staticmethod(_O.computegeom)
+        initblfv = staticmethod(_O.initblfv)
+        set_bndbl = staticmethod(_O.set_bndbl)
+
+    from oracle import oracle as O
+    c = cases.cyl_case(IM, JM, ops=OracleOps)
+    g, ph, it = c["grid"], c["phys"], c["interf"]
+    w = c["w"]
+    O.bc_noref(w, c["wbd"], "Jhi", it["Jhi"], g["nx"], g["ny"], ph["gam"], 3, IM, JM)
+    O.bc_wall(w, "Jlo", ph["gam"], it["Jlo"], 3, IM, JM)
+    for _ in range(2):
+        O.jn_match(w, it["prr1"], (3,) * 4, IM, JM, w, it["prd2"], (3,) * 4, IM, JM, it["tr"], 5)
+        O.jn_match(w, it["prr2"], (3,) * 4, IM, JM, w, it["prd1"], (3,) * 4, IM, JM, it["tr"], 5)
+    rng = np.random.default_rng(2)
+    wds = []
+    for _ in range(4):
+        wd = np.zeros_like(c["w"], order="F")
+        wd[3:-3, 3:-3, :] = rng.standard_normal((IM, JM, 5))
+        wds.append(wd)
+    lib = O.lib(openmp=True)
+    res = np.zeros_like(c["w"], order="F")
+    out = np.zeros_like(c["w"], order="F")
+    a = (O._p(g["nx"]), O._p(g["ny"]), O._p(g["vol"]), O._p(g["volf"]), g["gh"], *O._phys(ph), g["im"], g["jm"])
+    # one step = a bounded sample of the workload: 4 residual+JVP evaluations
+    per_step = 4
+
+    def step():
+        for k in range(per_step):
+            lib.orc_flux_num_dnc5_2d_d(O._p(res), O._p(out), O._p(c["w"]), O._p(wds[k]), 1, *a)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    el = time.perf_counter() - t0
+    v = IM * JM * per_step * args.steps / el / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "cylinder O-mesh %dx%d, Mach 0.1, Re 47, residual + JVP per direction" % (IM, JM),
+                       "directions_per_step": per_step},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                             "sample": "%d residual+JVP (1 direction) evaluations per step of the %dx%d grid, "
+                                       "OpenMP over j-rows" % (per_step, IM, JM)},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from broadcast_gb300 import _lib
+    from broadcast_gb300.operator import Dnc5Operator, to_device
+
+    c, wds = build_workload()
+    op = Dnc5Operator(c["grid"], c["phys"], device=dev)
+    w_dev = to_device(c["w"], dev)
+    wd_dev = torch.stack([to_device(x, dev) for x in wds])
+    res = op.new_state()
+    resd = op.new_state(NDIR)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        for k0 in range(0, NDIR, GROUP):
+            op.jvp(w_dev, wd_dev[k0:k0 + GROUP], res=res, resd=resd[k0:k0 + GROUP])
+
+    for _ in range(max(args.warmup, 1)):
+        step()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    if rank == 0:
+        sampler.start()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for s in range(args.steps):
+        flush.add_(1.0)
+        ev[s][0].record(stream)
+        step()
+        ev[s][1].record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    clocks = sampler.stop() if rank == 0 else None
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    tot_ms = sum(step_ms)
+    if ws > 1:
+        t = torch.tensor([tot_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_ms = float(t.item())
+    units = IM * JM * NDIR * args.steps * ws
+    value = units / (tot_ms / 1e3) / 1e6
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if rank == 0:
+        pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+        w_h = pin(c["w"].size)
+        w_h[:] = np.ravel(c["w"], order="F")
+        wd_h = pin(c["w"].size * NDIR)
+        for k in range(NDIR):
+            wd_h[k * c["w"].size:(k + 1) * c["w"].size] = np.ravel(wds[k], order="F")
+        g = c["grid"]
+        geo = {k: pin(g[k].size) for k in ("nx", "ny", "vol", "volf")}
+        for k in geo:
+            geo[k][:] = np.ravel(g[k], order="F")
+        res_h, resd_h = pin(c["w"].size), pin(c["w"].size * NDIR)
+        ph = [float(c["phys"][k]) for k in Dnc5Operator.PHYS_KEYS]
+
+        def e2e_step():
+            _lib.call("bcg_flux_num_dnc5_2d_dn", res_h, resd_h, w_h, wd_h, NDIR, None, None, geo["nx"], geo["ny"],
+                      None, None, geo["vol"], geo["volf"], 3, *ph, IM, JM)
+
+        for _ in range(max(args.warmup, 1)):
+            e2e_step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        el = time.perf_counter() - t0
+        np_, nn = (IM + 6) * (JM + 6), (IM + 7) * (JM + 7)
+        h2d = 8 * (5 * np_ * (1 + NDIR) + 4 * nn + 3 * np_)
+        d2h = 8 * 5 * IM * JM * (1 + NDIR)
+        e2e = {"value": IM * JM * NDIR * args.steps / el / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": el / args.steps * 1e3}
+
+    if rank == 0:
+        peak_fp64 = ctypes_double()
+        _lib.call("bcg_fp64_peak_tflops", peak_fp64)
+        peak_fp64 = peak_fp64[0]
+        primal, tangent = flop_counts(c)
+        per_group_ms = tot_ms / args.steps / (NDIR // GROUP) / ws
+        flops_group = primal + GROUP * tangent
+        bytes_group = algorithmic_bytes(IM, JM, 3, GROUP)
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+        hbm_peak = peaks.get("hbm_gbs", 6800.0)
+        ach_gbs = bytes_group / (per_group_ms / 1e3) / 1e9
+        ach_tf = flops_group / (per_group_ms / 1e3) / 1e12
+        traffic = _profiled_traffic()
+        cpu = cpu_baseline(c, wds[:4], seconds=args.cpu_seconds)
+        launches_per_group = 3 + (1 if c["phys"]["k2"] != 0 else 0)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": tot_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "cylinder O-mesh %dx%d (r 0.5..50 D, stretch 1.05), Mach 0.1, Re 47; residual + "
+                                   "JVP for %d seeded Gaussian directions per step" % (IM, JM, NDIR),
+                       "cells": IM * JM, "directions_per_step": NDIR, "directions_per_launch_group": GROUP,
+                       "l2": "flushed between steps (256 MB write)", "parallelism": "replicas" if ws > 1 else "single"},
+            "roofline": {"bound": "hbm", "achieved": ach_gbs, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": ach_gbs / hbm_peak, "traffic": traffic,
+                         "kernel": "fused residual+JVP pass (prim + faces + balance) per group of %d directions"
+                                   % GROUP,
+                         "fp64": {"achieved": ach_tf, "peak": peak_fp64, "unit": "TFLOP/s",
+                                  "frac": ach_tf / peak_fp64, "flops_per_group": flops_group,
+                                  "peak_source": "bcg_fp64_peak_tflops (FMA chains, measured in this run)"}},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches_per_group * (NDIR // GROUP) * args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(line))
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def ctypes_double():
+    return np.zeros(1)
+
+
+def _profiled_traffic():
+    """DRAM bytes per launch group from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "dnc5_jvp_cylinder256.md")
+    if not os.path.exists(p):
+        return None
+    for ln in open(p):
+        if ln.startswith("traffic_bytes_per_group:"):
+            try:
+                return float(ln.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

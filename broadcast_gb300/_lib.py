@@ -52,6 +52,7 @@ SIGNATURES = {
     "bcg_computegeom_2d": "pppppppp" + "iii",
     "bcg_set_bndbl_2d": "ppp" + "iii",
     "bcg_initblfv": "d" + "pppp" + "iii",
+    "bcg_fp64_peak_tflops": P,
 }
 _RESTYPE = {"bcg_get_stream": ctypes.c_void_p, "bcg_last_error_string": ctypes.c_char_p,
             "bcg_residual_scratch_bytes": ctypes.c_size_t}

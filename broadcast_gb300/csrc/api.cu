@@ -38,9 +38,10 @@ int residual_call(double* residu, double* residud, const double* w, const double
   Stager sg(st);
   const int hw = sg.in(w, np * 5 * 8), hnx = sg.in(nx, nn * 2 * 8), hny = sg.in(ny, nn * 2 * 8);
   const int hvol = sg.in(vol, np * 8), hvolf = sg.in(volf, np * 2 * 8);
-  const int hres = residu ? sg.inout(residu, np * 5 * 8) : -1;
+  const int ni = im + 2 * gh, nj = jm + 2 * gh;
+  const int hres = residu ? sg.out_interior(residu, ni, nj, 5, gh, im, jm) : -1;
   const int hwd = nd ? sg.in(wd, np * 5 * 8 * (size_t)nd) : -1;
-  const int hresd = nd ? sg.inout(residud, np * 5 * 8 * (size_t)nd) : -1;
+  const int hresd = nd ? sg.out_interior(residud, ni, nj, 5 * nd, gh, im, jm) : -1;
   int rc = sg.commit();
   if (rc) return rc;
   ResidualArgs a{};
@@ -61,12 +62,9 @@ int residual_call(double* residu, double* residud, const double* w, const double
     double* rdd = sg.dev<double>(hresd);
     for (int k0 = 0; k0 < nd; k0 += 4) {
       const int kk = std::min(4, nd - k0);
-      const int kc = kk == 3 ? 4 : kk;
-      // a 3-direction chunk runs as 4 directions over a zero pad is not
-      // needed: split it as 2 + 1 instead
+      // kernels exist for 1, 2 and 4 directions: a group of 3 runs as 2 + 1
       int parts[2] = {kk, 0};
       if (kk == 3) { parts[0] = 2; parts[1] = 1; }
-      (void)kc;
       int off = k0;
       for (int pi = 0; pi < 2 && parts[pi] > 0; ++pi) {
         a.ndir = parts[pi];

@@ -68,6 +68,13 @@ int Stager::add(const void* p, size_t bytes, bool inp, bool outp) {
   return (int)items_.size() - 1;
 }
 
+int Stager::out_interior(void* p, int ni, int nj, int nplanes, int gh, int im, int jm) {
+  const int h = add(p, (size_t)ni * nj * nplanes * sizeof(double), false, true);
+  Item& it = items_[h];
+  it.ni = ni; it.nj = nj; it.nplanes = nplanes; it.gh = gh; it.im = im; it.jm = jm;
+  return h;
+}
+
 int Stager::commit() {
   if (nstaged_ == 0) return BCG_OK;
   char* base = (char*)pool_get(POOL_STAGE, total_);
@@ -90,6 +97,19 @@ int Stager::finish() {
   for (size_t k = 0; k < items_.size(); ++k) {
     Item& it = items_[k];
     if (!it.staged || !it.outp) continue;
+    if (it.nplanes > 0) {
+      const size_t pitch = (size_t)it.ni * sizeof(double), plane = (size_t)it.ni * it.nj * sizeof(double);
+      const size_t off0 = ((size_t)it.gh + (size_t)it.gh * it.ni) * sizeof(double);
+      for (int pl = 0; pl < it.nplanes; ++pl) {
+        char* dst = (char*)const_cast<void*>(it.host) + pl * plane + off0;
+        const char* src = (const char*)ptrs_[k] + pl * plane + off0;
+        cudaError_t e = cudaMemcpy2DAsync(dst, pitch, src, pitch, (size_t)it.im * sizeof(double), it.jm,
+                                          cudaMemcpyDeviceToHost, st_);
+        if (e != cudaSuccess) return fail_cuda("device to host copy", e);
+      }
+      d2h_ += (size_t)it.nplanes * it.im * it.jm * sizeof(double);
+      continue;
+    }
     cudaError_t e = cudaMemcpyAsync(const_cast<void*>(it.host), ptrs_[k], it.bytes, cudaMemcpyDeviceToHost, st_);
     if (e != cudaSuccess) return fail_cuda("device to host copy", e);
     d2h_ += it.bytes;

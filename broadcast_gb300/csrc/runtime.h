@@ -38,6 +38,11 @@ class Stager {
   int in(const void* p, size_t bytes) { return add(p, bytes, true, false); }
   int inout(void* p, size_t bytes) { return add(p, bytes, true, true); }
   int out(void* p, size_t bytes) { return add(p, bytes, false, true); }
+  // output whose kernels write only the interior of nplanes padded planes of
+  // (ni, nj) doubles: nothing is copied in and only the interior
+  // [gh, gh+im) x [gh, gh+jm) of each plane is copied back, so the caller's
+  // ghost values stay untouched (the reference's intent(inout) semantics)
+  int out_interior(void* p, int ni, int nj, int nplanes, int gh, int im, int jm);
   int commit();                           // BCG_OK or an error code
   template <class T> T* dev(int h) const { return (T*)ptrs_[h]; }
   int finish();                           // copy outputs back; sync if anything was staged
@@ -46,7 +51,10 @@ class Stager {
   size_t d2h_bytes() const { return d2h_; }
 
  private:
-  struct Item { const void* host; size_t bytes, off; bool inp, outp, staged; };
+  struct Item {
+    const void* host; size_t bytes, off; bool inp, outp, staged;
+    int ni = 0, nj = 0, nplanes = 0, gh = 0, im = 0, jm = 0;  // interior-only output when nplanes > 0
+  };
   int add(const void* p, size_t bytes, bool inp, bool outp);
   cudaStream_t st_;
   std::vector<Item> items_;

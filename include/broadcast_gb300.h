@@ -136,6 +136,11 @@ int bcg_set_bndbl_2d(const double* w, double* field, double* wbd, int im, int jm
 /* initialisation.f90:2 */
 int bcg_initblfv(double muinf, const double* xc, const double* yc, double* w, double* field, int im, int gh, int jm);
 
+/* ---- calibration (no reference counterpart) ------------------------------------ */
+/* FP64 FMA throughput of the current GPU in TFLOP/s (FMA = 2 flops): the
+ * denominator of the FP64 roofline that bounds the residual kernels. */
+int bcg_fp64_peak_tflops(double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

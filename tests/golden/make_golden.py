@@ -1,0 +1,181 @@
+"""Generate the golden fixtures of tests/golden/ from the reference's own
+routines (oracle/_ref/libref.so, built by `python oracle/ref_build.py` from a
+reference checkout; see oracle/ref_translate.py).
+
+    python tests/golden/make_golden.py
+
+Each fixture holds the inputs (grid metrics, state, directions) and the
+reference outputs of one small case, so that the oracle and the CUDA path can
+be checked against the reference where the reference is not available.
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from broadcast_gb300 import cases  # noqa: E402
+from oracle import ref  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PHYS = ("cp", "cv", "prandtl", "gam", "rgaz", "cs", "muref", "tref", "s_suth", "k2", "k4")
+
+
+class RefOps:
+    @staticmethod
+    def computegeom(x0, y0, nx, ny, xc, yc, vol, volf, im, jm, gh):
+        ref.call("computegeom_2d", x0, y0, nx, ny, xc, yc, vol, volf, im, jm, gh)
+
+    @staticmethod
+    def initblfv(muinf, xc, yc, w, field, im, gh, jm):
+        ref.call("initblfv", muinf, xc, yc, w, field, im, gh, jm)
+
+    @staticmethod
+    def set_bndbl(w, field, wbd, im, jm, gh):
+        ref.call("set_bndbl_2d", w, field, wbd, im, jm, gh)
+
+
+def fi(a):
+    return np.asfortranarray(np.asarray(a, dtype=np.int32))
+
+
+def ref_bcs(c, w, wd=None):
+    """The drivers' boundary sequences through the reference routines."""
+    g, ph, it = c["grid"], c["phys"], c["interf"]
+    im, jm, gh = g["im"], g["jm"], g["gh"]
+    gam = ph["gam"]
+    if c["kind"] == "bl":
+        fld, wbd = c["field"], c["wbd"]
+        lm_f, lm_b = fld.shape[0], wbd.shape[0]
+        if wd is None:
+            ref.call("bc_supandsubinlet_2d", w, "Ilo", fi(it["Ilo"]), fld, g["nx"], g["ny"], gam, im, jm, lm_f, gh)
+            ref.call("bc_no_reflexion_2d", w, wbd, "Jhi", fi(it["Jhi"]), g["nx"], g["ny"], gam, gh, im, jm, lm_b)
+            ref.call("bc_extrapolate_o2_2d", w, "Ihi", fi(it["Ihi"]), im, jm, gh, 5)
+            ref.call("bc_wall_viscous_adia_2d", w, "Jlo", gam, fi(it["Jlo"]), gh, im, jm)
+        else:
+            ref.call("bc_supandsubinlet_2d_d", w, wd, "Ilo", fi(it["Ilo"]), fld, g["nx"], g["ny"], gam, im, jm, lm_f, gh)
+            ref.call("bc_no_reflexion_2d_d", w, wd, wbd, "Jhi", fi(it["Jhi"]), g["nx"], g["ny"], gam, gh, im, jm, lm_b)
+            ref.call("bc_extrapolate_o2_2d_d", w, wd, "Ihi", fi(it["Ihi"]), im, jm, gh, 5)
+            ref.call("bc_wall_viscous_adia_2d_d", w, wd, "Jlo", gam, fi(it["Jlo"]), gh, im, jm)
+    else:
+        wbd = c["wbd"]
+        if wd is None:
+            ref.call("bc_no_reflexion_2d", w, wbd, "Jhi", fi(it["Jhi"]), g["nx"], g["ny"], gam, gh, im, jm, wbd.shape[0])
+            ref.call("bc_wall_viscous_adia_2d", w, "Jlo", gam, fi(it["Jlo"]), gh, im, jm)
+        else:
+            ref.call("bc_no_reflexion_2d_d", w, wd, wbd, "Jhi", fi(it["Jhi"]), g["nx"], g["ny"], gam, gh, im, jm,
+                     wbd.shape[0])
+            ref.call("bc_wall_viscous_adia_2d_d", w, wd, "Jlo", gam, fi(it["Jlo"]), gh, im, jm)
+        # periodic joins (borders/jn_match.F90): block copies of gh columns
+        for a in ([w] if wd is None else [wd, w]):
+            a[gh + im:gh + im + gh] = a[gh:2 * gh]
+            a[0:gh] = a[im:im + gh]
+
+
+def residual_args(c):
+    g, ph = c["grid"], c["phys"]
+    return (g["x0"], g["y0"], g["nx"], g["ny"], g["xc"], g["yc"], g["vol"], g["volf"], g["gh"]) + tuple(
+        ph[k] for k in PHYS) + (g["im"], g["jm"])
+
+
+def make(kind, im, jm, seed):
+    c = cases.bl_case(im, jm, seed=seed, ops=RefOps) if kind == "bl" else cases.cyl_case(im, jm, seed=seed, ops=RefOps)
+    g, ph = c["grid"], c["phys"]
+    w_raw = c["w"].copy(order="F")
+    w = c["w"]
+    ref_bcs(c, w)
+    rng = np.random.default_rng(seed + 100)
+    out = {"kind": kind, "im": im, "jm": jm, "gh": g["gh"], "w_raw": w_raw, "w": w.copy(order="F")}
+    for k in ("x0", "y0", "nx", "ny", "xc", "yc", "vol", "volf"):
+        out[k] = g[k]
+    for k in PHYS:
+        out["phys_" + k] = ph[k]
+    if kind == "bl":
+        out["field"], out["wbd"] = c["field"], c["wbd"]
+    else:
+        out["wbd"] = c["wbd"]
+    res = np.zeros_like(w)
+    ref.call("flux_num_dnc5_2d", res, w, *residual_args(c))
+    out["res"] = res
+    # tangent: two directions, ghosts filled by the linearised boundary sequence
+    wds, resds = [], []
+    for d in range(2):
+        wd = np.zeros_like(w)
+        wd[3:-3, 3:-3] = rng.standard_normal((im, jm, 5))
+        wtmp = w.copy(order="F")
+        ref_bcs(c, wtmp, wd)
+        r, rd = np.zeros_like(w), np.zeros_like(w)
+        ref.call("flux_num_dnc5_2d_d", r, rd, w, wd, *residual_args(c))
+        wds.append(wd)
+        resds.append(rd)
+    out["wd"] = np.stack(wds)
+    out["resd"] = np.stack(resds)
+    # adjoint: one cotangent on the interior
+    rb = np.zeros_like(w)
+    rb[3:-3, 3:-3] = rng.standard_normal((im, jm, 5))
+    out["rb"] = rb.copy(order="F")
+    wb, r3 = np.zeros_like(w), np.zeros_like(w)
+    ref.call("flux_num_dnc5_2d_b", r3, rb, w, wb, *residual_args(c))
+    out["wb"] = wb
+    # norms of the residual
+    n2, nm = np.zeros(5), np.zeros(5)
+    ref.call("compute_norml2", n2, nm, res, im, jm, 3)
+    ni2, ninf = np.zeros(5), np.zeros(5)
+    ref.call("compute_norml2inf", ni2, ninf, res, im, jm, 3)
+    mx, imx, jmx = np.zeros(5), np.zeros(5, np.int32), np.zeros(5, np.int32)
+    ref.call("compute_maxnorm", mx, imx, jmx, res, im, jm, 3)
+    out.update(norml2=n2, nmoy=nm, ninf=ninf, maxnorm=mx, imax=imx, jmax=jmx)
+    return out
+
+
+def make_indexing(im=16, jm=11, gh=3, seed=7):
+    rng = np.random.default_rng(seed)
+    resd = np.asfortranarray(rng.standard_normal((im + 2 * gh, jm + 2 * gh, 5)))
+    coef = np.asfortranarray(rng.standard_normal((im, jm)))
+    nb = im * jm * 49 * 25
+    out = {"im": im, "jm": jm, "gh": gh, "resd": resd, "coefdiag": coef}
+    seeds = [(0, 0, 0), (2, 5, 1), (4, 6, 6), (1, 3, 4)]
+    for name in ("computejacobianfromjv", "computejacobianfromjv_relaxed", "computejacobianfromjv_relaxed_withjn",
+                 "computejacobianfromjv_withjn", "computejacobianfromdz"):
+        jac, ia, ja = np.zeros(nb), np.zeros(nb, np.int32), np.zeros(nb, np.int32)
+        for (m, l, k) in seeds:
+            if "relaxed" in name:
+                ref.call(name, jac, ia, ja, resd, m, l, k, gh, im, jm, nb, coef)
+            else:
+                ref.call(name, jac, ia, ja, resd, m, l, k, gh, im, jm, nb)
+        out[name + "_jac"], out[name + "_ia"], out[name + "_ja"] = jac, ia, ja
+    # the two-zone check variant: zone 0 then zone 1 into the same arrays
+    nb2 = nb * 2
+    jac, ia, ja = np.zeros(nb2), np.zeros(nb2, np.int32), np.zeros(nb2, np.int32)
+    for n in (0, 1):
+        for (m, l, k) in seeds:
+            ref.call("computejacobianfromjv_relaxed_withjnandcheck", jac, ia, ja, resd, m, l, k, gh, im, jm, nb2, coef,
+                     2e-16, n)
+    out["check_jac"], out["check_ia"], out["check_ja"] = jac, ia, ja
+    tv = []
+    for (m, l, k) in seeds:
+        wd = np.zeros((im + 2 * gh, jm + 2 * gh, 5), order="F")
+        ref.call("testvector", wd, m, l, k, gh, im, jm)
+        tv.append(wd)
+        wd = np.zeros((im + 2 * gh, jm + 2 * gh, 5), order="F")
+        ref.call("testvector_partial", wd, m, l, k, gh, im, jm, 2, im - 2, 0, jm - 1)
+        tv.append(wd)
+    out["testvectors"] = np.stack(tv)
+    out["seeds"] = np.array(seeds, dtype=np.int32)
+    return out
+
+
+def main():
+    if not ref.available():
+        raise SystemExit("oracle/_ref is not built: run python oracle/ref_build.py first")
+    for name, (kind, im, jm, seed) in {"bl_14x10": ("bl", 14, 10, 0), "cyl_14x8": ("cyl", 14, 8, 1),
+                                       "bl_23x17": ("bl", 23, 17, 3)}.items():
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **make(kind, im, jm, seed))
+    np.savez_compressed(os.path.join(HERE, "indexing_16x11.npz"), **make_indexing())
+    print("written:", sorted(f for f in os.listdir(HERE) if f.endswith(".npz")))
+
+
+if __name__ == "__main__":
+    main()
