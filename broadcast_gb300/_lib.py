@@ -53,6 +53,7 @@ SIGNATURES = {
     "bcg_set_bndbl_2d": "ppp" + "iii",
     "bcg_initblfv": "d" + "pppp" + "iii",
     "bcg_fp64_peak_tflops": P,
+    "bcg_flux_num_dnc5_2d_noalloc": "pppppppppp" + "i" + "d" * 11 + "ii",
 }
 _RESTYPE = {"bcg_get_stream": ctypes.c_void_p, "bcg_last_error_string": ctypes.c_char_p,
             "bcg_residual_scratch_bytes": ctypes.c_size_t}

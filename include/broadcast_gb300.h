@@ -136,6 +136,24 @@ int bcg_set_bndbl_2d(const double* w, double* field, double* wbd, int im, int jm
 /* initialisation.f90:2 */
 int bcg_initblfv(double muinf, const double* xc, const double* yc, double* w, double* field, int im, int gh, int jm);
 
+/* ---- allocation-free residual (no counterpart in the reference) --------------- */
+/* For callers that cannot let the library allocate device memory during a call
+ * (a framework allocator already owning the GPU's memory, a fixed memory
+ * budget, loops that cannot absorb cudaMalloc's synchronisation).  Same
+ * arguments and result as bcg_flux_num_dnc5_2d, but every array must be a
+ * device pointer and the working storage is a fixed 16 MiB static device
+ * array (held by every GPU that loads the library until the process exits):
+ * grids need 18*(im+6)*(jm+6) + 10*(im+1)*(jm+1) <= 2097152 doubles (256 x 256
+ * and 400 x 150 fit); larger ones return -1.  All calls share that array:
+ * calls that overlap on the GPU race, so serialise them.  The first call on a
+ * device looks up the array's address for that device; make it before any
+ * stream capture.  Queued on the library stream, returns without waiting. */
+int bcg_flux_num_dnc5_2d_noalloc(double* residu, const double* w, const double* x0, const double* y0,
+                                 const double* nx, const double* ny, const double* xc, const double* yc,
+                                 const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
+                                 double gam, double rgaz, double cs, double muref, double tref, double s_suth,
+                                 double k2, double k4, int im, int jm);
+
 /* ---- calibration (no reference counterpart) ------------------------------------ */
 /* FP64 FMA throughput of the current GPU in TFLOP/s (FMA = 2 flops): the
  * denominator of the FP64 roofline that bounds the residual kernels. */
