@@ -27,6 +27,7 @@ SIGNATURES = {
     "bcg_flux_num_dnc5_2d": "pppppppppp" + "i" + "d" * 11 + "ii",
     "bcg_flux_num_dnc5_2d_d": "pppp" + "pppppppp" + "i" + "d" * 11 + "ii",
     "bcg_flux_num_dnc5_2d_dn": "ppppi" + "pppppppp" + "i" + "d" * 11 + "ii",
+    "bcg_flux_num_dnc5_2d_b": "pppp" + "pppppppp" + "i" + "d" * 11 + "ii",
     "bcg_bc_wall_viscous_adia_2d": "psdpiii",
     "bcg_bc_wall_viscous_adia_2d_d": "ppsdpiii",
     "bcg_bc_no_reflexion_2d": "ppsppp" + "d" + "iiii",
@@ -53,6 +54,7 @@ SIGNATURES = {
     "bcg_set_bndbl_2d": "ppp" + "iii",
     "bcg_initblfv": "d" + "pppp" + "iii",
     "bcg_fp64_peak_tflops": P,
+    "bcg_jacobian_dnc5_bl_csr": "ppppp" + "i" + "d" * 11 + "ii" + "pppp" + "pipi" + "pdi" + "ppp" + "L" + "p",
     "bcg_flux_num_dnc5_2d_noalloc": "pppppppppp" + "i" + "d" * 11 + "ii",
 }
 _RESTYPE = {"bcg_get_stream": ctypes.c_void_p, "bcg_last_error_string": ctypes.c_char_p,

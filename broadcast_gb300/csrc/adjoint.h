@@ -1,0 +1,25 @@
+// Launch interface of the DNC5 adjoint (VJP) kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include "dnc5.cuh"
+
+namespace bcg {
+
+struct AdjointArgs {
+  int im, jm, gh;
+  Phys phys;
+  const double* w;      // (ni, nj, 5)
+  const double* nx;
+  const double* ny;
+  const double* vol;
+  const double* volf;
+  double* rb;           // residub (ni, nj, 5): interior read, then zeroed
+  double* wb;           // (ni, nj, 5): overwritten on every padded cell
+  double* scratch;      // adjoint_scratch_doubles(im, jm, gh) doubles
+};
+
+size_t adjoint_scratch_doubles(int im, int jm, int gh);
+cudaError_t run_adjoint(const AdjointArgs& a, cudaStream_t st);
+
+}  // namespace bcg

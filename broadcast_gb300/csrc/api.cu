@@ -11,6 +11,8 @@
 #include "residual.h"
 #include "runtime.h"
 #include "assembly.h"
+#include "adjoint.h"
+#include "jacobian.h"
 
 using namespace bcg;
 
@@ -191,6 +193,38 @@ int bcg_flux_num_dnc5_2d_dn(double* residu, double* residud, const double* w, co
   (void)x0; (void)y0; (void)xc; (void)yc;
   return residual_call(residu, residud, w, wd, nd, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref,
                        tref, s_suth, k2, k4, im, jm);
+}
+
+// ---- adjoint (srcfv/adjoint/flux_num_dnc5_b.f90:15) ------------------------
+// wb = (dR/dw)^T residub on every padded cell (wb overwritten); the interior
+// of residub is zeroed, as the Tapenade routine does.  residu is unused.
+int bcg_flux_num_dnc5_2d_b(double* residu, double* residub, const double* w, double* wb, const double* x0,
+                           const double* y0, const double* nx, const double* ny, const double* xc, const double* yc,
+                           const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
+                           double gam, double rgaz, double cs, double muref, double tref, double s_suth, double k2,
+                           double k4, int im, int jm) {
+  (void)residu; (void)x0; (void)y0; (void)xc; (void)yc;
+  if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
+  if (!dims_ok(im, jm, gh)) return fail_arg("flux_num_dnc5_2d_b: need gh == 3 and im, jm >= 6");
+  const size_t np = ncell(im, jm, gh), nn = nnode(im, jm, gh);
+  cudaStream_t st = current_stream();
+  Stager sg(st);
+  const int hw = sg.in(w, np * 5 * 8), hnx = sg.in(nx, nn * 2 * 8), hny = sg.in(ny, nn * 2 * 8);
+  const int hvol = sg.in(vol, np * 8), hvolf = sg.in(volf, np * 2 * 8);
+  const int hrb = sg.inout(residub, np * 5 * 8), hwb = sg.out(wb, np * 5 * 8);
+  int rc = sg.commit();
+  if (rc) return rc;
+  AdjointArgs a{};
+  a.im = im; a.jm = jm; a.gh = gh;
+  a.phys = Phys{cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4};
+  a.w = sg.dev<double>(hw); a.nx = sg.dev<double>(hnx); a.ny = sg.dev<double>(hny);
+  a.vol = sg.dev<double>(hvol); a.volf = sg.dev<double>(hvolf);
+  a.rb = sg.dev<double>(hrb); a.wb = sg.dev<double>(hwb);
+  a.scratch = (double*)pool_get(POOL_SCRATCH, adjoint_scratch_doubles(im, jm, gh) * 8);
+  if (!a.scratch) return fail_arg("scratch allocation failed"), BCG_ERR_NOMEM;
+  cudaError_t e = run_adjoint(a, st);
+  if (e != cudaSuccess) return fail_cuda("flux_num_dnc5_2d_b", e);
+  return sg.finish();
 }
 
 // ---- boundary conditions (srcfv/borders/*.F90, srcfv/tangent/bc_*_d.f90) ----
@@ -387,3 +421,78 @@ int bcg_compute_maxnorm(double* norm, int* imax, int* jmax, const double* rhs, i
   return norm_call(NORM_MAX, norm, nullptr, imax, jmax, rhs, im, jm, gh);
 }
 }  // extern "C"
+
+// ===========================================================================
+// Batched colored Jacobian of the boundary-layer configuration
+// (BROADCAST_npz.py:1068-1137, 1206-1210; misc/PETSc_func.py:71-96)
+// ===========================================================================
+extern "C" int bcg_jacobian_dnc5_bl_csr(const double* w, const double* nx, const double* ny, const double* vol,
+                                        const double* volf, int gh, double cp, double cv, double prandtl, double gam,
+                                        double rgaz, double cs, double muref, double tref, double s_suth, double k2,
+                                        double k4, int im, int jm, const int* interf_ilo, const int* interf_jhi,
+                                        const int* interf_ihi, const int* interf_jlo, const double* field,
+                                        int lm_field, const double* wbd, int lm_wbd, const double* coefdiag,
+                                        double mini, int divide_by_vol, int* indptr, int* indices, double* data,
+                                        long long capacity, long long* nnz) {
+  if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
+  if (!dims_ok(im, jm, gh)) return fail_arg("jacobian: need gh == 3 and im, jm >= 6");
+  if (!nnz || !interf_ilo || !interf_jhi || !interf_ihi || !interf_jlo) return fail_arg("jacobian: null argument");
+  const size_t np = ncell(im, jm, gh), nn = nnode(im, jm, gh);
+  const int nrow = 5 * im * jm;
+  cudaStream_t st = current_stream();
+  Stager sg(st);
+  const int hw = sg.in(w, np * 5 * 8), hnx = sg.in(nx, nn * 2 * 8), hny = sg.in(ny, nn * 2 * 8);
+  const int hvol = sg.in(vol, np * 8), hvolf = sg.in(volf, np * 2 * 8);
+  const int hf = sg.in(field, (size_t)lm_field * gh * 5 * 8), hb = sg.in(wbd, (size_t)lm_wbd * 5 * 8);
+  const int hc = coefdiag ? sg.in(coefdiag, (size_t)im * jm * 8) : -1;
+  int rc = sg.commit();
+  if (rc) return rc;
+  JacobianArgs a{};
+  a.im = im; a.jm = jm; a.gh = gh;
+  a.phys = Phys{cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4};
+  a.w = sg.dev<double>(hw); a.nx = sg.dev<double>(hnx); a.ny = sg.dev<double>(hny);
+  a.vol = sg.dev<double>(hvol); a.volf = sg.dev<double>(hvolf);
+  a.relaxed = coefdiag ? 1 : 0;
+  a.coefdiag = hc >= 0 ? sg.dev<double>(hc) : nullptr;
+  a.mini = mini; a.divide_by_vol = divide_by_vol; a.capacity = capacity; a.nnz = nnz;
+  // boundary chain of the boundary-layer drivers (BROADCAST_npz.py:1079-1082)
+  const struct { int kind; const char* loc; const int* it; const double* aux; int lm; } chain[4] = {
+      {BC_INLET, "Ilo", interf_ilo, sg.dev<double>(hf), lm_field}, {BC_NOREF, "Jhi", interf_jhi, sg.dev<double>(hb), lm_wbd},
+      {BC_EXTRAP, "Ihi", interf_ihi, nullptr, 0}, {BC_WALL, "Jlo", interf_jlo, nullptr, 0}};
+  for (const auto& c : chain) {
+    BcArgs b{};
+    b.kind = c.kind; b.im = im; b.jm = jm; b.gh = gh; b.em = 5; b.lm = c.lm; b.gam = gam; b.aux = c.aux;
+    b.nx = a.nx; b.ny = a.ny;
+    if (!make_side(c.loc, c.it, &b.side)) return fail_arg("jacobian: bad interface");
+    a.bcs.push_back(b);
+  }
+  a.scratch = (double*)pool_get(POOL_SCRATCH, jacobian_scratch_doubles(im, jm, gh) * 8);
+  if (!a.scratch) return fail_arg("jacobian: scratch allocation failed"), BCG_ERR_NOMEM;
+  a.iscratch = (int*)pool_get(POOL_AUX, jacobian_iscratch_ints(im, jm) * 4);
+  if (!a.iscratch) return fail_arg("jacobian: scratch allocation failed"), BCG_ERR_NOMEM;
+  // outputs: used in place when on the device, else produced in a device buffer
+  const bool dev_out = is_device_ptr(indptr) && is_device_ptr(indices) && is_device_ptr(data);
+  if (dev_out) {
+    a.indptr = indptr; a.indices = indices; a.data = data;
+    rc = run_jacobian(a, st);
+    if (rc) return rc;
+    return sg.finish();
+  }
+  // host outputs: the device copy is sized to the worst case 245 entries per row
+  const long long cap = (long long)nrow * 245;
+  char* ob = (char*)pool_get(POOL_STAGE_OUT, (size_t)(nrow + 1) * 4 + (size_t)cap * 12 + 512);
+  if (!ob) return fail_arg("jacobian: output allocation failed"), BCG_ERR_NOMEM;
+  a.indptr = (int*)ob;
+  a.indices = (int*)(ob + (((size_t)(nrow + 1) * 4 + 255) & ~(size_t)255));
+  a.data = (double*)((char*)a.indices + (((size_t)cap * 4 + 255) & ~(size_t)255));
+  a.capacity = cap;
+  rc = run_jacobian(a, st);
+  if (rc) return rc;
+  if (*nnz > capacity) return fail_arg("jacobian: CSR capacity too small (see nnz)");
+  cudaError_t e = cudaMemcpyAsync(indptr, a.indptr, (size_t)(nrow + 1) * 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(indices, a.indices, (size_t)*nnz * 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(data, a.data, (size_t)*nnz * 8, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail_cuda("jacobian: output copy", e);
+  return sg.finish();
+}

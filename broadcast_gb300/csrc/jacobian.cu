@@ -1,0 +1,223 @@
+// Colored Jacobian assembly of the DNC5 residual, all seeds in one call.
+//
+// Reference: the Newton loop of BROADCAST_npz.py:1068-1137 -- for every seed
+// (m, l, k) in 5 x 7 x 7: testvector (misc/ComputeJacobian.f90:357), the
+// linearised boundary chain (:1079-1082), the tangent residual (:1085),
+// computejacobianfromjv_relaxed (:1127); then remove_zero_jac (|a| > 2e-16,
+// :129-135 and :1136), the COO -> CSR conversion of createMatPetscCSR
+// (misc/PETSc_func.py:71-96) and, for the stored matrix, Jac / vol of the row
+// cell (:1206-1210).
+//
+// GB300 layout of the work: seeds run in groups of 4 as one 4-direction
+// tangent pass (boundary chain and residual), their outputs are kept in HBM
+// (245 padded states: 5.2 GB at 1024 x 512), and the CSR is then built row by
+// row: the candidate columns of a row are known in closed form from the seed
+// formulas, so each row is enumerated directly in ascending column order --
+// no global sort, two passes (count, fill) around one exclusive scan.
+#include <cstdio>
+#include <vector>
+#include "assembly.h"
+#include "bc.h"
+#include "jacobian.h"
+#include "residual.h"
+#include "runtime.h"
+
+namespace bcg {
+
+namespace {
+
+// 4 seeds into 4 stacked padded tangent states (testvector for each)
+__global__ void k_seed4(double* __restrict__ wd, int nseed, const int* __restrict__ seeds, int gh, int im, int jm) {
+  const int ni = im + 2 * gh, nj = jm + 2 * gh;
+  const size_t ns = (size_t)ni * nj * 5;
+  const int step = 1 + 2 * gh;
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < ns * nseed; q += (size_t)gridDim.x * blockDim.x) {
+    const int s = (int)(q / ns);
+    const size_t r = q % ns;
+    const int i = (int)(r % ni) + 1 - gh, j = (int)((r / ni) % nj) + 1 - gh, v = (int)(r / ((size_t)ni * nj));
+    const int m = seeds[3 * s], l = seeds[3 * s + 1], k = seeds[3 * s + 2];
+    const bool on = (v == m) && j >= k + 1 && j <= jm && (j - k - 1) % step == 0 && i >= l + 1 && i <= im &&
+                    (i - l - 1) % step == 0;
+    wd[q] = on ? 1.0 : 0.0;
+  }
+}
+
+// One thread per row (cell i, j, variable e): enumerate the candidate entries
+// in ascending column order.  pass 0 counts the kept entries, pass 1 writes.
+__global__ void __launch_bounds__(128) k_csr_rows(int pass, const double* __restrict__ resd_all, int gh, int im,
+                                                  int jm, int relaxed, const double* __restrict__ coefdiag, double mini,
+                                                  const double* __restrict__ vol, int* __restrict__ count,
+                                                  const long long* __restrict__ rowptr, int* __restrict__ indices,
+                                                  double* __restrict__ data) {
+  const int nrow = 5 * im * jm;
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= nrow) return;
+  // reference row numbering: row = e + 5 (j-1) + 5 jm (i-1)
+  const int e = row % 5, j = 1 + (row / 5) % jm, i = 1 + row / (5 * jm);
+  const int ni = im + 2 * gh, nj = jm + 2 * gh;
+  const size_t np = (size_t)ni * nj;
+  const size_t cell = (size_t)(i + gh - 1) + (size_t)(j + gh - 1) * ni;
+  const double cd = relaxed ? coefdiag[(i - 1) + (size_t)(j - 1) * im] : 0.0;
+  const double vinv = vol ? 1.0 / vol[cell] : 1.0;
+  // per l and per k, the seed cell index (0-based) or -1; sort l and k by it
+  int li[7], lv[7], ki[7], kv[7];
+  const int step = 1 + 2 * gh;
+  for (int l = 0; l < 7; ++l) {
+    li[l] = l;
+    int vali;
+    if (l <= gh) vali = (i <= l + 1 + gh) ? l : (i - (l + 1) + gh) / step * step + l;
+    else vali = (i <= l - gh) ? im + 1 : (i - (l + 1) + gh) / step * step + l;
+    lv[l] = vali < im ? vali : -1;
+  }
+  for (int k = 0; k < 7; ++k) {
+    ki[k] = k;
+    const int valj = (j <= k + 1 + gh) ? k : (j - gh - (k + 1) + 2 * gh) / step * step + k;
+    kv[k] = valj < jm ? valj : -1;
+  }
+  // insertion sorts (7 elements)
+  for (int a = 1; a < 7; ++a)
+    for (int b = a; b > 0 && lv[b - 1] > lv[b]; --b) { int t = lv[b]; lv[b] = lv[b - 1]; lv[b - 1] = t; t = li[b]; li[b] = li[b - 1]; li[b - 1] = t; }
+  for (int a = 1; a < 7; ++a)
+    for (int b = a; b > 0 && kv[b - 1] > kv[b]; --b) { int t = kv[b]; kv[b] = kv[b - 1]; kv[b - 1] = t; t = ki[b]; ki[b] = ki[b - 1]; ki[b - 1] = t; }
+  long long out = pass ? rowptr[row] : 0;
+  int n = 0;
+  for (int a = 0; a < 7; ++a) {
+    if (lv[a] < 0) continue;
+    const int l = li[a];
+    for (int b = 0; b < 7; ++b) {
+      if (kv[b] < 0) continue;
+      const int k = ki[b];
+      for (int m = 0; m < 5; ++m) {
+        const int col = m + kv[b] * 5 + lv[a] * jm * 5;
+        const int seed = k + 7 * l + 49 * m;  // the reference's slot order
+        const double r = resd_all[(size_t)seed * np * 5 + (size_t)e * np + cell];
+        double v = (relaxed && col == row) ? cd - r : -r;
+        if (!(fabs(v) > mini)) continue;
+        if (pass) { indices[out + n] = col; data[out + n] = v * vinv; }
+        ++n;
+      }
+    }
+  }
+  if (!pass) count[row] = n;
+}
+
+// exclusive scan of per-row counts into int64 row pointers (3 kernels)
+constexpr int kScanBlock = 1024;
+__global__ void k_scan_block(const int* __restrict__ cnt, long long* __restrict__ ptr, long long* __restrict__ bsum,
+                             int n) {
+  __shared__ long long s[kScanBlock];
+  const int t = threadIdx.x, g = blockIdx.x * kScanBlock + t;
+  s[t] = (g < n) ? cnt[g] : 0;
+  __syncthreads();
+  for (int o = 1; o < kScanBlock; o <<= 1) {
+    long long x = (t >= o) ? s[t - o] : 0;
+    __syncthreads();
+    s[t] += x;
+    __syncthreads();
+  }
+  if (g < n) ptr[g] = s[t] - ((g < n) ? cnt[g] : 0);
+  if (t == kScanBlock - 1) bsum[blockIdx.x] = s[t];
+}
+__global__ void k_scan_sums(long long* __restrict__ bsum, int nb, long long* __restrict__ total) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  long long acc = 0;
+  for (int b = 0; b < nb; ++b) { const long long x = bsum[b]; bsum[b] = acc; acc += x; }
+  *total = acc;
+}
+__global__ void k_scan_add(long long* __restrict__ ptr, const long long* __restrict__ bsum, int n,
+                           const long long* __restrict__ total) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < n) ptr[g] += bsum[g / kScanBlock];
+  if (g == n) ptr[n] = *total;
+}
+__global__ void k_ptr_to_int(const long long* __restrict__ p, int* __restrict__ out, int n) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g <= n) out[g] = (int)p[g];
+}
+
+}  // namespace
+
+size_t jacobian_scratch_doubles(int im, int jm, int gh) {
+  const size_t np = (size_t)(im + 2 * gh) * (jm + 2 * gh);
+  return 245 * np * 5      // tangent outputs of every seed
+         + 4 * np * 5      // 4 seeded tangent states
+         + np * 5          // state copy written by the linearised boundary fills
+         + residual_scratch_doubles(im, jm, gh, 4);
+}
+
+int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
+  const int im = a.im, jm = a.jm, gh = a.gh;
+  const size_t np = (size_t)(im + 2 * gh) * (jm + 2 * gh);
+  double* resd_all = a.scratch;
+  double* wd4 = resd_all + 245 * np * 5;
+  double* wcopy = wd4 + 4 * np * 5;
+  double* rscr = wcopy + np * 5;
+  int* seeds_dev = a.iscratch;                        // 245 x 3
+  long long* rowptr = (long long*)(a.iscratch + 1024);  // nrow + 1 (8-byte aligned offset)
+  const int nrow = 5 * im * jm;
+  long long* bsum = rowptr + nrow + 2;
+  const int nb = (nrow + kScanBlock - 1) / kScanBlock;
+  long long* total = bsum + nb + 1;
+  int* count = (int*)(total + 2);
+  // seed table in the reference's loop order: m, then l, then k
+  std::vector<int> seeds(245 * 3);
+  for (int m = 0, s = 0; m < 5; ++m)
+    for (int l = 0; l < 7; ++l)
+      for (int k = 0; k < 7; ++k, ++s) { seeds[3 * s] = m; seeds[3 * s + 1] = l; seeds[3 * s + 2] = k; }
+  cudaError_t e = cudaMemcpyAsync(seeds_dev, seeds.data(), seeds.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return fail_cuda("jacobian: seed table", e);
+  e = cudaMemcpyAsync(wcopy, a.w, np * 5 * sizeof(double), cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return fail_cuda("jacobian: state copy", e);
+  ResidualArgs ra{};
+  ra.im = im; ra.jm = jm; ra.gh = gh; ra.phys = a.phys; ra.w = wcopy; ra.nx = a.nx; ra.ny = a.ny;
+  ra.vol = a.vol; ra.volf = a.volf; ra.dstride = np * 5; ra.scratch = rscr; ra.res = nullptr;
+  for (int s0 = 0; s0 < 245; s0 += 4) {
+    const int ns = s0 + 4 <= 245 ? 4 : 245 - s0;
+    k_seed4<<<1024, 256, 0, st>>>(wd4, ns, seeds_dev + 3 * s0, gh, im, jm);
+    // linearised boundary chain on (state copy, tangents), 1, 2 or 4 directions
+    for (int pi = 0; pi < 2; ++pi) {
+      const int off = pi == 0 ? 0 : (ns == 3 ? 2 : ns);
+      const int nd = pi == 0 ? (ns == 3 ? 2 : ns) : (ns == 3 ? 1 : 0);
+      if (nd == 0) break;
+      for (const BcArgs& b0 : a.bcs) {
+        BcArgs b = b0;
+        b.ndir = nd; b.w = wcopy; b.wd = wd4 + (size_t)off * np * 5; b.dstride = np * 5;
+        e = launch_bc(b, st);
+        if (e != cudaSuccess) return fail_cuda("jacobian: boundary fill", e);
+      }
+      ra.ndir = nd;
+      ra.wd = wd4 + (size_t)off * np * 5;
+      ra.resd = resd_all + (size_t)(s0 + off) * np * 5;
+      e = run_residual(ra, st);
+      if (e != cudaSuccess) return fail_cuda("jacobian: tangent residual", e);
+    }
+  }
+  // CSR: count, scan, fill
+  const int B = 128;
+  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(0, resd_all, gh, im, jm, a.relaxed, a.coefdiag, a.mini,
+                                             a.divide_by_vol ? a.vol : nullptr, count, nullptr, nullptr, nullptr);
+  k_scan_block<<<nb, kScanBlock, 0, st>>>(count, rowptr, bsum, nrow);
+  k_scan_sums<<<1, 1, 0, st>>>(bsum, nb, total);
+  k_scan_add<<<(nrow + 1 + 255) / 256, 256, 0, st>>>(rowptr, bsum, nrow, total);
+  long long nnz = 0;
+  e = cudaMemcpyAsync(&nnz, total, sizeof nnz, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail_cuda("jacobian: nnz", e);
+  *a.nnz = nnz;
+  if (nnz > a.capacity) return fail_arg("jacobian: CSR capacity too small (see nnz)");
+  if (nnz >= (1LL << 31)) return fail_arg("jacobian: nnz exceeds 32-bit CSR indices");
+  k_ptr_to_int<<<(nrow + 1 + 255) / 256, 256, 0, st>>>(rowptr, a.indptr, nrow);
+  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(1, resd_all, gh, im, jm, a.relaxed, a.coefdiag, a.mini,
+                                             a.divide_by_vol ? a.vol : nullptr, count, rowptr, a.indices, a.data);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return fail_cuda("jacobian: csr", e);
+  return BCG_OK;
+}
+
+size_t jacobian_iscratch_ints(int im, int jm) {
+  const size_t nrow = 5 * (size_t)im * jm;
+  const size_t nb = (nrow + kScanBlock - 1) / kScanBlock;
+  return 1024 + 2 * (nrow + 2 + nb + 1 + 2) + nrow + 64;
+}
+
+}  // namespace bcg

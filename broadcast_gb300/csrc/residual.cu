@@ -395,6 +395,15 @@ static cudaError_t run_residual_t(const ResidualArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+void launch_primal_passes(const Ext& e, const Coef& c, const double* w, double* pr, double* gr, const double* nx,
+                          const double* ny, const double* vol, cudaStream_t st) {
+  const int B = 256;
+  k_prim<double><<<(unsigned)((e.np + B - 1) / B), B, 0, st>>>(e, c, State<double>{w}, Scratch<double>{pr, e.np});
+  if (c.k2 != 0.0)
+    k_grad<double><<<(unsigned)((e.im * e.jm + B - 1) / B), B, 0, st>>>(e, c, Scratch<double>{pr, e.np},
+                                                                        Scratch<double>{gr, e.np}, nx, ny, vol);
+}
+
 size_t residual_scratch_doubles(int im, int jm, int gh, int ndir) {
   const Ext e = make_ext(im, jm, gh);
   const size_t nn = (size_t)(im + 1) * (jm + 1);

@@ -23,6 +23,10 @@ struct ResidualArgs {
 };
 
 size_t residual_scratch_doubles(int im, int jm, int gh, int ndir);
+// primitives (and, when k2 != 0, gradients) of the primal state into scratch
+// fields laid out as F_* and G_* planes of np doubles
+void launch_primal_passes(const Ext& e, const Coef& c, const double* w, double* pr, double* gr, const double* nx,
+                          const double* ny, const double* vol, cudaStream_t st);
 cudaError_t run_residual(const ResidualArgs& a, cudaStream_t st);
 
 }  // namespace bcg

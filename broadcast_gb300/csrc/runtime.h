@@ -24,7 +24,7 @@ const char* last_error();
 
 // Grow-only device buffer per device and purpose.  Calls are serialised on the
 // library stream, so one buffer per purpose is reused across calls.
-enum PoolKind { POOL_SCRATCH = 0, POOL_STAGE = 1, POOL_AUX = 2, POOL_COUNT = 3 };
+enum PoolKind { POOL_SCRATCH = 0, POOL_STAGE = 1, POOL_AUX = 2, POOL_STAGE_OUT = 3, POOL_COUNT = 4 };
 void* pool_get(PoolKind k, size_t bytes);
 
 bool is_device_ptr(const void* p);

@@ -68,6 +68,15 @@ int bcg_flux_num_dnc5_2d_dn(double* residu, double* residud, const double* w, co
                             double prandtl, double gam, double rgaz, double cs, double muref, double tref,
                             double s_suth, double k2, double k4, int im, int jm);
 
+/* srcfv/adjoint/flux_num_dnc5_b.f90:15 (FLUX_NUM_DNC5_2D_B): wb = (dR/dw)^T residub
+ * on every padded cell (wb overwritten); the interior of residub is zeroed on
+ * return, as in the reference; residu is unused. */
+int bcg_flux_num_dnc5_2d_b(double* residu, double* residub, const double* w, double* wb, const double* x0,
+                           const double* y0, const double* nx, const double* ny, const double* xc, const double* yc,
+                           const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
+                           double gam, double rgaz, double cs, double muref, double tref, double s_suth, double k2,
+                           double k4, int im, int jm);
+
 /* ---- boundary conditions ---------------------------------------------------- */
 /* srcfv/borders/bc_wall_viscous.F90:2 ; tangent/bc_wall_viscous_d.f90:11 */
 int bcg_bc_wall_viscous_adia_2d(double* w, const char* loc, double gam, const int* interf, int gh, int im, int jm);
@@ -120,6 +129,23 @@ int bcg_computejacobianfromjv_relaxed_withjnandcheck(double* jac, int* ia, int* 
                                                      const double* coefdiag, double mini, int n);
 int bcg_computejacobianfromdz(double* jac, int* ia, int* ja, const double* dz, int m, int l, int k, int gh, int im,
                               int jm, long long nbentry);
+
+/* Batched assembly of the boundary-layer configuration's Jacobian, all 245
+ * colour seeds in one call, as CSR (the loop of BROADCAST_npz.py:1068-1137:
+ * testvector, the linearised boundary chain inlet Ilo / no-reflexion Jhi /
+ * extrapolation Ihi / wall Jlo, flux_num_dnc5_2d_d, computejacobianfromjv
+ * [_relaxed when coefdiag is not NULL], remove_zero_jac keeping |a| > mini; the
+ * COO -> CSR of misc/PETSc_func.py:71-96; with divide_by_vol, the Jacvol scaling
+ * of BROADCAST_npz.py:1206-1210).  w must hold the primal boundary fills.  Rows
+ * are 5*im*jm, columns sorted within a row; *nnz receives the entry count (also
+ * when capacity is too small, which returns -1). */
+int bcg_jacobian_dnc5_bl_csr(const double* w, const double* nx, const double* ny, const double* vol,
+                             const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz,
+                             double cs, double muref, double tref, double s_suth, double k2, double k4, int im, int jm,
+                             const int* interf_ilo, const int* interf_jhi, const int* interf_ihi,
+                             const int* interf_jlo, const double* field, int lm_field, const double* wbd, int lm_wbd,
+                             const double* coefdiag, double mini, int divide_by_vol, int* indptr, int* indices,
+                             double* data, long long capacity, long long* nnz);
 
 /* ---- norms (srcfv/norm.F90) ---------------------------------------------------- */
 /* :2 compute_norml2 ; :34 compute_norml2inf ; :79 compute_maxnorm (5-vectors) */

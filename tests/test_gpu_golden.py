@@ -1,0 +1,102 @@
+"""The CUDA path against the golden fixtures made from the reference's own
+routines (tests/golden/make_golden.py): boundary fills, residual, tangent,
+adjoint, norms and the colored-Jacobian indexing."""
+import numpy as np
+import pytest
+
+from tests import golden_io as G
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+
+def _args(c):
+    g, ph = c["grid"], c["phys"]
+    return (g["x0"], g["y0"], g["nx"], g["ny"], g["xc"], g["yc"], g["vol"], g["volf"], g["gh"], ph["cp"], ph["cv"],
+            ph["prandtl"], ph["gam"], ph["rgaz"], ph["cs"], ph["muref"], ph["tref"], ph["s_suth"], ph["k2"], ph["k4"])
+
+
+@pytest.mark.parametrize("name", G.CASES)
+def test_boundary_fills(name):
+    d = G.load(name)
+    c = G.as_case(d)
+    w = d["w_raw"].copy(order="F")
+    H.lib_bcs(c, w)
+    assert np.abs(w - d["w"]).max() / np.abs(d["w"]).max() < 1e-13
+
+
+@pytest.mark.parametrize("name", G.CASES)
+def test_residual(name):
+    from broadcast_gb300.srcfv import f_sch
+    d = G.load(name)
+    c = G.as_case(d)
+    res = np.zeros_like(c["w"])
+    f_sch.flux_num_dnc5_2d(res, c["w"], *_args(c))
+    assert H.rel_err(res, d["res"], H.flux_scale(c, c["w"])) < 1e-12
+
+
+@pytest.mark.parametrize("name", G.CASES)
+def test_tangent(name):
+    from broadcast_gb300.srcfv import f_lin
+    d = G.load(name)
+    c = G.as_case(d)
+    for k in range(d["wd"].shape[0]):
+        res, resd = np.zeros_like(c["w"]), np.zeros_like(c["w"])
+        f_lin.flux_num_dnc5_2d_d(res, resd, c["w"], np.asfortranarray(d["wd"][k]), *_args(c))
+        sc = np.abs(H.interior(d["resd"][k])).reshape(-1, 5).max(0)
+        assert H.rel_err(resd, d["resd"][k], sc) < 1e-11
+
+
+@pytest.mark.parametrize("name", G.CASES)
+def test_adjoint(name):
+    from broadcast_gb300.srcfv import f_adj
+    d = G.load(name)
+    c = G.as_case(d)
+    wb = np.zeros_like(c["w"])
+    f_adj.flux_num_dnc5_2d_b(None, d["rb"].copy(order="F"), c["w"], wb, *_args(c))
+    sc = np.abs(d["wb"]).reshape(-1, 5).max(0)
+    assert (np.abs(wb - d["wb"]).reshape(-1, 5).max(0) / sc).max() < 1e-11
+
+
+@pytest.mark.parametrize("name", G.CASES)
+def test_norms(name):
+    from broadcast_gb300.srcfv import f_norm
+    d = G.load(name)
+    im, jm = int(d["im"]), int(d["jm"])
+    a, b = f_norm.compute_norml2(d["res"], im, jm, 3)
+    assert np.allclose(a, d["norml2"], rtol=1e-13, atol=0) and np.allclose(b, d["nmoy"], rtol=1e-13, atol=0)
+    _, ninf = f_norm.compute_norml2inf(d["res"], im, jm, 3)
+    assert np.allclose(ninf, d["ninf"], rtol=1e-12, atol=0)
+    m, i, j = f_norm.compute_maxnorm(d["res"], im, jm, 3)
+    assert np.array_equal(m, d["maxnorm"]) and np.array_equal(i, d["imax"]) and np.array_equal(j, d["jmax"])
+
+
+def test_colored_indexing():
+    from broadcast_gb300.misc import f_misc
+    d = G.load("indexing_16x11")
+    im, jm, gh = int(d["im"]), int(d["jm"]), int(d["gh"])
+    nb = im * jm * 49 * 25
+    for name in ("computejacobianfromjv", "computejacobianfromjv_relaxed", "computejacobianfromjv_relaxed_withjn",
+                 "computejacobianfromjv_withjn", "computejacobianfromdz"):
+        jac, ia, ja = np.zeros(nb), np.zeros(nb, np.int32), np.zeros(nb, np.int32)
+        fn = getattr(f_misc, name)
+        for (m, l, k) in d["seeds"]:
+            if "relaxed" in name:
+                fn(jac, ia, ja, d["resd"], int(m), int(l), int(k), gh, d["coefdiag"])
+            else:
+                fn(jac, ia, ja, d["resd"], int(m), int(l), int(k), gh)
+        assert np.array_equal(jac, d[name + "_jac"]), name
+        assert np.array_equal(ia, d[name + "_ia"]) and np.array_equal(ja, d[name + "_ja"]), name
+    jac, ia, ja = np.zeros(2 * nb), np.zeros(2 * nb, np.int32), np.zeros(2 * nb, np.int32)
+    for n in (0, 1):
+        for (m, l, k) in d["seeds"]:
+            f_misc.computejacobianfromjv_relaxed_withjnandcheck(jac, ia, ja, d["resd"], int(m), int(l), int(k), gh,
+                                                                d["coefdiag"], 2e-16, n)
+    assert np.array_equal(jac, d["check_jac"]) and np.array_equal(ia, d["check_ia"]) and np.array_equal(ja, d["check_ja"])
+    for q, (m, l, k) in enumerate(d["seeds"]):
+        wd = np.zeros((im + 6, jm + 6, 5), order="F")
+        f_misc.testvector(wd, int(m), int(l), int(k), gh)
+        assert np.array_equal(wd, d["testvectors"][2 * q])
+        wd[:] = 0
+        f_misc.testvector_partial(wd, int(m), int(l), int(k), gh, im, jm, 2, im - 2, 0, jm - 1)
+        assert np.array_equal(wd, d["testvectors"][2 * q + 1])
