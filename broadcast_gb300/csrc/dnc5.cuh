@@ -66,7 +66,13 @@ inline Ext make_ext(int im, int jm, int gh) {
 }
 
 // Fields of the primitive scratch (pass 1)
-enum PField { F_U = 0, F_V, F_W, F_T, F_P, F_MU, F_F2, F_F3, F_F4, F_F5, F_G2, F_G3, F_G4, F_G5, F_NPRIM };
+enum PField {
+  F_U = 0, F_V, F_W, F_T, F_P, F_MU, F_F2, F_F3, F_F4, F_F5, F_G2, F_G3, F_G4, F_G5,
+  F_SR, F_SU, F_SV, F_SC,  // sqrt(rho) and sqrt(rho) * (u, v, c^2) for the Roe average
+  F_NPRIM
+};
+// Fields of the 4-point interpolation scratch (pass 1b): QI for u v w T mu, then QJ
+enum QField { Q_I = 0, Q_J = 5, Q_NQ = 10 };
 // Fields of the gradient scratch (pass 2)
 enum GField { G_UX = 0, G_UY, G_VX, G_VY, G_NGRAD };
 

@@ -11,8 +11,8 @@
 // exits.  Nothing here calls cudaMalloc, cudaFree or any allocating routine.
 //
 // Limits and sharing rules:
-//  - the scratch holds kNoAllocScratchDoubles doubles (16 MiB); a grid needs
-//    18*(im+2gh)*(jm+2gh) + 10*(im+1)*(jm+1) of them (e.g. 256 x 256 or
+//  - the scratch holds kNoAllocScratchDoubles doubles (32 MiB); a grid needs
+//    32*(im+2gh)*(jm+2gh) + 10*(im+1)*(jm+1) of them (e.g. 256 x 256 or
 //    400 x 150 fit), larger grids are rejected with BCG_ERR_ARG;
 //  - every call on a device uses the same array, which keeps the previous
 //    call's contents.  The residual kernels write every scratch entry they
@@ -29,7 +29,7 @@
 
 namespace {
 
-constexpr size_t kNoAllocScratchDoubles = (size_t)2 << 20;  // 2 Mi doubles = 16 MiB
+constexpr size_t kNoAllocScratchDoubles = (size_t)4 << 20;  // 4 Mi doubles = 32 MiB
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
 
 constexpr int kMaxDevices = 64;
@@ -69,8 +69,8 @@ int bcg_flux_num_dnc5_2d_noalloc(double* residu, const double* w, const double* 
   if (gh != 3 || im < 6 || jm < 6) return fail_arg("flux_num_dnc5_2d_noalloc: need gh == 3 and im, jm >= 6");
   const size_t need = residual_scratch_doubles(im, jm, gh, 0);
   if (need > kNoAllocScratchDoubles)
-    return fail_arg("flux_num_dnc5_2d_noalloc: grid too large for the fixed 16 MiB scratch "
-                    "(needs 18*(im+6)*(jm+6) + 10*(im+1)*(jm+1) <= 2097152 doubles)");
+    return fail_arg("flux_num_dnc5_2d_noalloc: grid too large for the fixed 32 MiB scratch "
+                    "(needs 32*(im+6)*(jm+6) + 10*(im+1)*(jm+1) <= 4194304 doubles)");
   const void* arrays[] = {residu, w, nx, ny, vol, volf};
   for (const void* a : arrays)
     if (!is_device_ptr(a)) return fail_arg("flux_num_dnc5_2d_noalloc: every array must be a device pointer");

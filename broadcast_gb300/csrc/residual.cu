@@ -31,6 +31,41 @@ __global__ void __launch_bounds__(256) k_prim(Ext e, Coef c, State<S> w, Scratch
   pr.st(F_F2, q, ru * u + p); pr.st(F_F3, q, ru * v); pr.st(F_F4, q, ru * ww); pr.st(F_F5, q, ru * htot);
   pr.st(F_G2, q, rv * u); pr.st(F_G3, q, rv * v + p); pr.st(F_G4, q, rv * ww); pr.st(F_G5, q, rv * htot);
   pr.st(F_MU, q, c.betas / (t + c.s_suth) * sqrt_t(t) * t);
+  // Roe-average ingredients: sqrt(rho), and sqrt(rho) times u, v and c^2
+  const S sr = sqrt_t(ro);
+  pr.st(F_SR, q, sr);
+  pr.st(F_SU, q, sr * u);
+  pr.st(F_SV, q, sr * v);
+  pr.st(F_SC, q, sr * (c.c2fac * t));
+}
+
+// ---------------------------------------------------------------------------
+// pass 1b: the 4-point interpolations (-a + 9b + 9c - d) that the 4th-order
+// viscous fluxes read, once per face location instead of once per face use:
+//   QI at i-face location (i, j): cells i-2..i+1 of row j,  i in [1, im+1], j in [-1, jm+2]
+//   QJ at j-face location (i, j): rows j-2..j+1 of column i, i in [-1, im+2], j in [2, jm+1]
+// for u, v, w, T and mu (rhs/flux_visqueux_o4_i.F, _j.F).
+template <class S>
+__global__ void __launch_bounds__(256) k_qrows(Ext e, Scratch<S> pr, Scratch<S> qr) {
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= e.np) return;
+  const int i = (int)(q % e.ni) + 1 - e.gh, j = (int)(q / e.ni) + 1 - e.gh;
+  const int fl[5] = {F_U, F_V, F_W, F_T, F_MU};
+  const int di = 1, dj = e.ni;
+  if (i >= 1 && i <= e.im + 1 && j >= -1 && j <= e.jm + 2) {
+#pragma unroll
+    for (int a = 0; a < 5; ++a) {
+      const S x0 = pr.ld(fl[a], q - 2 * di), x1 = pr.ld(fl[a], q - di), x2 = pr.ld(fl[a], q), x3 = pr.ld(fl[a], q + di);
+      qr.st(Q_I + a, q, 9.0 * (x1 + x2) - (x0 + x3));
+    }
+  }
+  if (i >= -1 && i <= e.im + 2 && j >= 2 && j <= e.jm + 1) {
+#pragma unroll
+    for (int a = 0; a < 5; ++a) {
+      const S x0 = pr.ld(fl[a], q - 2 * dj), x1 = pr.ld(fl[a], q - dj), x2 = pr.ld(fl[a], q), x3 = pr.ld(fl[a], q + dj);
+      qr.st(Q_J + a, q, 9.0 * (x1 + x2) - (x0 + x3));
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -68,7 +103,7 @@ struct FaceCtx {
   Ext e;
   Coef c;
   State<S> w;
-  Scratch<S> pr, gr;
+  Scratch<S> pr, gr, qr;
   const double* __restrict__ nx;
   const double* __restrict__ ny;
   const double* __restrict__ vol;
@@ -76,6 +111,7 @@ struct FaceCtx {
 
   BCG_HD S W(int i, int j, int v) const { return w((size_t)e.cidx(i, j) + (size_t)(v - 1) * e.np); }
   BCG_HD S P(int f, int i, int j) const { return pr.ld(f, e.cidx(i, j)); }
+  BCG_HD S Q(int f, int i, int j) const { return qr.ld(f, e.cidx(i, j)); }
   // Euler flux components f(.,.,v), g(.,.,v) with f1 = rho u, g1 = rho v
   BCG_HD S Fl(int v, int i, int j) const { return v == 1 ? W(i, j, 2) : P(F_F2 + v - 2, i, j); }
   BCG_HD S Gl(int v, int i, int j) const { return v == 1 ? W(i, j, 3) : P(F_G2 + v - 2, i, j); }
@@ -106,13 +142,18 @@ struct FaceCtx {
     gv[3] = lambda * ty + uu * gv[0] + vv * gv[1] + ww * gv[2];
   }
 
-  // viscous flux through i-face (i,j): o4 (rhs/flux_visqueux_o4_i.F) or o2
+  // Viscous flux through i-face (i,j): o4 (rhs/flux_visqueux_o4_i.F) or o2
+  // (rows 1-2).  The face gradients are linear in four point values N, S, E,
+  // O; the point stencils' constant factors (1/24, ccross, 1/4) and the face
+  // volume are folded into the geometric coefficients, and the cross rows come
+  // from the QI interpolations.
   BCG_HD void visc_i(int i, int j, bool o2, S fv[4], S gv[4]) const {
     const double volm1 = VOLF(i, j, 1);
-    const double nxN = 0.5 * (NX(i + 1, j, 1) + NX(i, j, 1)), nxS = -(0.5 * (NX(i - 1, j, 1) + NX(i, j, 1)));
-    const double nxO = 0.5 * (NX(i - 1, j + 1, 2) + NX(i, j + 1, 2)), nxE = -(0.5 * (NX(i - 1, j, 2) + NX(i, j, 2)));
-    const double nyN = 0.5 * (NY(i + 1, j, 1) + NY(i, j, 1)), nyS = -(0.5 * (NY(i - 1, j, 1) + NY(i, j, 1)));
-    const double nyO = 0.5 * (NY(i - 1, j + 1, 2) + NY(i, j + 1, 2)), nyE = -(0.5 * (NY(i - 1, j, 2) + NY(i, j, 2)));
+    const double fN = o2 ? volm1 : volm1 / 24.0, fE = o2 ? 0.25 * volm1 : c.ccross * volm1;
+    const double nxN = 0.5 * (NX(i + 1, j, 1) + NX(i, j, 1)) * fN, nxS = -(0.5 * (NX(i - 1, j, 1) + NX(i, j, 1))) * fN;
+    const double nxO = 0.5 * (NX(i - 1, j + 1, 2) + NX(i, j + 1, 2)) * fE, nxE = -(0.5 * (NX(i - 1, j, 2) + NX(i, j, 2))) * fE;
+    const double nyN = 0.5 * (NY(i + 1, j, 1) + NY(i, j, 1)) * fN, nyS = -(0.5 * (NY(i - 1, j, 1) + NY(i, j, 1))) * fN;
+    const double nyO = 0.5 * (NY(i - 1, j + 1, 2) + NY(i, j + 1, 2)) * fE, nyE = -(0.5 * (NY(i - 1, j, 2) + NY(i, j, 2))) * fE;
     S gx[4], gy[4];
     const int fl[4] = {F_U, F_V, F_W, F_T};
 #pragma unroll
@@ -120,49 +161,42 @@ struct FaceCtx {
       const int f = fl[a];
       S vN, vS, vE, vO;
       if (!o2) {
-        const double T24 = 1.0 / 24.0, cc = c.ccross;
-        vN = T24 * (-P(f, i + 1, j) + 26.0 * P(f, i, j) - P(f, i - 1, j));
-        vS = T24 * (-P(f, i, j) + 26.0 * P(f, i - 1, j) - P(f, i - 2, j));
-        const S r0 = q4(P(f, i - 2, j - 2), P(f, i - 1, j - 2), P(f, i, j - 2), P(f, i + 1, j - 2));
-        const S r1 = q4(P(f, i - 2, j - 1), P(f, i - 1, j - 1), P(f, i, j - 1), P(f, i + 1, j - 1));
-        const S r2 = q4(P(f, i - 2, j), P(f, i - 1, j), P(f, i, j), P(f, i + 1, j));
-        const S r3 = q4(P(f, i - 2, j + 1), P(f, i - 1, j + 1), P(f, i, j + 1), P(f, i + 1, j + 1));
-        const S r4 = q4(P(f, i - 2, j + 2), P(f, i - 1, j + 2), P(f, i, j + 2), P(f, i + 1, j + 2));
-        vE = cc * (-r0 + 7.0 * r1 + 7.0 * r2 - r3);
-        vO = cc * (-r1 + 7.0 * r2 + 7.0 * r3 - r4);
+        vN = 26.0 * P(f, i, j) - (P(f, i + 1, j) + P(f, i - 1, j));
+        vS = 26.0 * P(f, i - 1, j) - (P(f, i, j) + P(f, i - 2, j));
+        vE = 7.0 * (Q(Q_I + a, i, j - 1) + Q(Q_I + a, i, j)) - (Q(Q_I + a, i, j - 2) + Q(Q_I + a, i, j + 1));
+        vO = 7.0 * (Q(Q_I + a, i, j) + Q(Q_I + a, i, j + 1)) - (Q(Q_I + a, i, j - 1) + Q(Q_I + a, i, j + 2));
       } else {
         vN = P(f, i, j);
         vS = P(f, i - 1, j);
-        vE = 0.25 * (P(f, i, j) + P(f, i, j - 1) + P(f, i - 1, j) + P(f, i - 1, j - 1));
-        vO = 0.25 * (P(f, i, j) + P(f, i, j + 1) + P(f, i - 1, j) + P(f, i - 1, j + 1));
+        vE = (P(f, i, j) + P(f, i, j - 1)) + (P(f, i - 1, j) + P(f, i - 1, j - 1));
+        vO = (P(f, i, j) + P(f, i, j + 1)) + (P(f, i - 1, j) + P(f, i - 1, j + 1));
       }
-      gx[a] = (vN * nxN + vS * nxS + vO * nxO + vE * nxE) * volm1;
-      gy[a] = (vN * nyN + vS * nyS + vO * nyO + vE * nyE) * volm1;
+      gx[a] = vN * nxN + vS * nxS + vO * nxO + vE * nxE;
+      gy[a] = vN * nyN + vS * nyS + vO * nyO + vE * nyE;
     }
-    S uu, vv, ww, mmu, lambda;
+    S uu, vv, ww, mmu;
     if (!o2) {
-      uu = 0.0625 * q4(P(F_U, i - 2, j), P(F_U, i - 1, j), P(F_U, i, j), P(F_U, i + 1, j));
-      vv = 0.0625 * q4(P(F_V, i - 2, j), P(F_V, i - 1, j), P(F_V, i, j), P(F_V, i + 1, j));
-      ww = 0.0625 * q4(P(F_W, i - 2, j), P(F_W, i - 1, j), P(F_W, i, j), P(F_W, i + 1, j));
-      mmu = 0.0625 * q4(P(F_MU, i - 2, j), P(F_MU, i - 1, j), P(F_MU, i, j), P(F_MU, i + 1, j));
-      lambda = mmu * c.cpprandtl;
+      uu = 0.0625 * Q(Q_I + 0, i, j);
+      vv = 0.0625 * Q(Q_I + 1, i, j);
+      ww = 0.0625 * Q(Q_I + 2, i, j);
+      mmu = 0.0625 * Q(Q_I + 4, i, j);
     } else {
       uu = 0.5 * (P(F_U, i, j) + P(F_U, i - 1, j));
       vv = 0.5 * (P(F_V, i, j) + P(F_V, i - 1, j));
       ww = 0.5 * (P(F_W, i, j) + P(F_W, i - 1, j));
       mmu = 0.5 * (P(F_MU, i, j) + P(F_MU, i - 1, j));
-      lambda = 0.5 * (P(F_MU, i, j) + P(F_MU, i - 1, j)) * c.cpprandtl;
     }
-    visc_fluxes(mmu, lambda, uu, vv, ww, gx[0], gy[0], gx[1], gy[1], gx[2], gy[2], gx[3], gy[3], fv, gv);
+    visc_fluxes(mmu, mmu * c.cpprandtl, uu, vv, ww, gx[0], gy[0], gx[1], gy[1], gx[2], gy[2], gx[3], gy[3], fv, gv);
   }
 
-  // viscous flux through j-face (i,j): o4 (rhs/flux_visqueux_o4_j.F) or o2
+  // Viscous flux through j-face (i,j): o4 (rhs/flux_visqueux_o4_j.F) or o2 (row 2).
   BCG_HD void visc_j(int i, int j, bool o2, S fv[4], S gv[4]) const {
     const double volm1 = VOLF(i, j, 2);
-    const double nxN = 0.5 * (NX(i + 1, j - 1, 1) + NX(i + 1, j, 1)), nxS = -(0.5 * (NX(i, j - 1, 1) + NX(i, j, 1)));
-    const double nxO = 0.5 * (NX(i, j + 1, 2) + NX(i, j, 2)), nxE = -(0.5 * (NX(i, j - 1, 2) + NX(i, j, 2)));
-    const double nyN = 0.5 * (NY(i + 1, j - 1, 1) + NY(i + 1, j, 1)), nyS = -(0.5 * (NY(i, j - 1, 1) + NY(i, j, 1)));
-    const double nyO = 0.5 * (NY(i, j + 1, 2) + NY(i, j, 2)), nyE = -(0.5 * (NY(i, j - 1, 2) + NY(i, j, 2)));
+    const double fN = o2 ? 0.25 * volm1 : c.ccross * volm1, fE = o2 ? volm1 : volm1 / 24.0;
+    const double nxN = 0.5 * (NX(i + 1, j - 1, 1) + NX(i + 1, j, 1)) * fN, nxS = -(0.5 * (NX(i, j - 1, 1) + NX(i, j, 1))) * fN;
+    const double nxO = 0.5 * (NX(i, j + 1, 2) + NX(i, j, 2)) * fE, nxE = -(0.5 * (NX(i, j - 1, 2) + NX(i, j, 2))) * fE;
+    const double nyN = 0.5 * (NY(i + 1, j - 1, 1) + NY(i + 1, j, 1)) * fN, nyS = -(0.5 * (NY(i, j - 1, 1) + NY(i, j, 1))) * fN;
+    const double nyO = 0.5 * (NY(i, j + 1, 2) + NY(i, j, 2)) * fE, nyE = -(0.5 * (NY(i, j - 1, 2) + NY(i, j, 2))) * fE;
     S gx[4], gy[4];
     const int fl[4] = {F_U, F_V, F_W, F_T};
 #pragma unroll
@@ -170,40 +204,32 @@ struct FaceCtx {
       const int f = fl[a];
       S vN, vS, vE, vO;
       if (!o2) {
-        const double T24 = 1.0 / 24.0, cc = c.ccross;
-        const S k0 = q4(P(f, i - 2, j - 2), P(f, i - 2, j - 1), P(f, i - 2, j), P(f, i - 2, j + 1));
-        const S k1 = q4(P(f, i - 1, j - 2), P(f, i - 1, j - 1), P(f, i - 1, j), P(f, i - 1, j + 1));
-        const S k2 = q4(P(f, i, j - 2), P(f, i, j - 1), P(f, i, j), P(f, i, j + 1));
-        const S k3 = q4(P(f, i + 1, j - 2), P(f, i + 1, j - 1), P(f, i + 1, j), P(f, i + 1, j + 1));
-        const S k4 = q4(P(f, i + 2, j - 2), P(f, i + 2, j - 1), P(f, i + 2, j), P(f, i + 2, j + 1));
-        vN = cc * (-k1 + 7.0 * k2 + 7.0 * k3 - k4);
-        vS = cc * (-k0 + 7.0 * k1 + 7.0 * k2 - k3);
-        vE = T24 * (-P(f, i, j) + 26.0 * P(f, i, j - 1) - P(f, i, j - 2));
-        vO = T24 * (-P(f, i, j + 1) + 26.0 * P(f, i, j) - P(f, i, j - 1));
+        vN = 7.0 * (Q(Q_J + a, i, j) + Q(Q_J + a, i + 1, j)) - (Q(Q_J + a, i - 1, j) + Q(Q_J + a, i + 2, j));
+        vS = 7.0 * (Q(Q_J + a, i - 1, j) + Q(Q_J + a, i, j)) - (Q(Q_J + a, i - 2, j) + Q(Q_J + a, i + 1, j));
+        vE = 26.0 * P(f, i, j - 1) - (P(f, i, j) + P(f, i, j - 2));
+        vO = 26.0 * P(f, i, j) - (P(f, i, j + 1) + P(f, i, j - 1));
       } else {
-        vN = 0.25 * (P(f, i, j) + P(f, i + 1, j) + P(f, i, j - 1) + P(f, i + 1, j - 1));
-        vS = 0.25 * (P(f, i, j) + P(f, i - 1, j) + P(f, i, j - 1) + P(f, i - 1, j - 1));
+        vN = (P(f, i, j) + P(f, i + 1, j)) + (P(f, i, j - 1) + P(f, i + 1, j - 1));
+        vS = (P(f, i, j) + P(f, i - 1, j)) + (P(f, i, j - 1) + P(f, i - 1, j - 1));
         vO = P(f, i, j);
         vE = P(f, i, j - 1);
       }
-      gx[a] = (vN * nxN + vS * nxS + vO * nxO + vE * nxE) * volm1;
-      gy[a] = (vN * nyN + vS * nyS + vO * nyO + vE * nyE) * volm1;
+      gx[a] = vN * nxN + vS * nxS + vO * nxO + vE * nxE;
+      gy[a] = vN * nyN + vS * nyS + vO * nyO + vE * nyE;
     }
-    S uu, vv, ww, mmu, lambda;
+    S uu, vv, ww, mmu;
     if (!o2) {
-      uu = 0.0625 * q4(P(F_U, i, j - 2), P(F_U, i, j - 1), P(F_U, i, j), P(F_U, i, j + 1));
-      vv = 0.0625 * q4(P(F_V, i, j - 2), P(F_V, i, j - 1), P(F_V, i, j), P(F_V, i, j + 1));
-      ww = 0.0625 * q4(P(F_W, i, j - 2), P(F_W, i, j - 1), P(F_W, i, j), P(F_W, i, j + 1));
-      mmu = 0.0625 * q4(P(F_MU, i, j - 2), P(F_MU, i, j - 1), P(F_MU, i, j), P(F_MU, i, j + 1));
-      lambda = mmu * c.cpprandtl;
+      uu = 0.0625 * Q(Q_J + 0, i, j);
+      vv = 0.0625 * Q(Q_J + 1, i, j);
+      ww = 0.0625 * Q(Q_J + 2, i, j);
+      mmu = 0.0625 * Q(Q_J + 4, i, j);
     } else {
       uu = 0.5 * (P(F_U, i, j) + P(F_U, i, j - 1));
       vv = 0.5 * (P(F_V, i, j) + P(F_V, i, j - 1));
       ww = 0.5 * (P(F_W, i, j) + P(F_W, i, j - 1));
       mmu = 0.5 * (P(F_MU, i, j) + P(F_MU, i, j - 1));
-      lambda = 0.5 * (P(F_MU, i, j) + P(F_MU, i, j - 1)) * c.cpprandtl;
     }
-    visc_fluxes(mmu, lambda, uu, vv, ww, gx[0], gy[0], gx[1], gy[1], gx[2], gy[2], gx[3], gy[3], fv, gv);
+    visc_fluxes(mmu, mmu * c.cpprandtl, uu, vv, ww, gx[0], gy[0], gx[1], gy[1], gx[2], gy[2], gx[3], gy[3], fv, gv);
   }
 
   // spectral radius, Ducros/pressure sensor and dissipation through the face
@@ -211,15 +237,12 @@ struct FaceCtx {
   // dissipation_ducros_i.F); LL/RR extend the pressure stencil.
   BCG_HD void dissipation(int iL, int jL, int iR, int jR, int iLL, int jLL, int iRR, int jRR, double fnx, double fny,
                           const S pred[5], S diss[5]) const {
-    const S rhomr = W(iR, jR, 1), ur = W(iR, jR, 2) / rhomr, vr = W(iR, jR, 3) / rhomr;
-    const S c2r = c.c2fac * P(F_T, iR, jR);
-    const S rhoml = W(iL, jL, 1), ul = W(iL, jL, 2) / rhoml, vl = W(iL, jL, 3) / rhoml;
-    const S c2l = c.c2fac * P(F_T, iL, jL);
-    const S r = sqrt_t(rhomr / rhoml);
-    const S rr = 1.0 / (1.0 + r);
-    const S omrr = 1.0 - rr;
-    const S u = ul * rr + ur * omrr, v = vl * rr + vr * omrr;
-    const S c2x = c2l * rr + c2r * omrr;
+    // Roe average: rr = sqrt(rhoL)/(sqrt(rhoL)+sqrt(rhoR)), so
+    // u = (sL uL + sR uR)/(sL + sR), and likewise v and c^2
+    const S c2r = c.c2fac * P(F_T, iR, jR), c2l = c.c2fac * P(F_T, iL, jL);
+    const S inv = 1.0 / (P(F_SR, iL, jL) + P(F_SR, iR, jR));
+    const S u = (P(F_SU, iL, jL) + P(F_SU, iR, jR)) * inv, v = (P(F_SV, iL, jL) + P(F_SV, iR, jR)) * inv;
+    const S c2x = (P(F_SC, iL, jL) + P(F_SC, iR, jR)) * inv;
     const double nx2 = fnx * fnx + fny * fny;
     const S rspec = fabs_t(fnx * u + fny * v) + sqrt_t(c2x * nx2);
     S eps2 = Planes<S>::c(0.0), eps4 = Planes<S>::c(0.0 < c.k4 ? c.k4 : 0.0);
@@ -252,13 +275,11 @@ struct FaceCtx {
     }
   }
 
+  // flux assembly (rhs/fluxnumassembly_i.F): (fv nx/|n| + gv ny/|n|) |n| = fv nx + gv ny
   BCG_HD void assemble(double snx, double sny, const S fx[5], const S diss[5], const S fv[4], const S gv[4], S h[5]) const {
-    const double sn = sqrt(snx * snx + sny * sny);
-    const double invsn = 1.0 / sn;
-    const double nxl = snx * invsn, nyl = sny * invsn;
     h[0] = fx[0] - diss[0];
 #pragma unroll
-    for (int v5 = 2; v5 <= 5; ++v5) h[v5 - 1] = fx[v5 - 1] - diss[v5 - 1] - (fv[v5 - 2] * nxl + gv[v5 - 2] * nyl) * sn;
+    for (int v5 = 2; v5 <= 5; ++v5) h[v5 - 1] = fx[v5 - 1] - diss[v5 - 1] - (fv[v5 - 2] * snx + gv[v5 - 2] * sny);
   }
 
   // i-face (i,j), between cells (i-1,j) and (i,j)
@@ -380,7 +401,8 @@ static cudaError_t run_residual_t(const ResidualArgs& a, cudaStream_t st) {
   const size_t nn = (size_t)(a.im + 1) * (a.jm + 1);
   Scratch<S> pr{a.scratch, e.np};
   Scratch<S> gr{a.scratch + (size_t)F_NPRIM * NP * e.np, e.np};
-  Scratch<S> hn{a.scratch + (size_t)(F_NPRIM + G_NGRAD) * NP * e.np, nn};
+  Scratch<S> qr{a.scratch + (size_t)(F_NPRIM + G_NGRAD) * NP * e.np, e.np};
+  Scratch<S> hn{a.scratch + (size_t)(F_NPRIM + G_NGRAD + Q_NQ) * NP * e.np, nn};
   State<S> w;
   if constexpr (NP == 1) w = State<S>{a.w};
   else w = State<S>{a.w, a.wd, a.dstride};
@@ -388,7 +410,8 @@ static cudaError_t run_residual_t(const ResidualArgs& a, cudaStream_t st) {
   k_prim<S><<<(unsigned)((e.np + B - 1) / B), B, 0, st>>>(e, c, w, pr);
   if (c.k2 != 0.0)
     k_grad<S><<<(unsigned)((a.im * a.jm + B - 1) / B), B, 0, st>>>(e, c, pr, gr, a.nx, a.ny, a.vol);
-  FaceCtx<S> fc{e, c, w, pr, gr, a.nx, a.ny, a.vol, a.volf};
+  k_qrows<S><<<(unsigned)((e.np + B - 1) / B), B, 0, st>>>(e, pr, qr);
+  FaceCtx<S> fc{e, c, w, pr, gr, qr, a.nx, a.ny, a.vol, a.volf};
   const int BF = 128;
   k_faces<S><<<(unsigned)((nn + BF - 1) / BF), BF, 0, st>>>(fc, hn);
   k_balance<S><<<(unsigned)((a.im * a.jm + B - 1) / B), B, 0, st>>>(e, hn, a.res, a.resd, a.dstride);
@@ -407,7 +430,7 @@ void launch_primal_passes(const Ext& e, const Coef& c, const double* w, double* 
 size_t residual_scratch_doubles(int im, int jm, int gh, int ndir) {
   const Ext e = make_ext(im, jm, gh);
   const size_t nn = (size_t)(im + 1) * (jm + 1);
-  return (size_t)(ndir + 1) * ((size_t)(F_NPRIM + G_NGRAD) * e.np + 10 * nn);
+  return (size_t)(ndir + 1) * ((size_t)(F_NPRIM + G_NGRAD + Q_NQ) * e.np + 10 * nn);
 }
 
 cudaError_t run_residual(const ResidualArgs& a, cudaStream_t st) {
