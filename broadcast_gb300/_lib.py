@@ -56,6 +56,11 @@ SIGNATURES = {
     "bcg_fp64_peak_tflops": P,
     "bcg_jacobian_dnc5_bl_csr": "ppppp" + "i" + "d" * 11 + "ii" + "pppp" + "pipi" + "pdi" + "ppp" + "L" + "p",
     "bcg_flux_num_dnc5_2d_noalloc": "pppppppppp" + "i" + "d" * 11 + "ii",
+    "bcg_coeffs_5p_dz": "ppp" + "pppppppp" + "i" + "d" * 9 + "ii",
+    "bcg_coeffs_5p_dz2": "ppp" + "pppppppp" + "i" + "d" * 9 + "ii",
+    "bcg_coeffs_5p_dz_dn": "pppi" + "pppppppp" + "i" + "d" * 9 + "ii",
+    "bcg_coeffs_5p_dz2_dn": "pppi" + "pppppppp" + "i" + "d" * 9 + "ii",
+    "bcg_jacobian_dz_bl_csr": "ppppp" + "i" + "d" * 9 + "ii" + "pppp" + "pipi" + "id" + "ppp" + "L" + "p",
 }
 _RESTYPE = {"bcg_get_stream": ctypes.c_void_p, "bcg_last_error_string": ctypes.c_char_p,
             "bcg_residual_scratch_bytes": ctypes.c_size_t}

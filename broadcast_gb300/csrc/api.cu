@@ -13,6 +13,7 @@
 #include "assembly.h"
 #include "adjoint.h"
 #include "jacobian.h"
+#include "span.h"
 
 using namespace bcg;
 
@@ -193,6 +194,83 @@ int bcg_flux_num_dnc5_2d_dn(double* residu, double* residud, const double* w, co
   (void)x0; (void)y0; (void)xc; (void)yc;
   return residual_call(residu, residud, w, wd, nd, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref,
                        tref, s_suth, k2, k4, im, jm);
+}
+
+// ---- spanwise operators (srcfv/dz/coeffs_5p_dz.F90:10, coeffs_5p_dz2.F90:10) --
+// dz_out = Dz . wd (or Dzz . wd) on the interior; the ghosts of dz_out are
+// left as they are (intent(inout) in the reference).
+namespace {
+int span_call(int op, double* dz_out, const double* w, const double* wd, int nd, const double* nx, const double* ny,
+              const double* vol, int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs,
+              double muref, double tref, double s_suth, int im, int jm) {
+  const char* name = op == SPAN_DZ ? "coeffs_5p_dz" : "coeffs_5p_dz2";
+  if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
+  if (!dims_ok(im, jm, gh)) return fail_arg("coeffs_5p_dz: need gh == 3 and im, jm >= 6");
+  if (nd < 1) return fail_arg("coeffs_5p_dz: need at least one direction");
+  if (!dz_out || !w || !wd) return fail_arg("coeffs_5p_dz: null array");
+  if (op == SPAN_DZ && (!nx || !ny || !vol)) return fail_arg("coeffs_5p_dz: null metric array");
+  const size_t np = ncell(im, jm, gh), nn = nnode(im, jm, gh);
+  cudaStream_t st = current_stream();
+  Stager sg(st);
+  const int hw = sg.in(w, np * 5 * 8), hwd = sg.in(wd, np * 5 * 8 * (size_t)nd);
+  int hnx = -1, hny = -1, hvol = -1;
+  if (op == SPAN_DZ) { hnx = sg.in(nx, nn * 2 * 8); hny = sg.in(ny, nn * 2 * 8); hvol = sg.in(vol, np * 8); }
+  const int ho = sg.out_interior(dz_out, im + 2 * gh, jm + 2 * gh, 5 * nd, gh, im, jm);
+  int rc = sg.commit();
+  if (rc) return rc;
+  SpanArgs a{};
+  a.im = im; a.jm = jm; a.gh = gh; a.op = op;
+  a.phys = Phys{cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, 0.0, 0.0};
+  a.w = sg.dev<double>(hw); a.dstride = np * 5;
+  if (op == SPAN_DZ) { a.nx = sg.dev<double>(hnx); a.ny = sg.dev<double>(hny); a.vol = sg.dev<double>(hvol); }
+  const double* wdd = sg.dev<double>(hwd);
+  double* od = sg.dev<double>(ho);
+  for (int k0 = 0; k0 < nd;) {
+    const int kk = nd - k0 >= 4 ? 4 : (nd - k0 >= 2 ? 2 : 1);
+    a.ndir = kk; a.wd = wdd + (size_t)k0 * np * 5; a.out = od + (size_t)k0 * np * 5;
+    cudaError_t e = run_span(a, st);
+    if (e != cudaSuccess) return fail_cuda(name, e);
+    k0 += kk;
+  }
+  return sg.finish();
+}
+}  // namespace
+
+int bcg_coeffs_5p_dz(double* dz_out, const double* w, const double* wd, const double* x0, const double* y0,
+                     const double* nx, const double* ny, const double* xc, const double* yc, const double* vol,
+                     const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz,
+                     double cs, double muref, double tref, double s_suth, int im, int jm) {
+  (void)x0; (void)y0; (void)xc; (void)yc; (void)volf;
+  return span_call(SPAN_DZ, dz_out, w, wd, 1, nx, ny, vol, gh, cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth,
+                   im, jm);
+}
+
+int bcg_coeffs_5p_dz2(double* dz2_out, const double* w, const double* wd, const double* x0, const double* y0,
+                      const double* nx, const double* ny, const double* xc, const double* yc, const double* vol,
+                      const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz,
+                      double cs, double muref, double tref, double s_suth, int im, int jm) {
+  (void)x0; (void)y0; (void)xc; (void)yc; (void)volf;
+  return span_call(SPAN_DZZ, dz2_out, w, wd, 1, nx, ny, vol, gh, cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth,
+                   im, jm);
+}
+
+int bcg_coeffs_5p_dz_dn(double* dz_out, const double* w, const double* wd, int nd, const double* x0,
+                        const double* y0, const double* nx, const double* ny, const double* xc, const double* yc,
+                        const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
+                        double gam, double rgaz, double cs, double muref, double tref, double s_suth, int im, int jm) {
+  (void)x0; (void)y0; (void)xc; (void)yc; (void)volf;
+  return span_call(SPAN_DZ, dz_out, w, wd, nd, nx, ny, vol, gh, cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth,
+                   im, jm);
+}
+
+int bcg_coeffs_5p_dz2_dn(double* dz2_out, const double* w, const double* wd, int nd, const double* x0,
+                         const double* y0, const double* nx, const double* ny, const double* xc, const double* yc,
+                         const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
+                         double gam, double rgaz, double cs, double muref, double tref, double s_suth, int im,
+                         int jm) {
+  (void)x0; (void)y0; (void)xc; (void)yc; (void)volf;
+  return span_call(SPAN_DZZ, dz2_out, w, wd, nd, nx, ny, vol, gh, cp, cv, prandtl, gam, rgaz, cs, muref, tref,
+                   s_suth, im, jm);
 }
 
 // ---- adjoint (srcfv/adjoint/flux_num_dnc5_b.f90:15) ------------------------
@@ -426,14 +504,14 @@ int bcg_compute_maxnorm(double* norm, int* imax, int* jmax, const double* rhs, i
 // Batched colored Jacobian of the boundary-layer configuration
 // (BROADCAST_npz.py:1068-1137, 1206-1210; misc/PETSc_func.py:71-96)
 // ===========================================================================
-extern "C" int bcg_jacobian_dnc5_bl_csr(const double* w, const double* nx, const double* ny, const double* vol,
-                                        const double* volf, int gh, double cp, double cv, double prandtl, double gam,
-                                        double rgaz, double cs, double muref, double tref, double s_suth, double k2,
-                                        double k4, int im, int jm, const int* interf_ilo, const int* interf_jhi,
-                                        const int* interf_ihi, const int* interf_jlo, const double* field,
-                                        int lm_field, const double* wbd, int lm_wbd, const double* coefdiag,
-                                        double mini, int divide_by_vol, int* indptr, int* indices, double* data,
-                                        long long capacity, long long* nnz) {
+namespace {
+int jacobian_bl_csr(int op, const double* w, const double* nx, const double* ny, const double* vol,
+                    const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz,
+                    double cs, double muref, double tref, double s_suth, double k2, double k4, int im, int jm,
+                    const int* interf_ilo, const int* interf_jhi, const int* interf_ihi, const int* interf_jlo,
+                    const double* field, int lm_field, const double* wbd, int lm_wbd, const double* coefdiag,
+                    double mini, int divide_by_vol, int* indptr, int* indices, double* data, long long capacity,
+                    long long* nnz) {
   if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
   if (!dims_ok(im, jm, gh)) return fail_arg("jacobian: need gh == 3 and im, jm >= 6");
   if (!nnz || !interf_ilo || !interf_jhi || !interf_ihi || !interf_jlo) return fail_arg("jacobian: null argument");
@@ -452,6 +530,7 @@ extern "C" int bcg_jacobian_dnc5_bl_csr(const double* w, const double* nx, const
   a.phys = Phys{cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4};
   a.w = sg.dev<double>(hw); a.nx = sg.dev<double>(hnx); a.ny = sg.dev<double>(hny);
   a.vol = sg.dev<double>(hvol); a.volf = sg.dev<double>(hvolf);
+  a.op = op;
   a.relaxed = coefdiag ? 1 : 0;
   a.coefdiag = hc >= 0 ? sg.dev<double>(hc) : nullptr;
   a.mini = mini; a.divide_by_vol = divide_by_vol; a.capacity = capacity; a.nnz = nnz;
@@ -495,4 +574,31 @@ extern "C" int bcg_jacobian_dnc5_bl_csr(const double* w, const double* nx, const
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail_cuda("jacobian: output copy", e);
   return sg.finish();
+}
+}  // namespace
+
+extern "C" int bcg_jacobian_dnc5_bl_csr(const double* w, const double* nx, const double* ny, const double* vol,
+                                        const double* volf, int gh, double cp, double cv, double prandtl, double gam,
+                                        double rgaz, double cs, double muref, double tref, double s_suth, double k2,
+                                        double k4, int im, int jm, const int* interf_ilo, const int* interf_jhi,
+                                        const int* interf_ihi, const int* interf_jlo, const double* field,
+                                        int lm_field, const double* wbd, int lm_wbd, const double* coefdiag,
+                                        double mini, int divide_by_vol, int* indptr, int* indices, double* data,
+                                        long long capacity, long long* nnz) {
+  return jacobian_bl_csr(0, w, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4, im,
+                         jm, interf_ilo, interf_jhi, interf_ihi, interf_jlo, field, lm_field, wbd, lm_wbd, coefdiag,
+                         mini, divide_by_vol, indptr, indices, data, capacity, nnz);
+}
+
+extern "C" int bcg_jacobian_dz_bl_csr(const double* w, const double* nx, const double* ny, const double* vol,
+                                      const double* volf, int gh, double cp, double cv, double prandtl, double gam,
+                                      double rgaz, double cs, double muref, double tref, double s_suth, int im, int jm,
+                                      const int* interf_ilo, const int* interf_jhi, const int* interf_ihi,
+                                      const int* interf_jlo, const double* field, int lm_field, const double* wbd,
+                                      int lm_wbd, int which, double mini, int* indptr, int* indices, double* data,
+                                      long long capacity, long long* nnz) {
+  if (which != 1 && which != 2) return fail_arg("jacobian_dz: which must be 1 (Dz) or 2 (Dzz)");
+  return jacobian_bl_csr(which == 1 ? SPAN_DZ : SPAN_DZZ, w, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs,
+                         muref, tref, s_suth, 0.0, 0.0, im, jm, interf_ilo, interf_jhi, interf_ihi, interf_jlo, field,
+                         lm_field, wbd, lm_wbd, nullptr, mini, 0, indptr, indices, data, capacity, nnz);
 }

@@ -21,6 +21,7 @@
 #include "jacobian.h"
 #include "residual.h"
 #include "runtime.h"
+#include "span.h"
 
 namespace bcg {
 
@@ -44,7 +45,10 @@ __global__ void k_seed4(double* __restrict__ wd, int nseed, const int* __restric
 
 // One thread per row (cell i, j, variable e): enumerate the candidate entries
 // in ascending column order.  pass 0 counts the kept entries, pass 1 writes.
-__global__ void __launch_bounds__(128) k_csr_rows(int pass, const double* __restrict__ resd_all, int gh, int im,
+// op 0 stores -resd (+coefdiag on the diagonal when relaxed), the fill of
+// computejacobianfromjv(_relaxed) (ComputeJacobian.f90:292-355, 503-570);
+// op != 0 stores +dz with the row window of computejacobianfromdz (:708-779).
+__global__ void __launch_bounds__(128) k_csr_rows(int pass, int op, const double* __restrict__ resd_all, int gh, int im,
                                                   int jm, int relaxed, const double* __restrict__ coefdiag, double mini,
                                                   const double* __restrict__ vol, int* __restrict__ count,
                                                   const long long* __restrict__ rowptr, int* __restrict__ indices,
@@ -71,7 +75,9 @@ __global__ void __launch_bounds__(128) k_csr_rows(int pass, const double* __rest
   }
   for (int k = 0; k < 7; ++k) {
     ki[k] = k;
-    const int valj = (j <= k + 1 + gh) ? k : (j - gh - (k + 1) + 2 * gh) / step * step + k;
+    int valj;
+    if (op == 0 || k <= gh) valj = (j <= k + 1 + gh) ? k : (j - gh - (k + 1) + 2 * gh) / step * step + k;
+    else valj = (j <= k - gh) ? jm + 1 : (j - (k + 1) + gh) / step * step + k;
     kv[k] = valj < jm ? valj : -1;
   }
   // insertion sorts (7 elements)
@@ -91,7 +97,7 @@ __global__ void __launch_bounds__(128) k_csr_rows(int pass, const double* __rest
         const int col = m + kv[b] * 5 + lv[a] * jm * 5;
         const int seed = k + 7 * l + 49 * m;  // the reference's slot order
         const double r = resd_all[(size_t)seed * np * 5 + (size_t)e * np + cell];
-        double v = (relaxed && col == row) ? cd - r : -r;
+        double v = op ? r : ((relaxed && col == row) ? cd - r : -r);
         if (!(fabs(v) > mini)) continue;
         if (pass) { indices[out + n] = col; data[out + n] = v * vinv; }
         ++n;
@@ -185,16 +191,25 @@ int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
         e = launch_bc(b, st);
         if (e != cudaSuccess) return fail_cuda("jacobian: boundary fill", e);
       }
-      ra.ndir = nd;
-      ra.wd = wd4 + (size_t)off * np * 5;
-      ra.resd = resd_all + (size_t)(s0 + off) * np * 5;
-      e = run_residual(ra, st);
-      if (e != cudaSuccess) return fail_cuda("jacobian: tangent residual", e);
+      if (a.op == 0) {
+        ra.ndir = nd;
+        ra.wd = wd4 + (size_t)off * np * 5;
+        ra.resd = resd_all + (size_t)(s0 + off) * np * 5;
+        e = run_residual(ra, st);
+        if (e != cudaSuccess) return fail_cuda("jacobian: tangent residual", e);
+      } else {
+        SpanArgs sa{};
+        sa.im = im; sa.jm = jm; sa.gh = gh; sa.op = a.op; sa.ndir = nd; sa.phys = a.phys; sa.w = wcopy;
+        sa.wd = wd4 + (size_t)off * np * 5; sa.dstride = np * 5; sa.nx = a.nx; sa.ny = a.ny; sa.vol = a.vol;
+        sa.out = resd_all + (size_t)(s0 + off) * np * 5;
+        e = run_span(sa, st);
+        if (e != cudaSuccess) return fail_cuda("jacobian: spanwise operator", e);
+      }
     }
   }
   // CSR: count, scan, fill
   const int B = 128;
-  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(0, resd_all, gh, im, jm, a.relaxed, a.coefdiag, a.mini,
+  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(0, a.op, resd_all, gh, im, jm, a.relaxed, a.coefdiag, a.mini,
                                              a.divide_by_vol ? a.vol : nullptr, count, nullptr, nullptr, nullptr);
   k_scan_block<<<nb, kScanBlock, 0, st>>>(count, rowptr, bsum, nrow);
   k_scan_sums<<<1, 1, 0, st>>>(bsum, nb, total);
@@ -207,7 +222,7 @@ int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
   if (nnz > a.capacity) return fail_arg("jacobian: CSR capacity too small (see nnz)");
   if (nnz >= (1LL << 31)) return fail_arg("jacobian: nnz exceeds 32-bit CSR indices");
   k_ptr_to_int<<<(nrow + 1 + 255) / 256, 256, 0, st>>>(rowptr, a.indptr, nrow);
-  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(1, resd_all, gh, im, jm, a.relaxed, a.coefdiag, a.mini,
+  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(1, a.op, resd_all, gh, im, jm, a.relaxed, a.coefdiag, a.mini,
                                              a.divide_by_vol ? a.vol : nullptr, count, rowptr, a.indices, a.data);
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail_cuda("jacobian: csr", e);

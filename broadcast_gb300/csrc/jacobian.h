@@ -17,6 +17,7 @@ struct JacobianArgs {
   const double* vol;
   const double* volf;
   std::vector<BcArgs> bcs;  // linearised boundary chain, in the drivers' order
+  int op;                   // 0: residual tangent (Jacobian); SPAN_DZ / SPAN_DZZ: spanwise operators
   int relaxed;              // 1: coefdiag added on the diagonal (computejacobianfromjv_relaxed)
   const double* coefdiag;   // (im, jm)
   double mini;              // entries with |a| <= mini are dropped (remove_zero_jac)

@@ -147,6 +147,42 @@ int bcg_jacobian_dnc5_bl_csr(const double* w, const double* nx, const double* ny
                              const double* coefdiag, double mini, int divide_by_vol, int* indptr, int* indices,
                              double* data, long long capacity, long long* nnz);
 
+/* Same loop for the spanwise operators (BROADCAST_npz.py:1221-1249): per seed,
+ * testvector, the same linearised boundary chain, coeffs_5p_dz (which = 1) or
+ * coeffs_5p_dz2 (which = 2), computejacobianfromdz (+dz, its own row window),
+ * remove_zero_jac with mini; then CSR as above (no volume scaling). */
+int bcg_jacobian_dz_bl_csr(const double* w, const double* nx, const double* ny, const double* vol,
+                           const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz,
+                           double cs, double muref, double tref, double s_suth, int im, int jm, const int* interf_ilo,
+                           const int* interf_jhi, const int* interf_ihi, const int* interf_jlo, const double* field,
+                           int lm_field, const double* wbd, int lm_wbd, int which, double mini, int* indptr,
+                           int* indices, double* data, long long capacity, long long* nnz);
+
+/* ---- spanwise operators (srcfv/dz, module f_dz) -------------------------------- */
+/* coeffs_5p_dz.F90:10 coeffs_5p_dz : dz_out = Dz . wd (coefficient of i*beta)
+ * coeffs_5p_dz2.F90:10 coeffs_5p_dz2: dz2_out = Dzz . wd (coefficient of -beta^2)
+ * Interior of the output written, ghosts untouched; x0, y0, xc, yc, volf unused
+ * (as in the reference), nx, ny, vol unused by coeffs_5p_dz2. */
+int bcg_coeffs_5p_dz(double* dz_out, const double* w, const double* wd, const double* x0, const double* y0,
+                     const double* nx, const double* ny, const double* xc, const double* yc, const double* vol,
+                     const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz,
+                     double cs, double muref, double tref, double s_suth, int im, int jm);
+int bcg_coeffs_5p_dz2(double* dz2_out, const double* w, const double* wd, const double* x0, const double* y0,
+                      const double* nx, const double* ny, const double* xc, const double* yc, const double* vol,
+                      const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz,
+                      double cs, double muref, double tref, double s_suth, int im, int jm);
+/* nd directions at once (wd and the output hold nd stacked padded arrays);
+ * no reference counterpart, equivalent to nd calls of the routines above. */
+int bcg_coeffs_5p_dz_dn(double* dz_out, const double* w, const double* wd, int nd, const double* x0,
+                        const double* y0, const double* nx, const double* ny, const double* xc, const double* yc,
+                        const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
+                        double gam, double rgaz, double cs, double muref, double tref, double s_suth, int im, int jm);
+int bcg_coeffs_5p_dz2_dn(double* dz2_out, const double* w, const double* wd, int nd, const double* x0,
+                         const double* y0, const double* nx, const double* ny, const double* xc, const double* yc,
+                         const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
+                         double gam, double rgaz, double cs, double muref, double tref, double s_suth, int im,
+                         int jm);
+
 /* ---- norms (srcfv/norm.F90) ---------------------------------------------------- */
 /* :2 compute_norml2 ; :34 compute_norml2inf ; :79 compute_maxnorm (5-vectors) */
 int bcg_compute_norml2(double* norm, double* nmoy, const double* rhs, int im, int jm, int gh);

@@ -843,6 +843,193 @@ inline void computegeom_2d(double* x0_, double* y0_, double* nx_, double* ny_, d
 }
 
 // ===========================================================================
+// Spanwise operators (srcfv/dz)
+// ===========================================================================
+// Both operators are  out(i,j,e) = sum_k coeffs(i,j,e,k) * d func_k(i,j,e)/dw . wd
+// over the interior: the coefficients come from the base flow w, the func_k
+// are auxiliary fields of w whose tangents along wd the reference takes from
+// Tapenade (dz/function_5p_dz_d.f90, dz/function_5p_dz2_d.f90).  Here the
+// func_k are evaluated on Dual<N> numbers.
+//
+// Cell fields shared by both: rhs/primvisc.F (primitives and Sutherland
+// viscosity on every padded cell) and rhs/gradop_5pi.F, gradop_5pj.F,
+// geom/dxdy.F, gradient.F (4th-order gradients of u, v, w, mu).
+template <class T>
+struct SpanFields {
+  int im, jm, gh, ni, nj;
+  std::vector<T> velx, vely, velz, tloc, p, mu;
+  std::vector<T> gu, gv, gw, gmu;  // (x, y) pairs per cell, interior filled
+  size_t c(int i, int j) const { return (size_t)(i - (1 - gh)) + (size_t)(j - (1 - gh)) * ni; }
+
+  SpanFields(const T* w_, const double* nx_, const double* ny_, const double* vol_, int gh_, const Consts& k,
+             int im_, int jm_, bool gradients)
+      : im(im_), jm(jm_), gh(gh_), ni(im_ + 2 * gh_), nj(jm_ + 2 * gh_) {
+    const size_t np = (size_t)ni * nj;
+    FArr<const T> w(w_, ni, nj, 1 - gh);
+    FArr<const double> nx(nx_, ni + 1, nj + 1, 1 - gh), ny(ny_, ni + 1, nj + 1, 1 - gh), vol(vol_, ni, nj, 1 - gh);
+    velx.assign(np, T(0.0)); vely.assign(np, T(0.0)); velz.assign(np, T(0.0));
+    tloc.assign(np, T(0.0)); p.assign(np, T(0.0)); mu.assign(np, T(0.0));
+    const double ONE = 1.0, HALF = 0.5;
+    const double cvm1 = ONE / k.cv;
+    const double betas = k.muref * (k.tref + k.cs) / (std::sqrt(k.tref) * k.tref);
+    for (int j = 1 - gh; j <= jm + gh; ++j)
+      for (int i = 1 - gh; i <= im + gh; ++i) {
+        const size_t q = c(i, j);
+        const T ro = w(i, j, 1);
+        const T rom1 = ONE / ro;
+        velx[q] = w(i, j, 2) * rom1;
+        vely[q] = w(i, j, 3) * rom1;
+        velz[q] = w(i, j, 4) * rom1;
+        const T ec = HALF * (velx[q] * velx[q] + vely[q] * vely[q] + velz[q] * velz[q]);
+        const T eloc = (w(i, j, 5) - ec * ro) * rom1;
+        tloc[q] = eloc * cvm1;
+        p[q] = (k.gam - ONE) * ro * eloc;
+        mu[q] = betas / (tloc[q] + k.s_suth) * sqrt_t(tloc[q]) * tloc[q];
+      }
+    if (!gradients) return;
+    gu.assign(2 * np, T(0.0)); gv.assign(2 * np, T(0.0)); gw.assign(2 * np, T(0.0)); gmu.assign(2 * np, T(0.0));
+    const double b1 = 8.0 * (1.0 / 12.0), b2 = -(1.0 / 12.0);
+    for (int j = 1; j <= jm; ++j)
+      for (int i = 1; i <= im; ++i) {
+        auto di = [&](const std::vector<T>& f) {
+          return b1 * (f[c(i + 1, j)] - f[c(i - 1, j)]) + b2 * (f[c(i + 2, j)] - f[c(i - 2, j)]);
+        };
+        auto dj = [&](const std::vector<T>& f) {
+          return b1 * (f[c(i, j + 1)] - f[c(i, j - 1)]) + b2 * (f[c(i, j + 2)] - f[c(i, j - 2)]);
+        };
+        const T gui = di(velx), gvi = di(vely), gwi = di(velz), gmui = di(mu);
+        const T guj = dj(velx), gvj = dj(vely), gwj = dj(velz), gmuj = dj(mu);
+        const double volm1 = ONE / vol(i, j);
+        const double dxm1 = HALF * (nx(i, j, 1) + nx(i + 1, j, 1)) * volm1;
+        const double dxm2 = HALF * (nx(i, j, 2) + nx(i, j + 1, 2)) * volm1;
+        const double dym1 = HALF * (ny(i, j, 1) + ny(i + 1, j, 1)) * volm1;
+        const double dym2 = HALF * (ny(i, j, 2) + ny(i, j + 1, 2)) * volm1;
+        const size_t q = 2 * c(i, j);
+        gu[q] = dxm1 * gui + dxm2 * guj;   gu[q + 1] = dym1 * gui + dym2 * guj;
+        gv[q] = dxm1 * gvi + dxm2 * gvj;   gv[q + 1] = dym1 * gvi + dym2 * gvj;
+        gw[q] = dxm1 * gwi + dxm2 * gwj;   gw[q + 1] = dym1 * gwi + dym2 * gwj;
+        gmu[q] = dxm1 * gmui + dxm2 * gmuj; gmu[q + 1] = dym1 * gmui + dym2 * gmuj;
+      }
+  }
+};
+
+// coeffs_5p_dz (srcfv/dz/coeffs_5p_dz.F90:10-174): coefficients dz/coeffs_dz.F:1-97,
+// functions matrix_dz/function_dz.F, sum dz/sum_coeffs_dz.F.  N directions; the
+// interior of dz_out (N stacked padded arrays) is written, the ghosts are not.
+template <int N>
+void coeffs_5p_dz(double* dz_out, const double* w, const double* wd, const double* nx, const double* ny,
+                  const double* vol, int gh, const Consts& k, int im, int jm) {
+  const int ni = im + 2 * gh, nj = jm + 2 * gh;
+  const size_t n = (size_t)ni * nj * 5;
+  std::vector<Dual<N>> wdl(n);
+  for (size_t q = 0; q < n; ++q) {
+    wdl[q].v = w[q];
+    for (int d = 0; d < N; ++d) wdl[q].d[d] = wd[(size_t)d * n + q];
+  }
+  const SpanFields<double> B(w, nx, ny, vol, gh, k, im, jm, true);
+  const SpanFields<Dual<N>> D(wdl.data(), nx, ny, vol, gh, k, im, jm, true);
+  FArr<const Dual<N>> W(wdl.data(), ni, nj, 1 - gh);
+  const double ONE = 1.0, ZERO = 0.0, TWOTHIRD = 2.0 / 3.0;
+  for (int j = 1; j <= jm; ++j)
+    for (int i = 1; i <= im; ++i) {
+      const size_t q = B.c(i, j), g = 2 * q;
+      // base-flow coefficients, coeffs(e, kk) with kk = 1..16 (coeffs_dz.F)
+      const double mu = B.mu[q], velx = B.velx[q], vely = B.vely[q], velz = B.velz[q];
+      const double gu1 = B.gu[g], gv2 = B.gv[g + 1], gw1 = B.gw[g], gw2 = B.gw[g + 1];
+      const double gmu1 = B.gmu[g], gmu2 = B.gmu[g + 1];
+      double cf[5][16];
+      for (int e = 0; e < 5; ++e)
+        for (int kk = 0; kk < 16; ++kk) cf[e][kk] = (kk == 0) ? ONE : ZERO;
+      cf[1][1] = TWOTHIRD * gmu1; cf[2][1] = TWOTHIRD * gmu2; cf[3][1] = -gmu1;
+      cf[4][1] = TWOTHIRD * (gmu1 * velx + mu * gu1);
+      cf[1][2] = TWOTHIRD * mu; cf[2][2] = TWOTHIRD * mu; cf[3][2] = -gmu2; cf[4][2] = TWOTHIRD * mu * velx;
+      cf[3][3] = -mu; cf[4][3] = -(gmu1 * velz + mu * gw1);
+      cf[4][4] = -(mu * velz);
+      cf[4][5] = TWOTHIRD * (gmu2 * vely + mu * gv2);
+      cf[4][6] = TWOTHIRD * mu * vely;
+      cf[4][7] = -(gmu2 * velz + mu * gw2);
+      cf[4][8] = -(mu * velz);
+      cf[4][9] = -(mu * gw1);
+      cf[4][10] = -velx;
+      cf[4][11] = -(mu * gw2);
+      cf[4][12] = -vely;
+      cf[4][13] = TWOTHIRD * mu * (gu1 + gv2);
+      cf[4][14] = TWOTHIRD * velz * (gu1 + gv2);
+      cf[4][15] = TWOTHIRD * mu * velz;
+      // auxiliary functions on duals (function_dz.F), fn[kk][e]
+      const Dual<N> dmu = D.mu[q], dvx = D.velx[q], dvy = D.vely[q], dvz = D.velz[q], dp = D.p[q];
+      const Dual<N> dgu1 = D.gu[g], dgv2 = D.gv[g + 1], dgw1 = D.gw[g], dgw2 = D.gw[g + 1];
+      Dual<N> fn[16][5];
+      fn[0][0] = W(i, j, 4);
+      fn[0][1] = W(i, j, 2) * dvz - dmu * dgw1;
+      fn[0][2] = W(i, j, 3) * dvz - dmu * dgw2;
+      fn[0][3] = W(i, j, 4) * dvz + dp + TWOTHIRD * dmu * (dgu1 + dgv2);
+      fn[0][4] = (W(i, j, 5) + dp) * dvz;
+      fn[1][1] = dvz; fn[1][2] = dvz; fn[1][3] = dvx; fn[1][4] = dvz;
+      fn[2][1] = dgw1; fn[2][2] = dgw2; fn[2][3] = dvy; fn[2][4] = dgw1;
+      fn[3][3] = dgu1 + dgv2; fn[3][4] = dvx;
+      fn[4][4] = dgu1;
+      fn[5][4] = dvz;
+      fn[6][4] = dgw2;
+      fn[7][4] = dvy;
+      fn[8][4] = dgv2;
+      fn[9][4] = dvx;
+      fn[10][4] = dmu * dgw1;
+      fn[11][4] = dvy;
+      fn[12][4] = dmu * dgw2;
+      fn[13][4] = dvz;
+      fn[14][4] = dmu;
+      fn[15][4] = dgu1 + dgv2;
+      // sum_coeffs_dz.F: left to right over kk
+      for (int d = 0; d < N; ++d) {
+        FArr<double> out(dz_out + (size_t)d * n, ni, nj, 1 - gh);
+        for (int e = 0; e < 5; ++e) {
+          double acc = cf[e][0] * fn[0][e].d[d];
+          for (int kk = 1; kk < 16; ++kk) acc = acc + cf[e][kk] * fn[kk][e].d[d];
+          out(i, j, e + 1) = acc;
+        }
+      }
+    }
+}
+
+// coeffs_5p_dz2 (srcfv/dz/coeffs_5p_dz2.F90:10-147): coefficients dz/coeffs_dz2.F,
+// functions matrix_dz2/function_dz2.F, sum dz/sum_coeffs_dz2.F.
+template <int N>
+void coeffs_5p_dz2(double* dz_out, const double* w, const double* wd, int gh, const Consts& k, int im, int jm) {
+  const int ni = im + 2 * gh, nj = jm + 2 * gh;
+  const size_t n = (size_t)ni * nj * 5;
+  std::vector<Dual<N>> wdl(n);
+  for (size_t q = 0; q < n; ++q) {
+    wdl[q].v = w[q];
+    for (int d = 0; d < N; ++d) wdl[q].d[d] = wd[(size_t)d * n + q];
+  }
+  const SpanFields<double> B(w, nullptr, nullptr, nullptr, gh, k, im, jm, false);
+  const SpanFields<Dual<N>> D(wdl.data(), nullptr, nullptr, nullptr, gh, k, im, jm, false);
+  const double TWO = 2.0, TWOTHIRD = 2.0 / 3.0, cpprandtl = k.cp / k.prandtl;
+  for (int j = 1; j <= jm; ++j)
+    for (int i = 1; i <= im; ++i) {
+      const size_t q = B.c(i, j);
+      const double mu = B.mu[q];
+      double cf[5][4] = {};
+      cf[1][0] = -mu; cf[2][0] = -mu; cf[3][0] = -(TWO * TWOTHIRD * mu); cf[4][0] = -(mu * cpprandtl);
+      cf[4][1] = -(mu * B.velx[q]);
+      cf[4][2] = -(mu * B.vely[q]);
+      cf[4][3] = -(TWO * TWOTHIRD * mu * B.velz[q]);
+      Dual<N> fn[4][5];
+      fn[0][1] = D.velx[q]; fn[0][2] = D.vely[q]; fn[0][3] = D.velz[q]; fn[0][4] = D.tloc[q];
+      fn[1][4] = D.velx[q]; fn[2][4] = D.vely[q]; fn[3][4] = D.velz[q];
+      for (int d = 0; d < N; ++d) {
+        FArr<double> out(dz_out + (size_t)d * n, ni, nj, 1 - gh);
+        for (int e = 0; e < 5; ++e) {
+          double acc = cf[e][0] * fn[0][e].d[d];
+          for (int kk = 1; kk < 4; ++kk) acc = acc + cf[e][kk] * fn[kk][e].d[d];
+          out(i, j, e + 1) = acc;
+        }
+      }
+    }
+}
+
+// ===========================================================================
 // Norms (srcfv/norm.F90)
 // ===========================================================================
 inline void compute_norml2(double* norm, double* nmoy, const double* rhs_, int im, int jm, int gh) {

@@ -43,6 +43,7 @@ SIGS = {
     "orc_testvector_partial": [_P] + [_I] * 10,
     "orc_computejacobian": [_I, _P, _P, _P, _P] + [_I] * 6 + [_P],
     "orc_computejacobian_withjnandcheck": [_P, _P, _P, _P] + [_I] * 6 + [_P, _D, _I],
+    "orc_coeffs_5p_dz": [_P] * 3 + [_I] + [_P] * 3 + [_I] + [_D] * 9 + [_I] * 3,
 }
 
 _lock = threading.Lock()
@@ -122,6 +123,36 @@ def vjp(grid, ph, w, rb):
     lib().orc_flux_num_dnc5_2d_b(_p(rb), _p(_chk(w)), _p(wb), _p(grid["nx"]), _p(grid["ny"]), _p(grid["vol"]),
                                  _p(grid["volf"]), grid["gh"], *_phys(ph), grid["im"], grid["jm"])
     return wb
+
+
+def _span(which, grid, ph, w, wd, out):
+    wd = np.asarray(wd)
+    single = wd.ndim == 3
+    wds = wd[None] if single else wd
+    nd = wds.shape[0]
+    buf = np.concatenate([np.ravel(np.asfortranarray(x), order="F") for x in wds])
+    if out is None:
+        ob = np.zeros_like(buf)
+    else:
+        outs = out[None] if single else out
+        ob = np.concatenate([np.ravel(np.asfortranarray(x), order="F") for x in outs])
+    keys = ("cp", "cv", "prandtl", "gam", "rgaz", "cs", "muref", "tref", "s_suth")
+    lib().orc_coeffs_5p_dz(_p(ob), _p(_chk(w)), _p(buf), nd, _p(grid["nx"]), _p(grid["ny"]), _p(grid["vol"]),
+                           grid["gh"], *[float(ph[k]) for k in keys], grid["im"], grid["jm"], which)
+    n = w.size
+    r = [np.reshape(ob[k * n:(k + 1) * n], w.shape, order="F") for k in range(nd)]
+    return r[0] if single else np.stack(r)
+
+
+def dz(grid, ph, w, wd, out=None):
+    """coeffs_5p_dz: the Dz operator applied to wd (one padded state or a stack);
+    ghosts of `out` (zeros if None) are kept."""
+    return _span(1, grid, ph, w, wd, out)
+
+
+def dzz(grid, ph, w, wd, out=None):
+    """coeffs_5p_dz2: the Dzz operator applied to wd."""
+    return _span(2, grid, ph, w, wd, out)
 
 
 OP_KINDS = ("add_aa", "add_ap", "mul_aa", "mul_ap", "div_aa", "div_ap", "div_pa", "sqrt", "tanh", "abs", "max", "pow")

@@ -223,6 +223,24 @@ int orc_set_bndbl_2d(const double* w, double* field, double* wbd, int im, int jm
 }
 
 // ---- colored assembly indexing ---------------------------------------------
+// ---- spanwise operators (coeffs_5p_dz, coeffs_5p_dz2), nd stacked directions
+int orc_coeffs_5p_dz(double* dz_out, const double* w, const double* wd, int nd, const double* nx, const double* ny,
+                     const double* vol, int gh, double cp, double cv, double prandtl, double gam, double rgaz,
+                     double cs, double muref, double tref, double s_suth, int im, int jm, int which) {
+  const Consts c = mk(cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, 0.0, 0.0);
+  const size_t n = np_(im, jm, gh) * 5;
+  for (int k0 = 0; k0 < nd; k0 += 4) {
+    const int kk = std::min(4, nd - k0);
+    std::vector<double> buf((size_t)4 * n, 0.0), out((size_t)4 * n, 0.0);
+    std::copy(wd + (size_t)k0 * n, wd + (size_t)(k0 + kk) * n, buf.begin());
+    std::copy(dz_out + (size_t)k0 * n, dz_out + (size_t)(k0 + kk) * n, out.begin());
+    if (which == 1) coeffs_5p_dz<4>(out.data(), w, buf.data(), nx, ny, vol, gh, c, im, jm);
+    else coeffs_5p_dz2<4>(out.data(), w, buf.data(), gh, c, im, jm);
+    std::copy(out.begin(), out.begin() + (size_t)kk * n, dz_out + (size_t)k0 * n);
+  }
+  return 0;
+}
+
 int orc_testvector(double* wd, int m, int l, int k, int gh, int im, int jm) {
   testvector(wd, m, l, k, gh, im, jm);
   return 0;

@@ -8,6 +8,7 @@ Outputs go to oracle/_ref/ (git-ignored): libref.c, libref.so, signatures.json.
 """
 import json
 import os
+import re
 import subprocess
 import sys
 
@@ -37,10 +38,23 @@ ROUTINES = [
                                   "computejacobianfromjv_withjn", "computejacobianfromjv_relaxed_withjnandcheck",
                                   "computejacobianfromdz"]),
     ("srcfv/norm.F90", ["compute_norml2", "compute_norml2inf", "compute_maxnorm"]),
+    # compiled by f2py from the raw sources with their #include fragments
+    # (srcfv/compile_dz.py runs fpp with -I srcfv/)
+    ("srcfv/dz/coeffs_5p_dz.F90", ["function_5p_dz_d", "coeffs_5p_dz"]),
+    ("srcfv/dz/coeffs_5p_dz2.F90", ["function_5p_dz2_d", "coeffs_5p_dz2"]),
     ("srcfv/prepro/computegeom.f90", ["computegeom_2d"]),
     ("initialisation.f90", ["initblfv"]),
     ("set_bnd.f90", ["set_bndbl_2d"]),
 ]
+
+
+def _resolve_includes(path, inc_root):
+    """Expand `#include "x"` lines (paths relative to inc_root), as fpp does."""
+    out = []
+    for line in open(path, errors="replace"):
+        m = re.match(r'\s*#include\s+"([^"]+)"', line)
+        out.append(_resolve_includes(os.path.join(inc_root, m.group(1)), inc_root) if m else line)
+    return "".join(out)
 
 
 def build(ref_root=DEFAULT_REF, routines=ROUTINES, verbose=False):
@@ -53,7 +67,7 @@ def build(ref_root=DEFAULT_REF, routines=ROUTINES, verbose=False):
     failures = []
     for rel, names in routines:
         path = os.path.join(ref_root, rel)
-        text = open(path, errors="replace").read()
+        text = _resolve_includes(path, os.path.join(ref_root, "srcfv"))
         before = len(tr.subs)
         try:
             tr.translate_text(text, only=set(names))

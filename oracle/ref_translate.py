@@ -639,7 +639,28 @@ class Translator:
             e = sub.expr(args[0])
             kind = "r" if e.typ == "real" else "i"
             return "%s = f_pop_%s();" % (e.code, kind)
-        raise TranslateError("unsupported CALL %s" % name)
+        callee = next((c for c in self.subs if c.name == name), None)
+        if callee is None:
+            raise TranslateError("unsupported CALL %s" % name)
+        if len(args) != len(callee.args):
+            raise TranslateError("CALL %s: %d arguments for %d" % (name, len(args), len(callee.args)))
+        # Fortran passes by reference: whole arrays by their base pointer,
+        # scalar variables by address, expressions through a temporary
+        pre, actual = [], []
+        for k, a in enumerate(args):
+            a = a.strip()
+            if re.match(r"^\w+$", a) and a.lower() in sub.vars:
+                v = sub.vars[a.lower()]
+                if v.dims or v.typ == "char" or v.arg:
+                    actual.append(v.name)
+                else:
+                    actual.append("&" + v.name)
+                continue
+            e = sub.expr(a)
+            ct = "int" if e.typ == "int" else "double"
+            pre.append("%s _ca%d = (%s);" % (ct, k, e.code))
+            actual.append("&_ca%d" % k)
+        return "{ %s ref_%s(%s); }" % (" ".join(pre), name, ", ".join(actual))
 
     def _assign(self, sub, s, lines, pad):
         lhs, rhs = _split_assign(s)

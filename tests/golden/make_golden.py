@@ -112,6 +112,12 @@ def make(kind, im, jm, seed):
         resds.append(rd)
     out["wd"] = np.stack(wds)
     out["resd"] = np.stack(resds)
+    # spanwise operators applied to the first direction (coeffs_5p_dz, coeffs_5p_dz2)
+    span_args = residual_args(c)[:9] + tuple(ph[k] for k in PHYS[:9]) + (im, jm)
+    for name, key in (("coeffs_5p_dz", "dz"), ("coeffs_5p_dz2", "dzz")):
+        o = np.zeros_like(w)
+        ref.call(name, o, w, wds[0], *span_args)
+        out[key] = o
     # adjoint: one cotangent on the interior
     rb = np.zeros_like(w)
     rb[3:-3, 3:-3] = rng.standard_normal((im, jm, 5))

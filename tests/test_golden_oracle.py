@@ -62,6 +62,19 @@ def test_adjoint(name):
 
 
 @pytest.mark.parametrize("name", G.CASES)
+@pytest.mark.parametrize("op", ["dz", "dzz"])
+def test_spanwise_operators(name, op):
+    """coeffs_5p_dz / coeffs_5p_dz2 on the first tangent direction; ghosts untouched."""
+    d = G.load(name)
+    c = G.as_case(d)
+    fn = O.dz if op == "dz" else O.dzz
+    got = fn(c["grid"], c["phys"], c["w"], d["wd"][0])
+    sc = np.maximum(np.abs(H.interior(d[op])).reshape(-1, 5).max(0), 1e-300)
+    assert (np.abs(got - d[op]).reshape(-1, 5).max(0) / sc).max() < TOL_DERIV
+    assert not np.any(got[:3]) and not np.any(got[-3:]) and not np.any(got[:, :3]) and not np.any(got[:, -3:])
+
+
+@pytest.mark.parametrize("name", G.CASES)
 def test_norms(name):
     d = G.load(name)
     im, jm = int(d["im"]), int(d["jm"])

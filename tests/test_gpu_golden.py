@@ -1,6 +1,6 @@
 """The CUDA path against the golden fixtures made from the reference's own
 routines (tests/golden/make_golden.py): boundary fills, residual, tangent,
-adjoint, norms and the colored-Jacobian indexing."""
+adjoint, spanwise operators, norms and the colored-Jacobian indexing."""
 import numpy as np
 import pytest
 
@@ -45,6 +45,22 @@ def test_tangent(name):
         f_lin.flux_num_dnc5_2d_d(res, resd, c["w"], np.asfortranarray(d["wd"][k]), *_args(c))
         sc = np.abs(H.interior(d["resd"][k])).reshape(-1, 5).max(0)
         assert H.rel_err(resd, d["resd"][k], sc) < 1e-11
+
+
+@pytest.mark.parametrize("name", G.CASES)
+@pytest.mark.parametrize("op", ["dz", "dzz"])
+def test_spanwise_operators(name, op):
+    from broadcast_gb300.srcfv import f_dz
+    d = G.load(name)
+    c = G.as_case(d)
+    out = np.full_like(c["w"], 7.0)  # ghosts must stay untouched
+    fn = f_dz.coeffs_5p_dz if op == "dz" else f_dz.coeffs_5p_dz2
+    fn(out, c["w"], np.asfortranarray(d["wd"][0]), *_args(c)[:18])
+    sc = np.maximum(np.abs(H.interior(d[op])).reshape(-1, 5).max(0), 1e-300)
+    assert (np.abs(H.interior(out) - H.interior(d[op])).reshape(-1, 5).max(0) / sc).max() < 1e-12
+    ghost = np.ones(out.shape, bool)
+    ghost[3:-3, 3:-3] = False
+    assert np.all(out[ghost] == 7.0)
 
 
 @pytest.mark.parametrize("name", G.CASES)
