@@ -36,6 +36,11 @@ SIGNATURES = {
     "bcg_bc_supandsubinlet_2d_d": "ppsppppd" + "iiii",
     "bcg_bc_extrapolate_o2_2d": "pspiiii",
     "bcg_bc_extrapolate_o2_2d_d": "ppspiiii",
+    "bcg_bc_wall_viscous_adia_2d_b": "ppsdpiii",
+    "bcg_bc_no_reflexion_2d_b": "pppsppp" + "d" + "iiii",
+    "bcg_bc_supandsubinlet_2d_b": "ppsppppd" + "iiii",
+    "bcg_bc_extrapolate_o2_2d_b": "ppspiiii",
+    "bcg_jn_match_2d_b": "pppiiiiii" + "pppiiiiii" + "pi",
     "bcg_jn_match_2d": "ppiiiiii" + "ppiiiiii" + "pi",
     "bcg_jn_match_2d_d": "pppiiiiii" + "pppiiiiii" + "pi",
     "bcg_jn_match_geom_2d": "ppiiiiii" + "ppiiiiii" + "p",

@@ -91,6 +91,7 @@ int bc_call(int kind, double* w, double* wd, const double* aux, int lm, const ch
   if (gh < 1 || im < 1 || jm < 1 || !interf || !loc) return fail_arg("boundary condition: bad extents");
   BcSide side;
   if (!make_side(loc, interf, &side)) return fail_arg("boundary condition: loc must be Ilo, Ihi, Jlo or Jhi");
+  if (!side_in_bounds(side, im, jm, gh)) return fail_arg("boundary condition: interf outside the padded grid");
   const size_t np = ncell(im, jm, gh), nn = nnode(im, jm, gh);
   cudaStream_t st = current_stream();
   Stager sg(st);
@@ -113,9 +114,9 @@ int bc_call(int kind, double* w, double* wd, const double* aux, int lm, const ch
   return sg.finish();
 }
 
-int jn_call(double* wr, const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, int imr, int jmr, const double* wdn,
-            const int* prd, int gh1d, int gh2d, int gh3d, int gh4d, int imd, int jmd, const int* tr, int em) {
-  if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
+// index set-up of borders/jn_match.F90:3-66 shared by the copy and its adjoint
+int jn_args(const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, int imr, int jmr, const int* prd, int gh1d,
+            int gh2d, int gh3d, int gh4d, int imd, int jmd, const int* tr, int em, JnArgs* out) {
   if (!prr || !prd || !tr) return fail_arg("jn_match_2d: null index array");
   auto P = [](const int* a, int r, int c) { return a[(r - 1) + (c - 1) * 2]; };
   JnArgs a{};
@@ -136,6 +137,16 @@ int jn_call(double* wr, const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, 
   const int id_lo = a.prd1i, jd_lo = a.prd1j, id_hi = a.prd1i + ni - 1, jd_hi = a.prd1j + nj - 1;
   if (id_lo < a.lod_i || jd_lo < a.lod_j || id_hi > a.lod_i + a.nid - 1 || jd_hi > a.lod_j + a.njd - 1)
     return fail_arg("jn_match_2d: donor block outside the donor array");
+  *out = a;
+  return BCG_OK;
+}
+
+int jn_call(double* wr, const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, int imr, int jmr, const double* wdn,
+            const int* prd, int gh1d, int gh2d, int gh3d, int gh4d, int imd, int jmd, const int* tr, int em) {
+  if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
+  JnArgs a{};
+  int rc0 = jn_args(prr, gh1r, gh2r, gh3r, gh4r, imr, jmr, prd, gh1d, gh2d, gh3d, gh4d, imd, jmd, tr, em, &a);
+  if (rc0) return rc0;
   cudaStream_t st = current_stream();
   Stager sg(st);
   const size_t nr = (size_t)a.nir * a.njr * em, ndn = (size_t)a.nid * a.njd * em;
@@ -147,6 +158,59 @@ int jn_call(double* wr, const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, 
   a.wr = sg.dev<double>(hr); a.wd = sg.dev<double>(hd);
   cudaError_t e = launch_jn_match(a, st);
   if (e != cudaSuccess) return fail_cuda("jn_match_2d", e);
+  return sg.finish();
+}
+
+// adjoint of the join (adjoint/jn_match_2d_b.f90): wdb = 0, then
+// wdb(donor) += wrb(receiver) and wrb(receiver) = 0; wr and wd are not used
+int jn_b_call(double* wrb, const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, int imr, int jmr, double* wdb,
+              const int* prd, int gh1d, int gh2d, int gh3d, int gh4d, int imd, int jmd, const int* tr, int em) {
+  if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
+  if (!wrb || !wdb) return fail_arg("jn_match_2d_b: null adjoint array");
+  JnArgs a{};
+  int rc = jn_args(prr, gh1r, gh2r, gh3r, gh4r, imr, jmr, prd, gh1d, gh2d, gh3d, gh4d, imd, jmd, tr, em, &a);
+  if (rc) return rc;
+  cudaStream_t st = current_stream();
+  Stager sg(st);
+  const size_t nr = (size_t)a.nir * a.njr * em, ndn = (size_t)a.nid * a.njd * em;
+  int hr, hd;
+  if ((const void*)wrb == (const void*)wdb) { hr = sg.inout(wrb, std::max(nr, ndn) * 8); hd = hr; }
+  else { hr = sg.inout(wrb, nr * 8); hd = sg.out(wdb, ndn * 8); }
+  rc = sg.commit();
+  if (rc) return rc;
+  cudaError_t e = launch_jn_match_adjoint(a, sg.dev<double>(hr), sg.dev<double>(hd), st);
+  if (e != cudaSuccess) return fail_cuda("jn_match_2d_b", e);
+  return sg.finish();
+}
+
+// adjoint of a ghost fill (srcfv/adjoint/bc_*_b.f90): w read, wb updated
+int bc_b_call(int kind, const double* w, double* wb, const double* aux, int lm, const char* loc, const int* interf,
+              const double* nx, const double* ny, double gam, int gh, int im, int jm, int em) {
+  if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
+  if (gh != 3 || im < 1 || jm < 1 || !interf || !loc) return fail_arg("boundary condition adjoint: need gh == 3");
+  if (em < 1 || em > 5) return fail_arg("boundary condition adjoint: em must be 1..5");
+  BcSide side;
+  if (!make_side(loc, interf, &side)) return fail_arg("boundary condition: loc must be Ilo, Ihi, Jlo or Jhi");
+  if (!side_in_bounds(side, im, jm, gh)) return fail_arg("boundary condition: interf outside the padded grid");
+  const size_t np = ncell(im, jm, gh), nn = nnode(im, jm, gh);
+  cudaStream_t st = current_stream();
+  Stager sg(st);
+  const int hw = sg.in(w, np * em * 8);
+  const int hwb = sg.inout(wb, np * em * 8);
+  int haux = -1, hnx = -1, hny = -1;
+  if (kind == BC_NOREF) haux = sg.in(aux, (size_t)lm * 5 * 8);
+  if (kind == BC_INLET) haux = sg.in(aux, (size_t)lm * gh * 5 * 8);
+  if (kind == BC_NOREF || kind == BC_INLET) { hnx = sg.in(nx, nn * 2 * 8); hny = sg.in(ny, nn * 2 * 8); }
+  int rc = sg.commit();
+  if (rc) return rc;
+  BcArgs a{};
+  a.kind = kind; a.im = im; a.jm = jm; a.gh = gh; a.em = em; a.lm = lm; a.side = side; a.gam = gam;
+  a.w = const_cast<double*>(sg.dev<double>(hw));
+  a.aux = haux >= 0 ? sg.dev<double>(haux) : nullptr;
+  a.nx = hnx >= 0 ? sg.dev<double>(hnx) : nullptr;
+  a.ny = hny >= 0 ? sg.dev<double>(hny) : nullptr;
+  cudaError_t e = launch_bc_adjoint(a, sg.dev<double>(hwb), st);
+  if (e != cudaSuccess) return fail_cuda("boundary condition adjoint", e);
   return sg.finish();
 }
 }  // namespace
@@ -350,6 +414,29 @@ int bcg_jn_match_2d_d(double* wr, double* wrd, const int* prr, int gh1r, int gh2
   if (rc) return rc;
   return jn_call(wrd, prr, gh1r, gh2r, gh3r, gh4r, imr, jmr, wdd, prd, gh1d, gh2d, gh3d, gh4d, imd, jmd, tr, em);
 }
+// ---- adjoints of the fills (srcfv/adjoint/*_b.f90); w is left unchanged ------
+int bcg_bc_wall_viscous_adia_2d_b(double* w, double* wb, const char* loc, double gam, const int* interf, int gh,
+                                  int im, int jm) {
+  return bc_b_call(BC_WALL, w, wb, nullptr, 0, loc, interf, nullptr, nullptr, gam, gh, im, jm, 5);
+}
+int bcg_bc_no_reflexion_2d_b(double* w, double* wb, const double* wbd, const char* loc, const int* interf,
+                             const double* nx, const double* ny, double gam, int gh, int im, int jm, int lm) {
+  return bc_b_call(BC_NOREF, w, wb, wbd, lm, loc, interf, nx, ny, gam, gh, im, jm, 5);
+}
+int bcg_bc_supandsubinlet_2d_b(double* w, double* wb, const char* loc, const int* interf, const double* field,
+                               const double* nx, const double* ny, double gam, int im, int jm, int lm, int gh) {
+  return bc_b_call(BC_INLET, w, wb, field, lm, loc, interf, nx, ny, gam, gh, im, jm, 5);
+}
+int bcg_bc_extrapolate_o2_2d_b(double* w, double* wb, const char* loc, const int* interf, int im, int jm, int gh,
+                               int em) {
+  return bc_b_call(BC_EXTRAP, w, wb, nullptr, 0, loc, interf, nullptr, nullptr, 0.0, gh, im, jm, em);
+}
+int bcg_jn_match_2d_b(double* wr, double* wrb, const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, int imr,
+                      int jmr, const double* wd, double* wdb, const int* prd, int gh1d, int gh2d, int gh3d, int gh4d,
+                      int imd, int jmd, const int* tr, int em) {
+  (void)wr; (void)wd;
+  return jn_b_call(wrb, prr, gh1r, gh2r, gh3r, gh4r, imr, jmr, wdb, prd, gh1d, gh2d, gh3d, gh4d, imd, jmd, tr, em);
+}
 // geometric join (srcfv/borders/jn_match_geom.F90:7-69): one-variable copy
 int bcg_jn_match_geom_2d(double* wr, const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, int imr, int jmr,
                          const double* wd, const int* prd, int gh1d, int gh2d, int gh3d, int gh4d, int imd, int jmd,
@@ -542,7 +629,8 @@ int jacobian_bl_csr(int op, const double* w, const double* nx, const double* ny,
     BcArgs b{};
     b.kind = c.kind; b.im = im; b.jm = jm; b.gh = gh; b.em = 5; b.lm = c.lm; b.gam = gam; b.aux = c.aux;
     b.nx = a.nx; b.ny = a.ny;
-    if (!make_side(c.loc, c.it, &b.side)) return fail_arg("jacobian: bad interface");
+    if (!make_side(c.loc, c.it, &b.side) || !side_in_bounds(b.side, im, jm, gh))
+      return fail_arg("jacobian: bad interface");
     a.bcs.push_back(b);
   }
   a.scratch = (double*)pool_get(POOL_SCRATCH, jacobian_scratch_doubles(im, jm, gh) * 8);

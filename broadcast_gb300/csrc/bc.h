@@ -24,6 +24,18 @@ inline bool make_side(const char* loc, const int* interf, BcSide* s) {
   return true;
 }
 
+// Every cell a line touches, base +- gh along the inward normal for l in
+// [lmin, lmax], lies inside the padded (1-gh:im+gh, 1-gh:jm+gh) array.
+inline bool side_in_bounds(const BcSide& s, int im, int jm, int gh) {
+  if (s.lmax < s.lmin) return true;
+  const int l1 = s.lmin, l2 = s.lmax;
+  const int ia = s.imin + (l1 - s.lmin) * s.j0 * s.j0, ib = s.imin + (l2 - s.lmin) * s.j0 * s.j0;
+  const int ja = s.jmin + (l1 - s.lmin) * s.i0 * s.i0, jb = s.jmin + (l2 - s.lmin) * s.i0 * s.i0;
+  const int ilo = (ia < ib ? ia : ib) - gh * (s.i0 != 0), ihi = (ia > ib ? ia : ib) + gh * (s.i0 != 0);
+  const int jlo = (ja < jb ? ja : jb) - gh * (s.j0 != 0), jhi = (ja > jb ? ja : jb) + gh * (s.j0 != 0);
+  return ilo >= 1 - gh && ihi <= im + gh && jlo >= 1 - gh && jhi <= jm + gh;
+}
+
 enum BcKind { BC_WALL = 0, BC_NOREF = 1, BC_INLET = 2, BC_EXTRAP = 3 };
 
 struct BcArgs {
@@ -38,6 +50,9 @@ struct BcArgs {
   const double* ny;
 };
 cudaError_t launch_bc(const BcArgs& a, cudaStream_t st);
+// adjoint of the fill: wb(positions 0..gh of each line) += J^T wb(ghosts),
+// wb(written ghosts) = 0; a.w is read only (the primal state before the fill)
+cudaError_t launch_bc_adjoint(const BcArgs& a, double* wb, cudaStream_t st);
 
 struct JnArgs {
   double* wr;
@@ -49,5 +64,7 @@ struct JnArgs {
   int lod_i, lod_j, nid, njd;   // donor lower bounds and extents
 };
 cudaError_t launch_jn_match(const JnArgs& a, cudaStream_t st);
+// wdb = 0 over its whole extent, then wdb(donor) += wrb(receiver), wrb(receiver) = 0
+cudaError_t launch_jn_match_adjoint(const JnArgs& a, double* wrb, double* wdb, cudaStream_t st);
 
 }  // namespace bcg

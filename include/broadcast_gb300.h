@@ -103,6 +103,24 @@ int bcg_jn_match_2d(double* wr, const int* prr, int gh1r, int gh2r, int gh3r, in
 int bcg_jn_match_2d_d(double* wr, double* wrd, const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, int imr,
                       int jmr, const double* wd, const double* wdd, const int* prd, int gh1d, int gh2d, int gh3d,
                       int gh4d, int imd, int jmd, const int* tr, int em);
+/* ---- adjoints of the fills (srcfv/adjoint, module f_adj) ---------------------- */
+/* bc_wall_viscous_b.f90:11, bc_no_reflexion_b.f90:16, bc_supandsubinlet_b.f90:11,
+ * bc_extrapolateo2_b.f90:18: wb(cells the fill reads) += J^T wb(ghosts), then
+ * wb(written ghosts) = 0; w (the state before the fill) is left unchanged.
+ * jn_match_2d_b.f90:1: wdb = 0 over its whole extent, then wdb(donor) +=
+ * wrb(receiver) and wrb(receiver) = 0; wr and wd are not read. */
+int bcg_bc_wall_viscous_adia_2d_b(double* w, double* wb, const char* loc, double gam, const int* interf, int gh,
+                                  int im, int jm);
+int bcg_bc_no_reflexion_2d_b(double* w, double* wb, const double* wbd, const char* loc, const int* interf,
+                             const double* nx, const double* ny, double gam, int gh, int im, int jm, int lm);
+int bcg_bc_supandsubinlet_2d_b(double* w, double* wb, const char* loc, const int* interf, const double* field,
+                               const double* nx, const double* ny, double gam, int im, int jm, int lm, int gh);
+int bcg_bc_extrapolate_o2_2d_b(double* w, double* wb, const char* loc, const int* interf, int im, int jm, int gh,
+                               int em);
+int bcg_jn_match_2d_b(double* wr, double* wrb, const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, int imr,
+                      int jmr, const double* wd, double* wdb, const int* prd, int gh1d, int gh2d, int gh3d, int gh4d,
+                      int imd, int jmd, const int* tr, int em);
+
 /* srcfv/borders/jn_match_geom.F90:7 (tr(1) = +-1 only) */
 int bcg_jn_match_geom_2d(double* wr, const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, int imr, int jmr,
                          const double* wd, const int* prd, int gh1d, int gh2d, int gh3d, int gh4d, int imd, int jmd,

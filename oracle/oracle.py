@@ -44,6 +44,7 @@ SIGS = {
     "orc_computejacobian": [_I, _P, _P, _P, _P] + [_I] * 6 + [_P],
     "orc_computejacobian_withjnandcheck": [_P, _P, _P, _P] + [_I] * 6 + [_P, _D, _I],
     "orc_coeffs_5p_dz": [_P] * 3 + [_I] + [_P] * 3 + [_I] + [_D] * 9 + [_I] * 3,
+    "orc_bc_b": [_I, _P, _P, _P, _I, _S, _P, _P, _P, _D, _I, _I, _I, _I],
 }
 
 _lock = threading.Lock()
@@ -215,6 +216,18 @@ def bc_extrap(w, loc, interf, im, jm, gh, wd=None):
         lib().orc_bc_extrapolate_o2_2d(_p(w), loc.encode(), _p(it), im, jm, gh, em)
     else:
         lib().orc_bc_extrapolate_o2_2d_d(_p(w), _p(wd), loc.encode(), _p(it), im, jm, gh, em)
+
+
+BC_KIND = {"wall": 0, "noref": 1, "inlet": 2, "extrap": 3}
+
+
+def bc_adjoint(kind, w, wb, loc, interf, gh, im, jm, gam=1.4, aux=None, nx=None, ny=None, em=5):
+    """Transpose of a ghost fill (adjoint/bc_*_b.f90): wb updated in place."""
+    lm = 0 if aux is None else aux.shape[0]
+    lib().orc_bc_b(BC_KIND[kind], _p(_chk(w)), _p(_chk(wb)), None if aux is None else _p(aux), lm, loc.encode(),
+                   _p(_i4(interf)), None if nx is None else _p(nx), None if ny is None else _p(ny), float(gam), gh, im,
+                   jm, em)
+    return wb
 
 
 def jn_match(wr, prr, ghr, imr, jmr, wd, prd, ghd, imd, jmd, tr, em):

@@ -188,6 +188,47 @@ int orc_bc_extrapolate_o2_2d_d(double* w, double* wd, const char* loc, const int
   for (size_t q = 0; q < n; ++q) { w[q] = a[q].v; wd[q] = a[q].d[0]; }
   return 0;
 }
+// ---- adjoints of the ghost fills (the reference's adjoint/bc_*_b.f90) ----------
+// A fill writes the gh ghost layers of each boundary line from the line's
+// positions 0..gh only, and lines are disjoint, so the transpose is exact from
+// gh+1 Dual<5> runs, each seeding the 5 variables at one inward position p of
+// every line:  wb(p) += sum over ghosts of d ghost / d w(p) * wb(ghost), then
+// wb(ghosts) = 0.  kind: 0 wall, 1 no-reflexion, 2 inlet, 3 extrapolation.
+int orc_bc_b(int kind, const double* w, double* wb, const double* aux, int lm, const char* loc, const int* interf,
+             const double* nx, const double* ny, double gam, int gh, int im, int jm, int em) {
+  const Side s(loc, interf);
+  if (!s.ok) return -1;
+  const int ni = im + 2 * gh, nj = jm + 2 * gh, lo = 1 - gh;
+  const size_t n = (size_t)ni * nj * em;
+  FArr<double> WB(wb, ni, nj, lo);
+  std::vector<double> add(n, 0.0);
+  FArr<double> ADD(add.data(), ni, nj, lo);
+  for (int p = 0; p <= gh; ++p) {
+    std::vector<Dual<5>> a(n);
+    for (size_t q = 0; q < n; ++q) a[q] = Dual<5>(w[q]);
+    FArr<Dual<5>> A(a.data(), ni, nj, lo);
+    for (int l = s.lmin; l <= s.lmax; ++l)
+      for (int v = 1; v <= em; ++v) A(s.li(l) + p * s.i0, s.lj(l) + p * s.j0, v).d[v - 1] = 1.0;
+    if (kind == 0) bc_wall_viscous_adia_2d<Dual<5>>(a.data(), loc, gam, interf, gh, im, jm);
+    else if (kind == 1) bc_no_reflexion_2d<Dual<5>>(a.data(), aux, lm, loc, interf, nx, ny, gam, gh, im, jm);
+    else if (kind == 2) bc_supandsubinlet_2d<Dual<5>>(a.data(), loc, interf, aux, lm, nx, ny, gam, im, jm, gh);
+    else bc_extrapolate_o2_2d<Dual<5>>(a.data(), loc, interf, im, jm, gh, em);
+    for (int l = s.lmin; l <= s.lmax; ++l)
+      for (int k = 1; k <= em; ++k) {
+        double acc = 0.0;
+        for (int q = 1; q <= gh; ++q)
+          for (int v = 1; v <= em; ++v)
+            acc += A(s.li(l) - q * s.i0, s.lj(l) - q * s.j0, v).d[k - 1] * WB(s.li(l) - q * s.i0, s.lj(l) - q * s.j0, v);
+        ADD(s.li(l) + p * s.i0, s.lj(l) + p * s.j0, k) += acc;
+      }
+  }
+  for (int l = s.lmin; l <= s.lmax; ++l)
+    for (int q = 1; q <= gh; ++q)
+      for (int v = 1; v <= em; ++v) WB(s.li(l) - q * s.i0, s.lj(l) - q * s.j0, v) = 0.0;
+  for (size_t q = 0; q < n; ++q) wb[q] += add[q];
+  return 0;
+}
+
 int orc_jn_match_2d(double* wr, const int* prr, int gh1r, int gh2r, int gh3r, int gh4r, int imr, int jmr,
                     const double* wd, const int* prd, int gh1d, int gh2d, int gh3d, int gh4d, int imd, int jmd,
                     const int* tr, int em) {

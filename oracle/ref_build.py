@@ -33,6 +33,7 @@ ROUTINES = [
     ("srcfv/adjoint/bc_no_reflexion_b.f90", ["bc_no_reflexion_2d_b"]),
     ("srcfv/adjoint/bc_supandsubinlet_b.f90", ["bc_supandsubinlet_2d_b"]),
     ("srcfv/adjoint/bc_extrapolateo2_b.f90", ["bc_extrapolate_o2_2d_b"]),
+    ("srcfv/adjoint/jn_match_2d_b.f90", ["jn_match_2d_b"]),
     ("misc/ComputeJacobian.f90", ["testvector", "testvector_partial", "computejacobianfromjv",
                                   "computejacobianfromjv_relaxed", "computejacobianfromjv_relaxed_withjn",
                                   "computejacobianfromjv_withjn", "computejacobianfromjv_relaxed_withjnandcheck",

@@ -125,6 +125,43 @@ def make(kind, im, jm, seed):
     wb, r3 = np.zeros_like(w), np.zeros_like(w)
     ref.call("flux_num_dnc5_2d_b", r3, rb, w, wb, *residual_args(c))
     out["wb"] = wb
+    # adjoints of the ghost fills (adjoint/bc_*_b.f90), each applied to a
+    # random cotangent on the state just before that fill in the driver chain
+    it = c["interf"]
+    gam, gh = ph["gam"], g["gh"]
+    wst = w_raw.copy(order="F")
+    chain = [("inlet", "Ilo"), ("noref", "Jhi"), ("extrap", "Ihi"), ("wall", "Jlo")] if kind == "bl" else \
+        [("noref", "Jhi"), ("wall", "Jlo")]
+    for bk, loc in chain:
+        wb0 = np.asfortranarray(rng.standard_normal(w.shape))
+        wb = wb0.copy(order="F")
+        wcopy = wst.copy(order="F")
+        if bk == "inlet":
+            fld = c["field"]
+            ref.call("bc_supandsubinlet_2d_b", wcopy, wb, loc, fi(it[loc]), fld, g["nx"], g["ny"], gam, im, jm,
+                     fld.shape[0], gh)
+            ref.call("bc_supandsubinlet_2d", wst, loc, fi(it[loc]), fld, g["nx"], g["ny"], gam, im, jm, fld.shape[0], gh)
+        elif bk == "noref":
+            wbd = c["wbd"]
+            ref.call("bc_no_reflexion_2d_b", wcopy, wb, wbd, loc, fi(it[loc]), g["nx"], g["ny"], gam, gh, im, jm,
+                     wbd.shape[0])
+            ref.call("bc_no_reflexion_2d", wst, wbd, loc, fi(it[loc]), g["nx"], g["ny"], gam, gh, im, jm, wbd.shape[0])
+        elif bk == "extrap":
+            ref.call("bc_extrapolate_o2_2d_b", wcopy, wb, loc, fi(it[loc]), im, jm, gh, 5)
+            ref.call("bc_extrapolate_o2_2d", wst, loc, fi(it[loc]), im, jm, gh, 5)
+        else:
+            ref.call("bc_wall_viscous_adia_2d_b", wcopy, wb, loc, gam, fi(it[loc]), gh, im, jm)
+            ref.call("bc_wall_viscous_adia_2d", wst, loc, gam, fi(it[loc]), gh, im, jm)
+        out["bcb_%s_w" % bk] = wcopy
+        out["bcb_%s_in" % bk] = wb0
+        out["bcb_%s_out" % bk] = wb
+    if kind == "cyl":
+        # adjoint of one periodic join copy (adjoint/jn_match_2d_b.f90)
+        wrb0 = np.asfortranarray(rng.standard_normal(w.shape))
+        wrb, wdb = wrb0.copy(order="F"), np.asfortranarray(rng.standard_normal(w.shape))
+        ref.call("jn_match_2d_b", w.copy(order="F"), wrb, fi(it["prr1"]), gh, gh, gh, gh, im, jm, w.copy(order="F"),
+                 wdb, fi(it["prd2"]), gh, gh, gh, gh, im, jm, fi(it["tr"]), 5)
+        out.update(jnb_wrb_in=wrb0, jnb_wrb_out=wrb, jnb_wdb_out=wdb)
     # norms of the residual
     n2, nm = np.zeros(5), np.zeros(5)
     ref.call("compute_norml2", n2, nm, res, im, jm, 3)

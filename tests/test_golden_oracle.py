@@ -74,6 +74,32 @@ def test_spanwise_operators(name, op):
     assert not np.any(got[:3]) and not np.any(got[-3:]) and not np.any(got[:, :3]) and not np.any(got[:, -3:])
 
 
+def _fill_adjoint_cases():
+    out = []
+    for name in G.CASES:
+        kinds = ("inlet", "noref", "extrap", "wall") if name.startswith("bl") else ("noref", "wall")
+        out += [(name, k) for k in kinds]
+    return out
+
+
+LOCS = {"inlet": "Ilo", "noref": "Jhi", "extrap": "Ihi", "wall": "Jlo"}
+
+
+@pytest.mark.parametrize("name,kind", _fill_adjoint_cases())
+def test_fill_adjoints(name, kind):
+    """Transposes of the ghost fills against adjoint/bc_*_b.f90."""
+    d = G.load(name)
+    c = G.as_case(d)
+    g, ph = c["grid"], c["phys"]
+    loc = LOCS[kind]
+    wb = d["bcb_%s_in" % kind].copy(order="F")
+    aux = {"inlet": c.get("field"), "noref": c["wbd"]}.get(kind)
+    O.bc_adjoint(kind, d["bcb_%s_w" % kind], wb, loc, c["interf"][loc], g["gh"], g["im"], g["jm"], gam=ph["gam"],
+                 aux=aux, nx=g["nx"], ny=g["ny"])
+    ref = d["bcb_%s_out" % kind]
+    assert np.abs(wb - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
 @pytest.mark.parametrize("name", G.CASES)
 def test_norms(name):
     d = G.load(name)

@@ -48,3 +48,49 @@ def test_dot_product_identity():
     f_adj.flux_num_dnc5_2d_b(None, u.copy(order="F"), c["w"], wb, *_args(c))
     a, b = np.sum(H.interior(jv) * H.interior(u)), np.sum(v * wb)
     assert abs(a - b) <= 1e-12 * max(abs(a), abs(b)), (a, b)
+
+
+def test_boundary_chain_adjoint_dot_product():
+    """Full boundary-layer chain (inlet, no-reflexion, extrapolation, wall):
+    <T x, y> = <x, T^T y> with the tangent fills forward and the fill
+    adjoints in reverse order, on the GPU, against the oracle's adjoints."""
+    from broadcast_gb300.srcfv import f_adj, f_lin
+    c = H.bl_case(64, 40)
+    g, ph, it = c["grid"], c["phys"], c["interf"]
+    im, jm, gh = g["im"], g["jm"], g["gh"]
+    rng = np.random.default_rng(21)
+    x = np.asfortranarray(rng.standard_normal(c["w"].shape))
+    y = np.asfortranarray(rng.standard_normal(c["w"].shape))
+    # states before each fill
+    states = []
+    w = c["w"].copy(order="F")
+    steps = [("inlet", "Ilo"), ("noref", "Jhi"), ("extrap", "Ihi"), ("wall", "Jlo")]
+    tx = x.copy(order="F")
+    for kind, loc in steps:
+        states.append(w.copy(order="F"))
+        if kind == "inlet":
+            f_lin.bc_supandsubinlet_2d_d(w, tx, loc, it[loc], c["field"], g["nx"], g["ny"], ph["gam"], im, jm)
+        elif kind == "noref":
+            f_lin.bc_no_reflexion_2d_d(w, tx, c["wbd"], loc, it[loc], g["nx"], g["ny"], ph["gam"], gh, im, jm)
+        elif kind == "extrap":
+            f_lin.bc_extrapolate_o2_2d_d(w, tx, loc, it[loc], im, jm, gh)
+        else:
+            f_lin.bc_wall_viscous_adia_2d_d(w, tx, loc, ph["gam"], it[loc], gh, im, jm)
+    ty = y.copy(order="F")
+    oy = y.copy(order="F")
+    for (kind, loc), ws in zip(reversed(steps), reversed(states)):
+        wcopy = ws.copy(order="F")
+        aux = {"inlet": c["field"], "noref": c["wbd"]}.get(kind)
+        O.bc_adjoint(kind, ws, oy, loc, it[loc], gh, im, jm, gam=ph["gam"], aux=aux, nx=g["nx"], ny=g["ny"])
+        if kind == "inlet":
+            f_adj.bc_supandsubinlet_2d_b(wcopy, ty, loc, it[loc], c["field"], g["nx"], g["ny"], ph["gam"], im, jm)
+        elif kind == "noref":
+            f_adj.bc_no_reflexion_2d_b(wcopy, ty, c["wbd"], loc, it[loc], g["nx"], g["ny"], ph["gam"], gh, im, jm)
+        elif kind == "extrap":
+            f_adj.bc_extrapolate_o2_2d_b(wcopy, ty, loc, it[loc], im, jm, gh)
+        else:
+            f_adj.bc_wall_viscous_adia_2d_b(wcopy, ty, loc, ph["gam"], it[loc], gh, im, jm)
+        assert np.array_equal(wcopy, ws)
+    assert np.abs(ty - oy).max() <= 1e-12 * np.abs(oy).max()
+    lhs, rhs = float(np.vdot(tx, y)), float(np.vdot(x, ty))
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), np.abs(tx).max() * np.abs(y).sum())

@@ -63,6 +63,50 @@ def test_spanwise_operators(name, op):
     assert np.all(out[ghost] == 7.0)
 
 
+def _fill_adjoint_cases():
+    out = []
+    for name in G.CASES:
+        kinds = ("inlet", "noref", "extrap", "wall") if name.startswith("bl") else ("noref", "wall")
+        out += [(name, k) for k in kinds]
+    return out
+
+
+@pytest.mark.parametrize("name,kind", _fill_adjoint_cases())
+def test_fill_adjoints(name, kind):
+    from broadcast_gb300.srcfv import f_adj
+    d = G.load(name)
+    c = G.as_case(d)
+    g, ph, it = c["grid"], c["phys"], c["interf"]
+    im, jm, gh = g["im"], g["jm"], g["gh"]
+    w = d["bcb_%s_w" % kind].copy(order="F")
+    w0 = w.copy(order="F")
+    wb = d["bcb_%s_in" % kind].copy(order="F")
+    if kind == "inlet":
+        f_adj.bc_supandsubinlet_2d_b(w, wb, "Ilo", it["Ilo"], c["field"], g["nx"], g["ny"], ph["gam"], im, jm)
+    elif kind == "noref":
+        f_adj.bc_no_reflexion_2d_b(w, wb, c["wbd"], "Jhi", it["Jhi"], g["nx"], g["ny"], ph["gam"], gh, im, jm)
+    elif kind == "extrap":
+        f_adj.bc_extrapolate_o2_2d_b(w, wb, "Ihi", it["Ihi"], im, jm, gh)
+    else:
+        f_adj.bc_wall_viscous_adia_2d_b(w, wb, "Jlo", ph["gam"], it["Jlo"], gh, im, jm)
+    ref = d["bcb_%s_out" % kind]
+    assert np.abs(wb - ref).max() <= 1e-13 * np.abs(ref).max()
+    assert np.array_equal(w, w0)
+
+
+def test_join_adjoint():
+    from broadcast_gb300.srcfv import f_adj
+    d = G.load("cyl_14x8")
+    c = G.as_case(d)
+    g, it = c["grid"], c["interf"]
+    gh = g["gh"]
+    wrb = d["jnb_wrb_in"].copy(order="F")
+    wdb = np.full_like(wrb, 5.0)  # overwritten: zeroed, then accumulated
+    f_adj.jn_match_2d_b(c["w"], wrb, it["prr1"], gh, gh, gh, gh, g["im"], g["jm"], c["w"], wdb, it["prd2"], gh, gh,
+                        gh, gh, g["im"], g["jm"], it["tr"])
+    assert np.array_equal(wrb, d["jnb_wrb_out"]) and np.array_equal(wdb, d["jnb_wdb_out"])
+
+
 @pytest.mark.parametrize("name", G.CASES)
 def test_adjoint(name):
     from broadcast_gb300.srcfv import f_adj
