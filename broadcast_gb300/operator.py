@@ -72,3 +72,12 @@ class Dnc5Operator:
         _lib.call("bcg_flux_num_dnc5_2d_dn", res, resd, w, wds.contiguous(), wds.shape[0], None, None, self.nx,
                   self.ny, None, None, self.vol, self.volf, self.gh, *self.phys, self.im, self.jm)
         return res, (resd[0] if single else resd)
+
+    def vjp(self, w, rb, wb=None):
+        """wb = (dR/dw)^T rb over every padded cell (rb: interior cotangent,
+        left unchanged here; the library consumes a copy)."""
+        wb = self.new_state() if wb is None else wb
+        rbc = rb.detach().clone().contiguous()
+        _lib.call("bcg_flux_num_dnc5_2d_b", None, rbc, w, wb, None, None, self.nx, self.ny, None, None, self.vol,
+                  self.volf, self.gh, *self.phys, self.im, self.jm)
+        return wb
