@@ -63,23 +63,26 @@ int residual_call(double* residu, double* residud, const double* w, const double
   } else {
     const double* wdd = sg.dev<double>(hwd);
     double* rdd = sg.dev<double>(hresd);
-    for (int k0 = 0; k0 < nd; k0 += 4) {
-      const int kk = std::min(4, nd - k0);
-      // kernels exist for 1, 2 and 4 directions: a group of 3 runs as 2 + 1
-      int parts[2] = {kk, 0};
-      if (kk == 3) { parts[0] = 2; parts[1] = 1; }
-      int off = k0;
-      for (int pi = 0; pi < 2 && parts[pi] > 0; ++pi) {
-        a.ndir = parts[pi];
-        a.wd = wdd + (size_t)off * np * 5;
-        a.resd = rdd + (size_t)off * np * 5;
-        a.res = (off == 0) ? res : nullptr;
-        a.scratch = (double*)pool_get(POOL_SCRATCH, residual_scratch_doubles(im, jm, gh, a.ndir) * 8);
-        if (!a.scratch) return fail_arg("scratch allocation failed"), BCG_ERR_NOMEM;
-        cudaError_t e = run_residual(a, st);
-        if (e != cudaSuccess) return fail_cuda("flux_num_dnc5_2d_d", e);
-        off += parts[pi];
-      }
+    // full groups of 4 directions run as one launch per pass (blockIdx.y =
+    // group), as many groups at a time as fit a 2 GiB scratch budget; the
+    // remaining 1-3 directions run as 2 + 1
+    const size_t s4 = residual_scratch_doubles(im, jm, gh, 4);
+    const int gmax = (int)std::max<size_t>(1, ((size_t)2 << 30) / (s4 * 8));
+    int off = 0;
+    while (off < nd) {
+      const int left = nd - off;
+      int kk, ng;
+      if (left >= 4) { kk = 4; ng = std::min(left / 4, gmax); }
+      else { kk = left >= 2 ? 2 : 1; ng = 1; }
+      a.ndir = kk; a.ngroup = ng;
+      a.wd = wdd + (size_t)off * np * 5;
+      a.resd = rdd + (size_t)off * np * 5;
+      a.res = (off == 0) ? res : nullptr;
+      a.scratch = (double*)pool_get(POOL_SCRATCH, residual_scratch_doubles(im, jm, gh, kk) * 8 * (size_t)ng);
+      if (!a.scratch) return fail_arg("scratch allocation failed"), BCG_ERR_NOMEM;
+      cudaError_t e = run_residual(a, st);
+      if (e != cudaSuccess) return fail_cuda("flux_num_dnc5_2d_d", e);
+      off += kk * ng;
     }
   }
   return sg.finish();

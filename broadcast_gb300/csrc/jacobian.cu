@@ -14,6 +14,7 @@
 // row: the candidate columns of a row are known in closed form from the seed
 // formulas, so each row is enumerated directly in ascending column order --
 // no global sort, two passes (count, fill) around one exclusive scan.
+#include <algorithm>
 #include <cstdio>
 #include <vector>
 #include "assembly.h"
@@ -143,12 +144,22 @@ __global__ void k_ptr_to_int(const long long* __restrict__ p, int* __restrict__ 
 
 }  // namespace
 
+// seed groups of 4 per tangent launch: as many as fit an 8 GiB budget for
+// their seeded states and residual scratch (all 61 at 256 x 256)
+static int jacobian_groups(int im, int jm, int gh) {
+  const size_t np = (size_t)(im + 2 * gh) * (jm + 2 * gh);
+  const size_t per = (4 * np * 5 + residual_scratch_doubles(im, jm, gh, 4)) * 8;
+  const size_t g = ((size_t)8 << 30) / per;
+  return (int)std::max<size_t>(1, std::min<size_t>(61, g));
+}
+
 size_t jacobian_scratch_doubles(int im, int jm, int gh) {
   const size_t np = (size_t)(im + 2 * gh) * (jm + 2 * gh);
+  const size_t G = (size_t)jacobian_groups(im, jm, gh);
   return 245 * np * 5      // tangent outputs of every seed
-         + 4 * np * 5      // 4 seeded tangent states
+         + 4 * G * np * 5  // seeded tangent states of G groups
          + np * 5          // state copy written by the linearised boundary fills
-         + residual_scratch_doubles(im, jm, gh, 4);
+         + G * residual_scratch_doubles(im, jm, gh, 4);
 }
 
 int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
@@ -156,7 +167,7 @@ int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
   const size_t np = (size_t)(im + 2 * gh) * (jm + 2 * gh);
   double* resd_all = a.scratch;
   double* wd4 = resd_all + 245 * np * 5;
-  double* wcopy = wd4 + 4 * np * 5;
+  double* wcopy = wd4 + 4 * (size_t)jacobian_groups(im, jm, gh) * np * 5;
   double* rscr = wcopy + np * 5;
   int* seeds_dev = a.iscratch;                        // 245 x 3
   long long* rowptr = (long long*)(a.iscratch + 1024);  // nrow + 1 (8-byte aligned offset)
@@ -177,35 +188,41 @@ int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
   ResidualArgs ra{};
   ra.im = im; ra.jm = jm; ra.gh = gh; ra.phys = a.phys; ra.w = wcopy; ra.nx = a.nx; ra.ny = a.ny;
   ra.vol = a.vol; ra.volf = a.volf; ra.dstride = np * 5; ra.scratch = rscr; ra.res = nullptr;
-  for (int s0 = 0; s0 < 245; s0 += 4) {
-    const int ns = s0 + 4 <= 245 ? 4 : 245 - s0;
+  // chunks of G groups of 4 seeds: seed, linearised boundary chain per group,
+  // then one tangent launch per pass over the whole chunk (blockIdx.y = group);
+  // the last seed (245 = 61 * 4 + 1) runs as a 1-direction chunk
+  const int G = jacobian_groups(im, jm, gh);
+  ra.ndir = 4;
+  for (int s0 = 0; s0 < 245;) {
+    const int left = 245 - s0;
+    const int kk = left >= 4 ? 4 : 1;
+    const int ng = left >= 4 ? std::min(G, left / 4) : 1;
+    const int ns = kk * ng;
     k_seed4<<<1024, 256, 0, st>>>(wd4, ns, seeds_dev + 3 * s0, gh, im, jm);
-    // linearised boundary chain on (state copy, tangents), 1, 2 or 4 directions
-    for (int pi = 0; pi < 2; ++pi) {
-      const int off = pi == 0 ? 0 : (ns == 3 ? 2 : ns);
-      const int nd = pi == 0 ? (ns == 3 ? 2 : ns) : (ns == 3 ? 1 : 0);
-      if (nd == 0) break;
+    for (int g = 0; g < ng; ++g)
       for (const BcArgs& b0 : a.bcs) {
         BcArgs b = b0;
-        b.ndir = nd; b.w = wcopy; b.wd = wd4 + (size_t)off * np * 5; b.dstride = np * 5;
+        b.ndir = kk; b.w = wcopy; b.wd = wd4 + (size_t)g * kk * np * 5; b.dstride = np * 5;
         e = launch_bc(b, st);
         if (e != cudaSuccess) return fail_cuda("jacobian: boundary fill", e);
       }
-      if (a.op == 0) {
-        ra.ndir = nd;
-        ra.wd = wd4 + (size_t)off * np * 5;
-        ra.resd = resd_all + (size_t)(s0 + off) * np * 5;
-        e = run_residual(ra, st);
-        if (e != cudaSuccess) return fail_cuda("jacobian: tangent residual", e);
-      } else {
+    if (a.op == 0) {
+      ra.ndir = kk; ra.ngroup = ng;
+      ra.wd = wd4;
+      ra.resd = resd_all + (size_t)s0 * np * 5;
+      e = run_residual(ra, st);
+      if (e != cudaSuccess) return fail_cuda("jacobian: tangent residual", e);
+    } else {
+      for (int g = 0; g < ng; ++g) {
         SpanArgs sa{};
-        sa.im = im; sa.jm = jm; sa.gh = gh; sa.op = a.op; sa.ndir = nd; sa.phys = a.phys; sa.w = wcopy;
-        sa.wd = wd4 + (size_t)off * np * 5; sa.dstride = np * 5; sa.nx = a.nx; sa.ny = a.ny; sa.vol = a.vol;
-        sa.out = resd_all + (size_t)(s0 + off) * np * 5;
+        sa.im = im; sa.jm = jm; sa.gh = gh; sa.op = a.op; sa.ndir = kk; sa.phys = a.phys; sa.w = wcopy;
+        sa.wd = wd4 + (size_t)g * kk * np * 5; sa.dstride = np * 5; sa.nx = a.nx; sa.ny = a.ny; sa.vol = a.vol;
+        sa.out = resd_all + (size_t)(s0 + g * kk) * np * 5;
         e = run_span(sa, st);
         if (e != cudaSuccess) return fail_cuda("jacobian: spanwise operator", e);
       }
     }
+    s0 += ns;
   }
   // CSR: count, scan, fill
   const int B = 128;

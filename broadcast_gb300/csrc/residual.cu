@@ -12,12 +12,24 @@
 
 namespace bcg {
 
+// Direction groups: a launch may cover several groups of K directions, group
+// g = blockIdx.y reading tangents g*K .. g*K+K-1 and owning its own scratch.
+struct GroupStride {
+  size_t tangent;  // doubles between the tangent planes of consecutive groups (K * dstride)
+  size_t scratch;  // doubles between the scratch blocks of consecutive groups
+};
+BCG_HD void shift_state(State<double>&, size_t) {}
+template <int K> BCG_HD void shift_state(State<DK<K>>& w, size_t off) { w.d += off; }
+template <class S> BCG_HD void shift_scratch(Scratch<S>& s, size_t off) { s.p += off; }
+
 // ---------------------------------------------------------------------------
 // pass 1: primitives on every padded cell (phys/Primitives.F, phys/viscosity.F)
 template <class S>
-__global__ void __launch_bounds__(256) k_prim(Ext e, Coef c, State<S> w, Scratch<S> pr) {
+__global__ void __launch_bounds__(256) k_prim(Ext e, Coef c, State<S> w, Scratch<S> pr, GroupStride gs) {
   const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= e.np) return;
+  shift_state(w, blockIdx.y * gs.tangent);
+  shift_scratch(pr, blockIdx.y * gs.scratch);
   const size_t n = e.np;
   const S ro = w(q), ru = w(q + n), rv = w(q + 2 * n), rw = w(q + 3 * n), re = w(q + 4 * n);
   const S rom1 = 1.0 / ro;
@@ -46,9 +58,11 @@ __global__ void __launch_bounds__(256) k_prim(Ext e, Coef c, State<S> w, Scratch
 //   QJ at j-face location (i, j): rows j-2..j+1 of column i, i in [-1, im+2], j in [2, jm+1]
 // for u, v, w, T and mu (rhs/flux_visqueux_o4_i.F, _j.F).
 template <class S>
-__global__ void __launch_bounds__(256) k_qrows(Ext e, Scratch<S> pr, Scratch<S> qr) {
+__global__ void __launch_bounds__(256) k_qrows(Ext e, Scratch<S> pr, Scratch<S> qr, GroupStride gs) {
   const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= e.np) return;
+  shift_scratch(pr, blockIdx.y * gs.scratch);
+  shift_scratch(qr, blockIdx.y * gs.scratch);
   const int i = (int)(q % e.ni) + 1 - e.gh, j = (int)(q / e.ni) + 1 - e.gh;
   const int fl[5] = {F_U, F_V, F_W, F_T, F_MU};
   const int di = 1, dj = e.ni;
@@ -73,9 +87,12 @@ __global__ void __launch_bounds__(256) k_qrows(Ext e, Scratch<S> pr, Scratch<S> 
 // (rhs/gradop_5pi.F, gradop_5pj.F, gradient.F)
 template <class S>
 __global__ void __launch_bounds__(256) k_grad(Ext e, Coef c, Scratch<S> pr, Scratch<S> gr, const double* __restrict__ nx,
-                                              const double* __restrict__ ny, const double* __restrict__ vol) {
+                                              const double* __restrict__ ny, const double* __restrict__ vol,
+                                              GroupStride gs) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= e.im * e.jm) return;
+  shift_scratch(pr, blockIdx.y * gs.scratch);
+  shift_scratch(gr, blockIdx.y * gs.scratch);
   const int i = 1 + t % e.im, j = 1 + t / e.im;
   const size_t q = e.cidx(i, j);
   const int di = 1, dj = e.ni;
@@ -349,11 +366,17 @@ struct FaceCtx {
 // and the j-face (i <= im) of the node.  hn holds 10 fields (5 i-face, 5
 // j-face) on the (im+1) x (jm+1) node set.
 template <class S>
-__global__ void __launch_bounds__(128) k_faces(FaceCtx<S> fc, Scratch<S> hn) {
-  const Ext& e = fc.e;
+__global__ void __launch_bounds__(128) k_faces(FaceCtx<S> fc0, Scratch<S> hn, GroupStride gs) {
+  const Ext& e = fc0.e;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int nI = e.im + 1;
   if (t >= nI * (e.jm + 1)) return;
+  FaceCtx<S> fc = fc0;
+  shift_state(fc.w, blockIdx.y * gs.tangent);
+  shift_scratch(fc.pr, blockIdx.y * gs.scratch);
+  shift_scratch(fc.gr, blockIdx.y * gs.scratch);
+  shift_scratch(fc.qr, blockIdx.y * gs.scratch);
+  shift_scratch(hn, blockIdx.y * gs.scratch);
   const int i = 1 + t % nI, j = 1 + t / nI;
   S h[5];
   if (j <= e.jm) {
@@ -371,9 +394,11 @@ __global__ void __launch_bounds__(128) k_faces(FaceCtx<S> fc, Scratch<S> hn) {
 // balance (rhs/balance.F): residu = -(h1(i+1)-h1(i)) - (h2(j+1)-h2(j))
 template <class S>
 __global__ void __launch_bounds__(256) k_balance(Ext e, Scratch<S> hn, double* __restrict__ res, double* __restrict__ resd,
-                                                 size_t dstride) {
+                                                 size_t dstride, GroupStride gs) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= e.im * e.jm) return;
+  shift_scratch(hn, blockIdx.y * gs.scratch);
+  if (blockIdx.y > 0) { res = nullptr; resd += blockIdx.y * gs.tangent; }
   const int i = 1 + t % e.im, j = 1 + t / e.im;
   const int nI = e.im + 1;
   const int a = (i - 1) + (j - 1) * nI;
@@ -406,25 +431,29 @@ static cudaError_t run_residual_t(const ResidualArgs& a, cudaStream_t st) {
   State<S> w;
   if constexpr (NP == 1) w = State<S>{a.w};
   else w = State<S>{a.w, a.wd, a.dstride};
+  const unsigned ng = a.ngroup > 1 ? (unsigned)a.ngroup : 1u;
+  if (NP == 1 && ng > 1) return cudaErrorInvalidValue;
+  const GroupStride gs{(size_t)NDir<S>::value * a.dstride, residual_scratch_doubles(a.im, a.jm, a.gh, NDir<S>::value)};
   const int B = 256;
-  k_prim<S><<<(unsigned)((e.np + B - 1) / B), B, 0, st>>>(e, c, w, pr);
+  k_prim<S><<<dim3((unsigned)((e.np + B - 1) / B), ng), B, 0, st>>>(e, c, w, pr, gs);
   if (c.k2 != 0.0)
-    k_grad<S><<<(unsigned)((a.im * a.jm + B - 1) / B), B, 0, st>>>(e, c, pr, gr, a.nx, a.ny, a.vol);
-  k_qrows<S><<<(unsigned)((e.np + B - 1) / B), B, 0, st>>>(e, pr, qr);
+    k_grad<S><<<dim3((unsigned)((a.im * a.jm + B - 1) / B), ng), B, 0, st>>>(e, c, pr, gr, a.nx, a.ny, a.vol, gs);
+  k_qrows<S><<<dim3((unsigned)((e.np + B - 1) / B), ng), B, 0, st>>>(e, pr, qr, gs);
   FaceCtx<S> fc{e, c, w, pr, gr, qr, a.nx, a.ny, a.vol, a.volf};
   const int BF = 128;
-  k_faces<S><<<(unsigned)((nn + BF - 1) / BF), BF, 0, st>>>(fc, hn);
-  k_balance<S><<<(unsigned)((a.im * a.jm + B - 1) / B), B, 0, st>>>(e, hn, a.res, a.resd, a.dstride);
+  k_faces<S><<<dim3((unsigned)((nn + BF - 1) / BF), ng), BF, 0, st>>>(fc, hn, gs);
+  k_balance<S><<<dim3((unsigned)((a.im * a.jm + B - 1) / B), ng), B, 0, st>>>(e, hn, a.res, a.resd, a.dstride, gs);
   return cudaGetLastError();
 }
 
 void launch_primal_passes(const Ext& e, const Coef& c, const double* w, double* pr, double* gr, const double* nx,
                           const double* ny, const double* vol, cudaStream_t st) {
   const int B = 256;
-  k_prim<double><<<(unsigned)((e.np + B - 1) / B), B, 0, st>>>(e, c, State<double>{w}, Scratch<double>{pr, e.np});
+  const GroupStride gs{0, 0};
+  k_prim<double><<<(unsigned)((e.np + B - 1) / B), B, 0, st>>>(e, c, State<double>{w}, Scratch<double>{pr, e.np}, gs);
   if (c.k2 != 0.0)
     k_grad<double><<<(unsigned)((e.im * e.jm + B - 1) / B), B, 0, st>>>(e, c, Scratch<double>{pr, e.np},
-                                                                        Scratch<double>{gr, e.np}, nx, ny, vol);
+                                                                        Scratch<double>{gr, e.np}, nx, ny, vol, gs);
 }
 
 size_t residual_scratch_doubles(int im, int jm, int gh, int ndir) {

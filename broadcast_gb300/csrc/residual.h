@@ -19,7 +19,9 @@ struct ResidualArgs {
   const double* volf;    // (ni, nj, 2)
   double* res;           // (ni, nj, 5), interior written; may be null when ndir > 0
   double* resd;          // K stacked (ni, nj, 5), interior written
-  double* scratch;       // residual_scratch_doubles(im, jm, gh, ndir) doubles
+  double* scratch;       // ngroup * residual_scratch_doubles(im, jm, gh, ndir) doubles
+  int ngroup;            // 0 or 1: one group; G > 1 (ndir > 0): G groups of ndir directions in one launch,
+                         // group g reading wd + g*ndir*dstride and writing resd + g*ndir*dstride
 };
 
 size_t residual_scratch_doubles(int im, int jm, int gh, int ndir);
