@@ -377,6 +377,116 @@ def run_ours(args):
     return 0
 
 
+def bl_bcs(c, w):
+    """Boundary-layer sequence of BROADCAST_npz.py:1018-1021 through the library."""
+    from broadcast_gb300.srcfv import f_bnd
+    g, ph, it = c["grid"], c["phys"], c["interf"]
+    im, jm, gh = g["im"], g["jm"], g["gh"]
+    f_bnd.bc_supandsubinlet_2d(w, "Ilo", it["Ilo"], c["field"], g["nx"], g["ny"], ph["gam"], im, jm)
+    f_bnd.bc_no_reflexion_2d(w, c["wbd"], "Jhi", it["Jhi"], g["nx"], g["ny"], ph["gam"], gh, im, jm)
+    f_bnd.bc_extrapolate_o2_2d(w, "Ihi", it["Ihi"], im, jm, gh)
+    f_bnd.bc_wall_viscous_adia_2d(w, "Jlo", ph["gam"], it["Jlo"], gh, im, jm)
+
+
+def run_jacobian_workload(args):
+    """Batched colored Jacobian of the 1024 x 512 boundary layer (the
+    reference's third configuration): all 245 seeds (J / vol), Dz and Dzz as
+    CSR, then J(beta) = J - beta^2 Dzz + i beta Dz for 16 beta in [0, 2],
+    device-resident; beside it the reference loop (BROADCAST_npz.py:1068-1137)
+    through the oracle on a sample of seeds, scaled to 245."""
+    import torch
+    from broadcast_gb300 import _lib, cases
+    from broadcast_gb300._f2py import interf4
+    im, jm = args.im or 1024, args.jm or 512
+    c = cases.bl_case(im, jm, seed=3, ops=LibOps)
+    bl_bcs(c, c["w"])
+    g, ph, it = c["grid"], c["phys"], c["interf"]
+    gh = g["gh"]
+    nrow = 5 * im * jm
+    dev = torch.device("cuda", 0)
+    _lib.call("bcg_set_stream", torch.cuda.current_stream(dev).cuda_stream)
+    keys = ("cp", "cv", "prandtl", "gam", "rgaz", "cs", "muref", "tref", "s_suth")
+    common = [interf4(it["Ilo"]), interf4(it["Jhi"]), interf4(it["Ihi"]), interf4(it["Jlo"]), c["field"],
+              c["field"].shape[0], c["wbd"], c["wbd"].shape[0]]
+    geo = [c["w"], g["nx"], g["ny"], g["vol"], g["volf"], gh]
+    cap = nrow * 245
+    outs = {}
+    for name in ("J", "Dz", "Dzz"):
+        outs[name] = (torch.empty(nrow + 1, dtype=torch.int32, device=dev),
+                      torch.empty(cap, dtype=torch.int32, device=dev),
+                      torch.empty(cap, dtype=torch.float64, device=dev),
+                      np.zeros(1, np.int64))
+
+    def assemble(name):
+        ip, ix, dv, nnz = outs[name]
+        if name == "J":
+            _lib.call("bcg_jacobian_dnc5_bl_csr", *geo, *[float(ph[k]) for k in keys + ("k2", "k4")], im, jm,
+                      *common, None, 2e-16, 1, ip, ix, dv, ix.numel(), nnz)
+        else:
+            _lib.call("bcg_jacobian_dz_bl_csr", *geo, *[float(ph[k]) for k in keys], im, jm, *common,
+                      1 if name == "Dz" else 2, 2e-16, ip, ix, dv, ix.numel(), nnz)
+        return int(nnz[0])
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            r = fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps, r
+
+    t_j, nnz_j = timed(lambda: assemble("J"), args.steps)
+    t_dz, nnz_dz = timed(lambda: assemble("Dz"), args.steps)
+    t_dzz, nnz_dzz = timed(lambda: assemble("Dzz"), args.steps)
+    betas = torch.linspace(0.0, 2.0, 16, dtype=torch.float64)
+    nb = np.zeros(1, np.int64)
+    J, Dz, Dzz = outs["J"], outs["Dz"], outs["Dzz"]
+    bargs = (nrow, J[0], J[1], J[2], Dz[0], Dz[1], Dz[2], Dzz[0], Dzz[1], Dzz[2], 16, betas.numpy())
+    bp = torch.empty(nrow + 1, dtype=torch.int32, device=dev)
+    try:
+        _lib.call("bcg_csr_spanwise_beta", *bargs, bp, bp, bp, 0, nb)  # capacity 0: returns the union size
+    except _lib.BroadcastError:
+        pass
+    nnz_u = int(nb[0])
+    bi = torch.empty(nnz_u, dtype=torch.int32, device=dev)
+    bv = torch.empty(2 * 16 * nnz_u, dtype=torch.float64, device=dev)
+    t_beta, _ = timed(lambda: _lib.call("bcg_csr_spanwise_beta", *bargs, bp, bi, bv, nnz_u, nb), args.steps)
+    # reference loop through the oracle (OpenMP), a sample of seeds
+    from oracle import oracle as O
+    lib = O.lib(openmp=True)
+    nsample = 4
+    w = c["w"]
+    res, resd = np.zeros_like(w), np.zeros_like(w)
+    nb_ = im * jm * 49 * 25
+    jac, ia, ja = np.zeros(nb_), np.zeros(nb_, np.int32), np.zeros(nb_, np.int32)
+    t0 = time.perf_counter()
+    for s in range(nsample):
+        m, l, k = s % 5, (s // 5) % 7, s // 35
+        wd = O.testvector(m, l, k, gh, im, jm)
+        wtmp = w.copy(order="F")
+        O.bc_inlet(wtmp, "Ilo", it["Ilo"], c["field"], g["nx"], g["ny"], ph["gam"], im, jm, gh, wd=wd)
+        O.bc_noref(wtmp, c["wbd"], "Jhi", it["Jhi"], g["nx"], g["ny"], ph["gam"], gh, im, jm, wd=wd)
+        O.bc_extrap(wtmp, "Ihi", it["Ihi"], im, jm, gh, wd=wd)
+        O.bc_wall(wtmp, "Jlo", ph["gam"], it["Jlo"], gh, im, jm, wd=wd)
+        lib.orc_flux_num_dnc5_2d_d(O._p(res), O._p(resd), O._p(w), O._p(wd), 1, O._p(g["nx"]), O._p(g["ny"]),
+                                   O._p(g["vol"]), O._p(g["volf"]), gh, *O._phys(ph), im, jm)
+        O.computejacobian(O.JAC_PLAIN, jac, ia, ja, resd, m, l, k, gh, im, jm, None)
+    t_cpu = (time.perf_counter() - t0) / nsample * 245
+    line = {"workload": "jacobian", "metric": "batched Jacobian assembly, seed-cells/s", "unit": "Mcells/s",
+            "value": 245 * im * jm / t_j / 1e6, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"grid": "boundary layer %dx%d, Mach 0.5, Re_x0 1e5, stretch 1.03, seed 3" % (im, jm),
+                       "seeds": 245, "betas": 16, "steps": args.steps},
+            "seconds": {"jacobian_csr": t_j, "dz_csr": t_dz, "dzz_csr": t_dzz, "j_beta_16": t_beta},
+            "nnz": {"J": nnz_j, "Dz": nnz_dz, "Dzz": nnz_dzz, "union": nnz_u},
+            "cpu_baseline": {"seconds_245_seeds": t_cpu, "kind": "port", "cores": os.cpu_count(),
+                             "sample": "%d seeds of the reference loop (testvector, linearised boundary chain, "
+                                       "tangent residual, COO fill) through the oracle with OpenMP, scaled to 245"
+                                       % nsample}}
+    print(json.dumps(line))
+    return 0
+
+
 def ctypes_double():
     return np.zeros(1)
 
@@ -402,7 +512,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--workload", default="residual-jvp", choices=["residual-jvp", "jacobian"],
+                    help="residual-jvp: the 256x256 cylinder line (default); jacobian: the batched "
+                         "Jacobian / Dz / Dzz / J(beta) assembly of the 1024x512 boundary layer")
+    ap.add_argument("--im", type=int, default=0)
+    ap.add_argument("--jm", type=int, default=0)
     args = ap.parse_args()
+    if args.workload == "jacobian":
+        return run_jacobian_workload(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

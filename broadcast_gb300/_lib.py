@@ -65,6 +65,7 @@ SIGNATURES = {
     "bcg_coeffs_5p_dz2": "ppp" + "pppppppp" + "i" + "d" * 9 + "ii",
     "bcg_coeffs_5p_dz_dn": "pppi" + "pppppppp" + "i" + "d" * 9 + "ii",
     "bcg_coeffs_5p_dz2_dn": "pppi" + "pppppppp" + "i" + "d" * 9 + "ii",
+    "bcg_csr_spanwise_beta": "i" + "ppp" * 3 + "ip" + "ppp" + "L" + "p",
     "bcg_jacobian_dz_bl_csr": "ppppp" + "i" + "d" * 9 + "ii" + "pppp" + "pipi" + "id" + "ppp" + "L" + "p",
 }
 _RESTYPE = {"bcg_get_stream": ctypes.c_void_p, "bcg_last_error_string": ctypes.c_char_p,

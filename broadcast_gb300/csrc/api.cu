@@ -693,3 +693,79 @@ extern "C" int bcg_jacobian_dz_bl_csr(const double* w, const double* nx, const d
                          muref, tref, s_suth, 0.0, 0.0, im, jm, interf_ilo, interf_jhi, interf_ihi, interf_jlo, field,
                          lm_field, wbd, lm_wbd, nullptr, mini, 0, indptr, indices, data, capacity, nnz);
 }
+
+// ---- J(beta) = J - beta^2 Dzz + i beta Dz (biglobal.py:82) -------------------
+// Three CSR matrices of nrow rows (sorted columns) combine on the union of
+// their patterns for nbeta wavenumbers; values hold nbeta planes of nnz complex
+// numbers (re, im interleaved), plane k at values + 2*k*nnz.  Inputs and
+// outputs may be host or device arrays.
+namespace {
+long long csr_nnz(const int* indptr, int nrow, cudaStream_t st, int* rc) {
+  int v = 0;
+  if (is_device_ptr(indptr)) {
+    cudaError_t e = cudaMemcpyAsync(&v, indptr + nrow, sizeof v, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { *rc = fail_cuda("csr_spanwise_beta: indptr", e); return -1; }
+  } else {
+    v = indptr[nrow];
+  }
+  *rc = BCG_OK;
+  return v;
+}
+}  // namespace
+
+extern "C" int bcg_csr_spanwise_beta(int nrow, const int* j_indptr, const int* j_indices, const double* j_data,
+                                     const int* dz_indptr, const int* dz_indices, const double* dz_data,
+                                     const int* dzz_indptr, const int* dzz_indices, const double* dzz_data,
+                                     int nbeta, const double* betas, int* indptr, int* indices, double* values,
+                                     long long capacity, long long* nnz) {
+  if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
+  if (nrow < 1 || nbeta < 1 || !betas || !nnz || !j_indptr || !dz_indptr || !dzz_indptr)
+    return fail_arg("csr_spanwise_beta: bad arguments");
+  cudaStream_t st = current_stream();
+  int rc = 0;
+  const long long nj = csr_nnz(j_indptr, nrow, st, &rc);
+  if (rc) return rc;
+  const long long nz = csr_nnz(dz_indptr, nrow, st, &rc);
+  if (rc) return rc;
+  const long long nzz = csr_nnz(dzz_indptr, nrow, st, &rc);
+  if (rc) return rc;
+  Stager sg(st);
+  const size_t pb = (size_t)(nrow + 1) * 4;
+  const int h1 = sg.in(j_indptr, pb), h2 = sg.in(j_indices, (size_t)nj * 4), h3 = sg.in(j_data, (size_t)nj * 8);
+  const int h4 = sg.in(dz_indptr, pb), h5 = sg.in(dz_indices, (size_t)nz * 4), h6 = sg.in(dz_data, (size_t)nz * 8);
+  const int h7 = sg.in(dzz_indptr, pb), h8 = sg.in(dzz_indices, (size_t)nzz * 4);
+  const int h9 = sg.in(dzz_data, (size_t)nzz * 8), hb = sg.in(betas, (size_t)nbeta * 8);
+  rc = sg.commit();
+  if (rc) return rc;
+  CsrBetaArgs a{};
+  a.nrow = nrow;
+  a.j_p = sg.dev<int>(h1); a.j_i = sg.dev<int>(h2); a.j_v = sg.dev<double>(h3);
+  a.dz_p = sg.dev<int>(h4); a.dz_i = sg.dev<int>(h5); a.dz_v = sg.dev<double>(h6);
+  a.dzz_p = sg.dev<int>(h7); a.dzz_i = sg.dev<int>(h8); a.dzz_v = sg.dev<double>(h9);
+  a.nbeta = nbeta; a.betas = sg.dev<double>(hb); a.nnz = nnz;
+  a.iscratch = (int*)pool_get(POOL_AUX, csr_beta_iscratch_ints(nrow) * 4);
+  if (!a.iscratch) return fail_arg("csr_spanwise_beta: scratch allocation failed"), BCG_ERR_NOMEM;
+  const bool dev_out = is_device_ptr(indptr) && is_device_ptr(indices) && is_device_ptr(values);
+  if (dev_out) {
+    a.indptr = indptr; a.indices = indices; a.values = values; a.capacity = capacity;
+    rc = run_csr_beta(a, st);
+    if (rc) return rc;
+    return sg.finish();
+  }
+  // host outputs: device buffers sized to the sum of the three patterns
+  const long long cap = nj + nz + nzz;
+  const size_t ib = (((size_t)(nrow + 1) * 4 + 255) & ~(size_t)255), xb = (((size_t)cap * 4 + 255) & ~(size_t)255);
+  char* ob = (char*)pool_get(POOL_STAGE_OUT, ib + xb + (size_t)cap * 16 * nbeta + 256);
+  if (!ob) return fail_arg("csr_spanwise_beta: output allocation failed"), BCG_ERR_NOMEM;
+  a.indptr = (int*)ob; a.indices = (int*)(ob + ib); a.values = (double*)(ob + ib + xb); a.capacity = cap;
+  rc = run_csr_beta(a, st);
+  if (rc) return rc;
+  if (*nnz > capacity) return fail_arg("csr_spanwise_beta: capacity too small (see nnz)");
+  cudaError_t e = cudaMemcpyAsync(indptr, a.indptr, (size_t)(nrow + 1) * 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(indices, a.indices, (size_t)*nnz * 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(values, a.values, (size_t)*nnz * 16 * nbeta, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail_cuda("csr_spanwise_beta: output copy", e);
+  return sg.finish();
+}

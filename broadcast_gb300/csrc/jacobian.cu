@@ -246,6 +246,78 @@ int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
   return BCG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Spanwise-wavenumber operator of the global stability problem
+// (biglobal.py:82): J(beta) = J - beta^2 Dzz + i beta Dz, on the union of the
+// three sparsity patterns, for several beta at once.  One thread per row
+// merges the three sorted column lists; pass 0 counts, pass 1 writes.
+namespace {
+__global__ void __launch_bounds__(128) k_beta_rows(int pass, int nrow, const int* __restrict__ ja_p,
+                                                   const int* __restrict__ ja_i, const double* __restrict__ ja_v,
+                                                   const int* __restrict__ dz_p, const int* __restrict__ dz_i,
+                                                   const double* __restrict__ dz_v, const int* __restrict__ dzz_p,
+                                                   const int* __restrict__ dzz_i, const double* __restrict__ dzz_v,
+                                                   int nbeta, const double* __restrict__ betas, long long nnz_u,
+                                                   int* __restrict__ count, const long long* __restrict__ rowptr,
+                                                   int* __restrict__ indices, double2* __restrict__ vals) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= nrow) return;
+  int a = ja_p[row], ae = ja_p[row + 1], b = dz_p[row], be = dz_p[row + 1], c = dzz_p[row], ce = dzz_p[row + 1];
+  const int BIG = 0x7fffffff;
+  long long out = pass ? rowptr[row] : 0;
+  int n = 0;
+  while (a < ae || b < be || c < ce) {
+    const int ca = a < ae ? ja_i[a] : BIG, cb = b < be ? dz_i[b] : BIG, cc = c < ce ? dzz_i[c] : BIG;
+    const int col = min(ca, min(cb, cc));
+    double vj = 0.0, vz = 0.0, vzz = 0.0;
+    if (ca == col) vj = ja_v[a++];
+    if (cb == col) vz = dz_v[b++];
+    if (cc == col) vzz = dzz_v[c++];
+    if (pass) {
+      indices[out + n] = col;
+      for (int k = 0; k < nbeta; ++k) {
+        const double be_ = betas[k];
+        vals[(size_t)k * nnz_u + out + n] = make_double2(vj - be_ * be_ * vzz, be_ * vz);
+      }
+    }
+    ++n;
+  }
+  if (!pass) count[row] = n;
+}
+}  // namespace
+
+int run_csr_beta(const CsrBetaArgs& a, cudaStream_t st) {
+  const int nrow = a.nrow, B = 128;
+  const int nb = (nrow + kScanBlock - 1) / kScanBlock;
+  long long* rowptr = (long long*)a.iscratch;
+  long long* bsum = rowptr + nrow + 2;
+  long long* total = bsum + nb + 1;
+  int* count = (int*)(total + 2);
+  k_beta_rows<<<(nrow + B - 1) / B, B, 0, st>>>(0, nrow, a.j_p, a.j_i, a.j_v, a.dz_p, a.dz_i, a.dz_v, a.dzz_p,
+                                               a.dzz_i, a.dzz_v, 0, nullptr, 0, count, nullptr, nullptr, nullptr);
+  k_scan_block<<<nb, kScanBlock, 0, st>>>(count, rowptr, bsum, nrow);
+  k_scan_sums<<<1, 1, 0, st>>>(bsum, nb, total);
+  k_scan_add<<<(nrow + 1 + 255) / 256, 256, 0, st>>>(rowptr, bsum, nrow, total);
+  long long nnz = 0;
+  cudaError_t e = cudaMemcpyAsync(&nnz, total, sizeof nnz, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail_cuda("csr_spanwise_beta: nnz", e);
+  *a.nnz = nnz;
+  if (nnz > a.capacity) return fail_arg("csr_spanwise_beta: capacity too small (see nnz)");
+  k_ptr_to_int<<<(nrow + 1 + 255) / 256, 256, 0, st>>>(rowptr, a.indptr, nrow);
+  k_beta_rows<<<(nrow + B - 1) / B, B, 0, st>>>(1, nrow, a.j_p, a.j_i, a.j_v, a.dz_p, a.dz_i, a.dz_v, a.dzz_p,
+                                               a.dzz_i, a.dzz_v, a.nbeta, a.betas, nnz, count, rowptr, a.indices,
+                                               (double2*)a.values);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return fail_cuda("csr_spanwise_beta", e);
+  return BCG_OK;
+}
+
+size_t csr_beta_iscratch_ints(int nrow) {
+  const size_t nb = ((size_t)nrow + kScanBlock - 1) / kScanBlock;
+  return 2 * ((size_t)nrow + 2 + nb + 1 + 2) + nrow + 64;
+}
+
 size_t jacobian_iscratch_ints(int im, int jm) {
   const size_t nrow = 5 * (size_t)im * jm;
   const size_t nb = (nrow + kScanBlock - 1) / kScanBlock;

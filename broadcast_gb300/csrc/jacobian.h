@@ -31,6 +31,25 @@ struct JacobianArgs {
   int* iscratch;            // jacobian_iscratch_ints
 };
 
+// J(beta) = J - beta^2 Dzz + i beta Dz on the union pattern (biglobal.py:82);
+// values: nbeta planes of nnz complex numbers (re, im interleaved)
+struct CsrBetaArgs {
+  int nrow;
+  const int* j_p; const int* j_i; const double* j_v;
+  const int* dz_p; const int* dz_i; const double* dz_v;
+  const int* dzz_p; const int* dzz_i; const double* dzz_v;
+  int nbeta;
+  const double* betas;    // device, nbeta
+  int* indptr;            // nrow + 1
+  int* indices;           // capacity
+  double* values;         // 2 * nbeta * capacity
+  long long capacity;
+  long long* nnz;         // host
+  int* iscratch;          // csr_beta_iscratch_ints(nrow)
+};
+int run_csr_beta(const CsrBetaArgs& a, cudaStream_t st);
+size_t csr_beta_iscratch_ints(int nrow);
+
 size_t jacobian_scratch_doubles(int im, int jm, int gh);
 size_t jacobian_iscratch_ints(int im, int jm);
 int run_jacobian(const JacobianArgs& a, cudaStream_t st);

@@ -176,6 +176,17 @@ int bcg_jacobian_dz_bl_csr(const double* w, const double* nx, const double* ny, 
                            int lm_field, const double* wbd, int lm_wbd, int which, double mini, int* indptr,
                            int* indices, double* data, long long capacity, long long* nnz);
 
+/* Global-stability operator J(beta) = J - beta^2 Dzz + i beta Dz (biglobal.py:82,
+ * where PETSc adds the three matrices on the union of their patterns) for
+ * nbeta wavenumbers at once: CSR inputs of nrow rows with sorted columns (the
+ * outputs of the two calls above); indptr/indices receive the union pattern,
+ * values nbeta planes of *nnz complex numbers (re, im interleaved; plane k at
+ * values + 2*k*(*nnz)).  Returns -1 with *nnz set when capacity is too small. */
+int bcg_csr_spanwise_beta(int nrow, const int* j_indptr, const int* j_indices, const double* j_data,
+                          const int* dz_indptr, const int* dz_indices, const double* dz_data, const int* dzz_indptr,
+                          const int* dzz_indices, const double* dzz_data, int nbeta, const double* betas, int* indptr,
+                          int* indices, double* values, long long capacity, long long* nnz);
+
 /* ---- spanwise operators (srcfv/dz, module f_dz) -------------------------------- */
 /* coeffs_5p_dz.F90:10 coeffs_5p_dz : dz_out = Dz . wd (coefficient of i*beta)
  * coeffs_5p_dz2.F90:10 coeffs_5p_dz2: dz2_out = Dzz . wd (coefficient of -beta^2)

@@ -113,3 +113,54 @@ def test_batched_dz_csr_matches_reference_loop(which):
     assert np.array_equal(got.indptr, ref.indptr)
     assert np.array_equal(got.indices, ref.indices)
     assert np.abs(got.data - ref.data).max() <= 1e-12 * np.abs(ref.data).max()
+
+
+def _gpu_csr(c, fn, *extra):
+    sp = pytest.importorskip("scipy.sparse")
+    from broadcast_gb300 import _lib
+    from broadcast_gb300._f2py import interf4
+    g, ph, it = c["grid"], c["phys"], c["interf"]
+    im, jm, gh = g["im"], g["jm"], g["gh"]
+    nrow = 5 * im * jm
+    cap = nrow * 245
+    indptr, indices, data = np.zeros(nrow + 1, np.int32), np.zeros(cap, np.int32), np.zeros(cap)
+    nnz = np.zeros(1, np.int64)
+    if fn == "jac":
+        keys = SPAN + ("k2", "k4")
+        _lib.call("bcg_jacobian_dnc5_bl_csr", c["w"], g["nx"], g["ny"], g["vol"], g["volf"], gh,
+                  *[float(ph[k]) for k in keys], im, jm, interf4(it["Ilo"]), interf4(it["Jhi"]), interf4(it["Ihi"]),
+                  interf4(it["Jlo"]), c["field"], c["field"].shape[0], c["wbd"], c["wbd"].shape[0], None, 2e-16, 1,
+                  indptr, indices, data, cap, nnz)
+    else:
+        _lib.call("bcg_jacobian_dz_bl_csr", c["w"], g["nx"], g["ny"], g["vol"], g["volf"], gh,
+                  *[float(ph[k]) for k in SPAN], im, jm, interf4(it["Ilo"]), interf4(it["Jhi"]), interf4(it["Ihi"]),
+                  interf4(it["Jlo"]), c["field"], c["field"].shape[0], c["wbd"], c["wbd"].shape[0], extra[0], 2e-16,
+                  indptr, indices, data, cap, nnz)
+    n = int(nnz[0])
+    return sp.csr_matrix((data[:n].copy(), indices[:n].copy(), indptr.copy()), shape=(nrow, nrow))
+
+
+def test_spanwise_beta_operator():
+    """J(beta) = Jacvol - beta^2 Dzz + i beta Dz (biglobal.py:82) on the union pattern."""
+    from broadcast_gb300 import _lib
+    c = H.bl_case(20, 14)
+    H.oracle_bcs(c, c["w"])
+    J, Dz, Dzz = _gpu_csr(c, "jac"), _gpu_csr(c, "dz", 1), _gpu_csr(c, "dz", 2)
+    nrow = J.shape[0]
+    betas = np.array([0.0, 0.4, 1.7])
+    cap = J.nnz + Dz.nnz + Dzz.nnz
+    indptr, indices = np.zeros(nrow + 1, np.int32), np.zeros(cap, np.int32)
+    vals = np.zeros(2 * len(betas) * cap)
+    nnz = np.zeros(1, np.int64)
+    _lib.call("bcg_csr_spanwise_beta", nrow, J.indptr, J.indices, J.data, Dz.indptr, Dz.indices, Dz.data,
+              Dzz.indptr, Dzz.indices, Dzz.data, len(betas), betas, indptr, indices, vals, cap, nnz)
+    n = int(nnz[0])
+    union = (abs(J) + abs(Dz) + abs(Dzz)).tocsr()
+    union.sort_indices()
+    assert n == union.nnz
+    assert np.array_equal(indptr, union.indptr) and np.array_equal(indices[:n], union.indices)
+    cv = vals[:2 * len(betas) * n].reshape(len(betas), n, 2)
+    for k, b in enumerate(betas):
+        got = (cv[k, :, 0] + 1j * cv[k, :, 1])
+        ref = (J - b * b * Dzz + 1j * b * Dz).toarray()[np.repeat(np.arange(nrow), np.diff(indptr)), indices[:n]]
+        assert np.abs(got - ref).max() <= 1e-14 * np.abs(ref).max()
