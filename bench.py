@@ -487,6 +487,95 @@ def run_jacobian_workload(args):
     return 0
 
 
+def _flux_scale(c):
+    """Per-variable face-flux magnitude max(|f| + |g|) * max face length."""
+    w, g, gam = c["w"], c["grid"], c["phys"]["gam"]
+    ro = w[..., 0]
+    u, v, ww = w[..., 1] / ro, w[..., 2] / ro, w[..., 3] / ro
+    p = (gam - 1.0) * (w[..., 4] - 0.5 * ro * (u * u + v * v + ww * ww))
+    f = np.stack([w[..., 1], w[..., 1] * u + p, w[..., 1] * v, w[..., 1] * ww, (w[..., 4] + p) * u], -1)
+    h = np.stack([w[..., 2], w[..., 2] * u, w[..., 2] * v + p, w[..., 2] * ww, (w[..., 4] + p) * v], -1)
+    return (np.abs(f) + np.abs(h)).reshape(-1, 5).max(0) * np.sqrt(g["nx"] ** 2 + g["ny"] ** 2).max()
+
+
+def run_batch_workload(args):
+    """Uneven batch (the reference's fourth configuration): 64 boundary-layer
+    instances, nx ~ U{200..1200}, ny ~ U{80..300}, Mach ~ U(0.3, 0.8)
+    (default_rng(4)); residual + one JVP direction of every instance in one
+    set of persistent launches replayed from a CUDA graph, tile shapes from
+    the autotuner; per-instance error against the single-grid kernels and
+    against the oracle."""
+    import torch
+    from broadcast_gb300 import cases
+    from broadcast_gb300.batch import GridBatch
+    from broadcast_gb300.operator import Dnc5Operator, to_device, to_host
+    n = args.grids or 64
+    rng = np.random.default_rng(4)
+    spec = [(int(rng.integers(200, 1201)), int(rng.integers(80, 301)), float(rng.uniform(0.3, 0.8))) for _ in range(n)]
+    cs, wds = [], []
+    for k, (im, jm, mach) in enumerate(spec):
+        c = cases.bl_case(im, jm, mach=mach, seed=100 + k, ops=LibOps)
+        bl_bcs(c, c["w"])
+        wd = np.zeros_like(c["w"])
+        wd[3:-3, 3:-3] = rng.standard_normal((im, jm, 5))
+        cs.append(c)
+        wds.append(wd)
+    dev = torch.device("cuda", 0)
+    gb = GridBatch([c["grid"] for c in cs], [c["phys"] for c in cs], ndir=1, device=dev)
+    gb.set_states([to_device(c["w"], dev) for c in cs], [to_device(wd, dev) for wd in wds])
+    tune = gb.autotune(repeats=3, use_cache=False)
+    gb.run(use_graph=True)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for _ in range(max(args.warmup, 1)):
+        gb.run(use_graph=True)
+    torch.cuda.synchronize()
+    for s in range(args.steps):
+        flush.add_(1.0)
+        ev[s][0].record(stream)
+        gb.run(use_graph=True)
+        ev[s][1].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    # per-instance errors: single-grid kernels, oracle
+    from oracle import oracle as O
+    err_single, err_res, err_tan, kink_cells = [], [], [], 0
+    for g, c in enumerate(cs):
+        r, rd = to_host(gb.res[g]), to_host(gb.resd[g])
+        op = Dnc5Operator(c["grid"], c["phys"], device=dev)
+        r1, rd1 = op.jvp(to_device(c["w"], dev), to_device(wds[g], dev))
+        err_single.append(float(max(np.abs(r - to_host(r1)).max(), np.abs(rd - to_host(rd1)).max())))
+        ref, refd = O.jvp(c["grid"], c["phys"], c["w"], wds[g])
+        sc = _flux_scale(c)  # residual: relative to the face-flux magnitude
+        scd = np.abs(refd[3:-3, 3:-3]).reshape(-1, 5).max(0)
+        et = np.abs(rd - refd)[3:-3, 3:-3] / scd
+        err_res.append(float((np.abs(r - ref)[3:-3, 3:-3].reshape(-1, 5).max(0) / sc).max()))
+        err_tan.append(float(et.max()))
+        kink_cells += int((et.max(axis=2) > 1e-11).sum())
+    cells = gb.cells
+    line = {"workload": "batch", "metric": "FP64 residual+JVP Mcells/s, 64 uneven grids", "unit": "Mcells/s",
+            "value": cells / (ms / 1e3) / 1e6, "ms_per_step": ms, "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"grids": n, "cells": cells, "sizes": "nx U{200..1200}, ny U{80..300}, Mach U(0.3, 0.8), "
+                                                             "default_rng(4)", "graph": True,
+                       "tile": {"faces": tune["config"][0], "cells": tune["config"][1],
+                                "ctas_per_sm": tune["config"][2]},
+                       "l2": "flushed between steps (256 MB write)"},
+            "per_instance_error": {"vs_single_grid_max_abs": max(err_single),
+                                   "residual_vs_oracle_max": max(err_res),
+                                   "tangent_vs_oracle_max": max(err_tan),
+                                   "tangent_cells_above_1e-11": kink_cells,
+                                   "note": "residual relative to the face-flux magnitude, tangent to max|R'v| per "
+                                           "variable; cells above 1e-11 sit on an abs() kink of the pressure "
+                                           "sensor (second difference ~ 0 next to the extrapolated outflow)"},
+            "autotune_ms": {"%d/%d/%d" % tuple(c): t for c, t in tune["timings"]},
+            "gpu_launches": 5 * args.steps}
+    print(json.dumps(line))
+    return 0
+
+
 def ctypes_double():
     return np.zeros(1)
 
@@ -512,14 +601,18 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--workload", default="residual-jvp", choices=["residual-jvp", "jacobian"],
+    ap.add_argument("--workload", default="residual-jvp", choices=["residual-jvp", "jacobian", "batch"],
                     help="residual-jvp: the 256x256 cylinder line (default); jacobian: the batched "
-                         "Jacobian / Dz / Dzz / J(beta) assembly of the 1024x512 boundary layer")
+                         "Jacobian / Dz / Dzz / J(beta) assembly of the 1024x512 boundary layer; batch: "
+                         "residual + JVP of 64 uneven boundary-layer grids in one graph")
+    ap.add_argument("--grids", type=int, default=0)
     ap.add_argument("--im", type=int, default=0)
     ap.add_argument("--jm", type=int, default=0)
     args = ap.parse_args()
     if args.workload == "jacobian":
         return run_jacobian_workload(args)
+    if args.workload == "batch":
+        return run_batch_workload(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

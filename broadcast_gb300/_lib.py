@@ -65,6 +65,12 @@ SIGNATURES = {
     "bcg_coeffs_5p_dz2": "ppp" + "pppppppp" + "i" + "d" * 9 + "ii",
     "bcg_coeffs_5p_dz_dn": "pppi" + "pppppppp" + "i" + "d" * 9 + "ii",
     "bcg_coeffs_5p_dz2_dn": "pppi" + "pppppppp" + "i" + "d" * 9 + "ii",
+    "bcg_batch_create": "ipppip",
+    "bcg_batch_set_arrays": "L" + "p" * 8,
+    "bcg_batch_configure": "Liii",
+    "bcg_batch_run": "Li",
+    "bcg_batch_device_bytes": "Lp",
+    "bcg_batch_destroy": "L",
     "bcg_csr_spanwise_beta": "i" + "ppp" * 3 + "ip" + "ppp" + "L" + "p",
     "bcg_jacobian_dz_bl_csr": "ppppp" + "i" + "d" * 9 + "ii" + "pppp" + "pipi" + "id" + "ppp" + "L" + "p",
 }

@@ -7,6 +7,8 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include "bc.h"
 #include "residual.h"
 #include "runtime.h"
@@ -14,6 +16,7 @@
 #include "adjoint.h"
 #include "jacobian.h"
 #include "span.h"
+#include "batch.h"
 
 using namespace bcg;
 
@@ -768,4 +771,72 @@ extern "C" int bcg_csr_spanwise_beta(int nrow, const int* j_indptr, const int* j
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail_cuda("csr_spanwise_beta: output copy", e);
   return sg.finish();
+}
+
+// ---- uneven batch of grids (no reference counterpart: one grid per process
+// there) ----------------------------------------------------------------------
+namespace {
+std::mutex g_batch_mu;
+std::map<long long, BatchPlan*> g_batches;
+long long g_batch_next = 1;
+BatchPlan* batch_of(long long id) {
+  std::lock_guard<std::mutex> lk(g_batch_mu);
+  auto it = g_batches.find(id);
+  return it == g_batches.end() ? nullptr : it->second;
+}
+}  // namespace
+
+extern "C" int bcg_batch_create(int ngrid, const int* im, const int* jm, const double* phys, int ndir,
+                                long long* plan) {
+  if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
+  if (!plan) return fail_arg("batch_create: null plan");
+  BatchPlan* p = nullptr;
+  int rc = batch_create(ngrid, im, jm, phys, ndir, &p);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(g_batch_mu);
+  *plan = g_batch_next++;
+  g_batches[*plan] = p;
+  return BCG_OK;
+}
+
+extern "C" int bcg_batch_set_arrays(long long plan, const unsigned long long* w, const unsigned long long* wd,
+                                    const unsigned long long* nx, const unsigned long long* ny,
+                                    const unsigned long long* vol, const unsigned long long* volf,
+                                    const unsigned long long* res, const unsigned long long* resd) {
+  BatchPlan* p = batch_of(plan);
+  if (!p) return fail_arg("batch: unknown plan");
+  return batch_set_arrays(p, w, wd, nx, ny, vol, volf, res, resd);
+}
+
+extern "C" int bcg_batch_configure(long long plan, int tile_faces, int tile_cells, int ctas_per_sm) {
+  BatchPlan* p = batch_of(plan);
+  if (!p) return fail_arg("batch: unknown plan");
+  return batch_configure(p, tile_faces, tile_cells, ctas_per_sm);
+}
+
+extern "C" int bcg_batch_run(long long plan, int use_graph) {
+  BatchPlan* p = batch_of(plan);
+  if (!p) return fail_arg("batch: unknown plan");
+  return batch_run(p, use_graph, current_stream());
+}
+
+extern "C" int bcg_batch_device_bytes(long long plan, long long* bytes) {
+  BatchPlan* p = batch_of(plan);
+  if (!p || !bytes) return fail_arg("batch: unknown plan");
+  *bytes = (long long)batch_device_bytes(p);
+  return BCG_OK;
+}
+
+extern "C" int bcg_batch_destroy(long long plan) {
+  BatchPlan* p = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    auto it = g_batches.find(plan);
+    if (it == g_batches.end()) return fail_arg("batch: unknown plan");
+    p = it->second;
+    g_batches.erase(it);
+  }
+  cudaError_t e = cudaStreamSynchronize(current_stream());
+  batch_destroy(p);
+  return e == cudaSuccess ? BCG_OK : fail_cuda("batch_destroy", e);
 }

@@ -1,0 +1,304 @@
+// Residual (+ tangent) of many independent grids of uneven size, GB300 style.
+//
+// The reference runs one grid per process (BROADCAST_npz.py); a batch of
+// boundary-layer instances of different sizes would leave most of a GB300
+// idle per grid.  Here every pass of the DNC5 residual (primitives, Ducros
+// gradients, interpolation rows, faces, balance; the same per-element bodies
+// as the single-grid kernels, passes.cuh) is ONE persistent launch over a
+// tile list that concatenates the tiles of all grids: each CTA walks tiles
+// t = blockIdx.x, blockIdx.x + gridDim.x, ...; a tile belongs to one grid,
+// found by binary search in the pass's tile-start table, whose descriptor
+// (extents, coefficients, array addresses, scratch) the CTA stages in shared
+// memory.  The launches can be captured once in a CUDA graph and replayed.
+// Tile sizes and CTAs per SM are plan parameters, chosen by the autotuner in
+// broadcast_gb300/batch.py.
+#include <algorithm>
+#include <vector>
+#include "batch.h"
+#include "passes.cuh"
+#include "residual.h"
+#include "runtime.h"
+
+namespace bcg {
+
+namespace {
+
+enum { P_PRIM = 0, P_GRAD, P_QROWS, P_FACES, P_BAL, NPASS };
+
+struct GridDesc {
+  Ext e;
+  Coef c;
+  const double* w;
+  const double* wd;
+  size_t dstride;
+  const double* nx;
+  const double* ny;
+  const double* vol;
+  const double* volf;
+  double* res;
+  double* resd;
+  double* scratch;  // residual_scratch_doubles(im, jm, 3, K) doubles
+  int grad;         // k2 != 0: the Ducros gradients are needed
+};
+
+template <class S>
+struct Fields {
+  Scratch<S> pr, gr, qr, hn;
+};
+template <class S>
+BCG_HD Fields<S> fields_of(const GridDesc& G) {
+  constexpr int NP = NDir<S>::value + 1;
+  const Ext& e = G.e;
+  const size_t nn = (size_t)(e.im + 1) * (e.jm + 1);
+  Fields<S> f;
+  f.pr = Scratch<S>{G.scratch, e.np};
+  f.gr = Scratch<S>{G.scratch + (size_t)F_NPRIM * NP * e.np, e.np};
+  f.qr = Scratch<S>{G.scratch + (size_t)(F_NPRIM + G_NGRAD) * NP * e.np, e.np};
+  f.hn = Scratch<S>{G.scratch + (size_t)(F_NPRIM + G_NGRAD + Q_NQ) * NP * e.np, nn};
+  return f;
+}
+template <class S> BCG_HD State<S> state_of(const GridDesc& G);
+template <> BCG_HD State<double> state_of<double>(const GridDesc& G) { return State<double>{G.w}; }
+template <> BCG_HD State<DK<1>> state_of<DK<1>>(const GridDesc& G) { return State<DK<1>>{G.w, G.wd, G.dstride}; }
+
+// grid of tile t: the largest g with starts[g] <= t (starts has ngrid + 1 entries)
+__device__ __forceinline__ int tile_grid(const long long* __restrict__ starts, int ngrid, long long t) {
+  int lo = 0, hi = ngrid - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (starts[mid] <= t) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <class S, int PASS, int BT>
+__global__ void __launch_bounds__(BT) k_batch(const GridDesc* __restrict__ descs, const long long* __restrict__ starts,
+                                              int ngrid) {
+  const long long* st = starts + (size_t)PASS * (ngrid + 1);
+  const long long T = st[ngrid];
+  __shared__ int s_g;
+  __shared__ FaceCtx<S> s_fc;
+  __shared__ Scratch<S> s_hn;
+  for (long long t = blockIdx.x; t < T; t += gridDim.x) {
+    __syncthreads();  // the previous tile is done with the shared descriptor
+    if (threadIdx.x == 0) {
+      const int g = tile_grid(st, ngrid, t);
+      s_g = g;
+      if constexpr (PASS == P_FACES) {
+        const GridDesc& G = descs[g];
+        const Fields<S> f = fields_of<S>(G);
+        s_fc.e = G.e; s_fc.c = G.c; s_fc.w = state_of<S>(G);
+        s_fc.pr = f.pr; s_fc.gr = f.gr; s_fc.qr = f.qr;
+        s_fc.nx = G.nx; s_fc.ny = G.ny; s_fc.vol = G.vol; s_fc.volf = G.volf;
+        s_hn = f.hn;
+      }
+    }
+    __syncthreads();
+    const int g = s_g;
+    const long long el = (t - st[g]) * BT + threadIdx.x;
+    if constexpr (PASS == P_FACES) {
+      const Ext& e = s_fc.e;
+      if (el < (long long)(e.im + 1) * (e.jm + 1)) face_node<S>(s_fc, s_hn, (int)el);
+    } else {
+      const GridDesc& G = descs[g];
+      const Ext& e = G.e;
+      const Fields<S> f = fields_of<S>(G);
+      if constexpr (PASS == P_PRIM) {
+        if (el < (long long)e.np) prim_cell<S>(e, G.c, state_of<S>(G), f.pr, (size_t)el);
+      } else if constexpr (PASS == P_QROWS) {
+        if (el < (long long)e.np) qrows_cell<S>(e, f.pr, f.qr, (size_t)el);
+      } else if constexpr (PASS == P_GRAD) {
+        if (el < (long long)e.im * e.jm) grad_cell<S>(e, G.c, f.pr, f.gr, G.nx, G.ny, G.vol, (int)el);
+      } else {
+        if (el < (long long)e.im * e.jm) balance_cell<S>(e, f.hn, G.res, G.resd, G.dstride, (int)el);
+      }
+    }
+  }
+}
+
+}  // namespace
+
+struct BatchPlan {
+  int ngrid = 0, K = 0;
+  std::vector<GridDesc> h;
+  GridDesc* d = nullptr;
+  long long* dstarts = nullptr;
+  double* scratch = nullptr;
+  size_t scratch_doubles = 0;
+  int tile_faces = 128, tile_cells = 256, ctas = 2, nsm = 0;
+  long long ntiles[NPASS] = {0, 0, 0, 0, 0};
+  bool any_grad = false;
+  cudaStream_t cap = nullptr;  // capture stream (the caller's may be the legacy default stream)
+  cudaGraphExec_t exec = nullptr;
+};
+
+static long long pass_count(const Ext& e, int pass, bool grad) {
+  switch (pass) {
+    case P_PRIM: case P_QROWS: return (long long)e.np;
+    case P_GRAD: return grad ? (long long)e.im * e.jm : 0;
+    case P_FACES: return (long long)(e.im + 1) * (e.jm + 1);
+    default: return (long long)e.im * e.jm;
+  }
+}
+
+static int upload_starts(BatchPlan* p) {
+  const int n = p->ngrid;
+  std::vector<long long> st((size_t)NPASS * (n + 1));
+  for (int pass = 0; pass < NPASS; ++pass) {
+    const int bt = pass == P_FACES ? p->tile_faces : p->tile_cells;
+    long long acc = 0;
+    for (int g = 0; g < n; ++g) {
+      st[(size_t)pass * (n + 1) + g] = acc;
+      acc += (pass_count(p->h[g].e, pass, p->h[g].grad != 0) + bt - 1) / bt;
+    }
+    st[(size_t)pass * (n + 1) + n] = acc;
+    p->ntiles[pass] = acc;
+  }
+  cudaError_t e = cudaMemcpy(p->dstarts, st.data(), st.size() * sizeof(long long), cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? BCG_OK : fail_cuda("batch: tile table", e);
+}
+
+int batch_create(int ngrid, const int* im, const int* jm, const double* phys, int ndir, BatchPlan** out) {
+  if (ngrid < 1 || !im || !jm || !phys || !out) return fail_arg("batch: bad arguments");
+  if (ndir != 0 && ndir != 1) return fail_arg("batch: ndir must be 0 or 1");
+  BatchPlan* p = new BatchPlan();
+  p->ngrid = ngrid; p->K = ndir;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, dev);
+  p->h.resize(ngrid);
+  std::vector<size_t> off(ngrid);
+  for (int g = 0; g < ngrid; ++g) {
+    if (im[g] < 6 || jm[g] < 6) { delete p; return fail_arg("batch: every grid needs im, jm >= 6"); }
+    GridDesc& G = p->h[g];
+    G = GridDesc{};
+    G.e = make_ext(im[g], jm[g], 3);
+    const double* ph = phys + (size_t)11 * g;
+    const Phys P{ph[0], ph[1], ph[2], ph[3], ph[4], ph[5], ph[6], ph[7], ph[8], ph[9], ph[10]};
+    G.c = make_coef(P);
+    G.grad = (P.k2 != 0.0) ? 1 : 0;
+    p->any_grad = p->any_grad || G.grad;
+    G.dstride = G.e.np * 5;
+    off[g] = p->scratch_doubles;
+    p->scratch_doubles += (residual_scratch_doubles(im[g], jm[g], 3, ndir) + 31) & ~(size_t)31;
+  }
+  cudaError_t e = cudaMalloc(&p->scratch, p->scratch_doubles * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&p->d, sizeof(GridDesc) * ngrid);
+  if (e == cudaSuccess) e = cudaMalloc(&p->dstarts, sizeof(long long) * NPASS * (ngrid + 1));
+  if (e != cudaSuccess) { batch_destroy(p); return fail_cuda("batch: device allocation", e), BCG_ERR_NOMEM; }
+  for (int g = 0; g < ngrid; ++g) p->h[g].scratch = p->scratch + off[g];
+  int rc = upload_starts(p);
+  if (rc) { batch_destroy(p); return rc; }
+  *out = p;
+  return BCG_OK;
+}
+
+int batch_set_arrays(BatchPlan* p, const unsigned long long* w, const unsigned long long* wd,
+                     const unsigned long long* nx, const unsigned long long* ny, const unsigned long long* vol,
+                     const unsigned long long* volf, const unsigned long long* res, const unsigned long long* resd) {
+  if (!w || !nx || !ny || !vol || !volf || !res || (p->K && (!wd || !resd))) return fail_arg("batch: null array table");
+  for (int g = 0; g < p->ngrid; ++g) {
+    GridDesc& G = p->h[g];
+    G.w = (const double*)w[g]; G.wd = p->K ? (const double*)wd[g] : nullptr;
+    G.nx = (const double*)nx[g]; G.ny = (const double*)ny[g];
+    G.vol = (const double*)vol[g]; G.volf = (const double*)volf[g];
+    G.res = (double*)res[g]; G.resd = p->K ? (double*)resd[g] : nullptr;
+    const void* ptrs[8] = {G.w, G.nx, G.ny, G.vol, G.volf, G.res, p->K ? G.wd : G.w, p->K ? G.resd : G.res};
+    for (const void* q : ptrs)
+      if (!is_device_ptr(q)) return fail_arg("batch: every array must be a device pointer");
+  }
+  cudaError_t e = cudaMemcpy(p->d, p->h.data(), sizeof(GridDesc) * p->ngrid, cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? BCG_OK : fail_cuda("batch: descriptors", e);
+}
+
+int batch_configure(BatchPlan* p, int tile_faces, int tile_cells, int ctas_per_sm) {
+  if (tile_faces != 64 && tile_faces != 128 && tile_faces != 256) return fail_arg("batch: tile_faces must be 64, 128 or 256");
+  if (tile_cells != 128 && tile_cells != 256) return fail_arg("batch: tile_cells must be 128 or 256");
+  if (ctas_per_sm < 1 || ctas_per_sm > 8) return fail_arg("batch: ctas_per_sm must be 1..8");
+  p->tile_faces = tile_faces; p->tile_cells = tile_cells; p->ctas = ctas_per_sm;
+  if (p->exec) { cudaGraphExecDestroy(p->exec); p->exec = nullptr; }
+  return upload_starts(p);
+}
+
+template <class S, int PASS, int BT>
+static void launch_pass(const BatchPlan* p, int ctas, cudaStream_t st) {
+  const long long T = p->ntiles[PASS];
+  if (T == 0) return;
+  const long long g = std::min<long long>(T, (long long)p->nsm * ctas);
+  k_batch<S, PASS, BT><<<(unsigned)g, BT, 0, st>>>(p->d, p->dstarts, p->ngrid);
+}
+
+template <class S, int BT>
+static void launch_cells(const BatchPlan* p, int pass, cudaStream_t st) {
+  const int ctas = 2048 / BT;  // full residency of the light passes
+  switch (pass) {
+    case P_PRIM: launch_pass<S, P_PRIM, BT>(p, ctas, st); break;
+    case P_GRAD: launch_pass<S, P_GRAD, BT>(p, ctas, st); break;
+    case P_QROWS: launch_pass<S, P_QROWS, BT>(p, ctas, st); break;
+    default: launch_pass<S, P_BAL, BT>(p, ctas, st); break;
+  }
+}
+
+template <class S>
+static cudaError_t launch_all(const BatchPlan* p, cudaStream_t st) {
+  const int passes[4] = {P_PRIM, P_GRAD, P_QROWS, -1};
+  for (int q : passes) {
+    if (q < 0) break;
+    if (q == P_GRAD && !p->any_grad) continue;
+    if (p->tile_cells == 128) launch_cells<S, 128>(p, q, st); else launch_cells<S, 256>(p, q, st);
+  }
+  switch (p->tile_faces) {
+    case 64: launch_pass<S, P_FACES, 64>(p, p->ctas, st); break;
+    case 128: launch_pass<S, P_FACES, 128>(p, p->ctas, st); break;
+    default: launch_pass<S, P_FACES, 256>(p, p->ctas, st); break;
+  }
+  if (p->tile_cells == 128) launch_cells<S, 128>(p, P_BAL, st); else launch_cells<S, 256>(p, P_BAL, st);
+  return cudaGetLastError();
+}
+
+int batch_run(BatchPlan* p, int use_graph, cudaStream_t st) {
+  if (!p->h.empty() && !p->h[0].w) return fail_arg("batch: arrays not set");
+  auto launch = [&](cudaStream_t s) { return p->K ? launch_all<DK<1>>(p, s) : launch_all<double>(p, s); };
+  if (!use_graph) {
+    cudaError_t e = launch(st);
+    return e == cudaSuccess ? BCG_OK : fail_cuda("batch: launch", e);
+  }
+  if (!p->exec) {
+    // capture the pass launches once, on the plan's own stream (the caller's
+    // may be the legacy default stream, which cannot be captured); the
+    // descriptors the kernels read live in device memory, so new array
+    // addresses need no new capture
+    if (!p->cap) {
+      cudaError_t e0 = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
+      if (e0 != cudaSuccess) { p->cap = nullptr; return fail_cuda("batch: capture stream", e0); }
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return fail_cuda("batch: begin capture", e);
+    cudaError_t el = launch(p->cap);
+    e = cudaStreamEndCapture(p->cap, &graph);
+    if (el != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return fail_cuda("batch: capture launch", el); }
+    if (e != cudaSuccess) return fail_cuda("batch: end capture", e);
+    e = cudaGraphInstantiate(&p->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { p->exec = nullptr; return fail_cuda("batch: instantiate", e); }
+  }
+  cudaError_t e = cudaGraphLaunch(p->exec, st);
+  return e == cudaSuccess ? BCG_OK : fail_cuda("batch: graph launch", e);
+}
+
+void batch_destroy(BatchPlan* p) {
+  if (!p) return;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->cap) cudaStreamDestroy(p->cap);
+  if (p->scratch) cudaFree(p->scratch);
+  if (p->d) cudaFree(p->d);
+  if (p->dstarts) cudaFree(p->dstarts);
+  delete p;
+}
+
+size_t batch_device_bytes(const BatchPlan* p) {
+  return p->scratch_doubles * sizeof(double) + sizeof(GridDesc) * p->ngrid + sizeof(long long) * NPASS * (p->ngrid + 1);
+}
+
+}  // namespace bcg

@@ -1,0 +1,383 @@
+// Per-element bodies of the DNC5 residual passes, written over a scalar type S
+// (double, or DK<K> for the fused residual + K-direction JVP).  Included by
+// the single-grid kernels (residual.cu) and the uneven-batch kernels
+// (batch.cu), which differ only in how a thread finds its grid and element.
+//
+// Reference: srcfv/prepro/flux_num_dnc5.f90 (flattened
+// srcfv/rhs/flux_num_dnc5.F90 with its rhs/ and phys/ fragments).
+#pragma once
+#include "dnc5.cuh"
+
+namespace bcg {
+
+// ---------------------------------------------------------------------------
+// pass 1: primitives on padded cell q (phys/Primitives.F, phys/viscosity.F)
+template <class S>
+BCG_HD void prim_cell(const Ext& e, const Coef& c, const State<S>& w, const Scratch<S>& pr, size_t q) {
+  const size_t n = e.np;
+  const S ro = w(q), ru = w(q + n), rv = w(q + 2 * n), rw = w(q + 3 * n), re = w(q + 4 * n);
+  const S rom1 = 1.0 / ro;
+  const S u = ru * rom1, v = rv * rom1, ww = rw * rom1;
+  const S ec = 0.5 * (u * u + v * v + ww * ww);
+  const S eloc = (re - ec * ro) * rom1;
+  const S t = eloc * c.cvm1;
+  const S p = c.gam1 * ro * eloc;
+  const S htot = (re + p) * rom1;
+  pr.st(F_U, q, u); pr.st(F_V, q, v); pr.st(F_W, q, ww); pr.st(F_T, q, t); pr.st(F_P, q, p);
+  pr.st(F_F2, q, ru * u + p); pr.st(F_F3, q, ru * v); pr.st(F_F4, q, ru * ww); pr.st(F_F5, q, ru * htot);
+  pr.st(F_G2, q, rv * u); pr.st(F_G3, q, rv * v + p); pr.st(F_G4, q, rv * ww); pr.st(F_G5, q, rv * htot);
+  pr.st(F_MU, q, c.betas / (t + c.s_suth) * sqrt_t(t) * t);
+  // Roe-average ingredients: sqrt(rho), and sqrt(rho) times u, v and c^2
+  const S sr = sqrt_t(ro);
+  pr.st(F_SR, q, sr);
+  pr.st(F_SU, q, sr * u);
+  pr.st(F_SV, q, sr * v);
+  pr.st(F_SC, q, sr * (c.c2fac * t));
+}
+
+// ---------------------------------------------------------------------------
+// pass 1b: the 4-point interpolations (-a + 9b + 9c - d) that the 4th-order
+// viscous fluxes read, once per face location instead of once per face use:
+//   QI at i-face location (i, j): cells i-2..i+1 of row j,  i in [1, im+1], j in [-1, jm+2]
+//   QJ at j-face location (i, j): rows j-2..j+1 of column i, i in [-1, im+2], j in [2, jm+1]
+// for u, v, w, T and mu (rhs/flux_visqueux_o4_i.F, _j.F).
+template <class S>
+BCG_HD void qrows_cell(const Ext& e, const Scratch<S>& pr, const Scratch<S>& qr, size_t q) {
+  const int i = (int)(q % e.ni) + 1 - e.gh, j = (int)(q / e.ni) + 1 - e.gh;
+  const int fl[5] = {F_U, F_V, F_W, F_T, F_MU};
+  const int di = 1, dj = e.ni;
+  if (i >= 1 && i <= e.im + 1 && j >= -1 && j <= e.jm + 2) {
+#pragma unroll
+    for (int a = 0; a < 5; ++a) {
+      const S x0 = pr.ld(fl[a], q - 2 * di), x1 = pr.ld(fl[a], q - di), x2 = pr.ld(fl[a], q), x3 = pr.ld(fl[a], q + di);
+      qr.st(Q_I + a, q, 9.0 * (x1 + x2) - (x0 + x3));
+    }
+  }
+  if (i >= -1 && i <= e.im + 2 && j >= 2 && j <= e.jm + 1) {
+#pragma unroll
+    for (int a = 0; a < 5; ++a) {
+      const S x0 = pr.ld(fl[a], q - 2 * dj), x1 = pr.ld(fl[a], q - dj), x2 = pr.ld(fl[a], q), x3 = pr.ld(fl[a], q + dj);
+      qr.st(Q_J + a, q, 9.0 * (x1 + x2) - (x0 + x3));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// pass 2: 4th-order cell gradients of u and v on interior cell t (row-major
+// over the im x jm interior) (rhs/gradop_5pi.F, gradop_5pj.F, gradient.F)
+template <class S>
+BCG_HD void grad_cell(const Ext& e, const Coef& c, const Scratch<S>& pr, const Scratch<S>& gr,
+                      const double* __restrict__ nx, const double* __restrict__ ny, const double* __restrict__ vol,
+                      int t) {
+  const int i = 1 + t % e.im, j = 1 + t / e.im;
+  const size_t q = e.cidx(i, j);
+  const int di = 1, dj = e.ni;
+  auto g4 = [&](int f, int s) {
+    return c.b1 * (pr.ld(f, q + s) - pr.ld(f, q - s)) + c.b2 * (pr.ld(f, q + 2 * s) - pr.ld(f, q - 2 * s));
+  };
+  const S gui = g4(F_U, di), gvi = g4(F_V, di), guj = g4(F_U, dj), gvj = g4(F_V, dj);
+  const size_t nn = e.nn();
+  const int a = e.nidx(i, j);
+  const double volm1 = 1.0 / __ldg(vol + q);
+  const double dxm1 = 0.5 * (__ldg(nx + a) + __ldg(nx + a + 1)) * volm1;
+  const double dxm2 = 0.5 * (__ldg(nx + nn + a) + __ldg(nx + nn + a + e.ni + 1)) * volm1;
+  const double dym1 = 0.5 * (__ldg(ny + a) + __ldg(ny + a + 1)) * volm1;
+  const double dym2 = 0.5 * (__ldg(ny + nn + a) + __ldg(ny + nn + a + e.ni + 1)) * volm1;
+  gr.st(G_UX, q, dxm1 * gui + dxm2 * guj);
+  gr.st(G_VX, q, dxm1 * gvi + dxm2 * gvj);
+  gr.st(G_UY, q, dym1 * gui + dym2 * guj);
+  gr.st(G_VY, q, dym1 * gvi + dym2 * gvj);
+}
+
+// ---------------------------------------------------------------------------
+// pass 3: face fluxes
+template <class S>
+struct FaceCtx {
+  Ext e;
+  Coef c;
+  State<S> w;
+  Scratch<S> pr, gr, qr;
+  const double* __restrict__ nx;
+  const double* __restrict__ ny;
+  const double* __restrict__ vol;
+  const double* __restrict__ volf;
+
+  BCG_HD S W(int i, int j, int v) const { return w((size_t)e.cidx(i, j) + (size_t)(v - 1) * e.np); }
+  BCG_HD S P(int f, int i, int j) const { return pr.ld(f, e.cidx(i, j)); }
+  BCG_HD S Q(int f, int i, int j) const { return qr.ld(f, e.cidx(i, j)); }
+  // Euler flux components f(.,.,v), g(.,.,v) with f1 = rho u, g1 = rho v
+  BCG_HD S Fl(int v, int i, int j) const { return v == 1 ? W(i, j, 2) : P(F_F2 + v - 2, i, j); }
+  BCG_HD S Gl(int v, int i, int j) const { return v == 1 ? W(i, j, 3) : P(F_G2 + v - 2, i, j); }
+  BCG_HD double NX(int i, int j, int d) const { return __ldg(nx + (size_t)(d - 1) * e.nn() + e.nidx(i, j)); }
+  BCG_HD double NY(int i, int j, int d) const { return __ldg(ny + (size_t)(d - 1) * e.nn() + e.nidx(i, j)); }
+  BCG_HD double VOL(int i, int j) const { return __ldg(vol + e.cidx(i, j)); }
+  BCG_HD double VOLF(int i, int j, int d) const { return __ldg(volf + (size_t)(d - 1) * e.np + e.cidx(i, j)); }
+  // gradients, with the ghost lines the faces need (rhs/gradveloingh.F)
+  BCG_HD S G(int f, int i, int j) const {
+    if (i == 0) return 2.0 * gr.ld(f, e.cidx(1, j)) - gr.ld(f, e.cidx(2, j));
+    if (i == e.im + 1) return 2.0 * gr.ld(f, e.cidx(e.im, j)) - gr.ld(f, e.cidx(e.im - 1, j));
+    if (j == e.jm + 1) return 2.0 * gr.ld(f, e.cidx(i, e.jm)) - gr.ld(f, e.cidx(i, e.jm - 1));
+    return gr.ld(f, e.cidx(i, j));
+  }
+  BCG_HD static S q4(const S& a, const S& b, const S& cc, const S& d) { return -a + 9.0 * b + 9.0 * cc - d; }
+
+  BCG_HD void visc_fluxes(const S& mmu, const S& lambda, const S& uu, const S& vv, const S& ww, const S& ux,
+                          const S& uy, const S& vx, const S& vy, const S& wx, const S& wy, const S& tx, const S& ty,
+                          S fv[4], S gv[4]) const {
+    const double TWOTHIRD = 2.0 / 3.0;
+    fv[0] = TWOTHIRD * mmu * (2.0 * ux - vy);
+    fv[1] = mmu * (uy + vx);
+    fv[2] = mmu * (wx);
+    fv[3] = (lambda * tx + uu * fv[0] + vv * fv[1] + ww * fv[2]);
+    gv[0] = mmu * (uy + vx);
+    gv[1] = TWOTHIRD * mmu * (-ux + 2.0 * vy);
+    gv[2] = mmu * (wy);
+    gv[3] = lambda * ty + uu * gv[0] + vv * gv[1] + ww * gv[2];
+  }
+
+  // Viscous flux through i-face (i,j): o4 (rhs/flux_visqueux_o4_i.F) or o2
+  // (rows 1-2).  The face gradients are linear in four point values N, S, E,
+  // O; the point stencils' constant factors (1/24, ccross, 1/4) and the face
+  // volume are folded into the geometric coefficients, and the cross rows come
+  // from the QI interpolations.
+  BCG_HD void visc_i(int i, int j, bool o2, S fv[4], S gv[4]) const {
+    const double volm1 = VOLF(i, j, 1);
+    const double fN = o2 ? volm1 : volm1 / 24.0, fE = o2 ? 0.25 * volm1 : c.ccross * volm1;
+    const double nxN = 0.5 * (NX(i + 1, j, 1) + NX(i, j, 1)) * fN, nxS = -(0.5 * (NX(i - 1, j, 1) + NX(i, j, 1))) * fN;
+    const double nxO = 0.5 * (NX(i - 1, j + 1, 2) + NX(i, j + 1, 2)) * fE, nxE = -(0.5 * (NX(i - 1, j, 2) + NX(i, j, 2))) * fE;
+    const double nyN = 0.5 * (NY(i + 1, j, 1) + NY(i, j, 1)) * fN, nyS = -(0.5 * (NY(i - 1, j, 1) + NY(i, j, 1))) * fN;
+    const double nyO = 0.5 * (NY(i - 1, j + 1, 2) + NY(i, j + 1, 2)) * fE, nyE = -(0.5 * (NY(i - 1, j, 2) + NY(i, j, 2))) * fE;
+    S gx[4], gy[4];
+    const int fl[4] = {F_U, F_V, F_W, F_T};
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int f = fl[a];
+      S vN, vS, vE, vO;
+      if (!o2) {
+        vN = 26.0 * P(f, i, j) - (P(f, i + 1, j) + P(f, i - 1, j));
+        vS = 26.0 * P(f, i - 1, j) - (P(f, i, j) + P(f, i - 2, j));
+        vE = 7.0 * (Q(Q_I + a, i, j - 1) + Q(Q_I + a, i, j)) - (Q(Q_I + a, i, j - 2) + Q(Q_I + a, i, j + 1));
+        vO = 7.0 * (Q(Q_I + a, i, j) + Q(Q_I + a, i, j + 1)) - (Q(Q_I + a, i, j - 1) + Q(Q_I + a, i, j + 2));
+      } else {
+        vN = P(f, i, j);
+        vS = P(f, i - 1, j);
+        vE = (P(f, i, j) + P(f, i, j - 1)) + (P(f, i - 1, j) + P(f, i - 1, j - 1));
+        vO = (P(f, i, j) + P(f, i, j + 1)) + (P(f, i - 1, j) + P(f, i - 1, j + 1));
+      }
+      gx[a] = vN * nxN + vS * nxS + vO * nxO + vE * nxE;
+      gy[a] = vN * nyN + vS * nyS + vO * nyO + vE * nyE;
+    }
+    S uu, vv, ww, mmu;
+    if (!o2) {
+      uu = 0.0625 * Q(Q_I + 0, i, j);
+      vv = 0.0625 * Q(Q_I + 1, i, j);
+      ww = 0.0625 * Q(Q_I + 2, i, j);
+      mmu = 0.0625 * Q(Q_I + 4, i, j);
+    } else {
+      uu = 0.5 * (P(F_U, i, j) + P(F_U, i - 1, j));
+      vv = 0.5 * (P(F_V, i, j) + P(F_V, i - 1, j));
+      ww = 0.5 * (P(F_W, i, j) + P(F_W, i - 1, j));
+      mmu = 0.5 * (P(F_MU, i, j) + P(F_MU, i - 1, j));
+    }
+    visc_fluxes(mmu, mmu * c.cpprandtl, uu, vv, ww, gx[0], gy[0], gx[1], gy[1], gx[2], gy[2], gx[3], gy[3], fv, gv);
+  }
+
+  // Viscous flux through j-face (i,j): o4 (rhs/flux_visqueux_o4_j.F) or o2 (row 2).
+  BCG_HD void visc_j(int i, int j, bool o2, S fv[4], S gv[4]) const {
+    const double volm1 = VOLF(i, j, 2);
+    const double fN = o2 ? 0.25 * volm1 : c.ccross * volm1, fE = o2 ? volm1 : volm1 / 24.0;
+    const double nxN = 0.5 * (NX(i + 1, j - 1, 1) + NX(i + 1, j, 1)) * fN, nxS = -(0.5 * (NX(i, j - 1, 1) + NX(i, j, 1))) * fN;
+    const double nxO = 0.5 * (NX(i, j + 1, 2) + NX(i, j, 2)) * fE, nxE = -(0.5 * (NX(i, j - 1, 2) + NX(i, j, 2))) * fE;
+    const double nyN = 0.5 * (NY(i + 1, j - 1, 1) + NY(i + 1, j, 1)) * fN, nyS = -(0.5 * (NY(i, j - 1, 1) + NY(i, j, 1))) * fN;
+    const double nyO = 0.5 * (NY(i, j + 1, 2) + NY(i, j, 2)) * fE, nyE = -(0.5 * (NY(i, j - 1, 2) + NY(i, j, 2))) * fE;
+    S gx[4], gy[4];
+    const int fl[4] = {F_U, F_V, F_W, F_T};
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int f = fl[a];
+      S vN, vS, vE, vO;
+      if (!o2) {
+        vN = 7.0 * (Q(Q_J + a, i, j) + Q(Q_J + a, i + 1, j)) - (Q(Q_J + a, i - 1, j) + Q(Q_J + a, i + 2, j));
+        vS = 7.0 * (Q(Q_J + a, i - 1, j) + Q(Q_J + a, i, j)) - (Q(Q_J + a, i - 2, j) + Q(Q_J + a, i + 1, j));
+        vE = 26.0 * P(f, i, j - 1) - (P(f, i, j) + P(f, i, j - 2));
+        vO = 26.0 * P(f, i, j) - (P(f, i, j + 1) + P(f, i, j - 1));
+      } else {
+        vN = (P(f, i, j) + P(f, i + 1, j)) + (P(f, i, j - 1) + P(f, i + 1, j - 1));
+        vS = (P(f, i, j) + P(f, i - 1, j)) + (P(f, i, j - 1) + P(f, i - 1, j - 1));
+        vO = P(f, i, j);
+        vE = P(f, i, j - 1);
+      }
+      gx[a] = vN * nxN + vS * nxS + vO * nxO + vE * nxE;
+      gy[a] = vN * nyN + vS * nyS + vO * nyO + vE * nyE;
+    }
+    S uu, vv, ww, mmu;
+    if (!o2) {
+      uu = 0.0625 * Q(Q_J + 0, i, j);
+      vv = 0.0625 * Q(Q_J + 1, i, j);
+      ww = 0.0625 * Q(Q_J + 2, i, j);
+      mmu = 0.0625 * Q(Q_J + 4, i, j);
+    } else {
+      uu = 0.5 * (P(F_U, i, j) + P(F_U, i, j - 1));
+      vv = 0.5 * (P(F_V, i, j) + P(F_V, i, j - 1));
+      ww = 0.5 * (P(F_W, i, j) + P(F_W, i, j - 1));
+      mmu = 0.5 * (P(F_MU, i, j) + P(F_MU, i, j - 1));
+    }
+    visc_fluxes(mmu, mmu * c.cpprandtl, uu, vv, ww, gx[0], gy[0], gx[1], gy[1], gx[2], gy[2], gx[3], gy[3], fv, gv);
+  }
+
+  // spectral radius, Ducros/pressure sensor and dissipation through the face
+  // between cells L and R (rhs/spectralradius_i.F, ducrosfordnc_i.F,
+  // dissipation_ducros_i.F); LL/RR extend the pressure stencil.
+  BCG_HD void dissipation(int iL, int jL, int iR, int jR, int iLL, int jLL, int iRR, int jRR, double fnx, double fny,
+                          const S pred[5], S diss[5]) const {
+    // Roe average: rr = sqrt(rhoL)/(sqrt(rhoL)+sqrt(rhoR)), so
+    // u = (sL uL + sR uR)/(sL + sR), and likewise v and c^2
+    const S c2r = c.c2fac * P(F_T, iR, jR), c2l = c.c2fac * P(F_T, iL, jL);
+    const S inv = 1.0 / (P(F_SR, iL, jL) + P(F_SR, iR, jR));
+    const S u = (P(F_SU, iL, jL) + P(F_SU, iR, jR)) * inv, v = (P(F_SV, iL, jL) + P(F_SV, iR, jR)) * inv;
+    const S c2x = (P(F_SC, iL, jL) + P(F_SC, iR, jR)) * inv;
+    const double nx2 = fnx * fnx + fny * fny;
+    const S rspec = fabs_t(fnx * u + fny * v) + sqrt_t(c2x * nx2);
+    S eps2 = Planes<S>::c(0.0), eps4 = Planes<S>::c(0.0 < c.k4 ? c.k4 : 0.0);
+    if (c.k2 != 0.0) {
+      // with k2 = 0 the sensor is multiplied by zero: skipped (the reference
+      // value 0*coef is exactly 0 for the finite coef of a physical state)
+      const S pL = P(F_P, iL, jL), pR = P(F_P, iR, jR), pLL = P(F_P, iLL, jLL), pRR = P(F_P, iRR, jRR);
+      const S ks1 = fabs_t(pL - 2.0 * pR + pRR) / fabs_t(pL + 2.0 * pR + pRR);
+      const S ks2 = fabs_t(pLL - 2.0 * pL + pR) / fabs_t(pLL + 2.0 * pL + pR);
+      S divu = G(G_UX, iR, jR) + G(G_VY, iR, jR);
+      S divu2 = divu * divu;
+      S vo = G(G_VX, iR, jR) - G(G_UY, iR, jR);
+      S vort2 = vo * vo;
+      const S ducros1 = divu2 / (divu2 + vort2 + 1e-15);
+      const S dxm1 = 0.5 * (1.0 - tanh_t(2.5 + 10.0 * VOL(iR, jR) / (sqrt_t(c2r * nx2) + 1e-15) * divu));
+      divu = G(G_UX, iL, jL) + G(G_VY, iL, jL);
+      divu2 = divu * divu;
+      vo = G(G_VX, iL, jL) - G(G_UY, iL, jL);
+      vort2 = vo * vo;
+      const S ducros2 = divu2 / (divu2 + vort2 + 1e-15);
+      const S dxm2 = 0.5 * (1.0 - tanh_t(2.5 + 10.0 * VOL(iL, jL) / (sqrt_t(c2l * nx2) + 1e-15) * divu));
+      const S coef = fmax_t(ks1, ks2) * fmax_t(ducros1, ducros2) * fmax_t(dxm1, dxm2);
+      eps2 = c.k2 * coef;
+      eps4 = fmax_t(Planes<S>::c(0.0), c.k4 - eps2 * 12.0);
+    }
+#pragma unroll
+    for (int v5 = 1; v5 <= 5; ++v5) {
+      const S diff = 0.5 * (W(iR, jR, v5) - W(iL, jL, v5));
+      diss[v5 - 1] = rspec * (eps2 * diff + eps4 * pred[v5 - 1]);
+    }
+  }
+
+  // flux assembly (rhs/fluxnumassembly_i.F): (fv nx/|n| + gv ny/|n|) |n| = fv nx + gv ny
+  BCG_HD void assemble(double snx, double sny, const S fx[5], const S diss[5], const S fv[4], const S gv[4], S h[5]) const {
+    h[0] = fx[0] - diss[0];
+#pragma unroll
+    for (int v5 = 2; v5 <= 5; ++v5) h[v5 - 1] = fx[v5 - 1] - diss[v5 - 1] - (fv[v5 - 2] * snx + gv[v5 - 2] * sny);
+  }
+
+  // i-face (i,j), between cells (i-1,j) and (i,j)
+  BCG_HD void iface(int i, int j, S h[5]) const {
+    S fx[5], pred[5], diss[5], fv[4], gv[4];
+    const double fnx = NX(i, j, 1), fny = NY(i, j, 1);
+#pragma unroll
+    for (int v5 = 1; v5 <= 5; ++v5) {
+      fx[v5 - 1] = (c.c1 * (Fl(v5, i, j) + Fl(v5, i - 1, j)) + c.c2 * (Fl(v5, i + 1, j) + Fl(v5, i - 2, j)) +
+                    c.c3 * (Fl(v5, i + 2, j) + Fl(v5, i - 3, j))) * fnx +
+                   (c.c1 * (Gl(v5, i, j) + Gl(v5, i - 1, j)) + c.c2 * (Gl(v5, i + 1, j) + Gl(v5, i - 2, j)) +
+                    c.c3 * (Gl(v5, i + 2, j) + Gl(v5, i - 3, j))) * fny;
+      pred[v5 - 1] = -(c.d3 * W(i - 3, j, v5)) + c.d2 * W(i - 2, j, v5) - c.d1 * W(i - 1, j, v5) +
+                     c.d1 * W(i, j, v5) - c.d2 * W(i + 1, j, v5) + c.d3 * W(i + 2, j, v5);
+    }
+    visc_i(i, j, j <= 2, fv, gv);
+    dissipation(i - 1, j, i, j, i - 2, j, i + 1, j, fnx, fny, pred, diss);
+    assemble(fnx, fny, fx, diss, fv, gv, h);
+  }
+
+  // j-face (i,j), between cells (i,j-1) and (i,j); j >= 2
+  BCG_HD void jface(int i, int j, S h[5]) const {
+    S fx[5], pred[5], diss[5], fv[4], gv[4];
+    const double fnx = NX(i, j, 2), fny = NY(i, j, 2);
+#pragma unroll
+    for (int v5 = 1; v5 <= 5; ++v5) {
+      if (j >= 4) {
+        fx[v5 - 1] = (c.c1 * (Fl(v5, i, j) + Fl(v5, i, j - 1)) + c.c2 * (Fl(v5, i, j + 1) + Fl(v5, i, j - 2)) +
+                      c.c3 * (Fl(v5, i, j + 2) + Fl(v5, i, j - 3))) * fnx +
+                     (c.c1 * (Gl(v5, i, j) + Gl(v5, i, j - 1)) + c.c2 * (Gl(v5, i, j + 1) + Gl(v5, i, j - 2)) +
+                      c.c3 * (Gl(v5, i, j + 2) + Gl(v5, i, j - 3))) * fny;
+      } else {
+        const double* cw = (j == 3) ? c.c5 : c.c3w;  // rhs/nearbndfluxes5demi_7p.F, 3demi
+        fx[v5 - 1] = (cw[0] * Fl(v5, i, 1) + cw[1] * Fl(v5, i, 2) + cw[2] * Fl(v5, i, 3) + cw[3] * Fl(v5, i, 4) +
+                      cw[4] * Fl(v5, i, 5)) * fnx +
+                     (cw[0] * Gl(v5, i, 1) + cw[1] * Gl(v5, i, 2) + cw[2] * Gl(v5, i, 3) + cw[3] * Gl(v5, i, 4) +
+                      cw[4] * Gl(v5, i, 5)) * fny;
+      }
+      pred[v5 - 1] = -(c.d3 * W(i, j - 3, v5)) + c.d2 * W(i, j - 2, v5) - c.d1 * W(i, j - 1, v5) +
+                     c.d1 * W(i, j, v5) - c.d2 * W(i, j + 1, v5) + c.d3 * W(i, j + 2, v5);
+    }
+    visc_j(i, j, j == 2, fv, gv);
+    dissipation(i, j - 1, i, j, i, j - 2, i, j + 1, fnx, fny, pred, diss);
+    assemble(fnx, fny, fx, diss, fv, gv, h);
+  }
+
+  // adiabatic no-slip wall face j = 1 (rhs/fluxwall.F)
+  BCG_HD void wallface(int i, S h[5]) const {
+    const int j = 1;
+    const S pw = c.ct0 * P(F_P, i, j) + c.ct1 * P(F_P, i, j + 1);
+    const S mmu = P(F_MU, i, j);
+    const double nx2 = NX(i, j, 2), ny2 = NY(i, j, 2), vf = VOLF(i, j, 2);
+    const S ux = 2.0 * P(F_U, i, j) * nx2 * vf, vx = 2.0 * P(F_V, i, j) * nx2 * vf, wx = 2.0 * P(F_W, i, j) * nx2 * vf;
+    const S uy = 2.0 * P(F_U, i, j) * ny2 * vf, vy = 2.0 * P(F_V, i, j) * ny2 * vf, wy = 2.0 * P(F_W, i, j) * ny2 * vf;
+    const double TWOTHIRD = 2.0 / 3.0;
+    const S fvrou = TWOTHIRD * mmu * (2.0 * ux - vy), fvrov = mmu * (uy + vx), fvrow = mmu * (wx);
+    const S gvrou = mmu * (uy + vx), gvrov = TWOTHIRD * mmu * (-ux + 2.0 * vy), gvrow = mmu * (wy);
+    h[0] = Planes<S>::c(0.0);
+    h[1] = pw * nx2 - (fvrou * nx2 + gvrou * ny2);
+    h[2] = pw * ny2 - (fvrov * nx2 + gvrov * ny2);
+    h[3] = -(fvrow * nx2 + gvrow * ny2);
+    h[4] = Planes<S>::c(0.0);
+  }
+};
+
+// node t of the (im+1) x (jm+1) node set, i fastest: the i-face (j <= jm)
+// and the j-face (i <= im) of the node into hn (5 i-face, 5 j-face fields)
+template <class S>
+BCG_HD void face_node(const FaceCtx<S>& fc, const Scratch<S>& hn, int t) {
+  const Ext& e = fc.e;
+  const int nI = e.im + 1;
+  const int i = 1 + t % nI, j = 1 + t / nI;
+  S h[5];
+  if (j <= e.jm) {
+    fc.iface(i, j, h);
+#pragma unroll
+    for (int v5 = 0; v5 < 5; ++v5) hn.st(v5, t, h[v5]);
+  }
+  if (i <= e.im) {
+    if (j == 1) fc.wallface(i, h); else fc.jface(i, j, h);
+#pragma unroll
+    for (int v5 = 0; v5 < 5; ++v5) hn.st(5 + v5, t, h[v5]);
+  }
+}
+
+// balance (rhs/balance.F) of interior cell t: residu = -(h1(i+1)-h1(i)) - (h2(j+1)-h2(j))
+template <class S>
+BCG_HD void balance_cell(const Ext& e, const Scratch<S>& hn, double* __restrict__ res, double* __restrict__ resd,
+                         size_t dstride, int t) {
+  const int i = 1 + t % e.im, j = 1 + t / e.im;
+  const int nI = e.im + 1;
+  const int a = (i - 1) + (j - 1) * nI;
+  const size_t q = e.cidx(i, j);
+  constexpr int K = NDir<S>::value;
+#pragma unroll
+  for (int v5 = 0; v5 < 5; ++v5) {
+    const S r = -(hn.ld(v5, a + 1) - hn.ld(v5, a)) - (hn.ld(5 + v5, a + nI) - hn.ld(5 + v5, a));
+    if constexpr (K == 0) {
+      if (res) res[q + (size_t)v5 * e.np] = r;
+    } else {
+      if (res) res[q + (size_t)v5 * e.np] = r.v;
+#pragma unroll
+      for (int k = 0; k < K; ++k) resd[(size_t)k * dstride + q + (size_t)v5 * e.np] = r.d[k];
+    }
+  }
+}
+
+}  // namespace bcg

@@ -227,6 +227,30 @@ int bcg_set_bndbl_2d(const double* w, double* field, double* wbd, int im, int jm
 /* initialisation.f90:2 */
 int bcg_initblfv(double muinf, const double* xc, const double* yc, double* w, double* field, int im, int gh, int jm);
 
+/* ---- uneven batch of grids (no counterpart in the reference, which runs one
+ * grid per process) ---------------------------------------------------------- */
+/* A plan for ngrid independent grids (gh = 3, im, jm >= 6 each; phys holds the
+ * 11 scalars cp cv prandtl gam rgaz cs muref tref s_suth k2 k4 of each grid)
+ * computing the residual (ndir = 0) or the residual and one tangent direction
+ * (ndir = 1) of every grid: each pass of the DNC5 residual is one persistent
+ * launch over the tiles of all grids.  The plan owns its device scratch
+ * (bcg_batch_device_bytes) until bcg_batch_destroy. */
+int bcg_batch_create(int ngrid, const int* im, const int* jm, const double* phys, int ndir, long long* plan);
+/* Device addresses of each grid's arrays (host tables of ngrid entries): w, wd
+ * (one padded direction), nx, ny, vol, volf, residu, residud (interior
+ * written).  May be called again between runs; a captured graph stays valid. */
+int bcg_batch_set_arrays(long long plan, const unsigned long long* w, const unsigned long long* wd,
+                         const unsigned long long* nx, const unsigned long long* ny, const unsigned long long* vol,
+                         const unsigned long long* volf, const unsigned long long* res, const unsigned long long* resd);
+/* Tile shapes: threads per CTA of the face pass (64, 128, 256) and of the cell
+ * passes (128, 256), CTAs per SM of the face pass (1..8); drops a captured graph. */
+int bcg_batch_configure(long long plan, int tile_faces, int tile_cells, int ctas_per_sm);
+/* Queue one evaluation on the library stream; use_graph = 1 captures the
+ * launches into a CUDA graph on first use and replays it afterwards. */
+int bcg_batch_run(long long plan, int use_graph);
+int bcg_batch_device_bytes(long long plan, long long* bytes);
+int bcg_batch_destroy(long long plan);
+
 /* ---- allocation-free residual (no counterpart in the reference) --------------- */
 /* For callers that cannot let the library allocate device memory during a call
  * (a framework allocator already owning the GPU's memory, a fixed memory

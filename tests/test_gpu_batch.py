@@ -1,0 +1,98 @@
+"""Uneven batch of boundary-layer grids (broadcast_gb300.batch, bcg_batch_*):
+per-instance residual and tangent against the single-grid kernels and the
+oracle, graph replay with new array addresses, every tile configuration, and
+the autotuner's cache."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+
+def _cases(n=5, seed=4):
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        im, jm = int(rng.integers(20, 90)), int(rng.integers(10, 40))
+        c = H.bl_case(im, jm, mach=float(rng.uniform(0.3, 0.8)), seed=k)
+        H.oracle_bcs(c, c["w"])
+        wd = np.zeros_like(c["w"])
+        wd[3:-3, 3:-3] = rng.standard_normal((im, jm, 5))
+        H.oracle_bcs(c, c["w"].copy(order="F"), wd)
+        out.append((c, wd))
+    return out
+
+
+def _batch(cases, ndir=1):
+    from broadcast_gb300.batch import GridBatch
+    from broadcast_gb300.operator import to_device
+    gb = GridBatch([c["grid"] for c, _ in cases], [c["phys"] for c, _ in cases], ndir=ndir)
+    gb.set_states([to_device(c["w"]) for c, _ in cases], [to_device(wd) for _, wd in cases] if ndir else None)
+    return gb
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_batch_matches_single_grid_and_oracle(use_graph):
+    import torch
+    from broadcast_gb300.operator import Dnc5Operator, to_device, to_host
+    cases = _cases()
+    gb = _batch(cases)
+    gb.run(use_graph=use_graph)
+    torch.cuda.synchronize()
+    for g, (c, wd) in enumerate(cases):
+        op = Dnc5Operator(c["grid"], c["phys"])
+        r1, rd1 = op.jvp(to_device(c["w"]), to_device(wd))
+        r, rd = to_host(gb.res[g]), to_host(gb.resd[g])
+        sc = H.flux_scale(c, c["w"])
+        assert H.rel_err(r, to_host(r1), sc) < 1e-13
+        ref, refd = O.jvp(c["grid"], c["phys"], c["w"], wd)
+        assert H.rel_err(r, ref, sc) < 1e-12
+        scd = np.abs(H.interior(refd)).reshape(-1, 5).max(0)
+        assert H.rel_err(rd, refd, scd) < 1e-11
+        assert H.rel_err(rd, to_host(rd1), scd) < 1e-13
+
+
+def test_graph_replay_follows_new_arrays_and_every_tile_shape():
+    import torch
+    from broadcast_gb300.batch import CANDIDATES
+    from broadcast_gb300.operator import to_device, to_host
+    cases = _cases(4, seed=9)
+    gb = _batch(cases)
+    gb.run(use_graph=True)
+    torch.cuda.synchronize()
+    first = [to_host(r).copy() for r in gb.res]
+    # new states (different noise) through the same captured graph
+    cases2 = [(dict(c, w=c["w"] * 1.0001), wd) for c, wd in cases]
+    gb.set_states([to_device(c["w"]) for c, _ in cases2], [to_device(wd) for _, wd in cases2])
+    gb.run(use_graph=True)
+    torch.cuda.synchronize()
+    for g, (c, _) in enumerate(cases2):
+        ref = O.residual(c["grid"], c["phys"], c["w"])
+        assert H.rel_err(to_host(gb.res[g]), ref, H.flux_scale(c, c["w"])) < 1e-12
+        assert not np.array_equal(to_host(gb.res[g]), first[g])
+    for cand in CANDIDATES:
+        gb.configure(*cand)
+        gb.run(use_graph=False)
+        torch.cuda.synchronize()
+        for g, (c, _) in enumerate(cases2):
+            ref = O.residual(c["grid"], c["phys"], c["w"])
+            assert H.rel_err(to_host(gb.res[g]), ref, H.flux_scale(c, c["w"])) < 1e-12, cand
+
+
+def test_residual_only_batch_and_autotune_cache(tmp_path):
+    import torch
+    from broadcast_gb300.operator import to_host
+    cases = _cases(3, seed=2)
+    gb = _batch(cases, ndir=0)
+    cache = str(tmp_path / "tune.json")
+    entry = gb.autotune(repeats=2, cache=cache)
+    assert tuple(entry["config"]) == gb.config and len(entry["timings"]) > 4
+    again = gb.autotune(cache=cache)  # served from the cache
+    assert again["config"] == entry["config"]
+    gb.run(use_graph=True)
+    torch.cuda.synchronize()
+    for g, (c, _) in enumerate(cases):
+        ref = O.residual(c["grid"], c["phys"], c["w"])
+        assert H.rel_err(to_host(gb.res[g]), ref, H.flux_scale(c, c["w"])) < 1e-12
