@@ -1,0 +1,123 @@
+"""Pseudo-transient Newton (SER) iteration to a steady base flow: the
+'fixed_point' mode of the boundary-layer driver (BROADCAST_npz.py:985-1196),
+the immediate caller of the residual and Jacobian hot path.
+
+Per iteration, as the reference:
+  1. boundary fills (inlet Ilo, no-reflexion Jhi, extrapolation Ihi, wall Jlo);
+  2. residual R(w) and its L2 / L10 norms (srcfv/norm.F90);
+  3. relaxation 1/cfl = r / dt with r = max of the first three normalised norms
+     (:1079-1087) and coefdiag = (1/cfl) vol;
+  4. the relaxed Jacobian coefdiag - dR/dw for all 245 colour seeds as CSR
+     (computejacobianfromjv_relaxed + remove_zero_jac, :1088-1137);
+  5. solve J dw = R (:1146-1158: PETSc LU with MUMPS there) and w += dw,
+     stepping back and halving cfl when dw is not finite (:1167-1172).
+Steps 1, 2 and 4 run on the GPU through the library; step 5 calls `solver`,
+by default a SuperLU factorisation (scipy), the only sparse direct solver in
+this image; a PETSc/MUMPS or cuDSS solve can be passed in its place.
+"""
+import time
+
+import numpy as np
+
+from . import _lib
+
+PHYS = ("cp", "cv", "prandtl", "gam", "rgaz", "cs", "muref", "tref", "s_suth", "k2", "k4")
+
+
+def superlu_solve(A, b):
+    from scipy.sparse.linalg import splu
+    return splu(A.tocsc(), permc_spec="COLAMD").solve(b)
+
+
+class BLNewton:
+    """SER Newton on a boundary-layer case (broadcast_gb300.cases.bl_case layout);
+    cfl = 1e10 is the boundary-layer card's setting (card_bl2d_fv_npz.py:56):
+    the relaxation vanishes and the iteration is Newton's."""
+
+    def __init__(self, case, cfl=1.0e10, mach=None, solver=superlu_solve):
+        from ._f2py import interf4
+        _lib.load()
+        self.c = case
+        g, ph = case["grid"], case["phys"]
+        self.im, self.jm, self.gh = int(g["im"]), int(g["jm"]), int(g["gh"])
+        self.phys = [float(ph[k]) for k in PHYS]
+        self.mach = float(mach if mach is not None else ph.get("mach", 0.5))
+        self.cfl = float(cfl)
+        self.solver = solver
+        it = case["interf"]
+        self.interf = [interf4(it[k]) for k in ("Ilo", "Jhi", "Ihi", "Jlo")]
+        yc = g["yc"]
+        gh = self.gh
+        self.dt = self.cfl * (yc[gh, gh + 1] - yc[gh, gh]) / (1.0 / self.mach + 1.0)
+        self.history = []
+
+    def fill(self, w):
+        from .srcfv import f_bnd
+        c, g = self.c, self.c["grid"]
+        it, gam = c["interf"], self.c["phys"]["gam"]
+        f_bnd.bc_supandsubinlet_2d(w, "Ilo", it["Ilo"], c["field"], g["nx"], g["ny"], gam, self.im, self.jm)
+        f_bnd.bc_no_reflexion_2d(w, c["wbd"], "Jhi", it["Jhi"], g["nx"], g["ny"], gam, self.gh, self.im, self.jm)
+        f_bnd.bc_extrapolate_o2_2d(w, "Ihi", it["Ihi"], self.im, self.jm, self.gh)
+        f_bnd.bc_wall_viscous_adia_2d(w, "Jlo", gam, it["Jlo"], self.gh, self.im, self.jm)
+
+    def residual(self, w):
+        from .srcfv import f_norm, f_sch
+        g = self.c["grid"]
+        res = np.zeros_like(w)
+        f_sch.flux_num_dnc5_2d(res, w, g["x0"], g["y0"], g["nx"], g["ny"], g["xc"], g["yc"], g["vol"], g["volf"],
+                               self.gh, *self.phys, self.im, self.jm)
+        norm, ninf = f_norm.compute_norml2inf(res, self.im, self.jm, self.gh)
+        return res, np.asarray(norm), np.asarray(ninf)
+
+    def jacobian(self, w, coefdiag):
+        import scipy.sparse as sp
+        g, c = self.c["grid"], self.c
+        nrow = 5 * self.im * self.jm
+        cap = nrow * 245
+        indptr, indices, data = np.zeros(nrow + 1, np.int32), np.zeros(cap, np.int32), np.zeros(cap)
+        nnz = np.zeros(1, np.int64)
+        _lib.call("bcg_jacobian_dnc5_bl_csr", w, g["nx"], g["ny"], g["vol"], g["volf"], self.gh, *self.phys,
+                  self.im, self.jm, *self.interf, c["field"], c["field"].shape[0], c["wbd"], c["wbd"].shape[0],
+                  np.asfortranarray(coefdiag), 2e-16, 0, indptr, indices, data, cap, nnz)
+        n = int(nnz[0])
+        return sp.csr_matrix((data[:n].copy(), indices[:n].copy(), indptr), shape=(nrow, nrow))
+
+    def step(self, w, first=False):
+        """One SER Newton iteration on w (Fortran-ordered, updated in place)."""
+        t0 = time.perf_counter()
+        self.fill(w)
+        res, norm, ninf = self.residual(w)
+        if first:
+            self.norm0m1 = 1.0 / np.maximum(norm, 1e-15)
+            self.ninf0m1 = 1.0 / np.maximum(ninf, 1e-15)
+        r = np.max(np.concatenate([norm[:3] * self.norm0m1[:3], ninf[:3] * self.ninf0m1[:3]]))
+        cflm1 = r / self.dt
+        gh = self.gh
+        coefdiag = cflm1 * self.c["grid"]["vol"][gh:-gh, gh:-gh]
+        J = self.jacobian(w, coefdiag)
+        try:
+            dw = np.reshape(self.solver(J, np.ravel(res[gh:-gh, gh:-gh, :])), (self.im, self.jm, 5))
+        except RuntimeError:  # singular factorisation: treated like a non-finite update
+            dw = np.full((self.im, self.jm, 5), np.nan)
+        if np.all(np.isfinite(dw)):
+            w[gh:-gh, gh:-gh, :] += dw
+            self.dw_old = dw
+        else:
+            # step back and halve the CFL number (:1167-1172); here the time
+            # step follows the CFL number
+            if hasattr(self, "dw_old"):
+                w[gh:-gh, gh:-gh, :] -= self.dw_old
+            self.cfl /= 2.0
+            self.dt /= 2.0
+        self.history.append(dict(norm=norm.tolist(), cflm1=float(cflm1), nnz=int(J.nnz),
+                                 seconds=time.perf_counter() - t0))
+        return norm, dw
+
+    def solve(self, w, ite=50, tol=1e-10):
+        """Iterate until max L2 residual norm <= tol (absolute) or ite steps."""
+        for it in range(1, ite + 1):
+            norm, _ = self.step(w, first=(it == 1))
+            if norm.max() <= tol:
+                break
+        self.fill(w)
+        return w
