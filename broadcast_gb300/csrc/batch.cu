@@ -3,7 +3,7 @@
 // The reference runs one grid per process (BROADCAST_npz.py); a batch of
 // boundary-layer instances of different sizes would leave most of a GB300
 // idle per grid.  Here every pass of the DNC5 residual (primitives, Ducros
-// gradients, interpolation rows, faces, balance; the same per-element bodies
+// gradients, interpolation rows, viscous point values, faces, balance; the same per-element bodies
 // as the single-grid kernels, passes.cuh) is ONE persistent launch over a
 // tile list that concatenates the tiles of all grids: each CTA walks tiles
 // t = blockIdx.x, blockIdx.x + gridDim.x, ...; a tile belongs to one grid,
@@ -23,7 +23,7 @@ namespace bcg {
 
 namespace {
 
-enum { P_PRIM = 0, P_GRAD, P_QROWS, P_FACES, P_BAL, NPASS };
+enum { P_PRIM = 0, P_GRAD, P_QROWS, P_VPTS, P_FACES, P_BAL, NPASS };
 
 struct GridDesc {
   Ext e;
@@ -107,6 +107,8 @@ __global__ void __launch_bounds__(BT) k_batch(const GridDesc* __restrict__ descs
         if (el < (long long)e.np) prim_cell<S>(e, G.c, state_of<S>(G), f.pr, (size_t)el);
       } else if constexpr (PASS == P_QROWS) {
         if (el < (long long)e.np) qrows_cell<S>(e, f.pr, f.qr, (size_t)el);
+      } else if constexpr (PASS == P_VPTS) {
+        if (el < (long long)e.np) vpts_cell<S>(e, f.qr, (size_t)el);
       } else if constexpr (PASS == P_GRAD) {
         if (el < (long long)e.im * e.jm) grad_cell<S>(e, G.c, f.pr, f.gr, G.nx, G.ny, G.vol, (int)el);
       } else {
@@ -126,7 +128,7 @@ struct BatchPlan {
   double* scratch = nullptr;
   size_t scratch_doubles = 0;
   int tile_faces = 128, tile_cells = 256, ctas = 2, nsm = 0;
-  long long ntiles[NPASS] = {0, 0, 0, 0, 0};
+  long long ntiles[NPASS] = {0, 0, 0, 0, 0, 0};
   bool any_grad = false;
   cudaStream_t cap = nullptr;  // capture stream (the caller's may be the legacy default stream)
   cudaGraphExec_t exec = nullptr;
@@ -134,7 +136,7 @@ struct BatchPlan {
 
 static long long pass_count(const Ext& e, int pass, bool grad) {
   switch (pass) {
-    case P_PRIM: case P_QROWS: return (long long)e.np;
+    case P_PRIM: case P_QROWS: case P_VPTS: return (long long)e.np;
     case P_GRAD: return grad ? (long long)e.im * e.jm : 0;
     case P_FACES: return (long long)(e.im + 1) * (e.jm + 1);
     default: return (long long)e.im * e.jm;
@@ -235,13 +237,14 @@ static void launch_cells(const BatchPlan* p, int pass, cudaStream_t st) {
     case P_PRIM: launch_pass<S, P_PRIM, BT>(p, ctas, st); break;
     case P_GRAD: launch_pass<S, P_GRAD, BT>(p, ctas, st); break;
     case P_QROWS: launch_pass<S, P_QROWS, BT>(p, ctas, st); break;
+    case P_VPTS: launch_pass<S, P_VPTS, BT>(p, ctas, st); break;
     default: launch_pass<S, P_BAL, BT>(p, ctas, st); break;
   }
 }
 
 template <class S>
 static cudaError_t launch_all(const BatchPlan* p, cudaStream_t st) {
-  const int passes[4] = {P_PRIM, P_GRAD, P_QROWS, -1};
+  const int passes[5] = {P_PRIM, P_GRAD, P_QROWS, P_VPTS, -1};
   for (int q : passes) {
     if (q < 0) break;
     if (q == P_GRAD && !p->any_grad) continue;

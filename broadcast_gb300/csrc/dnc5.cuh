@@ -71,8 +71,11 @@ enum PField {
   F_SR, F_SU, F_SV, F_SC,  // sqrt(rho) and sqrt(rho) * (u, v, c^2) for the Roe average
   F_NPRIM
 };
-// Fields of the 4-point interpolation scratch (pass 1b): QI for u v w T mu, then QJ
-enum QField { Q_I = 0, Q_J = 5, Q_NQ = 10 };
+// Fields of the interpolation scratch (passes 1b and 1c): QI and QJ for
+// u v w T mu, then for u v w T the point values of the 4th-order viscous face
+// gradients, each shared by two faces: C (3-point along i), D (3-point along
+// j), EI (4-point across i-face rows), NJ (4-point across j-face columns)
+enum QField { Q_I = 0, Q_J = 5, V_C = 10, V_D = 14, V_EI = 18, V_NJ = 22, Q_NQ = 26 };
 // Fields of the gradient scratch (pass 2)
 enum GField { G_UX = 0, G_UY, G_VX, G_VY, G_NGRAD };
 

@@ -60,6 +60,37 @@ BCG_HD void qrows_cell(const Ext& e, const Scratch<S>& pr, const Scratch<S>& qr,
       qr.st(Q_J + a, q, 9.0 * (x1 + x2) - (x0 + x3));
     }
   }
+  // 3-point values 26 q(c) - (q(c+1) + q(c-1)) of u v w T:
+  //   C along i at i in [0, im+1], j in [3, jm]   (i-faces (i,j), (i+1,j), rows j >= 3)
+  //   D along j at i in [1, im], j in [2, jm+1]   (j-faces (i,j), (i,j+1), rows j >= 3)
+  if (i >= 0 && i <= e.im + 1 && j >= 3 && j <= e.jm) {
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+      qr.st(V_C + a, q, 26.0 * pr.ld(fl[a], q) - (pr.ld(fl[a], q + di) + pr.ld(fl[a], q - di)));
+  }
+  if (i >= 1 && i <= e.im && j >= 2 && j <= e.jm + 1) {
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+      qr.st(V_D + a, q, 26.0 * pr.ld(fl[a], q) - (pr.ld(fl[a], q + dj) + pr.ld(fl[a], q - dj)));
+  }
+}
+
+// pass 1c: the 4-point combinations 7 (b + c) - (a + d) of the interpolation
+// rows, at i in [1, im+1], j in [3, jm+1]:
+//   EI(i,j) from QI(i, j-2..j+1)  (vE / vO of the i-faces (i,j) / (i,j-1))
+//   NJ(i,j) from QJ(i-2..i+1, j)  (vS / vN of the j-faces (i,j) / (i-1,j))
+template <class S>
+BCG_HD void vpts_cell(const Ext& e, const Scratch<S>& qr, size_t q) {
+  const int i = (int)(q % e.ni) + 1 - e.gh, j = (int)(q / e.ni) + 1 - e.gh;
+  if (i < 1 || i > e.im + 1 || j < 3 || j > e.jm + 1) return;
+  const int di = 1, dj = e.ni;
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const S y0 = qr.ld(Q_I + a, q - 2 * dj), y1 = qr.ld(Q_I + a, q - dj), y2 = qr.ld(Q_I + a, q), y3 = qr.ld(Q_I + a, q + dj);
+    qr.st(V_EI + a, q, 7.0 * (y1 + y2) - (y0 + y3));
+    const S z0 = qr.ld(Q_J + a, q - 2 * di), z1 = qr.ld(Q_J + a, q - di), z2 = qr.ld(Q_J + a, q), z3 = qr.ld(Q_J + a, q + di);
+    qr.st(V_NJ + a, q, 7.0 * (z1 + z2) - (z0 + z3));
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -154,10 +185,10 @@ struct FaceCtx {
       const int f = fl[a];
       S vN, vS, vE, vO;
       if (!o2) {
-        vN = 26.0 * P(f, i, j) - (P(f, i + 1, j) + P(f, i - 1, j));
-        vS = 26.0 * P(f, i - 1, j) - (P(f, i, j) + P(f, i - 2, j));
-        vE = 7.0 * (Q(Q_I + a, i, j - 1) + Q(Q_I + a, i, j)) - (Q(Q_I + a, i, j - 2) + Q(Q_I + a, i, j + 1));
-        vO = 7.0 * (Q(Q_I + a, i, j) + Q(Q_I + a, i, j + 1)) - (Q(Q_I + a, i, j - 1) + Q(Q_I + a, i, j + 2));
+        vN = Q(V_C + a, i, j);
+        vS = Q(V_C + a, i - 1, j);
+        vE = Q(V_EI + a, i, j);
+        vO = Q(V_EI + a, i, j + 1);
       } else {
         vN = P(f, i, j);
         vS = P(f, i - 1, j);
@@ -197,10 +228,10 @@ struct FaceCtx {
       const int f = fl[a];
       S vN, vS, vE, vO;
       if (!o2) {
-        vN = 7.0 * (Q(Q_J + a, i, j) + Q(Q_J + a, i + 1, j)) - (Q(Q_J + a, i - 1, j) + Q(Q_J + a, i + 2, j));
-        vS = 7.0 * (Q(Q_J + a, i - 1, j) + Q(Q_J + a, i, j)) - (Q(Q_J + a, i - 2, j) + Q(Q_J + a, i + 1, j));
-        vE = 26.0 * P(f, i, j - 1) - (P(f, i, j) + P(f, i, j - 2));
-        vO = 26.0 * P(f, i, j) - (P(f, i, j + 1) + P(f, i, j - 1));
+        vN = Q(V_NJ + a, i + 1, j);
+        vS = Q(V_NJ + a, i, j);
+        vE = Q(V_D + a, i, j - 1);
+        vO = Q(V_D + a, i, j);
       } else {
         vN = (P(f, i, j) + P(f, i + 1, j)) + (P(f, i, j - 1) + P(f, i + 1, j - 1));
         vS = (P(f, i, j) + P(f, i - 1, j)) + (P(f, i, j - 1) + P(f, i - 1, j - 1));
@@ -279,12 +310,13 @@ struct FaceCtx {
   BCG_HD void iface(int i, int j, S h[5]) const {
     S fx[5], pred[5], diss[5], fv[4], gv[4];
     const double fnx = NX(i, j, 1), fny = NY(i, j, 1);
+    // centred weights times the face normal, once per face (rhs/euler_o6_i.F)
+    const double a1 = c.c1 * fnx, a2 = c.c2 * fnx, a3 = c.c3 * fnx, b1 = c.c1 * fny, b2 = c.c2 * fny, b3 = c.c3 * fny;
 #pragma unroll
     for (int v5 = 1; v5 <= 5; ++v5) {
-      fx[v5 - 1] = (c.c1 * (Fl(v5, i, j) + Fl(v5, i - 1, j)) + c.c2 * (Fl(v5, i + 1, j) + Fl(v5, i - 2, j)) +
-                    c.c3 * (Fl(v5, i + 2, j) + Fl(v5, i - 3, j))) * fnx +
-                   (c.c1 * (Gl(v5, i, j) + Gl(v5, i - 1, j)) + c.c2 * (Gl(v5, i + 1, j) + Gl(v5, i - 2, j)) +
-                    c.c3 * (Gl(v5, i + 2, j) + Gl(v5, i - 3, j))) * fny;
+      fx[v5 - 1] = a1 * (Fl(v5, i, j) + Fl(v5, i - 1, j)) + a2 * (Fl(v5, i + 1, j) + Fl(v5, i - 2, j)) +
+                   a3 * (Fl(v5, i + 2, j) + Fl(v5, i - 3, j)) + b1 * (Gl(v5, i, j) + Gl(v5, i - 1, j)) +
+                   b2 * (Gl(v5, i + 1, j) + Gl(v5, i - 2, j)) + b3 * (Gl(v5, i + 2, j) + Gl(v5, i - 3, j));
       pred[v5 - 1] = -(c.d3 * W(i - 3, j, v5)) + c.d2 * W(i - 2, j, v5) - c.d1 * W(i - 1, j, v5) +
                      c.d1 * W(i, j, v5) - c.d2 * W(i + 1, j, v5) + c.d3 * W(i + 2, j, v5);
     }
@@ -297,13 +329,13 @@ struct FaceCtx {
   BCG_HD void jface(int i, int j, S h[5]) const {
     S fx[5], pred[5], diss[5], fv[4], gv[4];
     const double fnx = NX(i, j, 2), fny = NY(i, j, 2);
+    const double a1 = c.c1 * fnx, a2 = c.c2 * fnx, a3 = c.c3 * fnx, b1 = c.c1 * fny, b2 = c.c2 * fny, b3 = c.c3 * fny;
 #pragma unroll
     for (int v5 = 1; v5 <= 5; ++v5) {
       if (j >= 4) {
-        fx[v5 - 1] = (c.c1 * (Fl(v5, i, j) + Fl(v5, i, j - 1)) + c.c2 * (Fl(v5, i, j + 1) + Fl(v5, i, j - 2)) +
-                      c.c3 * (Fl(v5, i, j + 2) + Fl(v5, i, j - 3))) * fnx +
-                     (c.c1 * (Gl(v5, i, j) + Gl(v5, i, j - 1)) + c.c2 * (Gl(v5, i, j + 1) + Gl(v5, i, j - 2)) +
-                      c.c3 * (Gl(v5, i, j + 2) + Gl(v5, i, j - 3))) * fny;
+        fx[v5 - 1] = a1 * (Fl(v5, i, j) + Fl(v5, i, j - 1)) + a2 * (Fl(v5, i, j + 1) + Fl(v5, i, j - 2)) +
+                     a3 * (Fl(v5, i, j + 2) + Fl(v5, i, j - 3)) + b1 * (Gl(v5, i, j) + Gl(v5, i, j - 1)) +
+                     b2 * (Gl(v5, i, j + 1) + Gl(v5, i, j - 2)) + b3 * (Gl(v5, i, j + 2) + Gl(v5, i, j - 3));
       } else {
         const double* cw = (j == 3) ? c.c5 : c.c3w;  // rhs/nearbndfluxes5demi_7p.F, 3demi
         fx[v5 - 1] = (cw[0] * Fl(v5, i, 1) + cw[1] * Fl(v5, i, 2) + cw[2] * Fl(v5, i, 3) + cw[3] * Fl(v5, i, 4) +

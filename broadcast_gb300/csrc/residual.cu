@@ -44,6 +44,14 @@ __global__ void __launch_bounds__(256) k_qrows(Ext e, Scratch<S> pr, Scratch<S> 
 }
 
 template <class S>
+__global__ void __launch_bounds__(256) k_vpts(Ext e, Scratch<S> qr, GroupStride gs) {
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= e.np) return;
+  shift_scratch(qr, blockIdx.y * gs.scratch);
+  vpts_cell<S>(e, qr, q);
+}
+
+template <class S>
 __global__ void __launch_bounds__(256) k_grad(Ext e, Coef c, Scratch<S> pr, Scratch<S> gr, const double* __restrict__ nx,
                                               const double* __restrict__ ny, const double* __restrict__ vol,
                                               GroupStride gs) {
@@ -100,6 +108,7 @@ static cudaError_t run_residual_t(const ResidualArgs& a, cudaStream_t st) {
   if (c.k2 != 0.0)
     k_grad<S><<<dim3((unsigned)((a.im * a.jm + B - 1) / B), ng), B, 0, st>>>(e, c, pr, gr, a.nx, a.ny, a.vol, gs);
   k_qrows<S><<<dim3((unsigned)((e.np + B - 1) / B), ng), B, 0, st>>>(e, pr, qr, gs);
+  k_vpts<S><<<dim3((unsigned)((e.np + B - 1) / B), ng), B, 0, st>>>(e, qr, gs);
   FaceCtx<S> fc{e, c, w, pr, gr, qr, a.nx, a.ny, a.vol, a.volf};
   const int BF = 128;
   k_faces<S><<<dim3((unsigned)((nn + BF - 1) / BF), ng), BF, 0, st>>>(fc, hn, gs);
