@@ -31,6 +31,95 @@ int has_device() {
   return 1;
 }
 
+// Copy streams of the pipelined host-array path (one pair per device,
+// created on first use, never destroyed).
+struct CopyStreams { cudaStream_t in = nullptr, out = nullptr; };
+int copy_streams(CopyStreams* cs) {
+  static std::mutex mu;
+  static std::map<int, CopyStreams> per_dev;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail_cuda("copy streams", e);
+  std::lock_guard<std::mutex> lk(mu);
+  CopyStreams& c = per_dev[dev];
+  if (!c.in) {
+    e = cudaStreamCreateWithFlags(&c.in, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.out, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { c = CopyStreams{}; return fail_cuda("copy streams", e); }
+  }
+  *cs = c;
+  return BCG_OK;
+}
+
+// device -> host copy of the interior of nplanes padded (ni, nj) planes
+cudaError_t copy_interior_d2h(double* host, const double* dev, int ni, int nj, int nplanes, int gh, int im, int jm,
+                              cudaStream_t st) {
+  const size_t pitch = (size_t)ni * sizeof(double), plane = (size_t)ni * nj;
+  const size_t off0 = (size_t)gh + (size_t)gh * ni;
+  for (int pl = 0; pl < nplanes; ++pl) {
+    cudaError_t e = cudaMemcpy2DAsync(host + pl * plane + off0, pitch, dev + pl * plane + off0, pitch,
+                                      (size_t)im * sizeof(double), jm, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// Host tangents and outputs of many directions: the directions run in two
+// chunks of whole 4-direction groups; chunk c's upload (copy stream in), its
+// residual passes (library stream) and its download (copy stream out) overlap
+// the other chunk's.  Uploads start only after the library stream's earlier
+// work, since the pool buffers they fill may still be in use.
+int residual_pipelined(ResidualArgs a, double* res, double* residud, const double* wd, int nd, cudaStream_t st) {
+  const int im = a.im, jm = a.jm, gh = a.gh, ni = im + 2 * gh, nj = jm + 2 * gh;
+  const size_t plane5 = (size_t)ni * nj * 5;
+  CopyStreams cs;
+  int rc = copy_streams(&cs);
+  if (rc) return rc;
+  double* wd_dev = (double*)pool_get(POOL_AUX, plane5 * nd * sizeof(double));
+  double* rd_dev = (double*)pool_get(POOL_STAGE_OUT, plane5 * nd * sizeof(double));
+  const int ng = nd / 4;
+  const int split = 4 * ((ng + 1) / 2);  // directions of the first chunk
+  const int bounds[3] = {0, split, nd};
+  const size_t s4 = residual_scratch_doubles(im, jm, gh, 4);
+  double* scr = (double*)pool_get(POOL_SCRATCH, s4 * 8 * (size_t)((ng + 1) / 2) + residual_scratch_doubles(im, jm, gh, 2) * 8);
+  if (!wd_dev || !rd_dev || !scr) return fail_arg("scratch allocation failed"), BCG_ERR_NOMEM;
+  cudaEvent_t ev[6] = {};
+  for (auto& x : ev)
+    if (cudaEventCreateWithFlags(&x, cudaEventDisableTiming) != cudaSuccess) return fail_cuda("events", cudaGetLastError());
+  struct Guard { cudaEvent_t* e; ~Guard() { for (int k = 0; k < 6; ++k) if (e[k]) cudaEventDestroy(e[k]); } } guard{ev};
+  cudaError_t e = cudaEventRecord(ev[0], st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(cs.in, ev[0], 0);
+  if (e != cudaSuccess) return fail_cuda("pipelined residual", e);
+  for (int c = 0; c < 2; ++c) {
+    const int d0 = bounds[c], d1 = bounds[c + 1];
+    if (d1 <= d0) continue;
+    e = cudaMemcpyAsync(wd_dev + plane5 * d0, wd + plane5 * d0, plane5 * (d1 - d0) * sizeof(double),
+                        cudaMemcpyHostToDevice, cs.in);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1 + c], cs.in);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev[1 + c], 0);
+    if (e != cudaSuccess) return fail_cuda("pipelined residual: upload", e);
+    for (int k0 = d0; k0 < d1;) {
+      const int left = d1 - k0;
+      const int kk = left >= 4 ? 4 : (left >= 2 ? 2 : 1);
+      a.ndir = kk; a.ngroup = left >= 4 ? left / 4 : 1;
+      a.wd = wd_dev + plane5 * k0; a.resd = rd_dev + plane5 * k0;
+      a.res = (k0 == 0) ? res : nullptr;
+      a.scratch = scr;
+      e = run_residual(a, st);
+      if (e != cudaSuccess) return fail_cuda("flux_num_dnc5_2d_d", e);
+      k0 += kk * a.ngroup;
+    }
+    e = cudaEventRecord(ev[3 + c], st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs.out, ev[3 + c], 0);
+    if (e == cudaSuccess)
+      e = copy_interior_d2h(residud + plane5 * d0, rd_dev + plane5 * d0, ni, nj, 5 * (d1 - d0), gh, im, jm, cs.out);
+    if (e != cudaSuccess) return fail_cuda("pipelined residual: download", e);
+  }
+  e = cudaEventRecord(ev[5], cs.out);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev[5], 0);
+  return e == cudaSuccess ? BCG_OK : fail_cuda("pipelined residual", e);
+}
+
 // shared body of the residual / JVP entry points
 int residual_call(double* residu, double* residud, const double* w, const double* wd, int nd, const double* nx,
                   const double* ny, const double* vol, const double* volf, int gh, double cp, double cv,
@@ -46,8 +135,10 @@ int residual_call(double* residu, double* residud, const double* w, const double
   const int hvol = sg.in(vol, np * 8), hvolf = sg.in(volf, np * 2 * 8);
   const int ni = im + 2 * gh, nj = jm + 2 * gh;
   const int hres = residu ? sg.out_interior(residu, ni, nj, 5, gh, im, jm) : -1;
-  const int hwd = nd ? sg.in(wd, np * 5 * 8 * (size_t)nd) : -1;
-  const int hresd = nd ? sg.out_interior(residud, ni, nj, 5 * nd, gh, im, jm) : -1;
+  // many directions in host memory: pipelined upload / compute / download
+  const bool pipelined = nd >= 8 && wd && residud && !is_device_ptr(wd) && !is_device_ptr(residud);
+  const int hwd = (nd && !pipelined) ? sg.in(wd, np * 5 * 8 * (size_t)nd) : -1;
+  const int hresd = (nd && !pipelined) ? sg.out_interior(residud, ni, nj, 5 * nd, gh, im, jm) : -1;
   int rc = sg.commit();
   if (rc) return rc;
   ResidualArgs a{};
@@ -57,6 +148,14 @@ int residual_call(double* residu, double* residud, const double* w, const double
   a.vol = sg.dev<double>(hvol); a.volf = sg.dev<double>(hvolf);
   a.dstride = np * 5;
   double* res = hres >= 0 ? sg.dev<double>(hres) : nullptr;
+  if (pipelined) {
+    rc = residual_pipelined(a, res, residud, wd, nd, st);
+    if (rc) return rc;
+    rc = sg.finish();
+    if (rc) return rc;
+    const cudaError_t e = cudaStreamSynchronize(st);  // host outputs complete on return
+    return e == cudaSuccess ? BCG_OK : fail_cuda("stream synchronize", e);
+  }
   if (nd == 0) {
     a.ndir = 0; a.res = res;
     a.scratch = (double*)pool_get(POOL_SCRATCH, residual_scratch_doubles(im, jm, gh, 0) * 8);
