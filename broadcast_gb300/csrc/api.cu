@@ -124,7 +124,7 @@ int residual_pipelined(ResidualArgs a, double* res, double* residud, const doubl
 int residual_call(double* residu, double* residud, const double* w, const double* wd, int nd, const double* nx,
                   const double* ny, const double* vol, const double* volf, int gh, double cp, double cv,
                   double prandtl, double gam, double rgaz, double cs, double muref, double tref, double s_suth,
-                  double k2, double k4, int im, int jm) {
+                  double k2, double k4, int im, int jm, int nowall = 0) {
   if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
   if (!dims_ok(im, jm, gh)) return fail_arg("flux_num_dnc5_2d: need gh == 3 and im, jm >= 6");
   if (nd < 0) return fail_arg("flux_num_dnc5_2d_dn: negative direction count");
@@ -147,6 +147,7 @@ int residual_call(double* residu, double* residud, const double* w, const double
   a.w = sg.dev<double>(hw); a.nx = sg.dev<double>(hnx); a.ny = sg.dev<double>(hny);
   a.vol = sg.dev<double>(hvol); a.volf = sg.dev<double>(hvolf);
   a.dstride = np * 5;
+  a.nowall = nowall;
   double* res = hres >= 0 ? sg.dev<double>(hres) : nullptr;
   if (pipelined) {
     rc = residual_pipelined(a, res, residud, wd, nd, st);
@@ -343,6 +344,27 @@ int bcg_flux_num_dnc5_2d(double* residu, const double* w, const double* x0, cons
   (void)x0; (void)y0; (void)xc; (void)yc;
   return residual_call(residu, nullptr, w, nullptr, 0, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref,
                        tref, s_suth, k2, k4, im, jm);
+}
+
+// ---- residual without the wall rows (srcfv/rhs/flux_num_dnc5_nowall.F90:7) and
+// its tangent (srcfv/tangent/flux_num_dnc5_nowall_d.f90) -----------------------
+int bcg_flux_num_dnc5_nowall_2d(double* residu, const double* w, const double* x0, const double* y0,
+                                const double* nx, const double* ny, const double* xc, const double* yc,
+                                const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
+                                double gam, double rgaz, double cs, double muref, double tref, double s_suth,
+                                double k2, double k4, int im, int jm) {
+  (void)x0; (void)y0; (void)xc; (void)yc;
+  return residual_call(residu, nullptr, w, nullptr, 0, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref,
+                       tref, s_suth, k2, k4, im, jm, 1);
+}
+int bcg_flux_num_dnc5_nowall_2d_d(double* residu, double* residud, const double* w, const double* wd,
+                                  const double* x0, const double* y0, const double* nx, const double* ny,
+                                  const double* xc, const double* yc, const double* vol, const double* volf, int gh,
+                                  double cp, double cv, double prandtl, double gam, double rgaz, double cs,
+                                  double muref, double tref, double s_suth, double k2, double k4, int im, int jm) {
+  (void)x0; (void)y0; (void)xc; (void)yc;
+  return residual_call(residu, residud, w, wd, 1, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref, tref,
+                       s_suth, k2, k4, im, jm, 1);
 }
 
 int bcg_flux_num_dnc5_2d_d(double* residu, double* residud, const double* w, const double* wd, const double* x0,

@@ -28,6 +28,7 @@ struct Coef {
   double b1, b2, c1, c2, c3, d1, d2, d3;
   double c5[5], c3w[5];
   double ct0, ct1, k2, k4, s_suth;
+  int wall;  // 1: adiabatic wall at j = 1 (flux_num_dnc5_2d); 0: centred rows everywhere (flux_num_dnc5_nowall_2d)
 };
 
 inline Coef make_coef(const Phys& p) {
@@ -47,6 +48,7 @@ inline Coef make_coef(const Phys& p) {
   c.c3w[0] = 12.0 * denom; c.c3w[1] = 77.0 * denom; c.c3w[2] = -43.0 * denom; c.c3w[3] = 17.0 * denom; c.c3w[4] = -3.0 * denom;
   c.ct0 = 1.125; c.ct1 = -0.125;
   c.k2 = p.k2; c.k4 = p.k4; c.s_suth = p.s_suth;
+  c.wall = 1;
   return c;
 }
 

@@ -53,7 +53,7 @@ BCG_HD void qrows_cell(const Ext& e, const Scratch<S>& pr, const Scratch<S>& qr,
       qr.st(Q_I + a, q, 9.0 * (x1 + x2) - (x0 + x3));
     }
   }
-  if (i >= -1 && i <= e.im + 2 && j >= 2 && j <= e.jm + 1) {
+  if (i >= -1 && i <= e.im + 2 && j >= 1 && j <= e.jm + 1) {
 #pragma unroll
     for (int a = 0; a < 5; ++a) {
       const S x0 = pr.ld(fl[a], q - 2 * dj), x1 = pr.ld(fl[a], q - dj), x2 = pr.ld(fl[a], q), x3 = pr.ld(fl[a], q + dj);
@@ -61,14 +61,15 @@ BCG_HD void qrows_cell(const Ext& e, const Scratch<S>& pr, const Scratch<S>& qr,
     }
   }
   // 3-point values 26 q(c) - (q(c+1) + q(c-1)) of u v w T:
-  //   C along i at i in [0, im+1], j in [3, jm]   (i-faces (i,j), (i+1,j), rows j >= 3)
-  //   D along j at i in [1, im], j in [2, jm+1]   (j-faces (i,j), (i,j+1), rows j >= 3)
-  if (i >= 0 && i <= e.im + 1 && j >= 3 && j <= e.jm) {
+  //   C along i at i in [0, im+1], j in [1, jm]   (i-faces (i,j), (i+1,j))
+  //   D along j at i in [1, im], j in [0, jm+1]   (j-faces (i,j), (i,j+1))
+  // (the wall rows use only j >= 3 and j >= 2 of them; without a wall all rows are centred)
+  if (i >= 0 && i <= e.im + 1 && j >= 1 && j <= e.jm) {
 #pragma unroll
     for (int a = 0; a < 4; ++a)
       qr.st(V_C + a, q, 26.0 * pr.ld(fl[a], q) - (pr.ld(fl[a], q + di) + pr.ld(fl[a], q - di)));
   }
-  if (i >= 1 && i <= e.im && j >= 2 && j <= e.jm + 1) {
+  if (i >= 1 && i <= e.im && j >= 0 && j <= e.jm + 1) {
 #pragma unroll
     for (int a = 0; a < 4; ++a)
       qr.st(V_D + a, q, 26.0 * pr.ld(fl[a], q) - (pr.ld(fl[a], q + dj) + pr.ld(fl[a], q - dj)));
@@ -76,13 +77,13 @@ BCG_HD void qrows_cell(const Ext& e, const Scratch<S>& pr, const Scratch<S>& qr,
 }
 
 // pass 1c: the 4-point combinations 7 (b + c) - (a + d) of the interpolation
-// rows, at i in [1, im+1], j in [3, jm+1]:
+// rows, at i in [1, im+1], j in [1, jm+1]:
 //   EI(i,j) from QI(i, j-2..j+1)  (vE / vO of the i-faces (i,j) / (i,j-1))
 //   NJ(i,j) from QJ(i-2..i+1, j)  (vS / vN of the j-faces (i,j) / (i-1,j))
 template <class S>
 BCG_HD void vpts_cell(const Ext& e, const Scratch<S>& qr, size_t q) {
   const int i = (int)(q % e.ni) + 1 - e.gh, j = (int)(q / e.ni) + 1 - e.gh;
-  if (i < 1 || i > e.im + 1 || j < 3 || j > e.jm + 1) return;
+  if (i < 1 || i > e.im + 1 || j < 1 || j > e.jm + 1) return;
   const int di = 1, dj = e.ni;
 #pragma unroll
   for (int a = 0; a < 4; ++a) {
@@ -148,6 +149,7 @@ struct FaceCtx {
     if (i == 0) return 2.0 * gr.ld(f, e.cidx(1, j)) - gr.ld(f, e.cidx(2, j));
     if (i == e.im + 1) return 2.0 * gr.ld(f, e.cidx(e.im, j)) - gr.ld(f, e.cidx(e.im - 1, j));
     if (j == e.jm + 1) return 2.0 * gr.ld(f, e.cidx(i, e.jm)) - gr.ld(f, e.cidx(i, e.jm - 1));
+    if (j == 0) return 2.0 * gr.ld(f, e.cidx(i, 1)) - gr.ld(f, e.cidx(i, 2));  // no-wall j-faces at j = 1
     return gr.ld(f, e.cidx(i, j));
   }
   BCG_HD static S q4(const S& a, const S& b, const S& cc, const S& d) { return -a + 9.0 * b + 9.0 * cc - d; }
@@ -320,7 +322,7 @@ struct FaceCtx {
       pred[v5 - 1] = -(c.d3 * W(i - 3, j, v5)) + c.d2 * W(i - 2, j, v5) - c.d1 * W(i - 1, j, v5) +
                      c.d1 * W(i, j, v5) - c.d2 * W(i + 1, j, v5) + c.d3 * W(i + 2, j, v5);
     }
-    visc_i(i, j, j <= 2, fv, gv);
+    visc_i(i, j, c.wall && j <= 2, fv, gv);
     dissipation(i - 1, j, i, j, i - 2, j, i + 1, j, fnx, fny, pred, diss);
     assemble(fnx, fny, fx, diss, fv, gv, h);
   }
@@ -332,7 +334,7 @@ struct FaceCtx {
     const double a1 = c.c1 * fnx, a2 = c.c2 * fnx, a3 = c.c3 * fnx, b1 = c.c1 * fny, b2 = c.c2 * fny, b3 = c.c3 * fny;
 #pragma unroll
     for (int v5 = 1; v5 <= 5; ++v5) {
-      if (j >= 4) {
+      if (j >= 4 || !c.wall) {
         fx[v5 - 1] = a1 * (Fl(v5, i, j) + Fl(v5, i, j - 1)) + a2 * (Fl(v5, i, j + 1) + Fl(v5, i, j - 2)) +
                      a3 * (Fl(v5, i, j + 2) + Fl(v5, i, j - 3)) + b1 * (Gl(v5, i, j) + Gl(v5, i, j - 1)) +
                      b2 * (Gl(v5, i, j + 1) + Gl(v5, i, j - 2)) + b3 * (Gl(v5, i, j + 2) + Gl(v5, i, j - 3));
@@ -346,7 +348,7 @@ struct FaceCtx {
       pred[v5 - 1] = -(c.d3 * W(i, j - 3, v5)) + c.d2 * W(i, j - 2, v5) - c.d1 * W(i, j - 1, v5) +
                      c.d1 * W(i, j, v5) - c.d2 * W(i, j + 1, v5) + c.d3 * W(i, j + 2, v5);
     }
-    visc_j(i, j, j == 2, fv, gv);
+    visc_j(i, j, c.wall && j == 2, fv, gv);
     dissipation(i, j - 1, i, j, i, j - 2, i, j + 1, fnx, fny, pred, diss);
     assemble(fnx, fny, fx, diss, fv, gv, h);
   }
@@ -384,7 +386,7 @@ BCG_HD void face_node(const FaceCtx<S>& fc, const Scratch<S>& hn, int t) {
     for (int v5 = 0; v5 < 5; ++v5) hn.st(v5, t, h[v5]);
   }
   if (i <= e.im) {
-    if (j == 1) fc.wallface(i, h); else fc.jface(i, j, h);
+    if (j == 1 && fc.c.wall) fc.wallface(i, h); else fc.jface(i, j, h);
 #pragma unroll
     for (int v5 = 0; v5 < 5; ++v5) hn.st(5 + v5, t, h[v5]);
   }

@@ -90,7 +90,8 @@ __global__ void __launch_bounds__(256) k_balance(Ext e, Scratch<S> hn, double* _
 template <class S>
 static cudaError_t run_residual_t(const ResidualArgs& a, cudaStream_t st) {
   const Ext e = make_ext(a.im, a.jm, a.gh);
-  const Coef c = make_coef(a.phys);
+  Coef c = make_coef(a.phys);
+  c.wall = a.nowall ? 0 : 1;
   constexpr int NP = NDir<S>::value + 1;
   const size_t nn = (size_t)(a.im + 1) * (a.jm + 1);
   Scratch<S> pr{a.scratch, e.np};

@@ -20,6 +20,7 @@ struct ResidualArgs {
   double* res;           // (ni, nj, 5), interior written; may be null when ndir > 0
   double* resd;          // K stacked (ni, nj, 5), interior written
   double* scratch;       // ngroup * residual_scratch_doubles(im, jm, gh, ndir) doubles
+  int nowall;            // 1: flux_num_dnc5_nowall_2d (centred rows everywhere, no wall face)
   int ngroup;            // 0 or 1: one group; G > 1 (ndir > 0): G groups of ndir directions in one launch,
                          // group g reading wd + g*ndir*dstride and writing resd + g*ndir*dstride
 };

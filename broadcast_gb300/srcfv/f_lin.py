@@ -1,6 +1,7 @@
 """Drop-in for the reference's srcfv.f_lin (Tapenade tangent routines).
 
 flux_num_dnc5_2d_d       : tangent/flux_num_dnc5_d.f90:15
+flux_num_dnc5_nowall_2d_d: tangent/flux_num_dnc5_nowall_d.f90
 bc_wall_viscous_adia_2d_d: tangent/bc_wall_viscous_d.f90:11
 bc_no_reflexion_2d_d     : tangent/bc_no_reflexion_d.f90:16
 bc_supandsubinlet_2d_d   : tangent/bc_supandsubinlet_d.f90:11
@@ -20,6 +21,16 @@ def flux_num_dnc5_2d_d(residu, residud, w, wd, x0, y0, nx, ny, xc, yc, vol, volf
     if im is None or jm is None:
         im, jm = dims_from_cell(w, gh)
     call("bcg_flux_num_dnc5_2d_d", arr(residu, "residu", True), arr(residud, "residud", True), arr(w, "w"),
+         arr(wd, "wd"), None, None, arr(nx, "nx"), arr(ny, "ny"), None, None, arr(vol, "vol"), arr(volf, "volf"), gh,
+         cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4, int(im), int(jm))
+
+
+def flux_num_dnc5_nowall_2d_d(residu, residud, w, wd, x0, y0, nx, ny, xc, yc, vol, volf, gh, cp, cv, prandtl, gam,
+                              rgaz, cs, muref, tref, s_suth, k2, k4, im=None, jm=None):
+    gh = int(gh)
+    if im is None or jm is None:
+        im, jm = dims_from_cell(w, gh)
+    call("bcg_flux_num_dnc5_nowall_2d_d", arr(residu, "residu", True), arr(residud, "residud", True), arr(w, "w"),
          arr(wd, "wd"), None, None, arr(nx, "nx"), arr(ny, "ny"), None, None, arr(vol, "vol"), arr(volf, "volf"), gh,
          cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4, int(im), int(jm))
 

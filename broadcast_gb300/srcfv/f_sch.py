@@ -1,6 +1,7 @@
 """Drop-in for the reference's srcfv.f_sch (residual routines).
 
-flux_num_dnc5_2d: srcfv/rhs/flux_num_dnc5.F90:7-8.
+flux_num_dnc5_2d       : srcfv/rhs/flux_num_dnc5.F90:7-8.
+flux_num_dnc5_nowall_2d: srcfv/rhs/flux_num_dnc5_nowall.F90:7 (centred rows everywhere, no wall).
 """
 from .._f2py import arr, call, dims_from_cell
 
@@ -16,3 +17,15 @@ def flux_num_dnc5_2d(residu, w, x0, y0, nx, ny, xc, yc, vol, volf, gh, cp, cv, p
     w, nx, ny, vol, volf = (arr(a, n) for a, n in ((w, "w"), (nx, "nx"), (ny, "ny"), (vol, "vol"), (volf, "volf")))
     call("bcg_flux_num_dnc5_2d", residu, w, None, None, nx, ny, None, None, vol, volf, gh, cp, cv, prandtl, gam, rgaz,
          cs, muref, tref, s_suth, k2, k4, int(im), int(jm))
+
+
+def flux_num_dnc5_nowall_2d(residu, w, x0, y0, nx, ny, xc, yc, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref,
+                            tref, s_suth, k2, k4, im=None, jm=None):
+    """The same residual without the wall rows: every row uses the centred fluxes."""
+    gh = int(gh)
+    if im is None or jm is None:
+        im, jm = dims_from_cell(w, gh)
+    residu = arr(residu, "residu", inout=True)
+    w, nx, ny, vol, volf = (arr(a, n) for a, n in ((w, "w"), (nx, "nx"), (ny, "ny"), (vol, "vol"), (volf, "volf")))
+    call("bcg_flux_num_dnc5_nowall_2d", residu, w, None, None, nx, ny, None, None, vol, volf, gh, cp, cv, prandtl,
+         gam, rgaz, cs, muref, tref, s_suth, k2, k4, int(im), int(jm))

@@ -68,6 +68,21 @@ int bcg_flux_num_dnc5_2d_dn(double* residu, double* residud, const double* w, co
                             double prandtl, double gam, double rgaz, double cs, double muref, double tref,
                             double s_suth, double k2, double k4, int im, int jm);
 
+/* srcfv/rhs/flux_num_dnc5_nowall.F90:7 flux_num_dnc5_nowall_2d and its tangent
+ * srcfv/tangent/flux_num_dnc5_nowall_d.f90 flux_num_dnc5_nowall_2d_d: the same
+ * scheme with the centred fluxes on every row j = 1..jm+1 (no near-wall rows,
+ * no wall face); same arguments as flux_num_dnc5_2d / _d. */
+int bcg_flux_num_dnc5_nowall_2d(double* residu, const double* w, const double* x0, const double* y0,
+                                const double* nx, const double* ny, const double* xc, const double* yc,
+                                const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
+                                double gam, double rgaz, double cs, double muref, double tref, double s_suth,
+                                double k2, double k4, int im, int jm);
+int bcg_flux_num_dnc5_nowall_2d_d(double* residu, double* residud, const double* w, const double* wd,
+                                  const double* x0, const double* y0, const double* nx, const double* ny,
+                                  const double* xc, const double* yc, const double* vol, const double* volf, int gh,
+                                  double cp, double cv, double prandtl, double gam, double rgaz, double cs,
+                                  double muref, double tref, double s_suth, double k2, double k4, int im, int jm);
+
 /* srcfv/adjoint/flux_num_dnc5_b.f90:15 (FLUX_NUM_DNC5_2D_B): wb = (dR/dw)^T residub
  * on every padded cell (wb overwritten); the interior of residub is zeroed on
  * return, as in the reference; residu is unused. */

@@ -462,15 +462,19 @@ struct Dnc5 {
     hn(i, j, 5, 2) = T(ZERO);
   }
 
-  void run(T* residu_) {
+  // wall = false: flux_num_dnc5_nowall_2d (rhs/flux_num_dnc5_nowall.F90:140), the
+  // centred fluxes on every row j = 1..jm+1, no near-wall rows, no wall face
+  void run(T* residu_, bool wall = true) {
     primitives();
     gradients();
 #pragma omp parallel for schedule(static)
-    for (int j = 4; j <= jm + 1; ++j)
+    for (int j = wall ? 4 : 1; j <= jm + 1; ++j)
       for (int i = 1; i <= im + 1; ++i) { iface(i, j, false); jface(i, j, 0, false); }
-    for (int i = 1; i <= im + 1; ++i) { iface(i, 3, false); jface(i, 3, 5, false); }
-    for (int i = 1; i <= im + 1; ++i) { iface(i, 2, true); jface(i, 2, 3, true); }
-    for (int i = 1; i <= im + 1; ++i) { iface(i, 1, true); wallface(i, 1); }
+    if (wall) {
+      for (int i = 1; i <= im + 1; ++i) { iface(i, 3, false); jface(i, 3, 5, false); }
+      for (int i = 1; i <= im + 1; ++i) { iface(i, 2, true); jface(i, 2, 3, true); }
+      for (int i = 1; i <= im + 1; ++i) { iface(i, 1, true); wallface(i, 1); }
+    }
     FArr<T> res(residu_, im + 2 * gh, jm + 2 * gh, 1 - gh);
 #pragma omp parallel for schedule(static)
     for (int j = 1; j <= jm; ++j)
@@ -482,9 +486,9 @@ struct Dnc5 {
 
 template <class T>
 void flux_num_dnc5_2d(T* residu, const T* w, const double* nx, const double* ny, const double* vol,
-                      const double* volf, int gh, const Consts& c, int im, int jm) {
+                      const double* volf, int gh, const Consts& c, int im, int jm, bool wall = true) {
   Dnc5<T> s(w, nx, ny, vol, volf, gh, c, im, jm);
-  s.run(residu);
+  s.run(residu, wall);
 }
 
 // ===========================================================================

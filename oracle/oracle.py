@@ -23,6 +23,8 @@ SIGS = {
     "orc_flux_num_dnc5_2d": [_P] * 6 + [_I] + _PHYS + [_I, _I],
     "orc_flux_num_dnc5_2d_d": [_P] * 4 + [_I] + [_P] * 4 + [_I] + _PHYS + [_I, _I],
     "orc_flux_num_dnc5_2d_b": [_P] * 3 + [_P] * 4 + [_I] + _PHYS + [_I, _I],
+    "orc_flux_num_dnc5_nowall_2d": [_P] * 6 + [_I] + _PHYS + [_I, _I],
+    "orc_flux_num_dnc5_nowall_2d_d": [_P] * 4 + [_I] + [_P] * 4 + [_I] + _PHYS + [_I, _I],
     "orc_flux_num_dnc5_2d_opcount": [_P] * 6 + [_I] + _PHYS + [_I, _I],
     "orc_bc_wall_viscous_adia_2d": [_P, _S, _D, _P, _I, _I, _I],
     "orc_bc_wall_viscous_adia_2d_d": [_P, _P, _S, _D, _P, _I, _I, _I],
@@ -93,14 +95,16 @@ def _chk(a):
 
 
 # ---- residual -----------------------------------------------------------------
-def residual(grid, ph, w):
+def residual(grid, ph, w, nowall=False):
+    """flux_num_dnc5_2d, or flux_num_dnc5_nowall_2d with nowall=True."""
     res = np.zeros_like(w, order="F")
-    lib().orc_flux_num_dnc5_2d(_p(res), _p(_chk(w)), _p(grid["nx"]), _p(grid["ny"]), _p(grid["vol"]),
-                               _p(grid["volf"]), grid["gh"], *_phys(ph), grid["im"], grid["jm"])
+    fn = lib().orc_flux_num_dnc5_nowall_2d if nowall else lib().orc_flux_num_dnc5_2d
+    fn(_p(res), _p(_chk(w)), _p(grid["nx"]), _p(grid["ny"]), _p(grid["vol"]), _p(grid["volf"]), grid["gh"],
+       *_phys(ph), grid["im"], grid["jm"])
     return res
 
 
-def jvp(grid, ph, w, wd):
+def jvp(grid, ph, w, wd, nowall=False):
     """wd: one padded state or a stack (nd, ...) of them; returns (res, resd)."""
     wd = np.asarray(wd)
     single = wd.ndim == 3
@@ -110,8 +114,9 @@ def jvp(grid, ph, w, wd):
     buf = np.concatenate([np.ravel(x, order="F") for x in flat])
     out = np.zeros_like(buf)
     res = np.zeros_like(w, order="F")
-    lib().orc_flux_num_dnc5_2d_d(_p(res), _p(out), _p(_chk(w)), _p(buf), nd, _p(grid["nx"]), _p(grid["ny"]),
-                                 _p(grid["vol"]), _p(grid["volf"]), grid["gh"], *_phys(ph), grid["im"], grid["jm"])
+    fn = lib().orc_flux_num_dnc5_nowall_2d_d if nowall else lib().orc_flux_num_dnc5_2d_d
+    fn(_p(res), _p(out), _p(_chk(w)), _p(buf), nd, _p(grid["nx"]), _p(grid["ny"]), _p(grid["vol"]),
+       _p(grid["volf"]), grid["gh"], *_phys(ph), grid["im"], grid["jm"])
     n = w.size
     resd = [np.reshape(out[k * n:(k + 1) * n], w.shape, order="F") for k in range(nd)]
     return res, (resd[0] if single else np.stack(resd))

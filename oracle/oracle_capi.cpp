@@ -24,14 +24,14 @@ inline size_t np_(int im, int jm, int gh) { return (size_t)(im + 2 * gh) * (jm +
 
 template <int K>
 void jvp_k(double* res, double* resd, const double* w, const double* wd, int nd, const double* nx, const double* ny,
-           const double* vol, const double* volf, int gh, const Consts& c, int im, int jm) {
+           const double* vol, const double* volf, int gh, const Consts& c, int im, int jm, bool wall = true) {
   const size_t n = np_(im, jm, gh) * 5;
   std::vector<Dual<K>> wdual(n), rdual(n);
   for (size_t q = 0; q < n; ++q) {
     wdual[q].v = w[q];
     for (int k = 0; k < K; ++k) wdual[q].d[k] = wd[(size_t)k * n + q];
   }
-  flux_num_dnc5_2d<Dual<K>>(rdual.data(), wdual.data(), nx, ny, vol, volf, gh, c, im, jm);
+  flux_num_dnc5_2d<Dual<K>>(rdual.data(), wdual.data(), nx, ny, vol, volf, gh, c, im, jm, wall);
   FArr<Dual<K>> r(rdual.data(), im + 2 * gh, jm + 2 * gh, 1 - gh);
   FArr<double> rv(res, im + 2 * gh, jm + 2 * gh, 1 - gh);
   for (int e = 1; e <= 5; ++e)
@@ -78,6 +78,29 @@ int orc_flux_num_dnc5_2d_d(double* residu, double* residud, const double* w, con
     else if (kk <= 2) jvp_k<2>(r0, residud + k0 * n, w, wd + k0 * n, kk, nx, ny, vol, volf, gh, c, im, jm);
     else if (kk <= 4) jvp_k<4>(r0, residud + k0 * n, w, wd + k0 * n, kk, nx, ny, vol, volf, gh, c, im, jm);
     else jvp_k<8>(r0, residud + k0 * n, w, wd + k0 * n, kk, nx, ny, vol, volf, gh, c, im, jm);
+  }
+  return 0;
+}
+
+// ---- residual and JVP without the wall rows (flux_num_dnc5_nowall_2d) ----------
+int orc_flux_num_dnc5_nowall_2d(double* residu, const double* w, const double* nx, const double* ny,
+                                const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
+                                double gam, double rgaz, double cs, double muref, double tref, double s_suth,
+                                double k2, double k4, int im, int jm) {
+  flux_num_dnc5_2d<double>(residu, w, nx, ny, vol, volf, gh, mk(cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4),
+                           im, jm, false);
+  return 0;
+}
+int orc_flux_num_dnc5_nowall_2d_d(double* residu, double* residud, const double* w, const double* wd, int nd,
+                                  const double* nx, const double* ny, const double* vol, const double* volf, int gh,
+                                  double cp, double cv, double prandtl, double gam, double rgaz, double cs,
+                                  double muref, double tref, double s_suth, double k2, double k4, int im, int jm) {
+  const Consts c = mk(cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4);
+  const size_t n = np_(im, jm, gh) * 5;
+  for (int k0 = 0; k0 < nd; k0 += 4) {
+    const int kk = std::min(4, nd - k0);
+    jvp_k<4>(k0 == 0 ? residu : nullptr, residud + k0 * n, w, wd + k0 * n, kk, nx, ny, vol, volf, gh, c, im, jm,
+             false);
   }
   return 0;
 }

@@ -19,6 +19,8 @@ DEFAULT_REF = "/root/reference"
 # (file relative to the reference root, routines taken from it)
 ROUTINES = [
     ("srcfv/prepro/flux_num_dnc5.f90", ["flux_num_dnc5_2d"]),
+    ("srcfv/prepro/flux_num_dnc5_nowall.f90", ["flux_num_dnc5_nowall_2d"]),
+    ("srcfv/tangent/flux_num_dnc5_nowall_d.f90", ["flux_num_dnc5_nowall_2d_d"]),
     ("srcfv/tangent/flux_num_dnc5_d.f90", ["flux_num_dnc5_2d_d"]),
     ("srcfv/adjoint/flux_num_dnc5_b.f90", ["flux_num_dnc5_2d_b"]),
     ("srcfv/prepro/bc_wall_viscous.f90", ["bc_wall_viscous_adia_2d"]),

@@ -112,6 +112,12 @@ def make(kind, im, jm, seed):
         resds.append(rd)
     out["wd"] = np.stack(wds)
     out["resd"] = np.stack(resds)
+    # the scheme without the wall rows (flux_num_dnc5_nowall_2d and its tangent) on the same state
+    res_nw = np.zeros_like(w)
+    ref.call("flux_num_dnc5_nowall_2d", res_nw, w, *residual_args(c))
+    r_nw, rd_nw = np.zeros_like(w), np.zeros_like(w)
+    ref.call("flux_num_dnc5_nowall_2d_d", r_nw, rd_nw, w, wds[0], *residual_args(c))
+    out["res_nowall"], out["resd_nowall"] = res_nw, rd_nw
     # spanwise operators applied to the first direction (coeffs_5p_dz, coeffs_5p_dz2)
     span_args = residual_args(c)[:9] + tuple(ph[k] for k in PHYS[:9]) + (im, jm)
     for name, key in (("coeffs_5p_dz", "dz"), ("coeffs_5p_dz2", "dzz")):

@@ -43,6 +43,18 @@ def test_residual(name):
 
 
 @pytest.mark.parametrize("name", G.CASES)
+def test_nowall_residual_and_tangent(name):
+    """flux_num_dnc5_nowall_2d and its Tapenade tangent."""
+    d = G.load(name)
+    c = G.as_case(d)
+    r = O.residual(c["grid"], c["phys"], c["w"], nowall=True)
+    assert H.rel_err(r, d["res_nowall"], H.flux_scale(c, c["w"])) < TOL_RES
+    _, rd = O.jvp(c["grid"], c["phys"], c["w"], d["wd"][0], nowall=True)
+    sc = np.abs(H.interior(d["resd_nowall"])).reshape(-1, 5).max(0)
+    assert H.rel_err(rd, d["resd_nowall"], sc) < TOL_DERIV
+
+
+@pytest.mark.parametrize("name", G.CASES)
 def test_tangent(name):
     d = G.load(name)
     c = G.as_case(d)

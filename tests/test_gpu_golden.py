@@ -36,6 +36,20 @@ def test_residual(name):
 
 
 @pytest.mark.parametrize("name", G.CASES)
+def test_nowall_residual_and_tangent(name):
+    from broadcast_gb300.srcfv import f_lin, f_sch
+    d = G.load(name)
+    c = G.as_case(d)
+    res = np.zeros_like(c["w"])
+    f_sch.flux_num_dnc5_nowall_2d(res, c["w"], *_args(c))
+    assert H.rel_err(res, d["res_nowall"], H.flux_scale(c, c["w"])) < 1e-12
+    r, rd = np.zeros_like(c["w"]), np.zeros_like(c["w"])
+    f_lin.flux_num_dnc5_nowall_2d_d(r, rd, c["w"], np.asfortranarray(d["wd"][0]), *_args(c))
+    sc = np.abs(H.interior(d["resd_nowall"])).reshape(-1, 5).max(0)
+    assert H.rel_err(rd, d["resd_nowall"], sc) < 1e-11
+
+
+@pytest.mark.parametrize("name", G.CASES)
 def test_tangent(name):
     from broadcast_gb300.srcfv import f_lin
     d = G.load(name)

@@ -171,3 +171,24 @@ def test_testvector_bit_exact():
         wd[:] = 9.0
         f_misc.testvector_partial(wd, m, l, k, gh, im, jm, 2, 15, 0, 16)
         assert np.array_equal(wd, O.testvector_partial(m, l, k, gh, im, jm, 2, 15, 0, 16))
+
+
+@pytest.mark.parametrize("kind,im,jm", [("bl", 40, 30), ("cyl", 64, 48)])
+def test_nowall_matches_oracle(kind, im, jm):
+    """flux_num_dnc5_nowall_2d (+ tangent): centred rows everywhere."""
+    from broadcast_gb300.srcfv import f_lin, f_sch
+    c = H.bl_case(im, jm) if kind == "bl" else H.cyl_case(im, jm)
+    H.oracle_bcs(c, c["w"])
+    g, ph = c["grid"], c["phys"]
+    args = (g["x0"], g["y0"], g["nx"], g["ny"], g["xc"], g["yc"], g["vol"], g["volf"], g["gh"]) + tuple(
+        ph[k] for k in ("cp", "cv", "prandtl", "gam", "rgaz", "cs", "muref", "tref", "s_suth", "k2", "k4"))
+    res = np.zeros_like(c["w"])
+    f_sch.flux_num_dnc5_nowall_2d(res, c["w"], *args)
+    assert H.rel_err(res, O.residual(g, ph, c["w"], nowall=True), H.flux_scale(c, c["w"])) < 1e-12
+    rng = np.random.default_rng(7)
+    wd = np.asfortranarray(rng.standard_normal(c["w"].shape))
+    r, rd = np.zeros_like(res), np.zeros_like(res)
+    f_lin.flux_num_dnc5_nowall_2d_d(r, rd, c["w"], wd, *args)
+    _, ref = O.jvp(g, ph, c["w"], wd, nowall=True)
+    sc = np.abs(H.interior(ref)).reshape(-1, 5).max(0)
+    assert H.rel_err(rd, ref, sc) < 1e-11
