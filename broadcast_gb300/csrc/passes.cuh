@@ -265,16 +265,23 @@ struct FaceCtx {
                           const S pred[5], S diss[5]) const {
     // Roe average: rr = sqrt(rhoL)/(sqrt(rhoL)+sqrt(rhoR)), so
     // u = (sL uL + sR uR)/(sL + sR), and likewise v and c^2
-    const S c2r = c.c2fac * P(F_T, iR, jR), c2l = c.c2fac * P(F_T, iL, jL);
     const S inv = 1.0 / (P(F_SR, iL, jL) + P(F_SR, iR, jR));
     const S u = (P(F_SU, iL, jL) + P(F_SU, iR, jR)) * inv, v = (P(F_SV, iL, jL) + P(F_SV, iR, jR)) * inv;
     const S c2x = (P(F_SC, iL, jL) + P(F_SC, iR, jR)) * inv;
     const double nx2 = fnx * fnx + fny * fny;
     const S rspec = fabs_t(fnx * u + fny * v) + sqrt_t(c2x * nx2);
-    S eps2 = Planes<S>::c(0.0), eps4 = Planes<S>::c(0.0 < c.k4 ? c.k4 : 0.0);
-    if (c.k2 != 0.0) {
-      // with k2 = 0 the sensor is multiplied by zero: skipped (the reference
-      // value 0*coef is exactly 0 for the finite coef of a physical state)
+    if (c.k2 == 0.0) {
+      // with k2 = 0 the sensor is multiplied by zero (0 * coef = 0 for the
+      // finite coef of a physical state, and so is its tangent): eps2 = 0,
+      // eps4 = max(0, k4), diss = (rspec eps4) pred
+      const S r4 = rspec * (0.0 < c.k4 ? c.k4 : 0.0);
+#pragma unroll
+      for (int v5 = 0; v5 < 5; ++v5) diss[v5] = r4 * pred[v5];
+      return;
+    }
+    S eps2, eps4;
+    {
+      const S c2r = c.c2fac * P(F_T, iR, jR), c2l = c.c2fac * P(F_T, iL, jL);
       const S pL = P(F_P, iL, jL), pR = P(F_P, iR, jR), pLL = P(F_P, iLL, jLL), pRR = P(F_P, iRR, jRR);
       const S ks1 = fabs_t(pL - 2.0 * pR + pRR) / fabs_t(pL + 2.0 * pR + pRR);
       const S ks2 = fabs_t(pLL - 2.0 * pL + pR) / fabs_t(pLL + 2.0 * pL + pR);
@@ -294,11 +301,10 @@ struct FaceCtx {
       eps2 = c.k2 * coef;
       eps4 = fmax_t(Planes<S>::c(0.0), c.k4 - eps2 * 12.0);
     }
+    // rspec (eps2 (wR - wL) / 2 + eps4 pred) with the face factors formed once
+    const S re2 = (0.5 * rspec) * eps2, re4 = rspec * eps4;
 #pragma unroll
-    for (int v5 = 1; v5 <= 5; ++v5) {
-      const S diff = 0.5 * (W(iR, jR, v5) - W(iL, jL, v5));
-      diss[v5 - 1] = rspec * (eps2 * diff + eps4 * pred[v5 - 1]);
-    }
+    for (int v5 = 1; v5 <= 5; ++v5) diss[v5 - 1] = re2 * (W(iR, jR, v5) - W(iL, jL, v5)) + re4 * pred[v5 - 1];
   }
 
   // flux assembly (rhs/fluxnumassembly_i.F): (fv nx/|n| + gv ny/|n|) |n| = fv nx + gv ny
