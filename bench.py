@@ -364,7 +364,12 @@ def run_ours(args):
                                    "%d directions; each launch covers the %d groups" % (GROUP, NDIR // GROUP),
                          "fp64": {"achieved": ach_tf, "peak": peak_fp64, "unit": "TFLOP/s",
                                   "frac": ach_tf / peak_fp64, "flops_per_group": flops_group,
-                                  "peak_source": "bcg_fp64_peak_tflops (FMA chains, measured in this run)"}},
+                                  "peak_source": "bcg_fp64_peak_tflops (FMA chains, measured in this run)",
+                                  "note": "flops of the reference's algorithm (the oracle's operation tally); the "
+                                          "kernels execute fewer FP64 operations than that algorithm (shared "
+                                          "point values, folded constants, Roe average from sqrt(rho) products), "
+                                          "so the fraction can exceed 1; the FP64-pipe busy share measured by ncu "
+                                          "is in profiles/dnc5_jvp_cylinder256.md"}},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": launches_per_step * args.steps,

@@ -154,18 +154,45 @@ struct FaceCtx {
   }
   BCG_HD static S q4(const S& a, const S& b, const S& cc, const S& d) { return -a + 9.0 * b + 9.0 * cc - d; }
 
-  BCG_HD void visc_fluxes(const S& mmu, const S& lambda, const S& uu, const S& vv, const S& ww, const S& ux,
-                          const S& uy, const S& vx, const S& vy, const S& wx, const S& wy, const S& tx, const S& ty,
-                          S fv[4], S gv[4]) const {
-    const double TWOTHIRD = 2.0 / 3.0;
-    fv[0] = TWOTHIRD * mmu * (2.0 * ux - vy);
-    fv[1] = mmu * (uy + vx);
-    fv[2] = mmu * (wx);
-    fv[3] = (lambda * tx + uu * fv[0] + vv * fv[1] + ww * fv[2]);
-    gv[0] = mmu * (uy + vx);
-    gv[1] = TWOTHIRD * mmu * (-ux + 2.0 * vy);
-    gv[2] = mmu * (wy);
-    gv[3] = lambda * ty + uu * gv[0] + vv * gv[1] + ww * gv[2];
+  // Normal viscous flux fv * snx + gv * sny (the only combination the face
+  // assembly uses, rhs/fluxnumassembly_i.F) from the point values v[a][p] of
+  // u v w T (a) at the points N, S, O, E (p) whose gradient coefficients are
+  // ax[p], ay[p] (ux = sum_p ax[p] u_p, uy = sum_p ay[p] u_p).  With the
+  // viscous fluxes of rhs/flux_visqueux_o4_i.F
+  //   fv = (2/3 mu (2ux - vy), mu (uy + vx), mu wx, lambda tx + uu fv0 + vv fv1 + ww fv2)
+  //   gv = (mu (uy + vx), 2/3 mu (2vy - ux), mu wy, lambda ty + uu gv0 + vv gv1 + ww gv2)
+  // the projections are linear in the point values with per-face scalar
+  // weights, formed once per face:
+  //   fn0 = mu sum_p [(4/3 ax snx + ay sny) u_p + (ax sny - 2/3 ay snx) v_p]
+  //   fn1 = mu sum_p [(ay snx - 2/3 ax sny) u_p + (ax snx + 4/3 ay sny) v_p]
+  //   fn2 = mu sum_p (ax snx + ay sny) w_p,  fn3 = lambda sum_p (ax snx + ay sny) T_p + uu fn0 + vv fn1 + ww fn2
+  template <class PV>
+  BCG_HD void visc_normal(const PV& val, const double ax[4], const double ay[4], double snx, double sny,
+                          const S& mmu, const S& uu, const S& vv, const S& ww, S fn[4]) const {
+    const double T3 = 1.0 / 3.0, TWOTHIRD = 2.0 / 3.0;
+    S an, bn, wn, tn;
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      const double xs = ax[p] * snx, ys = ay[p] * sny, xn = ax[p] * sny, yn = ay[p] * snx;
+      const double e = xs + ys, c00 = e + T3 * xs, c11 = e + T3 * ys;
+      const double c01 = xn - TWOTHIRD * yn, c10 = yn - TWOTHIRD * xn;
+      const S u = val(0, p), v = val(1, p);
+      if (p == 0) {
+        an = c00 * u + c01 * v;
+        bn = c10 * u + c11 * v;
+        wn = e * val(2, p);
+        tn = e * val(3, p);
+      } else {
+        an = an + c00 * u + c01 * v;
+        bn = bn + c10 * u + c11 * v;
+        wn = wn + e * val(2, p);
+        tn = tn + e * val(3, p);
+      }
+    }
+    fn[0] = mmu * an;
+    fn[1] = mmu * bn;
+    fn[2] = mmu * wn;
+    fn[3] = (mmu * c.cpprandtl) * tn + uu * fn[0] + vv * fn[1] + ww * fn[2];
   }
 
   // Viscous flux through i-face (i,j): o4 (rhs/flux_visqueux_o4_i.F) or o2
@@ -173,33 +200,28 @@ struct FaceCtx {
   // O; the point stencils' constant factors (1/24, ccross, 1/4) and the face
   // volume are folded into the geometric coefficients, and the cross rows come
   // from the QI interpolations.
-  BCG_HD void visc_i(int i, int j, bool o2, S fv[4], S gv[4]) const {
+  BCG_HD void visc_i(int i, int j, bool o2, double snx, double sny, S fn[4]) const {
     const double volm1 = VOLF(i, j, 1);
     const double fN = o2 ? volm1 : volm1 / 24.0, fE = o2 ? 0.25 * volm1 : c.ccross * volm1;
-    const double nxN = 0.5 * (NX(i + 1, j, 1) + NX(i, j, 1)) * fN, nxS = -(0.5 * (NX(i - 1, j, 1) + NX(i, j, 1))) * fN;
-    const double nxO = 0.5 * (NX(i - 1, j + 1, 2) + NX(i, j + 1, 2)) * fE, nxE = -(0.5 * (NX(i - 1, j, 2) + NX(i, j, 2))) * fE;
-    const double nyN = 0.5 * (NY(i + 1, j, 1) + NY(i, j, 1)) * fN, nyS = -(0.5 * (NY(i - 1, j, 1) + NY(i, j, 1))) * fN;
-    const double nyO = 0.5 * (NY(i - 1, j + 1, 2) + NY(i, j + 1, 2)) * fE, nyE = -(0.5 * (NY(i - 1, j, 2) + NY(i, j, 2))) * fE;
-    S gx[4], gy[4];
-    const int fl[4] = {F_U, F_V, F_W, F_T};
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-      const int f = fl[a];
-      S vN, vS, vE, vO;
+    // points N, S, O, E
+    const double ax[4] = {0.5 * (NX(i + 1, j, 1) + NX(i, j, 1)) * fN, -(0.5 * (NX(i - 1, j, 1) + NX(i, j, 1))) * fN,
+                          0.5 * (NX(i - 1, j + 1, 2) + NX(i, j + 1, 2)) * fE, -(0.5 * (NX(i - 1, j, 2) + NX(i, j, 2))) * fE};
+    const double ay[4] = {0.5 * (NY(i + 1, j, 1) + NY(i, j, 1)) * fN, -(0.5 * (NY(i - 1, j, 1) + NY(i, j, 1))) * fN,
+                          0.5 * (NY(i - 1, j + 1, 2) + NY(i, j + 1, 2)) * fE, -(0.5 * (NY(i - 1, j, 2) + NY(i, j, 2))) * fE};
+    // point value of variable a (u v w T) at point p
+    auto val = [&](int a, int p) -> S {
+      const int f = F_U + a;  // F_U, F_V, F_W, F_T are consecutive
       if (!o2) {
-        vN = Q(V_C + a, i, j);
-        vS = Q(V_C + a, i - 1, j);
-        vE = Q(V_EI + a, i, j);
-        vO = Q(V_EI + a, i, j + 1);
-      } else {
-        vN = P(f, i, j);
-        vS = P(f, i - 1, j);
-        vE = (P(f, i, j) + P(f, i, j - 1)) + (P(f, i - 1, j) + P(f, i - 1, j - 1));
-        vO = (P(f, i, j) + P(f, i, j + 1)) + (P(f, i - 1, j) + P(f, i - 1, j + 1));
+        if (p == 0) return Q(V_C + a, i, j);
+        if (p == 1) return Q(V_C + a, i - 1, j);
+        if (p == 2) return Q(V_EI + a, i, j + 1);
+        return Q(V_EI + a, i, j);
       }
-      gx[a] = vN * nxN + vS * nxS + vO * nxO + vE * nxE;
-      gy[a] = vN * nyN + vS * nyS + vO * nyO + vE * nyE;
-    }
+      if (p == 0) return P(f, i, j);
+      if (p == 1) return P(f, i - 1, j);
+      if (p == 2) return (P(f, i, j) + P(f, i, j + 1)) + (P(f, i - 1, j) + P(f, i - 1, j + 1));
+      return (P(f, i, j) + P(f, i, j - 1)) + (P(f, i - 1, j) + P(f, i - 1, j - 1));
+    };
     S uu, vv, ww, mmu;
     if (!o2) {
       uu = 0.0625 * Q(Q_I + 0, i, j);
@@ -212,37 +234,31 @@ struct FaceCtx {
       ww = 0.5 * (P(F_W, i, j) + P(F_W, i - 1, j));
       mmu = 0.5 * (P(F_MU, i, j) + P(F_MU, i - 1, j));
     }
-    visc_fluxes(mmu, mmu * c.cpprandtl, uu, vv, ww, gx[0], gy[0], gx[1], gy[1], gx[2], gy[2], gx[3], gy[3], fv, gv);
+    visc_normal(val, ax, ay, snx, sny, mmu, uu, vv, ww, fn);
   }
 
   // Viscous flux through j-face (i,j): o4 (rhs/flux_visqueux_o4_j.F) or o2 (row 2).
-  BCG_HD void visc_j(int i, int j, bool o2, S fv[4], S gv[4]) const {
+  BCG_HD void visc_j(int i, int j, bool o2, double snx, double sny, S fn[4]) const {
     const double volm1 = VOLF(i, j, 2);
     const double fN = o2 ? 0.25 * volm1 : c.ccross * volm1, fE = o2 ? volm1 : volm1 / 24.0;
-    const double nxN = 0.5 * (NX(i + 1, j - 1, 1) + NX(i + 1, j, 1)) * fN, nxS = -(0.5 * (NX(i, j - 1, 1) + NX(i, j, 1))) * fN;
-    const double nxO = 0.5 * (NX(i, j + 1, 2) + NX(i, j, 2)) * fE, nxE = -(0.5 * (NX(i, j - 1, 2) + NX(i, j, 2))) * fE;
-    const double nyN = 0.5 * (NY(i + 1, j - 1, 1) + NY(i + 1, j, 1)) * fN, nyS = -(0.5 * (NY(i, j - 1, 1) + NY(i, j, 1))) * fN;
-    const double nyO = 0.5 * (NY(i, j + 1, 2) + NY(i, j, 2)) * fE, nyE = -(0.5 * (NY(i, j - 1, 2) + NY(i, j, 2))) * fE;
-    S gx[4], gy[4];
-    const int fl[4] = {F_U, F_V, F_W, F_T};
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-      const int f = fl[a];
-      S vN, vS, vE, vO;
+    // points N, S, O, E
+    const double ax[4] = {0.5 * (NX(i + 1, j - 1, 1) + NX(i + 1, j, 1)) * fN, -(0.5 * (NX(i, j - 1, 1) + NX(i, j, 1))) * fN,
+                          0.5 * (NX(i, j + 1, 2) + NX(i, j, 2)) * fE, -(0.5 * (NX(i, j - 1, 2) + NX(i, j, 2))) * fE};
+    const double ay[4] = {0.5 * (NY(i + 1, j - 1, 1) + NY(i + 1, j, 1)) * fN, -(0.5 * (NY(i, j - 1, 1) + NY(i, j, 1))) * fN,
+                          0.5 * (NY(i, j + 1, 2) + NY(i, j, 2)) * fE, -(0.5 * (NY(i, j - 1, 2) + NY(i, j, 2))) * fE};
+    auto val = [&](int a, int p) -> S {
+      const int f = F_U + a;  // F_U, F_V, F_W, F_T are consecutive
       if (!o2) {
-        vN = Q(V_NJ + a, i + 1, j);
-        vS = Q(V_NJ + a, i, j);
-        vE = Q(V_D + a, i, j - 1);
-        vO = Q(V_D + a, i, j);
-      } else {
-        vN = (P(f, i, j) + P(f, i + 1, j)) + (P(f, i, j - 1) + P(f, i + 1, j - 1));
-        vS = (P(f, i, j) + P(f, i - 1, j)) + (P(f, i, j - 1) + P(f, i - 1, j - 1));
-        vO = P(f, i, j);
-        vE = P(f, i, j - 1);
+        if (p == 0) return Q(V_NJ + a, i + 1, j);
+        if (p == 1) return Q(V_NJ + a, i, j);
+        if (p == 2) return Q(V_D + a, i, j);
+        return Q(V_D + a, i, j - 1);
       }
-      gx[a] = vN * nxN + vS * nxS + vO * nxO + vE * nxE;
-      gy[a] = vN * nyN + vS * nyS + vO * nyO + vE * nyE;
-    }
+      if (p == 0) return (P(f, i, j) + P(f, i + 1, j)) + (P(f, i, j - 1) + P(f, i + 1, j - 1));
+      if (p == 1) return (P(f, i, j) + P(f, i - 1, j)) + (P(f, i, j - 1) + P(f, i - 1, j - 1));
+      if (p == 2) return P(f, i, j);
+      return P(f, i, j - 1);
+    };
     S uu, vv, ww, mmu;
     if (!o2) {
       uu = 0.0625 * Q(Q_J + 0, i, j);
@@ -255,7 +271,7 @@ struct FaceCtx {
       ww = 0.5 * (P(F_W, i, j) + P(F_W, i, j - 1));
       mmu = 0.5 * (P(F_MU, i, j) + P(F_MU, i, j - 1));
     }
-    visc_fluxes(mmu, mmu * c.cpprandtl, uu, vv, ww, gx[0], gy[0], gx[1], gy[1], gx[2], gy[2], gx[3], gy[3], fv, gv);
+    visc_normal(val, ax, ay, snx, sny, mmu, uu, vv, ww, fn);
   }
 
   // spectral radius, Ducros/pressure sensor and dissipation through the face
@@ -308,15 +324,15 @@ struct FaceCtx {
   }
 
   // flux assembly (rhs/fluxnumassembly_i.F): (fv nx/|n| + gv ny/|n|) |n| = fv nx + gv ny
-  BCG_HD void assemble(double snx, double sny, const S fx[5], const S diss[5], const S fv[4], const S gv[4], S h[5]) const {
+  BCG_HD void assemble(const S fx[5], const S diss[5], const S fn[4], S h[5]) const {
     h[0] = fx[0] - diss[0];
 #pragma unroll
-    for (int v5 = 2; v5 <= 5; ++v5) h[v5 - 1] = fx[v5 - 1] - diss[v5 - 1] - (fv[v5 - 2] * snx + gv[v5 - 2] * sny);
+    for (int v5 = 2; v5 <= 5; ++v5) h[v5 - 1] = fx[v5 - 1] - diss[v5 - 1] - fn[v5 - 2];
   }
 
   // i-face (i,j), between cells (i-1,j) and (i,j)
   BCG_HD void iface(int i, int j, S h[5]) const {
-    S fx[5], pred[5], diss[5], fv[4], gv[4];
+    S fx[5], pred[5], diss[5], fn[4];
     const double fnx = NX(i, j, 1), fny = NY(i, j, 1);
     // centred weights times the face normal, once per face (rhs/euler_o6_i.F)
     const double a1 = c.c1 * fnx, a2 = c.c2 * fnx, a3 = c.c3 * fnx, b1 = c.c1 * fny, b2 = c.c2 * fny, b3 = c.c3 * fny;
@@ -328,14 +344,14 @@ struct FaceCtx {
       pred[v5 - 1] = -(c.d3 * W(i - 3, j, v5)) + c.d2 * W(i - 2, j, v5) - c.d1 * W(i - 1, j, v5) +
                      c.d1 * W(i, j, v5) - c.d2 * W(i + 1, j, v5) + c.d3 * W(i + 2, j, v5);
     }
-    visc_i(i, j, c.wall && j <= 2, fv, gv);
+    visc_i(i, j, c.wall && j <= 2, fnx, fny, fn);
     dissipation(i - 1, j, i, j, i - 2, j, i + 1, j, fnx, fny, pred, diss);
-    assemble(fnx, fny, fx, diss, fv, gv, h);
+    assemble(fx, diss, fn, h);
   }
 
   // j-face (i,j), between cells (i,j-1) and (i,j); j >= 2
   BCG_HD void jface(int i, int j, S h[5]) const {
-    S fx[5], pred[5], diss[5], fv[4], gv[4];
+    S fx[5], pred[5], diss[5], fn[4];
     const double fnx = NX(i, j, 2), fny = NY(i, j, 2);
     const double a1 = c.c1 * fnx, a2 = c.c2 * fnx, a3 = c.c3 * fnx, b1 = c.c1 * fny, b2 = c.c2 * fny, b3 = c.c3 * fny;
 #pragma unroll
@@ -354,9 +370,9 @@ struct FaceCtx {
       pred[v5 - 1] = -(c.d3 * W(i, j - 3, v5)) + c.d2 * W(i, j - 2, v5) - c.d1 * W(i, j - 1, v5) +
                      c.d1 * W(i, j, v5) - c.d2 * W(i, j + 1, v5) + c.d3 * W(i, j + 2, v5);
     }
-    visc_j(i, j, c.wall && j == 2, fv, gv);
+    visc_j(i, j, c.wall && j == 2, fnx, fny, fn);
     dissipation(i, j - 1, i, j, i, j - 2, i, j + 1, fnx, fny, pred, diss);
-    assemble(fnx, fny, fx, diss, fv, gv, h);
+    assemble(fx, diss, fn, h);
   }
 
   // adiabatic no-slip wall face j = 1 (rhs/fluxwall.F)
