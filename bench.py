@@ -302,6 +302,25 @@ def run_ours(args):
     units = IM * JM * NDIR * args.steps * ws
     value = units / (tot_ms / 1e3) / 1e6
 
+    # adjoint (VJP) throughput on the same grid, device arrays, one cotangent per call
+    vjp = None
+    if rank == 0:
+        rb = torch.zeros_like(res)
+        rb[:, 3:-3, 3:-3] = 1.0
+        wb = op.new_state()
+        op.vjp(w_dev, rb, wb)
+        torch.cuda.synchronize()
+        a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        nv = 8
+        a_ev.record(stream)
+        for _ in range(nv):
+            op.vjp(w_dev, rb, wb)
+        b_ev.record(stream)
+        torch.cuda.synchronize()
+        vms = a_ev.elapsed_time(b_ev) / nv
+        vjp = {"value": IM * JM / (vms / 1e3) / 1e6, "unit": UNIT, "ms_per_vjp": vms,
+               "note": "flux_num_dnc5_2d_b (residual VJP, one cotangent) per call, device arrays, not L2-flushed"}
+
     # end to end through the C ABI with pinned host buffers
     e2e = None
     if rank == 0:
@@ -372,6 +391,7 @@ def run_ours(args):
                                           "is in profiles/dnc5_jvp_cylinder256.md"}},
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "vjp": vjp,
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clocks,
         }
