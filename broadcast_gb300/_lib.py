@@ -74,6 +74,7 @@ SIGNATURES = {
     "bcg_batch_device_bytes": "Lp",
     "bcg_batch_destroy": "L",
     "bcg_csr_spanwise_beta": "i" + "ppp" * 3 + "ip" + "ppp" + "L" + "p",
+    "bcg_jacobian_dnc5_cyl_csr": "ppppp" + "i" + "d" * 11 + "ii" + "pp" + "pi" + "ppppp" + "pdi" + "ppp" + "L" + "p",
     "bcg_jacobian_dz_bl_csr": "ppppp" + "i" + "d" * 9 + "ii" + "pppp" + "pipi" + "id" + "ppp" + "L" + "p",
 }
 _RESTYPE = {"bcg_get_stream": ctypes.c_void_p, "bcg_last_error_string": ctypes.c_char_p,

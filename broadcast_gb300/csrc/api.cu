@@ -719,6 +719,9 @@ int bcg_compute_maxnorm(double* norm, int* imax, int* jmax, const double* rhs, i
 // (BROADCAST_npz.py:1068-1137, 1206-1210; misc/PETSc_func.py:71-96)
 // ===========================================================================
 namespace {
+int jacobian_outputs(JacobianArgs& a, Stager& sg, int* indptr, int* indices, double* data, long long capacity,
+                     long long* nnz);
+
 int jacobian_bl_csr(int op, const double* w, const double* nx, const double* ny, const double* vol,
                     const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz,
                     double cs, double muref, double tref, double s_suth, double k2, double k4, int im, int jm,
@@ -730,7 +733,6 @@ int jacobian_bl_csr(int op, const double* w, const double* nx, const double* ny,
   if (!dims_ok(im, jm, gh)) return fail_arg("jacobian: need gh == 3 and im, jm >= 6");
   if (!nnz || !interf_ilo || !interf_jhi || !interf_ihi || !interf_jlo) return fail_arg("jacobian: null argument");
   const size_t np = ncell(im, jm, gh), nn = nnode(im, jm, gh);
-  const int nrow = 5 * im * jm;
   cudaStream_t st = current_stream();
   Stager sg(st);
   const int hw = sg.in(w, np * 5 * 8), hnx = sg.in(nx, nn * 2 * 8), hny = sg.in(ny, nn * 2 * 8);
@@ -760,6 +762,15 @@ int jacobian_bl_csr(int op, const double* w, const double* nx, const double* ny,
       return fail_arg("jacobian: bad interface");
     a.bcs.push_back(b);
   }
+  return jacobian_outputs(a, sg, indptr, indices, data, capacity, nnz);
+}
+
+// scratch, run and CSR outputs (host or device) of a prepared batched assembly
+int jacobian_outputs(JacobianArgs& a, Stager& sg, int* indptr, int* indices, double* data, long long capacity,
+                     long long* nnz) {
+  const int im = a.im, jm = a.jm, gh = a.gh, nrow = 5 * im * jm;
+  cudaStream_t st = current_stream();
+  int rc = 0;
   a.scratch = (double*)pool_get(POOL_SCRATCH, jacobian_scratch_doubles(im, jm, gh) * 8);
   if (!a.scratch) return fail_arg("jacobian: scratch allocation failed"), BCG_ERR_NOMEM;
   a.iscratch = (int*)pool_get(POOL_AUX, jacobian_iscratch_ints(im, jm) * 4);
@@ -803,6 +814,59 @@ extern "C" int bcg_jacobian_dnc5_bl_csr(const double* w, const double* nx, const
   return jacobian_bl_csr(0, w, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4, im,
                          jm, interf_ilo, interf_jhi, interf_ihi, interf_jlo, field, lm_field, wbd, lm_wbd, coefdiag,
                          mini, divide_by_vol, indptr, indices, data, capacity, nnz);
+}
+
+// Batched assembly for the periodic O-mesh of cylinder.py:900-980: seeds,
+// the tangent boundary chain of handleBC.applyBC (no-reflexion Jhi, wall Jlo,
+// then the two periodic joins twice), flux_num_dnc5_2d_d and
+// computejacobianfromjv[_relaxed]_withjn (columns wrap in i), CSR.
+extern "C" int bcg_jacobian_dnc5_cyl_csr(const double* w, const double* nx, const double* ny, const double* vol,
+                                         const double* volf, int gh, double cp, double cv, double prandtl,
+                                         double gam, double rgaz, double cs, double muref, double tref,
+                                         double s_suth, double k2, double k4, int im, int jm, const int* interf_jhi,
+                                         const int* interf_jlo, const double* wbd, int lm_wbd, const int* prr1,
+                                         const int* prd1, const int* prr2, const int* prd2, const int* tr,
+                                         const double* coefdiag, double mini, int divide_by_vol, int* indptr,
+                                         int* indices, double* data, long long capacity, long long* nnz) {
+  if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
+  if (!dims_ok(im, jm, gh)) return fail_arg("jacobian: need gh == 3 and im, jm >= 6");
+  if (!nnz || !interf_jhi || !interf_jlo || !prr1 || !prd1 || !prr2 || !prd2 || !tr)
+    return fail_arg("jacobian: null argument");
+  const size_t np = ncell(im, jm, gh), nn = nnode(im, jm, gh);
+  cudaStream_t st = current_stream();
+  Stager sg(st);
+  const int hw = sg.in(w, np * 5 * 8), hnx = sg.in(nx, nn * 2 * 8), hny = sg.in(ny, nn * 2 * 8);
+  const int hvol = sg.in(vol, np * 8), hvolf = sg.in(volf, np * 2 * 8);
+  const int hb = sg.in(wbd, (size_t)lm_wbd * 5 * 8);
+  const int hc = coefdiag ? sg.in(coefdiag, (size_t)im * jm * 8) : -1;
+  int rc = sg.commit();
+  if (rc) return rc;
+  JacobianArgs a{};
+  a.im = im; a.jm = jm; a.gh = gh;
+  a.phys = Phys{cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4};
+  a.w = sg.dev<double>(hw); a.nx = sg.dev<double>(hnx); a.ny = sg.dev<double>(hny);
+  a.vol = sg.dev<double>(hvol); a.volf = sg.dev<double>(hvolf);
+  a.op = 0; a.withjn = 1;
+  a.relaxed = coefdiag ? 1 : 0;
+  a.coefdiag = hc >= 0 ? sg.dev<double>(hc) : nullptr;
+  a.mini = mini; a.divide_by_vol = divide_by_vol; a.capacity = capacity; a.nnz = nnz;
+  const struct { int kind; const char* loc; const int* it; const double* aux; int lm; } chain[2] = {
+      {BC_NOREF, "Jhi", interf_jhi, sg.dev<double>(hb), lm_wbd}, {BC_WALL, "Jlo", interf_jlo, nullptr, 0}};
+  for (const auto& c : chain) {
+    BcArgs b{};
+    b.kind = c.kind; b.im = im; b.jm = jm; b.gh = gh; b.em = 5; b.lm = c.lm; b.gam = gam; b.aux = c.aux;
+    b.nx = a.nx; b.ny = a.ny;
+    if (!make_side(c.loc, c.it, &b.side) || !side_in_bounds(b.side, im, jm, gh))
+      return fail_arg("jacobian: bad interface");
+    a.bcs.push_back(b);
+  }
+  JnArgs j1{}, j2{};
+  rc = jn_args(prr1, gh, gh, gh, gh, im, jm, prd2, gh, gh, gh, gh, im, jm, tr, 5, &j1);
+  if (rc) return rc;
+  rc = jn_args(prr2, gh, gh, gh, gh, im, jm, prd1, gh, gh, gh, gh, im, jm, tr, 5, &j2);
+  if (rc) return rc;
+  for (int rep = 0; rep < 2; ++rep) { a.joins.push_back(j1); a.joins.push_back(j2); }
+  return jacobian_outputs(a, sg, indptr, indices, data, capacity, nnz);
 }
 
 extern "C" int bcg_jacobian_dz_bl_csr(const double* w, const double* nx, const double* ny, const double* vol,

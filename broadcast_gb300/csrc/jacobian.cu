@@ -49,8 +49,8 @@ __global__ void k_seed4(double* __restrict__ wd, int nseed, const int* __restric
 // op 0 stores -resd (+coefdiag on the diagonal when relaxed), the fill of
 // computejacobianfromjv(_relaxed) (ComputeJacobian.f90:292-355, 503-570);
 // op != 0 stores +dz with the row window of computejacobianfromdz (:708-779).
-__global__ void __launch_bounds__(128) k_csr_rows(int pass, int op, const double* __restrict__ resd_all, int gh, int im,
-                                                  int jm, int relaxed, const double* __restrict__ coefdiag, double mini,
+__global__ void __launch_bounds__(128) k_csr_rows(int pass, int op, int withjn, const double* __restrict__ resd_all, int gh,
+                                                  int im, int jm, int relaxed, const double* __restrict__ coefdiag, double mini,
                                                   const double* __restrict__ vol, int* __restrict__ count,
                                                   const long long* __restrict__ rowptr, int* __restrict__ indices,
                                                   double* __restrict__ data) {
@@ -70,9 +70,18 @@ __global__ void __launch_bounds__(128) k_csr_rows(int pass, int op, const double
   for (int l = 0; l < 7; ++l) {
     li[l] = l;
     int vali;
-    if (l <= gh) vali = (i <= l + 1 + gh) ? l : (i - (l + 1) + gh) / step * step + l;
-    else vali = (i <= l - gh) ? im + 1 : (i - (l + 1) + gh) / step * step + l;
-    lv[l] = vali < im ? vali : -1;
+    if (!withjn) {
+      if (l <= gh) vali = (i <= l + 1 + gh) ? l : (i - (l + 1) + gh) / step * step + l;
+      else vali = (i <= l - gh) ? im + 1 : (i - (l + 1) + gh) / step * step + l;
+      lv[l] = vali < im ? vali : -1;
+    } else {
+      // periodic in i (ComputeJacobian.f90:876-897): the seeded column left of
+      // the first ones wraps to im-1-2gh+l, the one past im back to l
+      if (l <= gh) vali = (i <= l + 1 + gh) ? l : (i - (l + 1) + gh) / step * step + l;
+      else vali = (i <= l - gh) ? im - 1 - 2 * gh + l : (i - (l + 1) + gh) / step * step + l;
+      if (vali >= im) vali = (vali - im <= gh - 1) ? l : -1;
+      lv[l] = vali;
+    }
   }
   for (int k = 0; k < 7; ++k) {
     ki[k] = k;
@@ -88,22 +97,34 @@ __global__ void __launch_bounds__(128) k_csr_rows(int pass, int op, const double
     for (int b = a; b > 0 && kv[b - 1] > kv[b]; --b) { int t = kv[b]; kv[b] = kv[b - 1]; kv[b - 1] = t; t = ki[b]; ki[b] = ki[b - 1]; ki[b - 1] = t; }
   long long out = pass ? rowptr[row] : 0;
   int n = 0;
-  for (int a = 0; a < 7; ++a) {
-    if (lv[a] < 0) continue;
-    const int l = li[a];
+  for (int a = 0; a < 7;) {
+    // run of seeds l with the same column (only with the periodic wrap when
+    // im is not a multiple of 7): their slots are duplicates, summed as the
+    // COO -> CSR conversion does, each slot filtered on its own first
+    int a2 = a + 1;
+    while (a2 < 7 && lv[a2] == lv[a]) ++a2;
+    if (lv[a] < 0) { a = a2; continue; }
     for (int b = 0; b < 7; ++b) {
       if (kv[b] < 0) continue;
       const int k = ki[b];
       for (int m = 0; m < 5; ++m) {
         const int col = m + kv[b] * 5 + lv[a] * jm * 5;
-        const int seed = k + 7 * l + 49 * m;  // the reference's slot order
-        const double r = resd_all[(size_t)seed * np * 5 + (size_t)e * np + cell];
-        double v = op ? r : ((relaxed && col == row) ? cd - r : -r);
-        if (!(fabs(v) > mini)) continue;
-        if (pass) { indices[out + n] = col; data[out + n] = v * vinv; }
+        double sum = 0.0;
+        bool kept = false;
+        for (int q = a; q < a2; ++q) {
+          const int seed = k + 7 * li[q] + 49 * m;  // the reference's slot order
+          const double r = resd_all[(size_t)seed * np * 5 + (size_t)e * np + cell];
+          const double v = op ? r : ((relaxed && col == row) ? cd - r : -r);
+          if (!(fabs(v) > mini)) continue;
+          sum += v;
+          kept = true;
+        }
+        if (!kept) continue;
+        if (pass) { indices[out + n] = col; data[out + n] = sum * vinv; }
         ++n;
       }
     }
+    a = a2;
   }
   if (!pass) count[row] = n;
 }
@@ -206,6 +227,15 @@ int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
         e = launch_bc(b, st);
         if (e != cudaSuccess) return fail_cuda("jacobian: boundary fill", e);
       }
+    // periodic joins of every seeded tangent (the primal copy is already joined)
+    for (int d = 0; d < ns && !a.joins.empty(); ++d)
+      for (const JnArgs& j0 : a.joins) {
+        JnArgs jn = j0;
+        jn.wr = wd4 + (size_t)d * np * 5;
+        jn.wd = jn.wr;
+        e = launch_jn_match(jn, st);
+        if (e != cudaSuccess) return fail_cuda("jacobian: periodic join", e);
+      }
     if (a.op == 0) {
       ra.ndir = kk; ra.ngroup = ng;
       ra.wd = wd4;
@@ -226,7 +256,7 @@ int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
   }
   // CSR: count, scan, fill
   const int B = 128;
-  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(0, a.op, resd_all, gh, im, jm, a.relaxed, a.coefdiag, a.mini,
+  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(0, a.op, a.withjn, resd_all, gh, im, jm, a.relaxed, a.coefdiag, a.mini,
                                              a.divide_by_vol ? a.vol : nullptr, count, nullptr, nullptr, nullptr);
   k_scan_block<<<nb, kScanBlock, 0, st>>>(count, rowptr, bsum, nrow);
   k_scan_sums<<<1, 1, 0, st>>>(bsum, nb, total);
@@ -239,7 +269,7 @@ int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
   if (nnz > a.capacity) return fail_arg("jacobian: CSR capacity too small (see nnz)");
   if (nnz >= (1LL << 31)) return fail_arg("jacobian: nnz exceeds 32-bit CSR indices");
   k_ptr_to_int<<<(nrow + 1 + 255) / 256, 256, 0, st>>>(rowptr, a.indptr, nrow);
-  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(1, a.op, resd_all, gh, im, jm, a.relaxed, a.coefdiag, a.mini,
+  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(1, a.op, a.withjn, resd_all, gh, im, jm, a.relaxed, a.coefdiag, a.mini,
                                              a.divide_by_vol ? a.vol : nullptr, count, rowptr, a.indices, a.data);
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail_cuda("jacobian: csr", e);

@@ -17,6 +17,8 @@ struct JacobianArgs {
   const double* vol;
   const double* volf;
   std::vector<BcArgs> bcs;  // linearised boundary chain, in the drivers' order
+  std::vector<JnArgs> joins;  // periodic joins applied to each tangent after the fills (wr = wd = the tangent)
+  int withjn;               // 1: columns wrap periodically in i (computejacobianfromjv[_relaxed]_withjn)
   int op;                   // 0: residual tangent (Jacobian); SPAN_DZ / SPAN_DZZ: spanwise operators
   int relaxed;              // 1: coefdiag added on the diagonal (computejacobianfromjv_relaxed)
   const double* coefdiag;   // (im, jm)

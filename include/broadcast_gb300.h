@@ -180,6 +180,20 @@ int bcg_jacobian_dnc5_bl_csr(const double* w, const double* nx, const double* ny
                              const double* coefdiag, double mini, int divide_by_vol, int* indptr, int* indices,
                              double* data, long long capacity, long long* nnz);
 
+/* Same for the periodic O-mesh of cylinder.py:900-980: the tangent boundary
+ * chain of handleBC.applyBC (no-reflexion Jhi, wall Jlo, the joins prr1 <- prd2
+ * and prr2 <- prd1 twice, as jn_match_2d_d), flux_num_dnc5_2d_d and
+ * computejacobianfromjv[_relaxed]_withjn, whose columns wrap periodically in
+ * i; where the wrap maps two seeds to one column (im not a multiple of 7) the
+ * slots are summed, as the COO -> CSR conversion does. */
+int bcg_jacobian_dnc5_cyl_csr(const double* w, const double* nx, const double* ny, const double* vol,
+                              const double* volf, int gh, double cp, double cv, double prandtl, double gam,
+                              double rgaz, double cs, double muref, double tref, double s_suth, double k2, double k4,
+                              int im, int jm, const int* interf_jhi, const int* interf_jlo, const double* wbd,
+                              int lm_wbd, const int* prr1, const int* prd1, const int* prr2, const int* prd2,
+                              const int* tr, const double* coefdiag, double mini, int divide_by_vol, int* indptr,
+                              int* indices, double* data, long long capacity, long long* nnz);
+
 /* Same loop for the spanwise operators (BROADCAST_npz.py:1221-1249): per seed,
  * testvector, the same linearised boundary chain, coeffs_5p_dz (which = 1) or
  * coeffs_5p_dz2 (which = 2), computejacobianfromdz (+dz, its own row window),

@@ -86,3 +86,54 @@ def test_batched_jacobian_columns_against_dense_jvp():
         _, resd = O.jvp(g, ph, c["w"], wd)
         dense = -np.transpose(H.interior(resd), (0, 1, 2)).reshape(-1)  # (i, j, e) C order = row numbering
         assert np.abs(got[:, col] - dense).max() <= 1e-11 * max(1.0, np.abs(dense).max())
+
+
+def _reference_cyl_csr(c, coefdiag, mini=2e-16):
+    g = c["grid"]
+    im, jm, gh = g["im"], g["jm"], g["gh"]
+    nb = im * jm * 49 * 25
+    jac, ia, ja = np.zeros(nb), np.zeros(nb, np.int32), np.zeros(nb, np.int32)
+    mode = O.JAC_RELAXED_WITHJN if coefdiag is not None else O.JAC_WITHJN
+    for m in range(5):
+        for l in range(7):
+            for k in range(7):
+                wd = O.testvector(m, l, k, gh, im, jm)
+                H.oracle_bcs(c, c["w"].copy(order="F"), wd)
+                _, resd = O.jvp(g, c["phys"], c["w"], wd)
+                O.computejacobian(mode, jac, ia, ja, resd, m, l, k, gh, im, jm, coefdiag)
+    keep = np.abs(jac) > mini
+    a = sp.csr_matrix((jac[keep], (ia[keep], ja[keep])), shape=(5 * im * jm, 5 * im * jm))
+    a.sum_duplicates()
+    a.sort_indices()
+    return a
+
+
+@pytest.mark.parametrize("im,relaxed", [(21, True), (20, False), (22, True)])
+def test_batched_cylinder_jacobian_matches_reference_loop(im, relaxed):
+    """Periodic O-mesh: joins in the tangent chain, columns wrapped in i
+    (computejacobianfromjv[_relaxed]_withjn), duplicates summed when im is not
+    a multiple of 7."""
+    from broadcast_gb300 import _lib
+    from broadcast_gb300._f2py import interf4
+    c = H.cyl_case(im, 10)
+    H.oracle_bcs(c, c["w"])
+    g, ph, it = c["grid"], c["phys"], c["interf"]
+    jm, gh = g["jm"], g["gh"]
+    coef = np.asfortranarray(np.random.default_rng(2).uniform(0.5, 2.0, (im, jm))) if relaxed else None
+    ref = _reference_cyl_csr(c, coef)
+    nrow = 5 * im * jm
+    cap = nrow * 245
+    indptr, indices, data = np.zeros(nrow + 1, np.int32), np.zeros(cap, np.int32), np.zeros(cap)
+    nnz = np.zeros(1, np.int64)
+    keys = ("cp", "cv", "prandtl", "gam", "rgaz", "cs", "muref", "tref", "s_suth", "k2", "k4")
+    pr = lambda a: interf4(a)
+    _lib.call("bcg_jacobian_dnc5_cyl_csr", c["w"], g["nx"], g["ny"], g["vol"], g["volf"], gh,
+              *[float(ph[k]) for k in keys], im, jm, pr(it["Jhi"]), pr(it["Jlo"]), c["wbd"], c["wbd"].shape[0],
+              pr(it["prr1"]), pr(it["prd1"]), pr(it["prr2"]), pr(it["prd2"]),
+              np.ascontiguousarray(np.asarray(it["tr"], dtype=np.int32).ravel()), coef, 2e-16, 0, indptr, indices,
+              data, cap, nnz)
+    n = int(nnz[0])
+    got = sp.csr_matrix((data[:n], indices[:n], indptr), shape=(nrow, nrow))
+    assert np.array_equal(got.indptr, ref.indptr)
+    assert np.array_equal(got.indices, ref.indices)
+    assert np.abs(got.data - ref.data).max() <= 1e-11 * np.abs(ref.data).max()
