@@ -41,8 +41,10 @@ template <int K> BCG_HD DK<K> operator-(const DK<K>& a) { DK<K> r; r.v = -a.v;
 template <int K> BCG_HD DK<K> operator*(const DK<K>& a, const DK<K>& b) { DK<K> r; r.v = a.v * b.v;
 #pragma unroll
   for (int k = 0; k < K; ++k) r.d[k] = fma(a.d[k], b.v, a.v * b.d[k]); return r; }
+// Divisions take one IEEE reciprocal, shared by the value and the tangents
+// (the value a * (1/b) is within an ulp of a / b).
 template <int K> BCG_HD DK<K> operator/(const DK<K>& a, const DK<K>& b) {
-  DK<K> r; const double inv = 1.0 / b.v; r.v = a.v / b.v;
+  DK<K> r; const double inv = 1.0 / b.v; r.v = a.v * inv;
 #pragma unroll
   for (int k = 0; k < K; ++k) r.d[k] = fma(-r.v, b.d[k], a.d[k]) * inv; return r; }
 
@@ -58,10 +60,11 @@ template <int K> BCG_HD DK<K> operator*(const DK<K>& a, double b) { DK<K> r; r.v
 template <int K> BCG_HD DK<K> operator*(double a, const DK<K>& b) { DK<K> r; r.v = a * b.v;
 #pragma unroll
   for (int k = 0; k < K; ++k) r.d[k] = a * b.d[k]; return r; }
-template <int K> BCG_HD DK<K> operator/(const DK<K>& a, double b) { DK<K> r; r.v = a.v / b; const double inv = 1.0 / b;
+template <int K> BCG_HD DK<K> operator/(const DK<K>& a, double b) { DK<K> r; const double inv = 1.0 / b; r.v = a.v * inv;
 #pragma unroll
   for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * inv; return r; }
-template <int K> BCG_HD DK<K> operator/(double a, const DK<K>& b) { DK<K> r; r.v = a / b.v; const double s = -r.v / b.v;
+template <int K> BCG_HD DK<K> operator/(double a, const DK<K>& b) {
+  DK<K> r; const double inv = 1.0 / b.v; r.v = a * inv; const double s = -r.v * inv;
 #pragma unroll
   for (int k = 0; k < K; ++k) r.d[k] = s * b.d[k]; return r; }
 
