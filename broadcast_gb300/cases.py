@@ -74,8 +74,8 @@ def geometric_nodes(n, first, ratio, start=0.0):
     return start + first * (ratio ** k - 1.0) / (ratio - 1.0)
 
 
-def bl_grid(im, jm, x_start=1.0e5, length=5.0e5, ratio=1.03, first=None, ops=None):
-    g = _alloc(im, jm)
+def bl_grid(im, jm, x_start=1.0e5, length=5.0e5, ratio=1.03, first=None, ops=None, gh=GH):
+    g = _alloc(im, jm, gh)
     gh = g["gh"]
     x = np.linspace(x_start, x_start + length, im + 1)
     if first is None:
@@ -94,11 +94,13 @@ def bl_interfaces(im, jm, gh=GH):
     return dict(Ilo=f(1, 1, 1, jm), Ihi=f(im, 1, im, jm + gh), Jlo=f(1 - gh, 1, im + gh, 1), Jhi=f(1 - gh, jm, im, jm))
 
 
-def bl_case(im=400, jm=150, mach=0.5, x_start=1.0e5, length=5.0e5, ratio=1.03, noise=1.0e-4, seed=0, ops=None):
+def bl_case(im=400, jm=150, mach=0.5, x_start=1.0e5, length=5.0e5, ratio=1.03, noise=1.0e-4, seed=0, ops=None,
+            gh=GH):
     """Boundary-layer workload: polynomial Blasius state (initialisation.f90)
-    plus seeded uniform noise on the interior conserved variables."""
+    plus seeded uniform noise on the interior conserved variables.  gh = 3 for
+    DNC5; the driver's (order+1)//2 (BROADCAST_npz.py:501-502) for the others."""
     ph = physics(mach, "bl")
-    g = bl_grid(im, jm, x_start, length, ratio, ops=ops)
+    g = bl_grid(im, jm, x_start, length, ratio, ops=ops, gh=gh)
     gh = g["gh"]
     ni, nj = im + 2 * gh, jm + 2 * gh
     w = np.zeros((ni, nj, 5), order="F")
@@ -113,8 +115,8 @@ def bl_case(im=400, jm=150, mach=0.5, x_start=1.0e5, length=5.0e5, ratio=1.03, n
     return dict(kind="bl", grid=g, phys=ph, w=w, field=field, wbd=wbd, interf=bl_interfaces(im, jm, gh))
 
 
-def cyl_grid(im, jm, r_in=0.5, r_out=50.0, ratio=1.05, ops=None):
-    g = _alloc(im, jm)
+def cyl_grid(im, jm, r_in=0.5, r_out=50.0, ratio=1.05, ops=None, gh=GH):
+    g = _alloc(im, jm, gh)
     gh = g["gh"]
     first = (r_out - r_in) * (ratio - 1.0) / (ratio ** jm - 1.0)
     r = geometric_nodes(jm, first, ratio, r_in)
@@ -148,11 +150,12 @@ def cyl_interfaces(im, jm, gh=GH):
                 prr2=f(1 - gh, jmin, 0, jmax), prd2=f(1, jmin, gh, jmax), tr=np.array([1, 2], dtype=np.int32))
 
 
-def cyl_case(im=256, jm=256, mach=0.1, reynolds=47.0, noise=1.0e-3, seed=1, r_out=50.0, ratio=1.05, ops=None):
+def cyl_case(im=256, jm=256, mach=0.1, reynolds=47.0, noise=1.0e-3, seed=1, r_out=50.0, ratio=1.05, ops=None,
+             gh=GH):
     """Cylinder workload: uniform flow plus seeded uniform noise (k2 = 0, k4 = 1
     as card_cyl2d.py:74-75)."""
     ph = physics(mach, "cyl", reynolds=reynolds, k2=0.0, k4=1.0)
-    g = cyl_grid(im, jm, r_out=r_out, ratio=ratio, ops=ops)
+    g = cyl_grid(im, jm, r_out=r_out, ratio=ratio, ops=ops, gh=gh)
     gh = g["gh"]
     ni, nj = im + 2 * gh, jm + 2 * gh
     w = np.zeros((ni, nj, 5), order="F")

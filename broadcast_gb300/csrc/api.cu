@@ -124,9 +124,16 @@ int residual_pipelined(ResidualArgs a, double* res, double* residud, const doubl
 int residual_call(double* residu, double* residud, const double* w, const double* wd, int nd, const double* nx,
                   const double* ny, const double* vol, const double* volf, int gh, double cp, double cv,
                   double prandtl, double gam, double rgaz, double cs, double muref, double tref, double s_suth,
-                  double k2, double k4, int im, int jm, int nowall = 0) {
+                  double k2, double k4, int im, int jm, int nowall = 0, int order = 5) {
   if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
-  if (!dims_ok(im, jm, gh)) return fail_arg("flux_num_dnc5_2d: need gh == 3 and im, jm >= 6");
+  if (order == 5) {
+    if (!dims_ok(im, jm, gh)) return fail_arg("flux_num_dnc5_2d: need gh == 3 and im, jm >= 6");
+  } else {
+    // DNC3/7/9: ghosts for the R-point stencils; the wall rows read the first nw cell rows
+    const int R = dnc_pairs(order), nw = order == 3 ? 2 : (order == 7 ? 9 : 11);
+    if (R == 0 || gh < R || im < std::max(6, nw) || jm < std::max(6, nw) || nd > 1)
+      return fail_arg("flux_num_dnc_2d: need order 3, 7 or 9, gh >= (order+1)/2, im, jm >= max(6, wall rows)");
+  }
   if (nd < 0) return fail_arg("flux_num_dnc5_2d_dn: negative direction count");
   const size_t np = ncell(im, jm, gh), nn = nnode(im, jm, gh);
   cudaStream_t st = current_stream();
@@ -148,6 +155,7 @@ int residual_call(double* residu, double* residud, const double* w, const double
   a.vol = sg.dev<double>(hvol); a.volf = sg.dev<double>(hvolf);
   a.dstride = np * 5;
   a.nowall = nowall;
+  a.order = order;
   double* res = hres >= 0 ? sg.dev<double>(hres) : nullptr;
   if (pipelined) {
     rc = residual_pipelined(a, res, residud, wd, nd, st);
@@ -366,6 +374,52 @@ int bcg_flux_num_dnc5_nowall_2d_d(double* residu, double* residud, const double*
   return residual_call(residu, residud, w, wd, 1, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref, tref,
                        s_suth, k2, k4, im, jm, 1);
 }
+
+// ---- the DNC schemes of order 3, 7 and 9 (srcfv/rhs/flux_num_dnc{3,7,9}.F90,
+// flux_num_dnc{3,7,9}_nowall.F90) and their tangents (srcfv/tangent/
+// flux_num_dnc{3,7,9}[_nowall]_d.f90); gh >= (order+1)/2 ------------------------
+#define BCG_DNC_ENTRIES(ORD)                                                                                         \
+  int bcg_flux_num_dnc##ORD##_2d(double* residu, const double* w, const double* x0, const double* y0,               \
+                                 const double* nx, const double* ny, const double* xc, const double* yc,             \
+                                 const double* vol, const double* volf, int gh, double cp, double cv,                \
+                                 double prandtl, double gam, double rgaz, double cs, double muref, double tref,      \
+                                 double s_suth, double k2, double k4, int im, int jm) {                              \
+    (void)x0; (void)y0; (void)xc; (void)yc;                                                                         \
+    return residual_call(residu, nullptr, w, nullptr, 0, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs,     \
+                         muref, tref, s_suth, k2, k4, im, jm, 0, ORD);                                              \
+  }                                                                                                                  \
+  int bcg_flux_num_dnc##ORD##_2d_d(double* residu, double* residud, const double* w, const double* wd,              \
+                                   const double* x0, const double* y0, const double* nx, const double* ny,           \
+                                   const double* xc, const double* yc, const double* vol, const double* volf,        \
+                                   int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs, \
+                                   double muref, double tref, double s_suth, double k2, double k4, int im, int jm) { \
+    (void)x0; (void)y0; (void)xc; (void)yc;                                                                         \
+    return residual_call(residu, residud, w, wd, 1, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref,   \
+                         tref, s_suth, k2, k4, im, jm, 0, ORD);                                                     \
+  }                                                                                                                  \
+  int bcg_flux_num_dnc##ORD##_nowall_2d(double* residu, const double* w, const double* x0, const double* y0,        \
+                                        const double* nx, const double* ny, const double* xc, const double* yc,      \
+                                        const double* vol, const double* volf, int gh, double cp, double cv,         \
+                                        double prandtl, double gam, double rgaz, double cs, double muref,            \
+                                        double tref, double s_suth, double k2, double k4, int im, int jm) {          \
+    (void)x0; (void)y0; (void)xc; (void)yc;                                                                         \
+    return residual_call(residu, nullptr, w, nullptr, 0, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs,     \
+                         muref, tref, s_suth, k2, k4, im, jm, 1, ORD);                                              \
+  }                                                                                                                  \
+  int bcg_flux_num_dnc##ORD##_nowall_2d_d(double* residu, double* residud, const double* w, const double* wd,       \
+                                          const double* x0, const double* y0, const double* nx, const double* ny,    \
+                                          const double* xc, const double* yc, const double* vol,                     \
+                                          const double* volf, int gh, double cp, double cv, double prandtl,          \
+                                          double gam, double rgaz, double cs, double muref, double tref,             \
+                                          double s_suth, double k2, double k4, int im, int jm) {                     \
+    (void)x0; (void)y0; (void)xc; (void)yc;                                                                         \
+    return residual_call(residu, residud, w, wd, 1, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref,   \
+                         tref, s_suth, k2, k4, im, jm, 1, ORD);                                                     \
+  }
+BCG_DNC_ENTRIES(3)
+BCG_DNC_ENTRIES(7)
+BCG_DNC_ENTRIES(9)
+#undef BCG_DNC_ENTRIES
 
 int bcg_flux_num_dnc5_2d_d(double* residu, double* residud, const double* w, const double* wd, const double* x0,
                            const double* y0, const double* nx, const double* ny, const double* xc, const double* yc,

@@ -95,9 +95,10 @@ BCG_HD void vpts_cell(const Ext& e, const Scratch<S>& qr, size_t q) {
 }
 
 // ---------------------------------------------------------------------------
-// pass 2: 4th-order cell gradients of u and v on interior cell t (row-major
-// over the im x jm interior) (rhs/gradop_5pi.F, gradop_5pj.F, gradient.F)
-template <class S>
+// pass 2: cell gradients of u and v on interior cell t (row-major over the
+// im x jm interior) (rhs/gradop_5pi.F, gradop_5pj.F, gradient.F; the 3p, 7p and
+// 9p operators for R = 2, 4, 5)
+template <class S, int R = 3>
 BCG_HD void grad_cell(const Ext& e, const Coef& c, const Scratch<S>& pr, const Scratch<S>& gr,
                       const double* __restrict__ nx, const double* __restrict__ ny, const double* __restrict__ vol,
                       int t) {
@@ -105,7 +106,10 @@ BCG_HD void grad_cell(const Ext& e, const Coef& c, const Scratch<S>& pr, const S
   const size_t q = e.cidx(i, j);
   const int di = 1, dj = e.ni;
   auto g4 = [&](int f, int s) {
-    return c.b1 * (pr.ld(f, q + s) - pr.ld(f, q - s)) + c.b2 * (pr.ld(f, q + 2 * s) - pr.ld(f, q - 2 * s));
+    S g = c.bb[0] * (pr.ld(f, q + s) - pr.ld(f, q - s));
+#pragma unroll
+    for (int n = 2; n < R; ++n) g = g + c.bb[n - 1] * (pr.ld(f, q + n * s) - pr.ld(f, q - n * s));
+    return g;
   };
   const S gui = g4(F_U, di), gvi = g4(F_V, di), guj = g4(F_U, dj), gvj = g4(F_V, dj);
   const size_t nn = e.nn();
@@ -122,9 +126,13 @@ BCG_HD void grad_cell(const Ext& e, const Coef& c, const Scratch<S>& pr, const S
 }
 
 // ---------------------------------------------------------------------------
-// pass 3: face fluxes
-template <class S>
+// pass 3: face fluxes of the DNC scheme with R point pairs (R = 3: DNC5)
+template <class S, int R = 3>
 struct FaceCtx {
+  // near-wall off-centred j-fluxes read the first NW cell rows
+  static constexpr int NW = R == 2 ? 2 : (R == 3 ? 5 : (R == 4 ? 9 : 11));
+  // DNC3 uses the 2nd-order viscous flux on every row (rhs/flux_visqueux_o2.F)
+  static constexpr bool ALL_O2 = (R == 2);
   Ext e;
   Coef c;
   State<S> w;
@@ -330,47 +338,80 @@ struct FaceCtx {
     for (int v5 = 2; v5 <= 5; ++v5) h[v5 - 1] = fx[v5 - 1] - diss[v5 - 1] - fn[v5 - 2];
   }
 
+  // Centred face flux of variable v5 along (di, dj) with the weights already
+  // multiplied by the face normal (a = cc fnx, b = cc fny), once per face:
+  // sum_n a_n (f(+n-1) + f(-n)) + sum_n b_n (g(+n-1) + g(-n))  (rhs/euler_o6_i.F,
+  // the o4, o8 and o10 forms for R = 2, 4, 5)
+  BCG_HD S centred(int v5, int i, int j, int di, int dj, const double a[R], const double b[R]) const {
+    S fx = a[0] * (Fl(v5, i, j) + Fl(v5, i - di, j - dj));
+#pragma unroll
+    for (int n = 2; n <= R; ++n)
+      fx = fx + a[n - 1] * (Fl(v5, i + (n - 1) * di, j + (n - 1) * dj) + Fl(v5, i - n * di, j - n * dj));
+#pragma unroll
+    for (int n = 1; n <= R; ++n)
+      fx = fx + b[n - 1] * (Gl(v5, i + (n - 1) * di, j + (n - 1) * dj) + Gl(v5, i - n * di, j - n * dj));
+    return fx;
+  }
+  // Predictor sum_n (-1)^n d_n (w(-n) - w(+n-1)), outermost point first
+  // (rhs/predictor_7p_i.F; 5p, 9p, 11p for R = 2, 4, 5)
+  BCG_HD S predictor(int v5, int i, int j, int di, int dj) const {
+    S p = c.dd[R - 1] * W(i - R * di, j - R * dj, v5);
+    if (R & 1) p = -p;
+#pragma unroll
+    for (int n = R - 1; n >= 1; --n) {
+      const S t = c.dd[n - 1] * W(i - n * di, j - n * dj, v5);
+      p = (n & 1) ? p - t : p + t;
+    }
+#pragma unroll
+    for (int n = 1; n <= R; ++n) {
+      const S t = c.dd[n - 1] * W(i + (n - 1) * di, j + (n - 1) * dj, v5);
+      p = (n & 1) ? p + t : p - t;
+    }
+    return p;
+  }
+
   // i-face (i,j), between cells (i-1,j) and (i,j)
   BCG_HD void iface(int i, int j, S h[5]) const {
     S fx[5], pred[5], diss[5], fn[4];
     const double fnx = NX(i, j, 1), fny = NY(i, j, 1);
-    // centred weights times the face normal, once per face (rhs/euler_o6_i.F)
-    const double a1 = c.c1 * fnx, a2 = c.c2 * fnx, a3 = c.c3 * fnx, b1 = c.c1 * fny, b2 = c.c2 * fny, b3 = c.c3 * fny;
+    double a[R], b[R];
+#pragma unroll
+    for (int n = 0; n < R; ++n) { a[n] = c.cc[n] * fnx; b[n] = c.cc[n] * fny; }
 #pragma unroll
     for (int v5 = 1; v5 <= 5; ++v5) {
-      fx[v5 - 1] = a1 * (Fl(v5, i, j) + Fl(v5, i - 1, j)) + a2 * (Fl(v5, i + 1, j) + Fl(v5, i - 2, j)) +
-                   a3 * (Fl(v5, i + 2, j) + Fl(v5, i - 3, j)) + b1 * (Gl(v5, i, j) + Gl(v5, i - 1, j)) +
-                   b2 * (Gl(v5, i + 1, j) + Gl(v5, i - 2, j)) + b3 * (Gl(v5, i + 2, j) + Gl(v5, i - 3, j));
-      pred[v5 - 1] = -(c.d3 * W(i - 3, j, v5)) + c.d2 * W(i - 2, j, v5) - c.d1 * W(i - 1, j, v5) +
-                     c.d1 * W(i, j, v5) - c.d2 * W(i + 1, j, v5) + c.d3 * W(i + 2, j, v5);
+      fx[v5 - 1] = centred(v5, i, j, 1, 0, a, b);
+      pred[v5 - 1] = predictor(v5, i, j, 1, 0);
     }
-    visc_i(i, j, c.wall && j <= 2, fnx, fny, fn);
+    visc_i(i, j, ALL_O2 || (c.wall && j <= 2), fnx, fny, fn);
     dissipation(i - 1, j, i, j, i - 2, j, i + 1, j, fnx, fny, pred, diss);
     assemble(fx, diss, fn, h);
   }
 
-  // j-face (i,j), between cells (i,j-1) and (i,j); j >= 2
+  // j-face (i,j), between cells (i,j-1) and (i,j); j >= 2 with a wall
   BCG_HD void jface(int i, int j, S h[5]) const {
     S fx[5], pred[5], diss[5], fn[4];
     const double fnx = NX(i, j, 2), fny = NY(i, j, 2);
-    const double a1 = c.c1 * fnx, a2 = c.c2 * fnx, a3 = c.c3 * fnx, b1 = c.c1 * fny, b2 = c.c2 * fny, b3 = c.c3 * fny;
+    double a[R], b[R];
+#pragma unroll
+    for (int n = 0; n < R; ++n) { a[n] = c.cc[n] * fnx; b[n] = c.cc[n] * fny; }
 #pragma unroll
     for (int v5 = 1; v5 <= 5; ++v5) {
-      if (j >= 4 || !c.wall) {
-        fx[v5 - 1] = a1 * (Fl(v5, i, j) + Fl(v5, i, j - 1)) + a2 * (Fl(v5, i, j + 1) + Fl(v5, i, j - 2)) +
-                     a3 * (Fl(v5, i, j + 2) + Fl(v5, i, j - 3)) + b1 * (Gl(v5, i, j) + Gl(v5, i, j - 1)) +
-                     b2 * (Gl(v5, i, j + 1) + Gl(v5, i, j - 2)) + b3 * (Gl(v5, i, j + 2) + Gl(v5, i, j - 3));
+      if (j > R || !c.wall) {
+        fx[v5 - 1] = centred(v5, i, j, 0, 1, a, b);
       } else {
-        const double* cw = (j == 3) ? c.c5 : c.c3w;  // rhs/nearbndfluxes5demi_7p.F, 3demi
-        fx[v5 - 1] = (cw[0] * Fl(v5, i, 1) + cw[1] * Fl(v5, i, 2) + cw[2] * Fl(v5, i, 3) + cw[3] * Fl(v5, i, 4) +
-                      cw[4] * Fl(v5, i, 5)) * fnx +
-                     (cw[0] * Gl(v5, i, 1) + cw[1] * Gl(v5, i, 2) + cw[2] * Gl(v5, i, 3) + cw[3] * Gl(v5, i, 4) +
-                      cw[4] * Gl(v5, i, 5)) * fny;
+        // off-centred flux of wall row j from rows 1..NW (rhs/nearbndfluxes5demi_7p.F, 3demi, ...)
+        const double* cw = c.cw[j - 2];
+        S sf = cw[0] * Fl(v5, i, 1), sg = cw[0] * Gl(v5, i, 1);
+#pragma unroll
+        for (int n = 1; n < NW; ++n) {
+          sf = sf + cw[n] * Fl(v5, i, n + 1);
+          sg = sg + cw[n] * Gl(v5, i, n + 1);
+        }
+        fx[v5 - 1] = sf * fnx + sg * fny;
       }
-      pred[v5 - 1] = -(c.d3 * W(i, j - 3, v5)) + c.d2 * W(i, j - 2, v5) - c.d1 * W(i, j - 1, v5) +
-                     c.d1 * W(i, j, v5) - c.d2 * W(i, j + 1, v5) + c.d3 * W(i, j + 2, v5);
+      pred[v5 - 1] = predictor(v5, i, j, 0, 1);
     }
-    visc_j(i, j, c.wall && j == 2, fnx, fny, fn);
+    visc_j(i, j, ALL_O2 || (c.wall && j == 2), fnx, fny, fn);
     dissipation(i, j - 1, i, j, i, j - 2, i, j + 1, fnx, fny, pred, diss);
     assemble(fx, diss, fn, h);
   }
@@ -396,8 +437,8 @@ struct FaceCtx {
 
 // node t of the (im+1) x (jm+1) node set, i fastest: the i-face (j <= jm)
 // and the j-face (i <= im) of the node into hn (5 i-face, 5 j-face fields)
-template <class S>
-BCG_HD void face_node(const FaceCtx<S>& fc, const Scratch<S>& hn, int t) {
+template <class S, int R = 3>
+BCG_HD void face_node(const FaceCtx<S, R>& fc, const Scratch<S>& hn, int t) {
   const Ext& e = fc.e;
   const int nI = e.im + 1;
   const int i = 1 + t % nI, j = 1 + t / nI;

@@ -23,6 +23,7 @@ struct ResidualArgs {
   int nowall;            // 1: flux_num_dnc5_nowall_2d (centred rows everywhere, no wall face)
   int ngroup;            // 0 or 1: one group; G > 1 (ndir > 0): G groups of ndir directions in one launch,
                          // group g reading wd + g*ndir*dstride and writing resd + g*ndir*dstride
+  int order;             // DNC scheme order: 0 or 5 (DNC5); 3, 7 or 9 (ndir 0 or 1; gh >= (order+1)/2)
 };
 
 size_t residual_scratch_doubles(int im, int jm, int gh, int ndir);
@@ -31,5 +32,7 @@ size_t residual_scratch_doubles(int im, int jm, int gh, int ndir);
 void launch_primal_passes(const Ext& e, const Coef& c, const double* w, double* pr, double* gr, const double* nx,
                           const double* ny, const double* vol, cudaStream_t st);
 cudaError_t run_residual(const ResidualArgs& a, cudaStream_t st);
+// the DNC3, DNC7 and DNC9 schemes (a.order 3, 7, 9; ndir 0 or 1), schemes.cu
+cudaError_t run_residual_scheme(const ResidualArgs& a, cudaStream_t st);
 
 }  // namespace bcg

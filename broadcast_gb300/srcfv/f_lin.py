@@ -2,6 +2,7 @@
 
 flux_num_dnc5_2d_d       : tangent/flux_num_dnc5_d.f90:15
 flux_num_dnc5_nowall_2d_d: tangent/flux_num_dnc5_nowall_d.f90
+flux_num_dnc{3,7,9}[_nowall]_2d_d: tangent/flux_num_dnc{3,7,9}[_nowall]_d.f90
 bc_wall_viscous_adia_2d_d: tangent/bc_wall_viscous_d.f90:11
 bc_no_reflexion_2d_d     : tangent/bc_no_reflexion_d.f90:16
 bc_supandsubinlet_2d_d   : tangent/bc_supandsubinlet_d.f90:11
@@ -33,6 +34,28 @@ def flux_num_dnc5_nowall_2d_d(residu, residud, w, wd, x0, y0, nx, ny, xc, yc, vo
     call("bcg_flux_num_dnc5_nowall_2d_d", arr(residu, "residu", True), arr(residud, "residud", True), arr(w, "w"),
          arr(wd, "wd"), None, None, arr(nx, "nx"), arr(ny, "ny"), None, None, arr(vol, "vol"), arr(volf, "volf"), gh,
          cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4, int(im), int(jm))
+
+
+def _scheme_d(symbol):
+    def tangent(residu, residud, w, wd, x0, y0, nx, ny, xc, yc, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref,
+                tref, s_suth, k2, k4, im=None, jm=None):
+        gh = int(gh)
+        if im is None or jm is None:
+            im, jm = dims_from_cell(w, gh)
+        call(symbol, arr(residu, "residu", True), arr(residud, "residud", True), arr(w, "w"), arr(wd, "wd"), None, None,
+             arr(nx, "nx"), arr(ny, "ny"), None, None, arr(vol, "vol"), arr(volf, "volf"), gh, cp, cv, prandtl, gam,
+             rgaz, cs, muref, tref, s_suth, k2, k4, int(im), int(jm))
+    tangent.__name__ = symbol[4:]
+    tangent.__doc__ = "Residual and tangent of the DNC scheme (srcfv/tangent/%s.f90)." % symbol[4:-3]
+    return tangent
+
+
+flux_num_dnc3_2d_d = _scheme_d("bcg_flux_num_dnc3_2d_d")
+flux_num_dnc7_2d_d = _scheme_d("bcg_flux_num_dnc7_2d_d")
+flux_num_dnc9_2d_d = _scheme_d("bcg_flux_num_dnc9_2d_d")
+flux_num_dnc3_nowall_2d_d = _scheme_d("bcg_flux_num_dnc3_nowall_2d_d")
+flux_num_dnc7_nowall_2d_d = _scheme_d("bcg_flux_num_dnc7_nowall_2d_d")
+flux_num_dnc9_nowall_2d_d = _scheme_d("bcg_flux_num_dnc9_nowall_2d_d")
 
 
 def bc_wall_viscous_adia_2d_d(w, wd, loc, gam, interf, gh, im=None, jm=None):

@@ -83,6 +83,61 @@ int bcg_flux_num_dnc5_nowall_2d_d(double* residu, double* residud, const double*
                                   double cp, double cv, double prandtl, double gam, double rgaz, double cs,
                                   double muref, double tref, double s_suth, double k2, double k4, int im, int jm);
 
+/* The schemes of order 3, 7 and 9 and their tangents, with the arguments of
+ * flux_num_dnc5_2d / _d (gh >= (order+1)/2; im, jm >= 6, and >= 9 for DNC7 and
+ * >= 11 for DNC9, whose wall rows read that many cell rows):
+ *   srcfv/rhs/flux_num_dnc3.F90:7, flux_num_dnc7.F90:7, flux_num_dnc9.F90:7
+ *   srcfv/rhs/flux_num_dnc{3,7,9}_nowall.F90:7
+ *   srcfv/tangent/flux_num_dnc{3,7,9}_d.f90, flux_num_dnc{3,7,9}_nowall_d.f90 */
+int bcg_flux_num_dnc3_2d(double* residu, const double* w, const double* x0, const double* y0, const double* nx,
+    const double* ny, const double* xc, const double* yc, const double* vol, const double* volf, int gh, double cp,
+    double cv, double prandtl, double gam, double rgaz, double cs, double muref, double tref, double s_suth, double k2,
+    double k4, int im, int jm);
+int bcg_flux_num_dnc3_2d_d(double* residu, double* residud, const double* w, const double* wd, const double* x0,
+    const double* y0, const double* nx, const double* ny, const double* xc, const double* yc, const double* vol,
+    const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs, double muref,
+    double tref, double s_suth, double k2, double k4, int im, int jm);
+int bcg_flux_num_dnc3_nowall_2d(double* residu, const double* w, const double* x0, const double* y0, const double* nx,
+    const double* ny, const double* xc, const double* yc, const double* vol, const double* volf, int gh, double cp,
+    double cv, double prandtl, double gam, double rgaz, double cs, double muref, double tref, double s_suth, double k2,
+    double k4, int im, int jm);
+int bcg_flux_num_dnc3_nowall_2d_d(double* residu, double* residud, const double* w, const double* wd, const double* x0,
+    const double* y0, const double* nx, const double* ny, const double* xc, const double* yc, const double* vol,
+    const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs, double muref,
+    double tref, double s_suth, double k2, double k4, int im, int jm);
+int bcg_flux_num_dnc7_2d(double* residu, const double* w, const double* x0, const double* y0, const double* nx,
+    const double* ny, const double* xc, const double* yc, const double* vol, const double* volf, int gh, double cp,
+    double cv, double prandtl, double gam, double rgaz, double cs, double muref, double tref, double s_suth, double k2,
+    double k4, int im, int jm);
+int bcg_flux_num_dnc7_2d_d(double* residu, double* residud, const double* w, const double* wd, const double* x0,
+    const double* y0, const double* nx, const double* ny, const double* xc, const double* yc, const double* vol,
+    const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs, double muref,
+    double tref, double s_suth, double k2, double k4, int im, int jm);
+int bcg_flux_num_dnc7_nowall_2d(double* residu, const double* w, const double* x0, const double* y0, const double* nx,
+    const double* ny, const double* xc, const double* yc, const double* vol, const double* volf, int gh, double cp,
+    double cv, double prandtl, double gam, double rgaz, double cs, double muref, double tref, double s_suth, double k2,
+    double k4, int im, int jm);
+int bcg_flux_num_dnc7_nowall_2d_d(double* residu, double* residud, const double* w, const double* wd, const double* x0,
+    const double* y0, const double* nx, const double* ny, const double* xc, const double* yc, const double* vol,
+    const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs, double muref,
+    double tref, double s_suth, double k2, double k4, int im, int jm);
+int bcg_flux_num_dnc9_2d(double* residu, const double* w, const double* x0, const double* y0, const double* nx,
+    const double* ny, const double* xc, const double* yc, const double* vol, const double* volf, int gh, double cp,
+    double cv, double prandtl, double gam, double rgaz, double cs, double muref, double tref, double s_suth, double k2,
+    double k4, int im, int jm);
+int bcg_flux_num_dnc9_2d_d(double* residu, double* residud, const double* w, const double* wd, const double* x0,
+    const double* y0, const double* nx, const double* ny, const double* xc, const double* yc, const double* vol,
+    const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs, double muref,
+    double tref, double s_suth, double k2, double k4, int im, int jm);
+int bcg_flux_num_dnc9_nowall_2d(double* residu, const double* w, const double* x0, const double* y0, const double* nx,
+    const double* ny, const double* xc, const double* yc, const double* vol, const double* volf, int gh, double cp,
+    double cv, double prandtl, double gam, double rgaz, double cs, double muref, double tref, double s_suth, double k2,
+    double k4, int im, int jm);
+int bcg_flux_num_dnc9_nowall_2d_d(double* residu, double* residud, const double* w, const double* wd, const double* x0,
+    const double* y0, const double* nx, const double* ny, const double* xc, const double* yc, const double* vol,
+    const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs, double muref,
+    double tref, double s_suth, double k2, double k4, int im, int jm);
+
 /* srcfv/adjoint/flux_num_dnc5_b.f90:15 (FLUX_NUM_DNC5_2D_B): wb = (dR/dw)^T residub
  * on every padded cell (wb overwritten); the interior of residub is zeroed on
  * return, as in the reference; residu is unused. */

@@ -41,7 +41,92 @@ struct Consts {
 };
 
 // ===========================================================================
-// Residual: srcfv/prepro/flux_num_dnc5.f90 (flattened srcfv/rhs/flux_num_dnc5.F90)
+// Stencil coefficients of the DNC schemes of order 3, 5, 7, 9 with R = (order+1)/2
+// point pairs (srcfv/rhs/flux_num_dnc{3,5,7,9}.F90 and rhs/coefnearbnd_*.F):
+//   bb[0..R-2]  cell-gradient weights        (rhs/gradop_{3,5,7,9}p{i,j}.F)
+//   cc[0..R-1]  centred face-flux weights    (rhs/euler_o{4,6,8,10}_{i,j}.F)
+//   dd[0..R-1]  predictor weights            (rhs/predictor_{5,7,9,11}p_{i,j}.F)
+//   cw[r][0..nw-1]  off-centred j-flux weights of wall row j = r + 2, from the
+//               first nw cell rows (rhs/nearbndfluxes{3,5,7,9}demi_*.F)
+// Each value is formed by the same floating-point operations as the reference.
+// ===========================================================================
+struct DncCoefs {
+  int order, R, nw;
+  double bb[4], cc[5], dd[5], cw[4][11];
+};
+
+inline DncCoefs dnc_coefs(int order) {
+  DncCoefs k{};
+  k.order = order;
+  k.R = (order + 1) / 2;
+  double denom;
+  if (order == 3) {  // flux_num_dnc3.F90:104-123
+    denom = 1.0 / 12.0;
+    k.bb[0] = 0.5;
+    k.cc[0] = 7.0 * denom; k.cc[1] = -denom;
+    k.dd[0] = 3.0 * denom; k.dd[1] = denom;
+    k.nw = 2;  // face 3/2: c3d0 = c3d1 = 1/2 (:172-173)
+    k.cw[0][0] = 0.5; k.cw[0][1] = 0.5;
+  } else if (order == 5) {  // flux_num_dnc5.F90:89-118, rhs/coefnearbnd_7p.F with denom 1/60
+    denom = 1.0 / 12.0;
+    k.bb[0] = 8.0 * denom; k.bb[1] = -denom;
+    denom = 1.0 / 60.0;
+    k.cc[0] = 37.0 * denom; k.cc[1] = -8.0 * denom; k.cc[2] = denom;
+    k.dd[0] = 10.0 * denom; k.dd[1] = 5.0 * denom; k.dd[2] = denom;
+    k.nw = 5;
+    const double c3[5] = {12.0, 77.0, -43.0, 17.0, -3.0}, c5[5] = {-3.0, 27.0, 47.0, -13.0, 2.0};
+    for (int n = 0; n < 5; ++n) { k.cw[0][n] = c3[n] * denom; k.cw[1][n] = c5[n] * denom; }
+  } else if (order == 7) {  // flux_num_dnc7.F90:92-128, rhs/coefnearbnd_9p.F with denom 1/840
+    denom = 1.0 / 60.0;
+    k.bb[0] = 45.0 * denom; k.bb[1] = -9.0 * denom; k.bb[2] = denom;
+    denom = 1.0 / 840.0;
+    k.cc[0] = 533.0 * denom; k.cc[1] = -139.0 * denom; k.cc[2] = 29.0 * denom; k.cc[3] = -3.0 * denom;
+    denom = 1.0 / 280.0;
+    k.dd[0] = 35.0 * denom; k.dd[1] = 21.0 * denom; k.dd[2] = 7.0 * denom; k.dd[3] = 1.0 * denom;
+    denom = 1.0 / 840.0;
+    k.nw = 9;
+    const double c3[9] = {92.0, 1547.0, -1861.0, 2171.0, -1917.0, 1191.0, -489.0, 119.0, -13.0};
+    const double c5[9] = {-13.0, 209.0, 1079.0, -769.0, 533.0, -279.0, 99.0, -21.0, 2.0};
+    const double c7[9] = {2.0, -31.0, 281.0, 911.0, -517.0, 281.0, -111.0, 27.0, -3.0};
+    for (int n = 0; n < 9; ++n) { k.cw[0][n] = c3[n] * denom; k.cw[1][n] = c5[n] * denom; k.cw[2][n] = c7[n] * denom; }
+  } else if (order == 9) {  // flux_num_dnc9.F90:100-128, rhs/coefnearbnd_11p.F
+    denom = 1.0 / 840.0;
+    k.bb[0] = 672.0 * denom; k.bb[1] = -168.0 * denom; k.bb[2] = 32.0 * denom; k.bb[3] = -3.0 * denom;
+    denom = 1.0 / 2520.0;
+    k.cc[0] = 1627.0 * denom; k.cc[1] = -473.0 * denom; k.cc[2] = 127.0 * denom; k.cc[3] = -23.0 * denom;
+    k.cc[4] = 2.0 * denom;
+    denom = 1.0 / 1260.0;
+    k.dd[0] = 126.0 * denom; k.dd[1] = 84.0 * denom; k.dd[2] = 36.0 * denom; k.dd[3] = 9.0 * denom; k.dd[4] = denom;
+    k.nw = 11;
+    // face 9/2 from the centred weights, then each lower face from the one
+    // above: Phi(f - 1) = Phi(f) - sum a_n f_n
+    const double a9[11] = {1.0 / 840.0, -(1.0 / 63.0), 3.0 / 28.0, -(4.0 / 7.0), -11.0 / 30.0, 6.0 / 5.0, -0.5,
+                           4.0 / 21.0, -(3.0 / 56.0), 1.0 / 105.0, -(1.0 / 1260.0)};
+    const double a7[11] = {-(1.0 / 360.0), 1.0 / 24.0, -(3.0 / 8.0), -(319.0 / 420.0), 1.75, -(21.0 / 20.0),
+                           7.0 / 12.0, -0.25, 0.075, -(1.0 / 72.0), 1.0 / 840.0};
+    const double a5[11] = {1.0 / 90.0, -(2.0 / 9.0), -(341.0 / 280.0), 8.0 / 3.0, -(7.0 / 3.0), 28.0 / 15.0,
+                           -(7.0 / 6.0), 8.0 / 15.0, -(1.0 / 6.0), 2.0 / 63.0, -(1.0 / 360.0)};
+    const double a3[11] = {-0.1, -(4609.0 / 2520.0), 4.5, -6.0, 7.0, -6.3, 21.0 * 0.2, -2.0, 9.0 / 14.0, -0.125,
+                           1.0 / 90.0};
+    const double cen[11] = {k.cc[4], k.cc[3], k.cc[2], k.cc[1], k.cc[0], k.cc[0], k.cc[1], k.cc[2], k.cc[3], k.cc[4], 0.0};
+    for (int n = 0; n < 11; ++n) {
+      k.cw[3][n] = n < 10 ? cen[n] - a9[n] : -a9[n];
+      k.cw[2][n] = k.cw[3][n] - a7[n];
+      k.cw[1][n] = k.cw[2][n] - a5[n];
+      k.cw[0][n] = k.cw[1][n] - a3[n];
+    }
+  } else {
+    k.order = 0;
+  }
+  return k;
+}
+
+// ===========================================================================
+// Residual: srcfv/prepro/flux_num_dnc5.f90 (flattened srcfv/rhs/flux_num_dnc5.F90),
+// and with order 3, 7 or 9 srcfv/prepro/flux_num_dnc{3,7,9}.f90: the same
+// passes with the stencils of DncCoefs, interior j-faces from row R+1,
+// off-centred j-fluxes on rows 2..R, 2nd-order viscous fluxes on row 2 (and
+// everywhere for DNC3)
 // ===========================================================================
 template <class T>
 struct Dnc5 {
@@ -50,8 +135,9 @@ struct Dnc5 {
   // coefficients (flux_num_dnc5.f90:69-122, 938-950)
   double HALF = 0.5, ONE = 1.0, ZERO = 0.0, TWO = 2.0, TWOTHIRD = 2.0 / 3.0, FOURTH = 0.25;
   double TWELFTH = 0.25 / 3.0, TWENTYFOURTH = 1.0 / 24.0, ccross, cpprandtl, cvm1, betas;
-  double b1, b2, c1, c2, c3, d1, d2, d3;
-  double c5d0, c5d1, c5d2, c5d3, c5d4, c3d0, c3d1, c3d2, c3d3, c3d4, ct0, ct1;
+  DncCoefs sc;
+  int R;
+  double ct0, ct1;
 
   FArr<const T> w;
   FArr<const double> nx, ny, vol, volf;
@@ -60,8 +146,8 @@ struct Dnc5 {
   int nni, nnj;  // node extents
 
   Dnc5(const T* w_, const double* nx_, const double* ny_, const double* vol_, const double* volf_,
-       int gh_, const Consts& c, int im_, int jm_)
-      : im(im_), jm(jm_), gh(gh_), k(c),
+       int gh_, const Consts& c, int im_, int jm_, int order = 5)
+      : im(im_), jm(jm_), gh(gh_), k(c), sc(dnc_coefs(order)), R(sc.R),
         w(w_, im_ + 2 * gh_, jm_ + 2 * gh_, 1 - gh_),
         nx(nx_, im_ + 2 * gh_ + 1, jm_ + 2 * gh_ + 1, 1 - gh_),
         ny(ny_, im_ + 2 * gh_ + 1, jm_ + 2 * gh_ + 1, 1 - gh_),
@@ -86,15 +172,7 @@ struct Dnc5 {
     cpprandtl = k.cp / k.prandtl;
     cvm1 = ONE / k.cv;
     ccross = TWELFTH * 0.0625;
-    double denom = 1.0 / 12.0;
-    b1 = 8.0 * denom; b2 = -denom;
-    denom = 1.0 / 60.0;
-    c1 = 37.0 * denom; c2 = -8.0 * denom; c3 = denom;
-    d1 = 10.0 * denom; d2 = 5.0 * denom; d3 = denom;
     betas = k.muref * (k.tref + k.cs) / (std::sqrt(k.tref) * k.tref);
-    // near-wall off-centred coefficients (rhs/coefnearbnd_7p.F)
-    c5d0 = -3.0 * denom; c5d1 = 27.0 * denom; c5d2 = 47.0 * denom; c5d3 = -13.0 * denom; c5d4 = 2.0 * denom;
-    c3d0 = 12.0 * denom; c3d1 = 77.0 * denom; c3d2 = -43.0 * denom; c3d3 = 17.0 * denom; c3d4 = -3.0 * denom;
     ct0 = 1.125; ct1 = -0.125;
   }
 
@@ -139,10 +217,14 @@ struct Dnc5 {
 #pragma omp parallel for schedule(static)
     for (int j = 1; j <= jm; ++j)
       for (int i = 1; i <= im; ++i) {
-        const T gui = (b1 * (velx(i + 1, j) - velx(i - 1, j)) + b2 * (velx(i + 2, j) - velx(i - 2, j)));
-        const T gvi = (b1 * (vely(i + 1, j) - vely(i - 1, j)) + b2 * (vely(i + 2, j) - vely(i - 2, j)));
-        const T guj = (b1 * (velx(i, j + 1) - velx(i, j - 1)) + b2 * (velx(i, j + 2) - velx(i, j - 2)));
-        const T gvj = (b1 * (vely(i, j + 1) - vely(i, j - 1)) + b2 * (vely(i, j + 2) - vely(i, j - 2)));
+        T gui = sc.bb[0] * (velx(i + 1, j) - velx(i - 1, j)), gvi = sc.bb[0] * (vely(i + 1, j) - vely(i - 1, j));
+        T guj = sc.bb[0] * (velx(i, j + 1) - velx(i, j - 1)), gvj = sc.bb[0] * (vely(i, j + 1) - vely(i, j - 1));
+        for (int n = 2; n < R; ++n) {
+          gui = gui + sc.bb[n - 1] * (velx(i + n, j) - velx(i - n, j));
+          gvi = gvi + sc.bb[n - 1] * (vely(i + n, j) - vely(i - n, j));
+          guj = guj + sc.bb[n - 1] * (velx(i, j + n) - velx(i, j - n));
+          gvj = gvj + sc.bb[n - 1] * (vely(i, j + n) - vely(i, j - n));
+        }
         const double volm1 = ONE / vol(i, j);
         const double dxm1 = HALF * (nx(i, j, 1) + nx(i + 1, j, 1)) * volm1;
         const double dxm2 = HALF * (nx(i, j, 2) + nx(i, j + 1, 2)) * volm1;
@@ -186,41 +268,53 @@ struct Dnc5 {
   static inline T q4(const T& a, const T& b, const T& c, const T& d) { return -a + 9.0 * b + 9.0 * c - d; }
 
   // --- i-face pieces -------------------------------------------------------
-  // Centred 6th-order Euler flux through i-face (i,j) (rhs/euler_o6_i.F)
-  void euler_i(int i, int j, T fx[5]) {
-    for (int e = 1; e <= 5; ++e)
-      fx[e - 1] = (c1 * (f(i, j, e) + f(i - 1, j, e)) + c2 * (f(i + 1, j, e) + f(i - 2, j, e)) +
-                   c3 * (f(i + 2, j, e) + f(i - 3, j, e))) * nx(i, j, 1) +
-                  (c1 * (g(i, j, e) + g(i - 1, j, e)) + c2 * (g(i + 1, j, e) + g(i - 2, j, e)) +
-                   c3 * (g(i + 2, j, e) + g(i - 3, j, e))) * ny(i, j, 1);
+  // Centred face flux (rhs/euler_o6_i.F; o4, o8, o10 for DNC3, 7, 9):
+  // (sum_n c_n (f(i+n-1) + f(i-n))) nx + (same for g) ny along direction (di, dj)
+  void euler_c(int i, int j, int di, int dj, int dir, T fx[5]) {
+    for (int e = 1; e <= 5; ++e) {
+      T sf = sc.cc[0] * (f(i, j, e) + f(i - di, j - dj, e));
+      T sg = sc.cc[0] * (g(i, j, e) + g(i - di, j - dj, e));
+      for (int n = 2; n <= R; ++n) {
+        sf = sf + sc.cc[n - 1] * (f(i + (n - 1) * di, j + (n - 1) * dj, e) + f(i - n * di, j - n * dj, e));
+        sg = sg + sc.cc[n - 1] * (g(i + (n - 1) * di, j + (n - 1) * dj, e) + g(i - n * di, j - n * dj, e));
+      }
+      fx[e - 1] = sf * nx(i, j, dir) + sg * ny(i, j, dir);
+    }
   }
-  void euler_j(int i, int j, T fx[5]) {
-    for (int e = 1; e <= 5; ++e)
-      fx[e - 1] = (c1 * (f(i, j, e) + f(i, j - 1, e)) + c2 * (f(i, j + 1, e) + f(i, j - 2, e)) +
-                   c3 * (f(i, j + 2, e) + f(i, j - 3, e))) * nx(i, j, 2) +
-                  (c1 * (g(i, j, e) + g(i, j - 1, e)) + c2 * (g(i, j + 1, e) + g(i, j - 2, e)) +
-                   c3 * (g(i, j + 2, e) + g(i, j - 3, e))) * ny(i, j, 2);
+  void euler_i(int i, int j, T fx[5]) { euler_c(i, j, 1, 0, 1, fx); }
+  void euler_j(int i, int j, T fx[5]) { euler_c(i, j, 0, 1, 2, fx); }
+  // Off-centred near-wall j-flux of row j from rows 1..nw
+  // (rhs/nearbndfluxes5demi_7p.F, nearbndfluxes3demi_7p.F and the 5p, 9p, 11p forms)
+  void euler_j_wall(int i, int j, T fx[5]) {
+    const double* c = sc.cw[j - 2];
+    for (int e = 1; e <= 5; ++e) {
+      T sf = c[0] * f(i, 1, e), sg = c[0] * g(i, 1, e);
+      for (int n = 1; n < sc.nw; ++n) {
+        sf = sf + c[n] * f(i, n + 1, e);
+        sg = sg + c[n] * g(i, n + 1, e);
+      }
+      fx[e - 1] = sf * nx(i, j, 2) + sg * ny(i, j, 2);
+    }
   }
-  // Off-centred near-wall j-flux from rows 1..5 (rhs/nearbndfluxes5demi_7p.F,
-  // nearbndfluxes3demi_7p.F)
-  void euler_j_wall(int i, int j, const double c[5], T fx[5]) {
-    for (int e = 1; e <= 5; ++e)
-      fx[e - 1] = (c[0] * f(i, 1, e) + c[1] * f(i, 2, e) + c[2] * f(i, 3, e) + c[3] * f(i, 4, e) +
-                   c[4] * f(i, 5, e)) * nx(i, j, 2) +
-                  (c[0] * g(i, 1, e) + c[1] * g(i, 2, e) + c[2] * g(i, 3, e) + c[3] * g(i, 4, e) +
-                   c[4] * g(i, 5, e)) * ny(i, j, 2);
+  // Predictor (rhs/predictor_7p_i.F, _j.F; 5p, 9p, 11p for DNC3, 7, 9):
+  //   sum_n (-1)^n d_n (w(i-n) - w(i+n-1)), outermost point first
+  void pred_c(int i, int j, int di, int dj, T pr[5]) {
+    for (int e = 1; e <= 5; ++e) {
+      T acc = sc.dd[R - 1] * w(i - R * di, j - R * dj, e);
+      if (R & 1) acc = -acc;
+      for (int n = R - 1; n >= 1; --n) {
+        const T t = sc.dd[n - 1] * w(i - n * di, j - n * dj, e);
+        acc = (n & 1) ? acc - t : acc + t;
+      }
+      for (int n = 1; n <= R; ++n) {
+        const T t = sc.dd[n - 1] * w(i + (n - 1) * di, j + (n - 1) * dj, e);
+        acc = (n & 1) ? acc + t : acc - t;
+      }
+      pr[e - 1] = acc;
+    }
   }
-  // 7-point predictor (rhs/predictor_7p_i.F, predictor_7p_j.F)
-  void pred_i(int i, int j, T pr[5]) {
-    for (int e = 1; e <= 5; ++e)
-      pr[e - 1] = -(d3 * w(i - 3, j, e)) + d2 * w(i - 2, j, e) - d1 * w(i - 1, j, e) + d1 * w(i, j, e) -
-                  d2 * w(i + 1, j, e) + d3 * w(i + 2, j, e);
-  }
-  void pred_j(int i, int j, T pr[5]) {
-    for (int e = 1; e <= 5; ++e)
-      pr[e - 1] = -(d3 * w(i, j - 3, e)) + d2 * w(i, j - 2, e) - d1 * w(i, j - 1, e) + d1 * w(i, j, e) -
-                  d2 * w(i, j + 1, e) + d3 * w(i, j + 2, e);
-  }
+  void pred_i(int i, int j, T pr[5]) { pred_c(i, j, 1, 0, pr); }
+  void pred_j(int i, int j, T pr[5]) { pred_c(i, j, 0, 1, pr); }
 
   // viscous fluxes from the face gradients (rhs/flux_visqueux_o4_i.F:80-103)
   void visc_fluxes(const T& mmu, const T& lambda, const T& uu, const T& vv, const T& ww, const T& ux,
@@ -422,16 +516,11 @@ struct Dnc5 {
     dissipation(i - 1, j, i, j, i - 2, j, i + 1, j, nx(i, j, 1), ny(i, j, 1), pr, diss);
     assemble(i, j, 1, fx, diss, fv, gv);
   }
-  // j-face (i,j): between cells (i,j-1) and (i,j).  euler: 0 centred, 5 or 3
-  // off-centred near-wall formula.
-  void jface(int i, int j, int euler, bool o2) {
+  // j-face (i,j): between cells (i,j-1) and (i,j); offc: the off-centred
+  // near-wall formula of row j.
+  void jface(int i, int j, bool offc, bool o2) {
     T fx[5], pr[5], diss[5], fv[4], gv[4];
-    if (euler == 0) euler_j(i, j, fx);
-    else {
-      const double c5[5] = {c5d0, c5d1, c5d2, c5d3, c5d4};
-      const double c3[5] = {c3d0, c3d1, c3d2, c3d3, c3d4};
-      euler_j_wall(i, j, euler == 5 ? c5 : c3, fx);
-    }
+    if (offc) euler_j_wall(i, j, fx); else euler_j(i, j, fx);
     pred_j(i, j, pr);
     if (o2) visc_j_o2(i, j, fv, gv); else visc_j_o4(i, j, fv, gv);
     dissipation(i, j - 1, i, j, i, j - 2, i, j + 1, nx(i, j, 2), ny(i, j, 2), pr, diss);
@@ -467,12 +556,13 @@ struct Dnc5 {
   void run(T* residu_, bool wall = true) {
     primitives();
     gradients();
+    const bool all_o2 = (R == 2);  // DNC3: rhs/flux_visqueux_o2.F on every row
 #pragma omp parallel for schedule(static)
-    for (int j = wall ? 4 : 1; j <= jm + 1; ++j)
-      for (int i = 1; i <= im + 1; ++i) { iface(i, j, false); jface(i, j, 0, false); }
+    for (int j = wall ? R + 1 : 1; j <= jm + 1; ++j)
+      for (int i = 1; i <= im + 1; ++i) { iface(i, j, all_o2); jface(i, j, false, all_o2); }
     if (wall) {
-      for (int i = 1; i <= im + 1; ++i) { iface(i, 3, false); jface(i, 3, 5, false); }
-      for (int i = 1; i <= im + 1; ++i) { iface(i, 2, true); jface(i, 2, 3, true); }
+      for (int j = R; j >= 2; --j)
+        for (int i = 1; i <= im + 1; ++i) { iface(i, j, all_o2 || j == 2); jface(i, j, true, all_o2 || j == 2); }
       for (int i = 1; i <= im + 1; ++i) { iface(i, 1, true); wallface(i, 1); }
     }
     FArr<T> res(residu_, im + 2 * gh, jm + 2 * gh, 1 - gh);
@@ -486,8 +576,8 @@ struct Dnc5 {
 
 template <class T>
 void flux_num_dnc5_2d(T* residu, const T* w, const double* nx, const double* ny, const double* vol,
-                      const double* volf, int gh, const Consts& c, int im, int jm, bool wall = true) {
-  Dnc5<T> s(w, nx, ny, vol, volf, gh, c, im, jm);
+                      const double* volf, int gh, const Consts& c, int im, int jm, bool wall = true, int order = 5) {
+  Dnc5<T> s(w, nx, ny, vol, volf, gh, c, im, jm, order);
   s.run(residu, wall);
 }
 

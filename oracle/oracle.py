@@ -26,6 +26,8 @@ SIGS = {
     "orc_flux_num_dnc5_nowall_2d": [_P] * 6 + [_I] + _PHYS + [_I, _I],
     "orc_flux_num_dnc5_nowall_2d_d": [_P] * 4 + [_I] + [_P] * 4 + [_I] + _PHYS + [_I, _I],
     "orc_flux_num_dnc5_2d_opcount": [_P] * 6 + [_I] + _PHYS + [_I, _I],
+    "orc_flux_num_dnc_2d": [_I, _I] + [_P] * 6 + [_I] + _PHYS + [_I, _I],
+    "orc_flux_num_dnc_2d_d": [_I, _I] + [_P] * 4 + [_I] + [_P] * 4 + [_I] + _PHYS + [_I, _I],
     "orc_bc_wall_viscous_adia_2d": [_P, _S, _D, _P, _I, _I, _I],
     "orc_bc_wall_viscous_adia_2d_d": [_P, _P, _S, _D, _P, _I, _I, _I],
     "orc_bc_no_reflexion_2d": [_P, _P, _I, _S, _P, _P, _P, _D, _I, _I, _I],
@@ -95,16 +97,22 @@ def _chk(a):
 
 
 # ---- residual -----------------------------------------------------------------
-def residual(grid, ph, w, nowall=False):
-    """flux_num_dnc5_2d, or flux_num_dnc5_nowall_2d with nowall=True."""
+def residual(grid, ph, w, nowall=False, order=5):
+    """flux_num_dnc{order}_2d, or flux_num_dnc{order}_nowall_2d with nowall=True
+    (order 3, 5, 7 or 9)."""
     res = np.zeros_like(w, order="F")
+    args = (_p(res), _p(_chk(w)), _p(grid["nx"]), _p(grid["ny"]), _p(grid["vol"]), _p(grid["volf"]), grid["gh"],
+            *_phys(ph), grid["im"], grid["jm"])
+    if order != 5:
+        if lib().orc_flux_num_dnc_2d(order, 0 if nowall else 1, *args):
+            raise ValueError("flux_num_dnc%d_2d: bad order or ghost width" % order)
+        return res
     fn = lib().orc_flux_num_dnc5_nowall_2d if nowall else lib().orc_flux_num_dnc5_2d
-    fn(_p(res), _p(_chk(w)), _p(grid["nx"]), _p(grid["ny"]), _p(grid["vol"]), _p(grid["volf"]), grid["gh"],
-       *_phys(ph), grid["im"], grid["jm"])
+    fn(*args)
     return res
 
 
-def jvp(grid, ph, w, wd, nowall=False):
+def jvp(grid, ph, w, wd, nowall=False, order=5):
     """wd: one padded state or a stack (nd, ...) of them; returns (res, resd)."""
     wd = np.asarray(wd)
     single = wd.ndim == 3
@@ -114,9 +122,14 @@ def jvp(grid, ph, w, wd, nowall=False):
     buf = np.concatenate([np.ravel(x, order="F") for x in flat])
     out = np.zeros_like(buf)
     res = np.zeros_like(w, order="F")
-    fn = lib().orc_flux_num_dnc5_nowall_2d_d if nowall else lib().orc_flux_num_dnc5_2d_d
-    fn(_p(res), _p(out), _p(_chk(w)), _p(buf), nd, _p(grid["nx"]), _p(grid["ny"]), _p(grid["vol"]),
-       _p(grid["volf"]), grid["gh"], *_phys(ph), grid["im"], grid["jm"])
+    args = (_p(res), _p(out), _p(_chk(w)), _p(buf), nd, _p(grid["nx"]), _p(grid["ny"]), _p(grid["vol"]),
+            _p(grid["volf"]), grid["gh"], *_phys(ph), grid["im"], grid["jm"])
+    if order != 5:
+        if lib().orc_flux_num_dnc_2d_d(order, 0 if nowall else 1, *args):
+            raise ValueError("flux_num_dnc%d_2d_d: bad order or ghost width" % order)
+    else:
+        fn = lib().orc_flux_num_dnc5_nowall_2d_d if nowall else lib().orc_flux_num_dnc5_2d_d
+        fn(*args)
     n = w.size
     resd = [np.reshape(out[k * n:(k + 1) * n], w.shape, order="F") for k in range(nd)]
     return res, (resd[0] if single else np.stack(resd))

@@ -24,14 +24,15 @@ inline size_t np_(int im, int jm, int gh) { return (size_t)(im + 2 * gh) * (jm +
 
 template <int K>
 void jvp_k(double* res, double* resd, const double* w, const double* wd, int nd, const double* nx, const double* ny,
-           const double* vol, const double* volf, int gh, const Consts& c, int im, int jm, bool wall = true) {
+           const double* vol, const double* volf, int gh, const Consts& c, int im, int jm, bool wall = true,
+           int order = 5) {
   const size_t n = np_(im, jm, gh) * 5;
   std::vector<Dual<K>> wdual(n), rdual(n);
   for (size_t q = 0; q < n; ++q) {
     wdual[q].v = w[q];
     for (int k = 0; k < K; ++k) wdual[q].d[k] = wd[(size_t)k * n + q];
   }
-  flux_num_dnc5_2d<Dual<K>>(rdual.data(), wdual.data(), nx, ny, vol, volf, gh, c, im, jm, wall);
+  flux_num_dnc5_2d<Dual<K>>(rdual.data(), wdual.data(), nx, ny, vol, volf, gh, c, im, jm, wall, order);
   FArr<Dual<K>> r(rdual.data(), im + 2 * gh, jm + 2 * gh, 1 - gh);
   FArr<double> rv(res, im + 2 * gh, jm + 2 * gh, 1 - gh);
   for (int e = 1; e <= 5; ++e)
@@ -101,6 +102,32 @@ int orc_flux_num_dnc5_nowall_2d_d(double* residu, double* residud, const double*
     const int kk = std::min(4, nd - k0);
     jvp_k<4>(k0 == 0 ? residu : nullptr, residud + k0 * n, w, wd + k0 * n, kk, nx, ny, vol, volf, gh, c, im, jm,
              false);
+  }
+  return 0;
+}
+
+// ---- residual and JVP of the DNC schemes of order 3, 5, 7, 9, with or without
+// the wall rows (flux_num_dnc{3,5,7,9}[_nowall]_2d[_d]) --------------------------
+int orc_flux_num_dnc_2d(int order, int wall, double* residu, const double* w, const double* nx, const double* ny,
+                        const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
+                        double gam, double rgaz, double cs, double muref, double tref, double s_suth, double k2,
+                        double k4, int im, int jm) {
+  if (dnc_coefs(order).order == 0 || gh < (order + 1) / 2) return -1;
+  flux_num_dnc5_2d<double>(residu, w, nx, ny, vol, volf, gh, mk(cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4),
+                           im, jm, wall != 0, order);
+  return 0;
+}
+int orc_flux_num_dnc_2d_d(int order, int wall, double* residu, double* residud, const double* w, const double* wd,
+                          int nd, const double* nx, const double* ny, const double* vol, const double* volf, int gh,
+                          double cp, double cv, double prandtl, double gam, double rgaz, double cs, double muref,
+                          double tref, double s_suth, double k2, double k4, int im, int jm) {
+  if (dnc_coefs(order).order == 0 || gh < (order + 1) / 2) return -1;
+  const Consts c = mk(cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4);
+  const size_t n = np_(im, jm, gh) * 5;
+  for (int k0 = 0; k0 < nd; k0 += 4) {
+    const int kk = std::min(4, nd - k0);
+    jvp_k<4>(k0 == 0 ? residu : nullptr, residud + k0 * n, w, wd + k0 * n, kk, nx, ny, vol, volf, gh, c, im, jm,
+             wall != 0, order);
   }
   return 0;
 }

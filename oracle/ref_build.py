@@ -23,6 +23,18 @@ ROUTINES = [
     ("srcfv/tangent/flux_num_dnc5_nowall_d.f90", ["flux_num_dnc5_nowall_2d_d"]),
     ("srcfv/tangent/flux_num_dnc5_d.f90", ["flux_num_dnc5_2d_d"]),
     ("srcfv/adjoint/flux_num_dnc5_b.f90", ["flux_num_dnc5_2d_b"]),
+    ("srcfv/prepro/flux_num_dnc3.f90", ["flux_num_dnc3_2d"]),
+    ("srcfv/prepro/flux_num_dnc3_nowall.f90", ["flux_num_dnc3_nowall_2d"]),
+    ("srcfv/tangent/flux_num_dnc3_d.f90", ["flux_num_dnc3_2d_d"]),
+    ("srcfv/tangent/flux_num_dnc3_nowall_d.f90", ["flux_num_dnc3_nowall_2d_d"]),
+    ("srcfv/prepro/flux_num_dnc7.f90", ["flux_num_dnc7_2d"]),
+    ("srcfv/prepro/flux_num_dnc7_nowall.f90", ["flux_num_dnc7_nowall_2d"]),
+    ("srcfv/tangent/flux_num_dnc7_d.f90", ["flux_num_dnc7_2d_d"]),
+    ("srcfv/tangent/flux_num_dnc7_nowall_d.f90", ["flux_num_dnc7_nowall_2d_d"]),
+    ("srcfv/prepro/flux_num_dnc9.f90", ["flux_num_dnc9_2d"]),
+    ("srcfv/prepro/flux_num_dnc9_nowall.f90", ["flux_num_dnc9_nowall_2d"]),
+    ("srcfv/tangent/flux_num_dnc9_d.f90", ["flux_num_dnc9_2d_d"]),
+    ("srcfv/tangent/flux_num_dnc9_nowall_d.f90", ["flux_num_dnc9_nowall_2d_d"]),
     ("srcfv/prepro/bc_wall_viscous.f90", ["bc_wall_viscous_adia_2d"]),
     ("srcfv/prepro/bc_no_reflexion.f90", ["bc_no_reflexion_2d"]),
     ("srcfv/prepro/bc_supandsubinlet.f90", ["bc_supandsubinlet_2d"]),

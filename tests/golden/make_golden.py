@@ -216,6 +216,42 @@ def make_indexing(im=16, jm=11, gh=3, seed=7):
     return out
 
 
+SCHEMES = {"dnc%d_%s_12x11" % (o, k): (o, k) for o in (3, 7, 9) for k in ("bl", "cyl")}
+
+
+def make_scheme(order, kind, im=12, jm=11, seed=11):
+    """flux_num_dnc{order}_2d, its tangent and the _nowall pair on one small
+    case with the driver's ghost width gh = (order+1)//2: the boundary layer
+    with k2 = 1.01 (sensor on) or the cylinder with k2 = 0."""
+    gh = (order + 1) // 2
+    c = cases.bl_case(im, jm, seed=seed, ops=RefOps, gh=gh) if kind == "bl" else \
+        cases.cyl_case(im, jm, seed=seed, ops=RefOps, gh=gh)
+    g, ph = c["grid"], c["phys"]
+    w = c["w"]
+    ref_bcs(c, w)
+    rng = np.random.default_rng(seed + 100)
+    out = {"kind": kind, "order": order, "im": im, "jm": jm, "gh": gh, "w": w.copy(order="F")}
+    for k in ("x0", "y0", "nx", "ny", "xc", "yc", "vol", "volf"):
+        out[k] = g[k]
+    for k in PHYS:
+        out["phys_" + k] = ph[k]
+    out["wbd"] = c["wbd"]
+    if kind == "bl":
+        out["field"] = c["field"]
+    wd = np.zeros_like(w)
+    wd[gh:-gh, gh:-gh] = rng.standard_normal((im, jm, 5))
+    ref_bcs(c, w.copy(order="F"), wd)
+    out["wd"] = wd
+    for suffix in ("", "_nowall"):
+        name = "flux_num_dnc%d%s_2d" % (order, suffix)
+        res = np.zeros_like(w)
+        ref.call(name, res, w, *residual_args(c))
+        r, rd = np.zeros_like(w), np.zeros_like(w)
+        ref.call(name + "_d", r, rd, w, wd, *residual_args(c))
+        out["res" + suffix], out["resd" + suffix] = res, rd
+    return out
+
+
 def main():
     if not ref.available():
         raise SystemExit("oracle/_ref is not built: run python oracle/ref_build.py first")
@@ -223,6 +259,8 @@ def main():
                                        "bl_23x17": ("bl", 23, 17, 3)}.items():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **make(kind, im, jm, seed))
     np.savez_compressed(os.path.join(HERE, "indexing_16x11.npz"), **make_indexing())
+    for name, (order, kind) in SCHEMES.items():
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **make_scheme(order, kind))
     print("written:", sorted(f for f in os.listdir(HERE) if f.endswith(".npz")))
 
 

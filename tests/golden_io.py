@@ -7,6 +7,8 @@ import numpy as np
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 PHYS = ("cp", "cv", "prandtl", "gam", "rgaz", "cs", "muref", "tref", "s_suth", "k2", "k4")
 CASES = ["bl_14x10", "cyl_14x8", "bl_23x17"]
+# the DNC schemes of order 3, 7 and 9 (gh = (order+1)//2)
+SCHEME_CASES = ["dnc%d_%s_12x11" % (o, k) for o in (3, 7, 9) for k in ("bl", "cyl")]
 
 
 def load(name):

@@ -91,7 +91,7 @@ def interior(a, gh=GH):
     return a[gh:-gh, gh:-gh, ...]
 
 
-def rel_err(a, b, scale):
+def rel_err(a, b, scale, gh=GH):
     """max-norm error per variable scaled by `scale` (5-vector); returns the max."""
-    d = np.abs(interior(a) - interior(b)).reshape(-1, 5).max(0)
+    d = np.abs(interior(a, gh) - interior(b, gh)).reshape(-1, 5).max(0)
     return float((d / scale).max())

@@ -54,6 +54,20 @@ def test_nowall_residual_and_tangent(name):
     assert H.rel_err(rd, d["resd_nowall"], sc) < TOL_DERIV
 
 
+@pytest.mark.parametrize("name", G.SCHEME_CASES)
+def test_scheme_orders(name):
+    """flux_num_dnc{3,7,9}_2d, their tangents and the _nowall pairs."""
+    d = G.load(name)
+    c = G.as_case(d)
+    order, gh = int(d["order"]), int(d["gh"])
+    for nowall, sfx in ((False, ""), (True, "_nowall")):
+        r = O.residual(c["grid"], c["phys"], c["w"], nowall=nowall, order=order)
+        assert H.rel_err(r, d["res" + sfx], H.flux_scale(c, c["w"]), gh) < TOL_RES
+        _, rd = O.jvp(c["grid"], c["phys"], c["w"], d["wd"], nowall=nowall, order=order)
+        sc = np.abs(H.interior(d["resd" + sfx], gh)).reshape(-1, 5).max(0)
+        assert H.rel_err(rd, d["resd" + sfx], sc, gh) < TOL_DERIV
+
+
 @pytest.mark.parametrize("name", G.CASES)
 def test_tangent(name):
     d = G.load(name)

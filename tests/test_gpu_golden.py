@@ -49,6 +49,24 @@ def test_nowall_residual_and_tangent(name):
     assert H.rel_err(rd, d["resd_nowall"], sc) < 1e-11
 
 
+@pytest.mark.parametrize("name", G.SCHEME_CASES)
+def test_scheme_orders(name):
+    """flux_num_dnc{3,7,9}[_nowall]_2d and _2d_d through the drop-in modules."""
+    from broadcast_gb300.srcfv import f_lin, f_sch
+    d = G.load(name)
+    c = G.as_case(d)
+    order, gh = int(d["order"]), int(d["gh"])
+    for sfx in ("", "_nowall"):
+        res = np.zeros_like(c["w"])
+        getattr(f_sch, "flux_num_dnc%d%s_2d" % (order, sfx))(res, c["w"], *_args(c))
+        assert H.rel_err(res, d["res" + sfx], H.flux_scale(c, c["w"]), gh) < 1e-12
+        r, rd = np.zeros_like(c["w"]), np.zeros_like(c["w"])
+        getattr(f_lin, "flux_num_dnc%d%s_2d_d" % (order, sfx))(r, rd, c["w"], np.asfortranarray(d["wd"]), *_args(c))
+        assert H.rel_err(r, d["res" + sfx], H.flux_scale(c, c["w"]), gh) < 1e-12
+        sc = np.abs(H.interior(d["resd" + sfx], gh)).reshape(-1, 5).max(0)
+        assert H.rel_err(rd, d["resd" + sfx], sc, gh) < 1e-11
+
+
 @pytest.mark.parametrize("name", G.CASES)
 def test_tangent(name):
     from broadcast_gb300.srcfv import f_lin

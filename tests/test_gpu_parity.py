@@ -192,3 +192,70 @@ def test_nowall_matches_oracle(kind, im, jm):
     _, ref = O.jvp(g, ph, c["w"], wd, nowall=True)
     sc = np.abs(H.interior(ref)).reshape(-1, 5).max(0)
     assert H.rel_err(rd, ref, sc) < 1e-11
+
+
+@pytest.mark.parametrize("order", [3, 7, 9])
+@pytest.mark.parametrize("kind,im,jm", [("bl", 40, 30), ("cyl", 64, 48)])
+def test_scheme_orders_match_oracle(order, kind, im, jm):
+    """flux_num_dnc{3,7,9}[_nowall]_2d (+ tangent) with the driver's ghost width
+    gh = (order+1)//2, host arrays, against the oracle."""
+    from broadcast_gb300.srcfv import f_lin, f_sch
+    gh = (order + 1) // 2
+    c = H.bl_case(im, jm, gh=gh) if kind == "bl" else H.cyl_case(im, jm, gh=gh)
+    H.oracle_bcs(c, c["w"])
+    g, ph = c["grid"], c["phys"]
+    rng = np.random.default_rng(order)
+    wd = np.asfortranarray(rng.standard_normal(c["w"].shape))
+    for nowall, sfx in ((False, ""), (True, "_nowall")):
+        res = np.full_like(c["w"], 7.0)
+        getattr(f_sch, "flux_num_dnc%d%s_2d" % (order, sfx))(res, c["w"], *_args(c))
+        ref = O.residual(g, ph, c["w"], nowall=nowall, order=order)
+        assert H.rel_err(res, ref, H.flux_scale(c, c["w"]), gh) < RES_TOL
+        assert (res[:gh] == 7.0).all() and (res[:, -gh:] == 7.0).all()
+        r, rd = np.zeros_like(res), np.zeros_like(res)
+        getattr(f_lin, "flux_num_dnc%d%s_2d_d" % (order, sfx))(r, rd, c["w"], wd, *_args(c))
+        _, refd = O.jvp(g, ph, c["w"], wd, nowall=nowall, order=order)
+        sc = np.abs(H.interior(refd, gh)).reshape(-1, 5).max(0)
+        assert H.rel_err(rd, refd, sc, gh) < JVP_TOL
+
+
+@pytest.mark.parametrize("order", [3, 7, 9])
+def test_scheme_orders_device_arrays(order):
+    """The same entry points on torch CUDA tensors (Fortran strides), queued on
+    the library stream."""
+    import torch
+    from broadcast_gb300.operator import to_device, to_host
+    from broadcast_gb300.srcfv import f_lin, f_sch
+    gh = (order + 1) // 2
+    c = H.bl_case(48, 36, gh=gh)
+    H.oracle_bcs(c, c["w"])
+    g, ph = c["grid"], c["phys"]
+    dev = lambda a: to_device(a).permute(*reversed(range(a.ndim)))
+    w = dev(c["w"])
+    wd_h = np.asfortranarray(np.random.default_rng(5).standard_normal(c["w"].shape))
+    args = (None, None, dev(g["nx"]), dev(g["ny"]), None, None, dev(g["vol"]), dev(g["volf"]), gh) + _args(c)[9:]
+    res, r, rd = (dev(np.zeros_like(c["w"])) for _ in range(3))
+    getattr(f_sch, "flux_num_dnc%d_2d" % order)(res, w, *args)
+    getattr(f_lin, "flux_num_dnc%d_2d_d" % order)(r, rd, w, dev(wd_h), *args)
+    torch.cuda.synchronize()
+    host = lambda t: to_host(t.permute(*reversed(range(t.ndim))))
+    ref = O.residual(g, ph, c["w"], order=order)
+    assert H.rel_err(host(res), ref, H.flux_scale(c, c["w"]), gh) < RES_TOL
+    _, refd = O.jvp(g, ph, c["w"], wd_h, order=order)
+    sc = np.abs(H.interior(refd, gh)).reshape(-1, 5).max(0)
+    assert H.rel_err(host(rd), refd, sc, gh) < JVP_TOL
+
+
+def test_scheme_orders_reject_bad_extents():
+    """Too few ghost layers for the stencil, or too few rows for the wall
+    formulas, are refused before any launch."""
+    from broadcast_gb300._lib import BroadcastError
+    from broadcast_gb300.srcfv import f_sch
+    c = H.bl_case(40, 30)  # gh = 3 < 5 needed by DNC9
+    res = np.zeros_like(c["w"])
+    with pytest.raises(BroadcastError):
+        f_sch.flux_num_dnc9_2d(res, c["w"], *_args(c))
+    c = H.bl_case(40, 8, gh=5)  # DNC9's wall rows read 11 cell rows
+    res = np.zeros_like(c["w"])
+    with pytest.raises(BroadcastError):
+        f_sch.flux_num_dnc9_2d(res, c["w"], *_args(c))
