@@ -17,6 +17,7 @@
 #include "jacobian.h"
 #include "span.h"
 #include "batch.h"
+#include "impli.h"
 
 using namespace bcg;
 
@@ -420,6 +421,38 @@ BCG_DNC_ENTRIES(3)
 BCG_DNC_ENTRIES(7)
 BCG_DNC_ENTRIES(9)
 #undef BCG_DNC_ENTRIES
+
+// ---- matrix-free implicit phase (srcfv/lhs/impli_matrix_free.F90:7) -------------
+// dwi (intent inout in the reference, fully overwritten: interior = the
+// increment after lmax sweeps, every ghost zero); dw is the right-hand side.
+int bcg_impli_matrix_free_2d(double* dwi, const double* nx, const double* ny, const double* w, const double* dw,
+                             const double* vol, const double* volf, double dtcoef, double cfl, double gam, double rgaz,
+                             double prandtl, int lmax, int gh, double cv, double cs, double muref, double tref,
+                             double s_suth, int im, int jm, int em) {
+  if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
+  if (em != 5 || gh < 1 || im < 1 || jm < 1 || lmax < 0)
+    return fail_arg("impli_matrix_free_2d: need em == 5, gh >= 1, im, jm >= 1, lmax >= 0");
+  if (lmax > 0 && jm > impli_max_rows()) return fail_arg("impli_matrix_free_2d: jm above the sweep kernel's row limit");
+  const size_t np = ncell(im, jm, gh), nn = nnode(im, jm, gh);
+  cudaStream_t st = current_stream();
+  Stager sg(st);
+  const int hnx = sg.in(nx, nn * 2 * 8), hny = sg.in(ny, nn * 2 * 8), hw = sg.in(w, np * 5 * 8);
+  const int hdw = sg.in(dw, np * 5 * 8), hvol = sg.in(vol, np * 8), hvolf = sg.in(volf, np * 2 * 8);
+  const int hdwi = sg.out(dwi, np * 5 * 8);
+  int rc = sg.commit();
+  if (rc) return rc;
+  ImpliArgs a{};
+  a.im = im; a.jm = jm; a.gh = gh; a.lmax = lmax;
+  a.dtcoef = dtcoef; a.cfl = cfl; a.gam = gam; a.rgaz = rgaz; a.prandtl = prandtl; a.cv = cv; a.cs = cs;
+  a.muref = muref; a.tref = tref; a.s_suth = s_suth;
+  a.nx = sg.dev<double>(hnx); a.ny = sg.dev<double>(hny); a.w = sg.dev<double>(hw); a.dw = sg.dev<double>(hdw);
+  a.vol = sg.dev<double>(hvol); a.volf = sg.dev<double>(hvolf); a.dwi = sg.dev<double>(hdwi);
+  a.scratch = (double*)pool_get(POOL_SCRATCH, impli_scratch_doubles(im, jm, gh) * 8);
+  if (!a.scratch) return fail_arg("impli_matrix_free_2d: scratch allocation failed"), BCG_ERR_NOMEM;
+  const cudaError_t e = run_impli(a, st);
+  if (e != cudaSuccess) return fail_cuda("impli_matrix_free_2d", e);
+  return sg.finish();
+}
 
 int bcg_flux_num_dnc5_2d_d(double* residu, double* residud, const double* w, const double* wd, const double* x0,
                            const double* y0, const double* nx, const double* ny, const double* xc, const double* yc,

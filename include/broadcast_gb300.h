@@ -138,6 +138,17 @@ int bcg_flux_num_dnc9_nowall_2d_d(double* residu, double* residud, const double*
     const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs, double muref,
     double tref, double s_suth, double k2, double k4, int im, int jm);
 
+/* srcfv/lhs/impli_matrix_free.F90:7 (IMPLI_MATRIX_FREE_2D): the implicit phase
+ * of the 'impli' time marching (BROADCAST_npz.py:911-941): lmax symmetric
+ * Gauss-Seidel sweeps of the scalar-diagonal implicit operator on the
+ * right-hand side dw (the residual); dwi is overwritten with the increment
+ * (every ghost zero).  em must be 5.  The sweeps run as one launch of one
+ * thread-block cluster (anti-diagonal wavefront, cluster barrier per diagonal). */
+int bcg_impli_matrix_free_2d(double* dwi, const double* nx, const double* ny, const double* w, const double* dw,
+                             const double* vol, const double* volf, double dtcoef, double cfl, double gam, double rgaz,
+                             double prandtl, int lmax, int gh, double cv, double cs, double muref, double tref,
+                             double s_suth, int im, int jm, int em);
+
 /* srcfv/adjoint/flux_num_dnc5_b.f90:15 (FLUX_NUM_DNC5_2D_B): wb = (dR/dw)^T residub
  * on every padded cell (wb overwritten); the interior of residub is zeroed on
  * return, as in the reference; residu is unused. */

@@ -19,6 +19,7 @@
 #pragma once
 #include <cstddef>
 #include <cstring>
+#include <algorithm>
 #include <vector>
 #include <cmath>
 #include "dual.hpp"
@@ -1267,6 +1268,127 @@ inline void computejacobian_withjnandcheck(double* jac, int* ia, int* ja, const 
           }
         }
       }
+}
+
+// ===========================================================================
+// Matrix-free implicit phase: srcfv/lhs/impli_matrix_free.F90:7-300
+// (flattened srcfv/prepro/impli_matrix_free.f90).  lmax symmetric Gauss-Seidel
+// sweeps (forward on odd l, backward on even l) of the scalar-diagonal
+// implicit operator on the right-hand side dw; dwi returns the increment.
+// ===========================================================================
+inline void impli_matrix_free_2d(double* dwi_, const double* nx_, const double* ny_, const double* w_,
+                                 const double* dw_, const double* vol_, const double* volf_, double dtcoef, double cfl,
+                                 double gam, double rgaz, double prandtl, int lmax, int gh, double cv, double cs,
+                                 double muref, double tref, double s_suth, int im, int jm) {
+  const int ni = im + 2 * gh, nj = jm + 2 * gh, lo = 1 - gh;
+  const size_t np = (size_t)ni * nj;
+  FArr<double> dwi(dwi_, ni, nj, lo);
+  FArr<const double> nx(nx_, ni + 1, nj + 1, lo), ny(ny_, ni + 1, nj + 1, lo), w(w_, ni, nj, lo),
+      dw(dw_, ni, nj, lo), vol(vol_, ni, nj, lo), volf(volf_, ni, nj, lo);
+  std::vector<double> tau0_(np), tloc_(np), mu_(np), d1w_(np * 5), f_(np * 5), g_(np * 5), ssor_(np * 5),
+      coefdiag_(np), coef_(np * 2);
+  FArr<double> tau0(tau0_.data(), ni, nj, lo), tloc(tloc_.data(), ni, nj, lo), mu(mu_.data(), ni, nj, lo),
+      d1w(d1w_.data(), ni, nj, lo), f(f_.data(), ni, nj, lo), g(g_.data(), ni, nj, lo), ssor(ssor_.data(), ni, nj, lo),
+      coefdiag(coefdiag_.data(), ni, nj, lo), coef(coef_.data(), ni, nj, lo);
+  const double HALF = 0.5, ZERO = 0.0, TWO = 2.0, ONE = 1.0;
+  for (size_t q = 0; q < np * 5; ++q) dwi_[q] = ZERO;
+  const double gampr = 2.0 * gam / prandtl, gam1 = gam - ONE, cflm1 = ONE / cfl, cvm1 = ONE / cv;
+  const double betas = muref * (tref + cs) / (std::sqrt(tref) * tref);
+  (void)cflm1;
+  // primitives, fluxes, viscosity and local time step on every padded cell
+  // (lhs/PrimitivesLhs.F, phys/viscosity.F, lhs/time_step.F)
+  for (int j = lo; j <= jm + gh; ++j)
+    for (int i = lo; i <= im + gh; ++i) {
+      const double ror = w(i, j, 1), rom1 = ONE / ror;
+      const double velxi = w(i, j, 2) * rom1, velyi = w(i, j, 3) * rom1, velzi = w(i, j, 4) * rom1;
+      const double ec = HALF * (velxi * velxi + velyi * velyi + velzi * velzi);
+      const double eloc = (w(i, j, 5) - ec * ror) * rom1;
+      tloc(i, j) = eloc * cvm1;
+      const double pint = ror * rgaz * tloc(i, j);
+      const double htot = (w(i, j, 5) + pint) * rom1;
+      f(i, j, 1) = w(i, j, 2); f(i, j, 2) = w(i, j, 2) * velxi + pint; f(i, j, 3) = w(i, j, 2) * velyi;
+      f(i, j, 4) = w(i, j, 2) * velzi; f(i, j, 5) = w(i, j, 2) * htot;
+      g(i, j, 1) = w(i, j, 3); g(i, j, 2) = w(i, j, 3) * velxi; g(i, j, 3) = w(i, j, 3) * velyi + pint;
+      g(i, j, 4) = w(i, j, 3) * velzi; g(i, j, 5) = w(i, j, 3) * htot;
+      mu(i, j) = betas / (tloc(i, j) + s_suth) * std::sqrt(tloc(i, j)) * tloc(i, j);
+      const double dist = vol(i, j) / (std::sqrt(nx(i, j, 1) * nx(i, j, 1) + ny(i, j, 1) * ny(i, j, 1)) +
+                                       std::sqrt(nx(i, j, 2) * nx(i, j, 2) + ny(i, j, 2) * ny(i, j, 2)));
+      const double cc = std::sqrt(gam * pint * rom1);
+      const double vitc = std::sqrt(velxi * velxi + velyi * velyi) + cc;
+      const double dt_euler = dist / vitc;
+      const double dt_ns = 2.0 * dist * dist * ror / (gampr * mu(i, j));
+      const double dt = std::max(std::min(dt_euler, dt_ns), 1e-15) * cfl;
+      tau0(i, j) = dt / vol(i, j);
+    }
+  // face spectral radii, convective plus viscous (lhs/specrad_ns.F)
+  for (int kdir = 1; kdir <= 2; ++kdir) {
+    const int i0 = -kdir + 2, j0 = kdir - 1;
+    for (int j = 1; j <= jm + j0; ++j)
+      for (int i = 1; i <= im + i0; ++i) {
+        const double rol = w(i - i0, j - j0, 1), ror = w(i, j, 1);
+        const double rom1l = ONE / rol, rom1r = ONE / ror, iro = 2.0 / (rol + ror);
+        const double uu = HALF * (w(i - i0, j - j0, 2) * rom1l + w(i, j, 2) * rom1r);
+        const double vv = HALF * (w(i - i0, j - j0, 3) * rom1l + w(i, j, 3) * rom1r);
+        const double cc = gam * rgaz * HALF * (tloc(i - i0, j - j0) + tloc(i, j));
+        const double norm = nx(i, j, kdir) * nx(i, j, kdir) + ny(i, j, kdir) * ny(i, j, kdir);
+        const double mutot = HALF * gampr * (mu(i - i0, j - j0) + mu(i, j));
+        const double specdiff = mutot * norm * volf(i, j, kdir) * iro;
+        coef(i, j, kdir) = ONE * (std::fabs(uu * nx(i, j, kdir) + vv * ny(i, j, kdir)) + std::sqrt(cc * norm) +
+                                  TWO * specdiff);
+      }
+  }
+  for (int j = 1; j <= jm; ++j)
+    for (int i = 1; i <= im; ++i) {
+      coefdiag(i, j) = tau0(i, j) * (coef(i, j, 1) + coef(i + 1, j, 1) + coef(i, j, 2) + coef(i, j + 1, 2)) + dtcoef;
+      for (int e = 1; e <= 5; ++e) d1w(i, j, e) = dw(i, j, e) * tau0(i, j);
+    }
+  // lmax sweeps
+  for (int l = 1; l <= lmax; ++l) {
+    const double step = (l % 2 == 1) ? 1.0 : -1.0;  // (-1)**(l-1)
+    const int ipas = (l % 2 == 1) ? 1 : -1;
+    for (int j = 1; j <= jm; ++j)
+      for (int i = 1; i <= im; ++i)
+        for (int e = 1; e <= 5; ++e) { dwi(i, j, e) = d1w(i, j, e) + ssor(i, j, e); ssor(i, j, e) = ZERO; }
+    for (int jj = 0; jj < jm; ++jj)
+      for (int ii = 0; ii < im; ++ii) {
+        const int i = ipas > 0 ? 1 + ii : im - ii, j = ipas > 0 ? 1 + jj : jm - jj;
+        double d2w[5] = {ZERO, ZERO, ZERO, ZERO, ZERO};
+        for (int kdir = 1; kdir <= 2; ++kdir) {
+          const int i0 = ipas * (-kdir + 2), j0 = ipas * (kdir - 1);
+          const int ip = i - i0, jp = j - j0;
+          const int irspec = i - i0 * (1 - ipas) / 2, jrspec = j - j0 * (1 - ipas) / 2;
+          const double nxloc = nx(irspec, jrspec, kdir), nyloc = ny(irspec, jrspec, kdir);
+          double wi[5], fi[5], gi[5];
+          for (int e = 1; e <= 5; ++e) wi[e - 1] = w(ip, jp, e) + dwi(ip, jp, e);
+          const double rhom1 = ONE / wi[0];
+          const double velxi = wi[1] * rhom1, velyi = wi[2] * rhom1, velzi = wi[3] * rhom1;
+          const double pint = gam1 * (wi[4] - HALF * wi[0] * (velxi * velxi + velyi * velyi + velzi * velzi));
+          fi[0] = wi[1]; fi[1] = wi[1] * velxi + pint; fi[2] = wi[1] * velyi; fi[3] = wi[1] * velzi;
+          fi[4] = velxi * (wi[4] + pint);
+          gi[0] = wi[2]; gi[1] = wi[2] * velxi; gi[2] = wi[2] * velyi + pint; gi[3] = wi[2] * velzi;
+          gi[4] = velyi * (wi[4] + pint);
+          const double multi = HALF * step, multi2 = coef(irspec, jrspec, kdir);
+          for (int e = 1; e <= 5; ++e) {
+            const double dfi = fi[e - 1] - f(ip, jp, e), dgi = gi[e - 1] - g(ip, jp, e);
+            d2w[e - 1] = d2w[e - 1] + multi * (dfi * nxloc + dgi * nyloc) + multi2 * dwi(ip, jp, e);
+          }
+        }
+        const double cdiagm1 = ONE / coefdiag(i, j);
+        for (int e = 1; e <= 5; ++e) {
+          d2w[e - 1] = d2w[e - 1] * tau0(i, j);
+          ssor(i, j, e) = d2w[e - 1] + ssor(i, j, e);
+          dwi(i, j, e) = (d2w[e - 1] + dwi(i, j, e)) * cdiagm1;
+        }
+      }
+    // ghost rows and columns of dwi: zero-gradient copies between sweeps, zero after the last
+    const bool last = (l == lmax);
+    for (int e = 1; e <= 5; ++e) {
+      for (int i = 1; i <= im; ++i) dwi(i, jm + 1, e) = last ? ZERO : dwi(i, jm, e);
+      for (int i = 1; i <= im; ++i) dwi(i, 0, e) = last ? ZERO : dwi(i, 1, e);
+      for (int j = 1; j <= jm; ++j) dwi(im + 1, j, e) = last ? ZERO : dwi(im, j, e);
+      for (int j = 1; j <= jm; ++j) dwi(0, j, e) = last ? ZERO : dwi(1, j, e);
+    }
+  }
 }
 
 // ===========================================================================

@@ -27,6 +27,7 @@ SIGS = {
     "orc_flux_num_dnc5_nowall_2d_d": [_P] * 4 + [_I] + [_P] * 4 + [_I] + _PHYS + [_I, _I],
     "orc_flux_num_dnc5_2d_opcount": [_P] * 6 + [_I] + _PHYS + [_I, _I],
     "orc_flux_num_dnc_2d": [_I, _I] + [_P] * 6 + [_I] + _PHYS + [_I, _I],
+    "orc_impli_matrix_free_2d": [_P] * 7 + [_D] * 5 + [_I, _I] + [_D] * 5 + [_I, _I],
     "orc_flux_num_dnc_2d_d": [_I, _I] + [_P] * 4 + [_I] + [_P] * 4 + [_I] + _PHYS + [_I, _I],
     "orc_bc_wall_viscous_adia_2d": [_P, _S, _D, _P, _I, _I, _I],
     "orc_bc_wall_viscous_adia_2d_d": [_P, _P, _S, _D, _P, _I, _I, _I],
@@ -133,6 +134,18 @@ def jvp(grid, ph, w, wd, nowall=False, order=5):
     n = w.size
     resd = [np.reshape(out[k * n:(k + 1) * n], w.shape, order="F") for k in range(nd)]
     return res, (resd[0] if single else np.stack(resd))
+
+
+def impli_matrix_free(grid, ph, w, dw, dtcoef, cfl, lmax):
+    """impli_matrix_free_2d: the increment dwi for right-hand side dw (the
+    driver passes the residual), lmax Gauss-Seidel sweeps; s_suth = cs as the
+    drivers call it."""
+    dwi = np.zeros_like(w, order="F")
+    lib().orc_impli_matrix_free_2d(_p(dwi), _p(grid["nx"]), _p(grid["ny"]), _p(_chk(w)), _p(_chk(dw)),
+                                   _p(grid["vol"]), _p(grid["volf"]), dtcoef, cfl, ph["gam"], ph["rgaz"],
+                                   ph["prandtl"], lmax, grid["gh"], ph["cv"], ph["cs"], ph["muref"], ph["tref"],
+                                   ph["cs"], grid["im"], grid["jm"])
+    return dwi
 
 
 def vjp(grid, ph, w, rb):

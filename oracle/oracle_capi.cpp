@@ -132,6 +132,16 @@ int orc_flux_num_dnc_2d_d(int order, int wall, double* residu, double* residud, 
   return 0;
 }
 
+// ---- matrix-free implicit phase (srcfv/lhs/impli_matrix_free.F90:7) ------------
+int orc_impli_matrix_free_2d(double* dwi, const double* nx, const double* ny, const double* w, const double* dw,
+                             const double* vol, const double* volf, double dtcoef, double cfl, double gam, double rgaz,
+                             double prandtl, int lmax, int gh, double cv, double cs, double muref, double tref,
+                             double s_suth, int im, int jm) {
+  impli_matrix_free_2d(dwi, nx, ny, w, dw, vol, volf, dtcoef, cfl, gam, rgaz, prandtl, lmax, gh, cv, cs, muref, tref,
+                       s_suth, im, jm);
+  return 0;
+}
+
 // VJP: wb = (dR/dw)^T residub over every padded cell (the reference's
 // adjoint/flux_num_dnc5_b.f90 overwrites wb and zeroes the interior of
 // residub).  Computed exactly with Dual<5> sweeps over a period-9 colouring of

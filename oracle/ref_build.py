@@ -58,6 +58,7 @@ ROUTINES = [
     ("srcfv/dz/coeffs_5p_dz.F90", ["function_5p_dz_d", "coeffs_5p_dz"]),
     ("srcfv/dz/coeffs_5p_dz2.F90", ["function_5p_dz2_d", "coeffs_5p_dz2"]),
     ("srcfv/prepro/computegeom.f90", ["computegeom_2d"]),
+    ("srcfv/prepro/impli_matrix_free.f90", ["impli_matrix_free_2d"]),
     ("initialisation.f90", ["initblfv"]),
     ("set_bnd.f90", ["set_bndbl_2d"]),
 ]

@@ -532,6 +532,8 @@ class Translator:
         return "\n".join(lines)
 
     def _block(self, sub, stmts, lines, ind):
+        # named DO constructs ("name: do ...", "enddo name"): drop the label
+        stmts = [re.sub(r"^\w+\s*:\s*(?=do\b)", "", x, flags=re.I) for x in stmts]
         i = 0
         pad = "  " * ind
         while i < len(stmts):

@@ -252,6 +252,35 @@ def make_scheme(order, kind, im=12, jm=11, seed=11):
     return out
 
 
+def make_impli(kind, im, jm, seed, lmaxes=(1, 2, 10), dtcoef=1.0, cfl=5.0):
+    """impli_matrix_free_2d on the residual of a small case, as the 'impli' time
+    marching calls it (BROADCAST_npz.py:941, s_suth = cs)."""
+    c = cases.bl_case(im, jm, seed=seed, ops=RefOps) if kind == "bl" else cases.cyl_case(im, jm, seed=seed, ops=RefOps)
+    g, ph = c["grid"], c["phys"]
+    w = c["w"]
+    ref_bcs(c, w)
+    res = np.zeros_like(w)
+    ref.call("flux_num_dnc5_2d", res, w, *residual_args(c))
+    out = {"kind": kind, "im": im, "jm": jm, "gh": g["gh"], "w": w.copy(order="F"), "dw": res, "dtcoef": dtcoef,
+           "cfl": cfl, "lmax": np.array(lmaxes, dtype=np.int32), "wbd": c["wbd"]}
+    if kind == "bl":
+        out["field"] = c["field"]
+    for k in ("x0", "y0", "nx", "ny", "xc", "yc", "vol", "volf"):
+        out[k] = g[k]
+    for k in PHYS:
+        out["phys_" + k] = ph[k]
+    for lm in lmaxes:
+        dwi = np.full_like(w, 3.0)
+        ref.call("impli_matrix_free_2d", dwi, g["nx"], g["ny"], w, res, g["vol"], g["volf"], dtcoef, cfl, ph["gam"],
+                 ph["rgaz"], ph["prandtl"], int(lm), g["gh"], ph["cv"], ph["cs"], ph["muref"], ph["tref"], ph["cs"], im,
+                 jm, 5)
+        out["dwi_%d" % lm] = dwi
+    return out
+
+
+IMPLI = {"impli_bl_16x10": ("bl", 16, 10, 5), "impli_cyl_14x8": ("cyl", 14, 8, 6)}
+
+
 def main():
     if not ref.available():
         raise SystemExit("oracle/_ref is not built: run python oracle/ref_build.py first")
@@ -261,6 +290,8 @@ def main():
     np.savez_compressed(os.path.join(HERE, "indexing_16x11.npz"), **make_indexing())
     for name, (order, kind) in SCHEMES.items():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **make_scheme(order, kind))
+    for name, args in IMPLI.items():
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **make_impli(*args))
     print("written:", sorted(f for f in os.listdir(HERE) if f.endswith(".npz")))
 
 

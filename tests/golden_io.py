@@ -9,6 +9,8 @@ PHYS = ("cp", "cv", "prandtl", "gam", "rgaz", "cs", "muref", "tref", "s_suth", "
 CASES = ["bl_14x10", "cyl_14x8", "bl_23x17"]
 # the DNC schemes of order 3, 7 and 9 (gh = (order+1)//2)
 SCHEME_CASES = ["dnc%d_%s_12x11" % (o, k) for o in (3, 7, 9) for k in ("bl", "cyl")]
+# impli_matrix_free_2d on the residual of a small case, lmax = 1, 2, 10
+IMPLI_CASES = ["impli_bl_16x10", "impli_cyl_14x8"]
 
 
 def load(name):

@@ -68,6 +68,17 @@ def test_scheme_orders(name):
         assert H.rel_err(rd, d["resd" + sfx], sc, gh) < TOL_DERIV
 
 
+@pytest.mark.parametrize("name", G.IMPLI_CASES)
+def test_impli_matrix_free(name):
+    """impli_matrix_free_2d: the whole dwi array (interior increment, zero ghosts)."""
+    d = G.load(name)
+    c = G.as_case(d)
+    for lm in np.atleast_1d(d["lmax"]):
+        dwi = O.impli_matrix_free(c["grid"], c["phys"], c["w"], d["dw"], d["dtcoef"], d["cfl"], int(lm))
+        ref = d["dwi_%d" % lm]
+        assert np.abs(dwi - ref).max() <= TOL_RES * np.abs(ref).max(), lm
+
+
 @pytest.mark.parametrize("name", G.CASES)
 def test_tangent(name):
     d = G.load(name)

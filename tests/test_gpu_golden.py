@@ -67,6 +67,22 @@ def test_scheme_orders(name):
         assert H.rel_err(rd, d["resd" + sfx], sc, gh) < 1e-11
 
 
+@pytest.mark.parametrize("name", G.IMPLI_CASES)
+def test_impli_matrix_free(name):
+    """impli_matrix_free_2d through srcfv.f_lhs: the whole dwi array."""
+    from broadcast_gb300.srcfv import f_lhs
+    d = G.load(name)
+    c = G.as_case(d)
+    g, ph = c["grid"], c["phys"]
+    for lm in np.atleast_1d(d["lmax"]):
+        dwi = np.full_like(c["w"], 3.0)
+        f_lhs.impli_matrix_free_2d(dwi, g["nx"], g["ny"], c["w"], d["dw"], g["vol"], g["volf"], d["dtcoef"], d["cfl"],
+                                   ph["gam"], ph["rgaz"], ph["prandtl"], int(lm), g["gh"], ph["cv"], ph["cs"],
+                                   ph["muref"], ph["tref"], ph["cs"])
+        ref = d["dwi_%d" % lm]
+        assert np.abs(dwi - ref).max() <= 1e-12 * np.abs(ref).max(), lm
+
+
 @pytest.mark.parametrize("name", G.CASES)
 def test_tangent(name):
     from broadcast_gb300.srcfv import f_lin

@@ -259,3 +259,43 @@ def test_scheme_orders_reject_bad_extents():
     res = np.zeros_like(c["w"])
     with pytest.raises(BroadcastError):
         f_sch.flux_num_dnc9_2d(res, c["w"], *_args(c))
+
+
+def _impli(c, dw, lmax, cfl=5.0, dtcoef=1.0, dwi=None):
+    from broadcast_gb300.srcfv import f_lhs
+    g, ph = c["grid"], c["phys"]
+    dwi = np.full_like(c["w"], 3.0) if dwi is None else dwi
+    f_lhs.impli_matrix_free_2d(dwi, g["nx"], g["ny"], c["w"], dw, g["vol"], g["volf"], dtcoef, cfl, ph["gam"],
+                               ph["rgaz"], ph["prandtl"], lmax, g["gh"], ph["cv"], ph["cs"], ph["muref"], ph["tref"],
+                               ph["cs"])
+    return dwi
+
+
+@pytest.mark.parametrize("kind,im,jm,lmax", [("bl", 400, 150, 10), ("cyl", 64, 48, 10), ("bl", 40, 30, 3),
+                                             ("cyl", 9, 7, 4)])
+def test_impli_matrix_free_matches_oracle(kind, im, jm, lmax):
+    """The cluster wavefront sweeps against the oracle's sequential loops, on the
+    residual as the 'impli' time marching passes it (BROADCAST_npz.py:941)."""
+    c = _prepared(kind, im, jm)
+    g, ph = c["grid"], c["phys"]
+    dw = O.residual(g, ph, c["w"])
+    ref = O.impli_matrix_free(g, ph, c["w"], dw, 1.0, 5.0, lmax)
+    dwi = _impli(c, dw, lmax)
+    assert np.abs(dwi - ref).max() <= 1e-12 * np.abs(ref).max()
+    gh = g["gh"]
+    assert (dwi[:gh] == 0).all() and (dwi[-gh:] == 0).all() and (dwi[:, :gh] == 0).all() and (dwi[:, -gh:] == 0).all()
+
+
+def test_impli_matrix_free_edge_cases():
+    """lmax = 0 leaves dwi all zero; em != 5 is refused."""
+    from broadcast_gb300._lib import BroadcastError
+    from broadcast_gb300.srcfv import f_lhs
+    c = _prepared("bl", 24, 16)
+    g, ph = c["grid"], c["phys"]
+    dw = O.residual(g, ph, c["w"])
+    assert (_impli(c, dw, 0) == 0).all()
+    dwi = np.zeros_like(c["w"])
+    with pytest.raises(BroadcastError):
+        f_lhs.impli_matrix_free_2d(dwi, g["nx"], g["ny"], c["w"], dw, g["vol"], g["volf"], 1.0, 5.0, ph["gam"],
+                                   ph["rgaz"], ph["prandtl"], 2, g["gh"], ph["cv"], ph["cs"], ph["muref"], ph["tref"],
+                                   ph["cs"], 24, 16, 4)
