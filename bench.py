@@ -601,6 +601,99 @@ def run_batch_workload(args):
     return 0
 
 
+def run_impli_workload(args):
+    """The matrix-free implicit phase of the 'impli' time marching
+    (impli_matrix_free_2d, BROADCAST_npz.py:911-941): lmax = 10 symmetric
+    Gauss-Seidel sweeps on the residual of the boundary layer 400x150 (the
+    reference's first configuration), cfl 5, dtcoef 1.  The sweeps are a
+    wavefront of im + jm - 1 dependent anti-diagonals each, so the bound is
+    the latency of one diagonal step, reported beside the throughput."""
+    import torch
+    from broadcast_gb300 import _lib, cases
+    from broadcast_gb300.operator import to_device
+    from broadcast_gb300.srcfv import f_lhs, f_sch
+    from oracle import oracle as O
+    im, jm, lmax, cfl, dtcoef = args.im or 400, args.jm or 150, 10, 5.0, 1.0
+    c = cases.bl_case(im, jm, seed=0, ops=LibOps)
+    bl_bcs(c, c["w"])
+    g, ph = c["grid"], c["phys"]
+    dev = torch.device("cuda", 0)
+    _lib.call("bcg_set_stream", torch.cuda.current_stream(dev).cuda_stream)
+    res = np.zeros_like(c["w"])
+    f_sch.flux_num_dnc5_2d(res, c["w"], g["x0"], g["y0"], g["nx"], g["ny"], g["xc"], g["yc"], g["vol"], g["volf"],
+                           g["gh"], ph["cp"], ph["cv"], ph["prandtl"], ph["gam"], ph["rgaz"], ph["cs"], ph["muref"],
+                           ph["tref"], ph["cs"], ph["k2"], ph["k4"], im, jm)
+    fdev = lambda a: to_device(a, dev).permute(*reversed(range(a.ndim)))
+    arrs = [fdev(g["nx"]), fdev(g["ny"]), fdev(c["w"]), fdev(res), fdev(g["vol"]), fdev(g["volf"])]
+    dwi = fdev(np.zeros_like(c["w"]))
+    scal = (dtcoef, cfl, ph["gam"], ph["rgaz"], ph["prandtl"], lmax, g["gh"], ph["cv"], ph["cs"], ph["muref"],
+            ph["tref"], ph["cs"])
+    call = lambda out, a: f_lhs.impli_matrix_free_2d(out, *a, *scal)
+    for _ in range(max(args.warmup, 3)):
+        call(dwi, arrs)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for s in range(args.steps):
+        flush.add_(1.0)
+        ev[s][0].record(stream)
+        call(dwi, arrs)
+        ev[s][1].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    from broadcast_gb300.operator import to_host
+    out = to_host(dwi.permute(*reversed(range(3))))
+    # end to end: host arrays (uploads of w, dw and the metrics, download of dwi)
+    host_args = [g["nx"], g["ny"], c["w"], res, g["vol"], g["volf"]]
+    dwi_h = np.zeros_like(c["w"])
+    call(dwi_h, host_args)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        call(dwi_h, host_args)
+    e2e_ms = (time.perf_counter() - t0) / args.steps * 1e3
+    # the CPU reference: the oracle's sequential sweeps (the algorithm is a
+    # Gauss-Seidel recurrence, one thread), and the parity of the GPU result
+    t0 = time.perf_counter()
+    nrep = 0
+    while True:
+        ref = O.impli_matrix_free(g, ph, c["w"], res, dtcoef, cfl, lmax)
+        nrep += 1
+        if time.perf_counter() - t0 >= min(args.cpu_seconds, 10.0) and nrep >= 2:
+            break
+    cpu_ms = (time.perf_counter() - t0) / nrep * 1e3
+    err = float(np.abs(out - ref).max() / np.abs(ref).max())
+    steps = lmax * (im + jm - 1)
+    cells = im * jm
+    nbytes = 8 * (2 * 5 * (im + 6) * (jm + 6) + 4 * (im + 7) * (jm + 7) + 3 * (im + 6) * (jm + 6) + 5 * (im + 6) * (jm + 6))
+    line = {"workload": "impli", "metric": "impli_matrix_free_2d calls/s (lmax 10, BL 400x150)", "unit": "calls/s",
+            "value": 1e3 / ms, "ms_per_step": ms, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "boundary layer %dx%d, residual as right-hand side, lmax %d, cfl %g, dtcoef %g"
+                                   % (im, jm, lmax, cfl, dtcoef), "l2": "flushed between steps (256 MB write)"},
+            "latency": {"dependent_diagonal_steps": steps, "us_per_step": ms * 1e3 / steps,
+                        "note": "each sweep is im + jm - 1 dependent anti-diagonal steps; one cluster barrier "
+                                "per step"},
+            "roofline": {"bound": "hbm", "achieved": nbytes / (ms / 1e3) / 1e9, "peak": _hbm_peak(), "unit": "GB/s",
+                         "frac": nbytes / (ms / 1e3) / 1e9 / _hbm_peak(), "traffic": None,
+                         "note": "formal: latency-bound wavefront (see latency), not bandwidth-bound"},
+            "e2e": {"value": 1e3 / e2e_ms, "unit": "calls/s", "h2d_bytes_per_step": int(nbytes - 8 * 5 * (im + 6) * (jm + 6)),
+                    "d2h_bytes_per_step": int(8 * 5 * (im + 6) * (jm + 6)), "ms_per_step": e2e_ms},
+            "cpu_baseline": {"value": 1e3 / cpu_ms, "unit": "calls/s", "cores": 1, "kind": "port",
+                             "sample": "%d oracle calls (sequential sweeps, the reference's loop order), %.1f ms each"
+                                       % (nrep, cpu_ms)},
+            "parity": {"max_abs_err_rel_to_max": err, "tolerance": 1e-12, "cells": cells},
+            "gpu_launches": 5 * args.steps}  # cells, faces, diag, sweeps, out
+    print(json.dumps(line))
+    return 0
+
+
+def _hbm_peak():
+    try:
+        return float(json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")))["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
+
+
 def ctypes_double():
     return np.zeros(1)
 
@@ -626,7 +719,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--workload", default="residual-jvp", choices=["residual-jvp", "jacobian", "batch"],
+    ap.add_argument("--workload", default="residual-jvp", choices=["residual-jvp", "jacobian", "batch", "impli"],
                     help="residual-jvp: the 256x256 cylinder line (default); jacobian: the batched "
                          "Jacobian / Dz / Dzz / J(beta) assembly of the 1024x512 boundary layer; batch: "
                          "residual + JVP of 64 uneven boundary-layer grids in one graph")
@@ -636,6 +729,8 @@ def main():
     args = ap.parse_args()
     if args.workload == "jacobian":
         return run_jacobian_workload(args)
+    if args.workload == "impli":
+        return run_impli_workload(args)
     if args.workload == "batch":
         return run_batch_workload(args)
     if args.impl == "reference":

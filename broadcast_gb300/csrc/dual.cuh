@@ -22,6 +22,16 @@ struct DK {
 
 #define BCG_HD __device__ __forceinline__
 
+// 1/x correctly rounded (round to nearest): the device intrinsic, which
+// yields the same value as the IEEE division 1.0/x with a shorter sequence
+BCG_HD double rcp_rn(double x) {
+#ifdef __CUDA_ARCH__
+  return __drcp_rn(x);
+#else
+  return 1.0 / x;
+#endif
+}
+
 template <int K> BCG_HD DK<K> mkc(double x) { DK<K> r; r.v = x;
 #pragma unroll
   for (int k = 0; k < K; ++k) r.d[k] = 0.0; return r; }
@@ -44,7 +54,7 @@ template <int K> BCG_HD DK<K> operator*(const DK<K>& a, const DK<K>& b) { DK<K> 
 // Divisions take one IEEE reciprocal, shared by the value and the tangents
 // (the value a * (1/b) is within an ulp of a / b).
 template <int K> BCG_HD DK<K> operator/(const DK<K>& a, const DK<K>& b) {
-  DK<K> r; const double inv = 1.0 / b.v; r.v = a.v * inv;
+  DK<K> r; const double inv = rcp_rn(b.v); r.v = a.v * inv;
 #pragma unroll
   for (int k = 0; k < K; ++k) r.d[k] = fma(-r.v, b.d[k], a.d[k]) * inv; return r; }
 
@@ -60,11 +70,11 @@ template <int K> BCG_HD DK<K> operator*(const DK<K>& a, double b) { DK<K> r; r.v
 template <int K> BCG_HD DK<K> operator*(double a, const DK<K>& b) { DK<K> r; r.v = a * b.v;
 #pragma unroll
   for (int k = 0; k < K; ++k) r.d[k] = a * b.d[k]; return r; }
-template <int K> BCG_HD DK<K> operator/(const DK<K>& a, double b) { DK<K> r; const double inv = 1.0 / b; r.v = a.v * inv;
+template <int K> BCG_HD DK<K> operator/(const DK<K>& a, double b) { DK<K> r; const double inv = rcp_rn(b); r.v = a.v * inv;
 #pragma unroll
   for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * inv; return r; }
 template <int K> BCG_HD DK<K> operator/(double a, const DK<K>& b) {
-  DK<K> r; const double inv = 1.0 / b.v; r.v = a * inv; const double s = -r.v * inv;
+  DK<K> r; const double inv = rcp_rn(b.v); r.v = a * inv; const double s = -r.v * inv;
 #pragma unroll
   for (int k = 0; k < K; ++k) r.d[k] = s * b.d[k]; return r; }
 
@@ -73,7 +83,7 @@ template <int K> BCG_HD bool operator<(const DK<K>& a, double b) { return a.v < 
 template <int K> BCG_HD bool operator<(double a, const DK<K>& b) { return a < b.v; }
 
 template <int K> BCG_HD DK<K> sqrt_t(const DK<K>& a) { DK<K> r; r.v = sqrt(a.v);
-  const double s = (a.v == 0.0) ? 0.0 : 0.5 / r.v;
+  const double s = (a.v == 0.0) ? 0.0 : 0.5 * rcp_rn(r.v);  // = 0.5/r.v exactly
 #pragma unroll
   for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * s; return r; }
 BCG_HD double sqrt_t(double a) { return sqrt(a); }
