@@ -613,7 +613,7 @@ def run_impli_workload(args):
     from broadcast_gb300.operator import to_device
     from broadcast_gb300.srcfv import f_lhs, f_sch
     from oracle import oracle as O
-    im, jm, lmax, cfl, dtcoef = args.im or 400, args.jm or 150, 10, 5.0, 1.0
+    im, jm, lmax, cfl, dtcoef = args.im or 400, args.jm or 150, args.lmax, 5.0, 1.0
     c = cases.bl_case(im, jm, seed=0, ops=LibOps)
     bl_bcs(c, c["w"])
     g, ph = c["grid"], c["phys"]
@@ -666,7 +666,8 @@ def run_impli_workload(args):
     steps = lmax * (im + jm - 1)
     cells = im * jm
     nbytes = 8 * (2 * 5 * (im + 6) * (jm + 6) + 4 * (im + 7) * (jm + 7) + 3 * (im + 6) * (jm + 6) + 5 * (im + 6) * (jm + 6))
-    line = {"workload": "impli", "metric": "impli_matrix_free_2d calls/s (lmax 10, BL 400x150)", "unit": "calls/s",
+    line = {"workload": "impli", "metric": "impli_matrix_free_2d calls/s (lmax %d, BL %dx%d)" % (lmax, im, jm),
+            "unit": "calls/s",
             "value": 1e3 / ms, "ms_per_step": ms, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "boundary layer %dx%d, residual as right-hand side, lmax %d, cfl %g, dtcoef %g"
                                    % (im, jm, lmax, cfl, dtcoef), "l2": "flushed between steps (256 MB write)"},
@@ -719,6 +720,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--lmax", type=int, default=10, help="impli workload: Gauss-Seidel sweeps per call")
     ap.add_argument("--workload", default="residual-jvp", choices=["residual-jvp", "jacobian", "batch", "impli"],
                     help="residual-jvp: the 256x256 cylinder line (default); jacobian: the batched "
                          "Jacobian / Dz / Dzz / J(beta) assembly of the 1024x512 boundary layer; batch: "
