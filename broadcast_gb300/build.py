@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libbroadcast_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CU_SOURCES = ["residual.cu", "bc.cu", "assembly.cu", "runtime.cu", "api.cu", "calib.cu", "noalloc.cu", "adjoint.cu", "jacobian.cu", "span.cu", "batch.cu", "schemes.cu", "impli.cu"]
+CU_SOURCES = ["residual.cu", "bc.cu", "assembly.cu", "runtime.cu", "api.cu", "calib.cu", "noalloc.cu", "adjoint.cu", "jacobian.cu", "span.cu", "batch.cu", "schemes.cu", "impli.cu", "bandlu.cu"]
 CPP_SOURCES = ["host.cpp"]
 
 
@@ -71,7 +71,7 @@ def build(verbose=False, force=False):
                 if verbose and out:
                     sys.stdout.write(out)
     if force or jobs or _stale(LIB, objs):
-        _run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lcudart"])
+        _run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lcudart", "-lcublas", "-lcusolver"])
     return LIB
 
 

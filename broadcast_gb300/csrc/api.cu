@@ -18,6 +18,7 @@
 #include "span.h"
 #include "batch.h"
 #include "impli.h"
+#include "bandlu.h"
 
 using namespace bcg;
 
@@ -421,6 +422,30 @@ BCG_DNC_ENTRIES(3)
 BCG_DNC_ENTRIES(7)
 BCG_DNC_ENTRIES(9)
 #undef BCG_DNC_ENTRIES
+
+// ---- Newton linear solve (BROADCAST_npz.py:1146-1158; MUMPS LU there) -----------
+// x = A^-1 b for the n x n CSR matrix A (int32 indptr/indices, nnz entries,
+// duplicates summed) by band LU with partial pivoting on the GPU; nb is the
+// block size (0: 128).  Returns BCG_ERR_SINGULAR with *info = first zero pivot
+// (1-based) for a singular matrix.
+int bcg_csr_band_lu_solve(int n, const int* indptr, const int* indices, const double* data, long long nnz,
+                          const double* b, double* x, int nb, int* info) {
+  if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
+  if (n < 1 || nnz < 0 || !indptr || !indices || !data || !b || !x) return fail_arg("csr_band_lu_solve: bad arguments");
+  cudaStream_t st = current_stream();
+  Stager sg(st);
+  const int hp = sg.in(indptr, (size_t)(n + 1) * 4), hi = sg.in(indices, (size_t)nnz * 4);
+  const int hd = sg.in(data, (size_t)nnz * 8), hb = sg.in(b, (size_t)n * 8), hx = sg.out(x, (size_t)n * 8);
+  int rc = sg.commit();
+  if (rc) return rc;
+  BandLuInfo bi{};
+  const int r = band_lu_solve(n, sg.dev<int>(hp), sg.dev<int>(hi), sg.dev<double>(hd), sg.dev<double>(hb),
+                              sg.dev<double>(hx), nb > 0 ? nb : 128, st, &bi);
+  if (info) *info = bi.info;
+  if (r == 1) return fail_arg("csr_band_lu_solve: singular matrix"), BCG_ERR_SINGULAR;
+  if (r != 0) return fail_arg(band_lu_error()), BCG_ERR_CUDA;
+  return sg.finish();
+}
 
 // ---- matrix-free implicit phase (srcfv/lhs/impli_matrix_free.F90:7) -------------
 // dwi (intent inout in the reference, fully overwritten: interior = the

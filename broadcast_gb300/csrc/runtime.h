@@ -14,6 +14,7 @@ enum {
   BCG_ERR_CUDA = -2,    // a CUDA call failed (see bcg_last_error_string)
   BCG_ERR_NOMEM = -3,   // device allocation failed
   BCG_ERR_NODEV = -4,   // no usable CUDA device
+  BCG_ERR_SINGULAR = -5,  // the linear solve met a zero pivot
 };
 
 cudaStream_t current_stream();

@@ -1,0 +1,34 @@
+"""Linear solves of the Newton iteration on the GPU.
+
+The reference factorises the Newton matrix with PETSc/MUMPS on the host
+(BROADCAST_npz.py:1146-1158, misc/PETSc_func.py:137-152).  `band_lu_solve`
+factorises it on the GPU instead: the boundary-layer Jacobian rows are ordered
+(i, j, e) with i slowest, so the matrix is banded with bandwidth ~15 jm, and a
+blocked band LU with partial pivoting (bcg_csr_band_lu_solve) is a direct
+solve of the same accuracy class as MUMPS's LU.  It needs 8 n (3 kl + ku + 2 nb
++ 1) bytes of device memory (17 GB for the 400 x 150 boundary layer).
+"""
+import numpy as np
+
+from . import _lib
+
+
+def band_lu_solve(A, b, nb=128):
+    """x = A^-1 b for a scipy sparse matrix A (converted to CSR) and vector b.
+
+    Raises RuntimeError for a singular matrix (as scipy's splu does)."""
+    A = A.tocsr()
+    n = A.shape[0]
+    indptr = np.ascontiguousarray(A.indptr, dtype=np.int32)
+    indices = np.ascontiguousarray(A.indices, dtype=np.int32)
+    data = np.ascontiguousarray(A.data, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(n)
+    info = np.zeros(1, np.int32)
+    try:
+        _lib.call("bcg_csr_band_lu_solve", n, indptr, indices, data, int(A.nnz), b, x, int(nb), info)
+    except _lib.BroadcastError as e:
+        if "singular" in str(e):
+            raise RuntimeError("singular matrix (zero pivot at row %d)" % int(info[0])) from e
+        raise
+    return x

@@ -12,14 +12,16 @@ Per iteration, as the reference:
   5. solve J dw = R (:1146-1158: PETSc LU with MUMPS there) and w += dw,
      stepping back and halving cfl when dw is not finite (:1167-1172).
 Steps 1, 2 and 4 run on the GPU through the library; step 5 calls `solver`,
-by default a SuperLU factorisation (scipy), the only sparse direct solver in
-this image; a PETSc/MUMPS or cuDSS solve can be passed in its place.
+by default the GPU band LU (broadcast_gb300.linsolve.band_lu_solve: the
+Jacobian is banded with bandwidth ~15 jm in its (i, j, e) row order);
+`superlu_solve` (scipy, host) or a PETSc/MUMPS solve can be passed instead.
 """
 import time
 
 import numpy as np
 
 from . import _lib
+from .linsolve import band_lu_solve
 
 PHYS = ("cp", "cv", "prandtl", "gam", "rgaz", "cs", "muref", "tref", "s_suth", "k2", "k4")
 
@@ -34,7 +36,7 @@ class BLNewton:
     cfl = 1e10 is the boundary-layer card's setting (card_bl2d_fv_npz.py:56):
     the relaxation vanishes and the iteration is Newton's."""
 
-    def __init__(self, case, cfl=1.0e10, mach=None, solver=superlu_solve):
+    def __init__(self, case, cfl=1.0e10, mach=None, solver=band_lu_solve):
         from ._f2py import interf4
         _lib.load()
         self.c = case

@@ -19,7 +19,8 @@
  *    "Jlo", "Jhi" (3 characters, no terminator needed).  These small index
  *    arrays are always host pointers.
  *  - Every function returns 0 on success or a negative code: -1 bad arguments,
- *    -2 CUDA failure, -3 device allocation failure, -4 no CUDA device.
+ *    -2 CUDA failure, -3 device allocation failure, -4 no CUDA device, -5 a
+ *    singular matrix in the linear solve.
  *    bcg_last_error_string() describes the last failure of the calling thread.
  *  - Trailing dimension arguments that f2py infers from array shapes (lm, em,
  *    nbentry) are explicit here.
@@ -137,6 +138,19 @@ int bcg_flux_num_dnc9_nowall_2d_d(double* residu, double* residud, const double*
     const double* y0, const double* nx, const double* ny, const double* xc, const double* yc, const double* vol,
     const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs, double muref,
     double tref, double s_suth, double k2, double k4, int im, int jm);
+
+/* The linear solve of the SER Newton iteration (BROADCAST_npz.py:1146-1158,
+ * where the reference factorises J with PETSc/MUMPS, misc/PETSc_func.py:137-152):
+ * x = A^-1 b for the n x n CSR matrix A (int32 indptr[n+1] and indices[nnz],
+ * double data[nnz]; duplicates summed) by band LU with partial pivoting on the
+ * GPU (LAPACK's blocked dgbtrf/dgbtrs algorithm through cuSOLVER getrf panels
+ * and cuBLAS trsm/gemm on views of the band storage, which takes
+ * 8 n (3 kl + ku + 2 nb + 1) bytes of device memory for bandwidths kl, ku).
+ * nb: block size (0: 128).  Returns -5 with *info = the first zero pivot
+ * (1-based) for a singular matrix.  No reference counterpart in f2py: the
+ * reference calls PETSc here. */
+int bcg_csr_band_lu_solve(int n, const int* indptr, const int* indices, const double* data, long long nnz,
+                          const double* b, double* x, int nb, int* info);
 
 /* srcfv/lhs/impli_matrix_free.F90:7 (IMPLI_MATRIX_FREE_2D): the implicit phase
  * of the 'impli' time marching (BROADCAST_npz.py:911-941): lmax symmetric
