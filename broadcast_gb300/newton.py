@@ -89,6 +89,7 @@ class BLNewton:
         t0 = time.perf_counter()
         self.fill(w)
         res, norm, ninf = self.residual(w)
+        t1 = time.perf_counter()
         if first:
             self.norm0m1 = 1.0 / np.maximum(norm, 1e-15)
             self.ninf0m1 = 1.0 / np.maximum(ninf, 1e-15)
@@ -97,6 +98,7 @@ class BLNewton:
         gh = self.gh
         coefdiag = cflm1 * self.c["grid"]["vol"][gh:-gh, gh:-gh]
         J = self.jacobian(w, coefdiag)
+        t2 = time.perf_counter()
         try:
             dw = np.reshape(self.solver(J, np.ravel(res[gh:-gh, gh:-gh, :])), (self.im, self.jm, 5))
         except RuntimeError:  # singular factorisation: treated like a non-finite update
@@ -111,8 +113,9 @@ class BLNewton:
                 w[gh:-gh, gh:-gh, :] -= self.dw_old
             self.cfl /= 2.0
             self.dt /= 2.0
-        self.history.append(dict(norm=norm.tolist(), cflm1=float(cflm1), nnz=int(J.nnz),
-                                 seconds=time.perf_counter() - t0))
+        t3 = time.perf_counter()
+        self.history.append(dict(norm=norm.tolist(), cflm1=float(cflm1), nnz=int(J.nnz), seconds=t3 - t0,
+                                 seconds_residual=t1 - t0, seconds_jacobian=t2 - t1, seconds_solve=t3 - t2))
         return norm, dw
 
     def solve(self, w, ite=50, tol=1e-10):
