@@ -73,7 +73,19 @@ def _resolve_includes(path, inc_root):
     return "".join(out)
 
 
-def build(ref_root=DEFAULT_REF, routines=ROUTINES, verbose=False):
+def _up_to_date():
+    so = os.path.join(OUT, "libref.so")
+    if not (os.path.exists(so) and os.path.exists(os.path.join(OUT, "signatures.json"))):
+        return False
+    t = os.path.getmtime(so)
+    return all(os.path.getmtime(os.path.join(HERE, f)) < t for f in ("ref_translate.py", "ref_build.py"))
+
+
+def build(ref_root=DEFAULT_REF, routines=ROUTINES, verbose=False, force=False):
+    """Translate and compile; skipped when oracle/_ref is newer than the
+    translator and this routine list (the reference sources do not change)."""
+    if not force and routines is ROUTINES and _up_to_date():
+        return os.path.join(OUT, "libref.so"), []
     sys.path.insert(0, HERE)
     import ref_translate as rt
     if not os.path.isdir(ref_root):
@@ -117,5 +129,5 @@ def build(ref_root=DEFAULT_REF, routines=ROUTINES, verbose=False):
 
 
 if __name__ == "__main__":
-    so, fails = build(sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REF, verbose=True)
+    so, fails = build(sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REF, verbose=True, force=True)
     print(so)
