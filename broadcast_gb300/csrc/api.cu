@@ -66,33 +66,42 @@ cudaError_t copy_interior_d2h(double* host, const double* dev, int ni, int nj, i
   return cudaSuccess;
 }
 
-// Host tangents and outputs of many directions: the directions run in two
-// chunks of whole 4-direction groups; chunk c's upload (copy stream in), its
-// residual passes (library stream) and its download (copy stream out) overlap
-// the other chunk's.  Uploads start only after the library stream's earlier
-// work, since the pool buffers they fill may still be in use.
+// Host tangents and outputs of many directions: the directions run in up to
+// four chunks of whole 4-direction groups; chunk c's upload (copy stream in),
+// its residual passes (library stream) and its download (copy stream out)
+// overlap the other chunks'.  Only the first chunk's upload and the last
+// chunk's download are exposed, so more chunks shrink them, while each launch
+// still covers at least one group per chunk of the residual passes.  Uploads
+// start only after the library stream's earlier work, since the pool buffers
+// they fill may still be in use.
 int residual_pipelined(ResidualArgs a, double* res, double* residud, const double* wd, int nd, cudaStream_t st) {
   const int im = a.im, jm = a.jm, gh = a.gh, ni = im + 2 * gh, nj = jm + 2 * gh;
   const size_t plane5 = (size_t)ni * nj * 5;
   CopyStreams cs;
   int rc = copy_streams(&cs);
   if (rc) return rc;
+  constexpr int kMaxChunk = 4;
+  const int ng = nd / 4;
+  const int nch = std::max(1, std::min(kMaxChunk, ng));
+  int bounds[kMaxChunk + 1];
+  for (int c = 0; c < nch; ++c) bounds[c] = 4 * (int)((long long)ng * c / nch);
+  bounds[nch] = nd;  // the last chunk also takes the 1-3 directions beyond the groups
+  int gmax = 0;
+  for (int c = 0; c < nch; ++c) gmax = std::max(gmax, (bounds[c + 1] - bounds[c]) / 4);
   double* wd_dev = (double*)pool_get(POOL_AUX, plane5 * nd * sizeof(double));
   double* rd_dev = (double*)pool_get(POOL_STAGE_OUT, plane5 * nd * sizeof(double));
-  const int ng = nd / 4;
-  const int split = 4 * ((ng + 1) / 2);  // directions of the first chunk
-  const int bounds[3] = {0, split, nd};
   const size_t s4 = residual_scratch_doubles(im, jm, gh, 4);
-  double* scr = (double*)pool_get(POOL_SCRATCH, s4 * 8 * (size_t)((ng + 1) / 2) + residual_scratch_doubles(im, jm, gh, 2) * 8);
+  double* scr = (double*)pool_get(POOL_SCRATCH, s4 * 8 * (size_t)std::max(gmax, 1) + residual_scratch_doubles(im, jm, gh, 2) * 8);
   if (!wd_dev || !rd_dev || !scr) return fail_arg("scratch allocation failed"), BCG_ERR_NOMEM;
-  cudaEvent_t ev[6] = {};
+  constexpr int kEv = 2 * kMaxChunk + 2;
+  cudaEvent_t ev[kEv] = {};  // 0: start; 1 + c: chunk c uploaded; 1 + nch + c: chunk c computed; last: downloads done
   for (auto& x : ev)
     if (cudaEventCreateWithFlags(&x, cudaEventDisableTiming) != cudaSuccess) return fail_cuda("events", cudaGetLastError());
-  struct Guard { cudaEvent_t* e; ~Guard() { for (int k = 0; k < 6; ++k) if (e[k]) cudaEventDestroy(e[k]); } } guard{ev};
+  struct Guard { cudaEvent_t* e; ~Guard() { for (int k = 0; k < kEv; ++k) if (e[k]) cudaEventDestroy(e[k]); } } guard{ev};
   cudaError_t e = cudaEventRecord(ev[0], st);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(cs.in, ev[0], 0);
   if (e != cudaSuccess) return fail_cuda("pipelined residual", e);
-  for (int c = 0; c < 2; ++c) {
+  for (int c = 0; c < nch; ++c) {
     const int d0 = bounds[c], d1 = bounds[c + 1];
     if (d1 <= d0) continue;
     e = cudaMemcpyAsync(wd_dev + plane5 * d0, wd + plane5 * d0, plane5 * (d1 - d0) * sizeof(double),
@@ -111,14 +120,14 @@ int residual_pipelined(ResidualArgs a, double* res, double* residud, const doubl
       if (e != cudaSuccess) return fail_cuda("flux_num_dnc5_2d_d", e);
       k0 += kk * a.ngroup;
     }
-    e = cudaEventRecord(ev[3 + c], st);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs.out, ev[3 + c], 0);
+    e = cudaEventRecord(ev[1 + nch + c], st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs.out, ev[1 + nch + c], 0);
     if (e == cudaSuccess)
       e = copy_interior_d2h(residud + plane5 * d0, rd_dev + plane5 * d0, ni, nj, 5 * (d1 - d0), gh, im, jm, cs.out);
     if (e != cudaSuccess) return fail_cuda("pipelined residual: download", e);
   }
-  e = cudaEventRecord(ev[5], cs.out);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev[5], 0);
+  e = cudaEventRecord(ev[kEv - 1], cs.out);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev[kEv - 1], 0);
   return e == cudaSuccess ? BCG_OK : fail_cuda("pipelined residual", e);
 }
 

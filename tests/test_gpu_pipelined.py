@@ -1,6 +1,6 @@
 """The host-array JVP path with many directions (bcg_flux_num_dnc5_2d_dn with
-numpy inputs): uploads, residual passes and downloads run pipelined in two
-chunks on separate streams.  Results must equal the device-array path, the
+numpy inputs): uploads, residual passes and downloads run pipelined in up to
+four chunks of whole 4-direction groups on separate streams.  Results must equal the device-array path, the
 ghosts of the host outputs must stay untouched, and back-to-back calls must
 not see each other's buffers."""
 import numpy as np
@@ -28,7 +28,7 @@ def _host_call(c, wd, nd, pinned):
                                                    for k in range(nd)]
 
 
-@pytest.mark.parametrize("nd,pinned", [(8, True), (13, True), (32, False)])
+@pytest.mark.parametrize("nd,pinned", [(8, True), (13, True), (20, True), (32, False)])
 def test_pipelined_host_path_equals_device_path(nd, pinned):
     from broadcast_gb300.operator import Dnc5Operator, to_device, to_host
     import torch
