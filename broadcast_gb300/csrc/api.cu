@@ -435,7 +435,7 @@ BCG_DNC_ENTRIES(9)
 // ---- Newton linear solve (BROADCAST_npz.py:1146-1158; MUMPS LU there) -----------
 // x = A^-1 b for the n x n CSR matrix A (int32 indptr/indices, nnz entries,
 // duplicates summed) by band LU with partial pivoting on the GPU; nb is the
-// block size (0: 128).  Returns BCG_ERR_SINGULAR with *info = first zero pivot
+// block size (0: 256).  Returns BCG_ERR_SINGULAR with *info = first zero pivot
 // (1-based) for a singular matrix.
 int bcg_csr_band_lu_solve(int n, const int* indptr, const int* indices, const double* data, long long nnz,
                           const double* b, double* x, int nb, int* info) {
@@ -449,7 +449,7 @@ int bcg_csr_band_lu_solve(int n, const int* indptr, const int* indices, const do
   if (rc) return rc;
   BandLuInfo bi{};
   const int r = band_lu_solve(n, sg.dev<int>(hp), sg.dev<int>(hi), sg.dev<double>(hd), sg.dev<double>(hb),
-                              sg.dev<double>(hx), nb > 0 ? nb : 128, st, &bi);
+                              sg.dev<double>(hx), nb > 0 ? nb : 256, st, &bi);
   if (info) *info = bi.info;
   if (r == 1) return fail_arg("csr_band_lu_solve: singular matrix"), BCG_ERR_SINGULAR;
   if (r != 0) return fail_arg(band_lu_error()), BCG_ERR_CUDA;

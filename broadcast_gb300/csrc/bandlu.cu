@@ -77,8 +77,10 @@ __global__ void k_swap_vec(double* __restrict__ b, const int* __restrict__ ipiv,
 }
 
 struct Handles {
-  cublasHandle_t blas = nullptr;
+  cublasHandle_t blas = nullptr;    // on the caller's stream (panel path)
+  cublasHandle_t blas_b = nullptr;  // on the trailing-update stream
   cusolverDnHandle_t sol = nullptr;
+  cudaStream_t sb = nullptr;        // trailing-update stream
 };
 Handles g_h;
 
@@ -86,7 +88,12 @@ const char* g_err = "";
 
 bool handles() {
   if (!g_h.blas && cublasCreate(&g_h.blas) != CUBLAS_STATUS_SUCCESS) { g_err = "cublasCreate failed"; return false; }
+  if (!g_h.blas_b && cublasCreate(&g_h.blas_b) != CUBLAS_STATUS_SUCCESS) { g_err = "cublasCreate failed"; return false; }
   if (!g_h.sol && cusolverDnCreate(&g_h.sol) != CUSOLVER_STATUS_SUCCESS) { g_err = "cusolverDnCreate failed"; return false; }
+  if (!g_h.sb && cudaStreamCreateWithFlags(&g_h.sb, cudaStreamNonBlocking) != cudaSuccess) {
+    g_err = "stream creation failed";
+    return false;
+  }
   return true;
 }
 
@@ -100,8 +107,11 @@ int band_lu_solve(int n, const int* indptr, const int* indices, const double* da
   if (n < 1) { g_err = "empty system"; return -1; }
   if (!handles()) return -1;
   cublasSetStream(g_h.blas, st);
+  cublasSetStream(g_h.blas_b, g_h.sb);
   cusolverDnSetStream(g_h.sol, st);
   cublasSetPointerMode(g_h.blas, CUBLAS_POINTER_MODE_HOST);
+  cublasSetPointerMode(g_h.blas_b, CUBLAS_POINTER_MODE_HOST);
+  cudaEvent_t ev_a = nullptr, ev_b = nullptr;  // panel done (stream st), trailing update done (stream sb)
   int* d_klku = nullptr;
   int* d_ipiv = nullptr;
   int* d_info = nullptr;
@@ -134,29 +144,53 @@ int band_lu_solve(int n, const int* indptr, const int* indices, const double* da
     if (cusolverDnDgetrf_bufferSize(g_h.sol, std::min(kl + nb, n), nb, D(0, 0), (int)ldd, &lwork) !=
         CUSOLVER_STATUS_SUCCESS) { fail("getrf buffer size failed"); break; }
     if (cudaMalloc(&work, (size_t)std::max(lwork, 1) * sizeof(double)) != cudaSuccess) { fail("allocation failed"); break; }
-    // factorisation
+    // factorisation, with a lookahead of one panel: on the caller's stream the
+    // panel is factorised and the NEXT panel's columns are updated (swaps,
+    // trsm, gemm), on the second stream the rest of the trailing columns; the
+    // next panel's factorisation then overlaps this step's large trailing
+    // gemm.  The operations and their operands are those of the plain
+    // right-looking order, split over disjoint column sets.
+    if (cudaEventCreateWithFlags(&ev_a, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev_b, cudaEventDisableTiming) != cudaSuccess) { fail("event creation failed"); break; }
     int first_singular = 0;
     const double one = 1.0, mone = -1.0;
+    // the swaps, trsm and gemm of panel (j0, jb, m) on columns [c0, c0 + nc)
+    auto update = [&](cublasHandle_t h, cudaStream_t s, int j0, int jb, int m, int c0, int nc) -> bool {
+      if (nc <= 0) return true;
+      k_laswp<<<(nc + 127) / 128, 128, 0, s>>>(D(j0, c0), ldd, nc, d_ipiv + j0, jb);
+      if (cublasDtrsm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_UNIT, jb, nc, &one,
+                      D(j0, j0), (int)ldd, D(j0, c0), (int)ldd) != CUBLAS_STATUS_SUCCESS) { fail("trsm failed"); return false; }
+      if (m > jb && cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, m - jb, nc, jb, &mone, D(j0 + jb, j0), (int)ldd,
+                                D(j0, c0), (int)ldd, &one, D(j0 + jb, c0), (int)ldd) != CUBLAS_STATUS_SUCCESS) {
+        fail("gemm failed");
+        return false;
+      }
+      return true;
+    };
     for (int j0 = 0; j0 < n && rc == 0; j0 += nb) {
       const int jb = std::min(nb, n - j0);
       const int m = std::min(kl + jb, n - j0);
+      // panel j0 has all its updates: from the previous step's lookahead (this stream)
       if (cusolverDnDgetrf(g_h.sol, m, jb, D(j0, j0), (int)ldd, work, d_ipiv + j0, d_info) != CUSOLVER_STATUS_SUCCESS) {
         fail("getrf failed");
         break;
       }
       k_note_info<<<1, 1, 0, st>>>(d_info, d_klku + 2, j0);
       const int ncol = std::min(n - j0 - jb, kl + ku);
-      if (ncol > 0) {
-        k_laswp<<<(ncol + 127) / 128, 128, 0, st>>>(D(j0, j0 + jb), ldd, ncol, d_ipiv + j0, jb);
-        if (cublasDtrsm(g_h.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_UNIT, jb, ncol, &one,
-                        D(j0, j0), (int)ldd, D(j0, j0 + jb), (int)ldd) != CUBLAS_STATUS_SUCCESS) { fail("trsm failed"); break; }
-        if (m > jb &&
-            cublasDgemm(g_h.blas, CUBLAS_OP_N, CUBLAS_OP_N, m - jb, ncol, jb, &mone, D(j0 + jb, j0), (int)ldd,
-                        D(j0, j0 + jb), (int)ldd, &one, D(j0 + jb, j0 + jb), (int)ldd) != CUBLAS_STATUS_SUCCESS) {
-          fail("gemm failed");
-          break;
-        }
-      }
+      const int nnext = std::min(ncol, nb);  // the next panel's columns
+      // the rest of the trailing columns waits for this panel and runs on the second stream
+      cudaEventRecord(ev_a, st);
+      cudaStreamWaitEvent(g_h.sb, ev_a, 0);
+      if (!update(g_h.blas_b, g_h.sb, j0, jb, m, j0 + jb + nnext, ncol - nnext)) break;
+      // the next panel's columns were last updated by the previous step's rest
+      // (recorded in ev_b before this step's rest was queued)
+      if (j0 > 0) cudaStreamWaitEvent(st, ev_b, 0);
+      if (!update(g_h.blas, st, j0, jb, m, j0 + jb, nnext)) break;
+      cudaEventRecord(ev_b, g_h.sb);
+    }
+    if (rc == 0) {  // join the second stream
+      cudaEventRecord(ev_b, g_h.sb);
+      cudaStreamWaitEvent(st, ev_b, 0);
     }
     if (rc) break;
     if (cudaMemcpyAsync(&first_singular, d_klku + 2, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
@@ -196,6 +230,8 @@ int band_lu_solve(int n, const int* indptr, const int* indices, const double* da
   } while (false);
   const cudaError_t e = cudaStreamSynchronize(st);
   if (e != cudaSuccess && rc == 0) { g_err = cudaGetErrorString(e); rc = -1; }
+  if (ev_a) cudaEventDestroy(ev_a);
+  if (ev_b) cudaEventDestroy(ev_b);
   cudaFree(work);
   cudaFree(d_info);
   cudaFree(d_ipiv);

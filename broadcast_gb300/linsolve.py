@@ -7,13 +7,16 @@ factorises it on the GPU instead: the boundary-layer Jacobian rows are ordered
 blocked band LU with partial pivoting (bcg_csr_band_lu_solve) is a direct
 solve of the same accuracy class as MUMPS's LU.  It needs 8 n (3 kl + ku + 2 nb
 + 1) bytes of device memory (17 GB for the 400 x 150 boundary layer).
+The trailing updates are DGEMMs of kl x (kl + ku) x nb, which cuBLAS runs at
+~1.05 TFLOP/s on GB300 (its FP64 GEMM ceiling is ~1.1), so a factorisation
+costs about 2 n kl (kl + ku) / 1.05e12 s plus the panels.
 """
 import numpy as np
 
 from . import _lib
 
 
-def band_lu_solve(A, b, nb=128):
+def band_lu_solve(A, b, nb=256):
     """x = A^-1 b for a scipy sparse matrix A (converted to CSR) and vector b.
 
     Raises RuntimeError for a singular matrix (as scipy's splu does)."""

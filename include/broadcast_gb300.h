@@ -146,7 +146,7 @@ int bcg_flux_num_dnc9_nowall_2d_d(double* residu, double* residud, const double*
  * GPU (LAPACK's blocked dgbtrf/dgbtrs algorithm through cuSOLVER getrf panels
  * and cuBLAS trsm/gemm on views of the band storage, which takes
  * 8 n (3 kl + ku + 2 nb + 1) bytes of device memory for bandwidths kl, ku).
- * nb: block size (0: 128).  Returns -5 with *info = the first zero pivot
+ * nb: block size (0: 256).  Returns -5 with *info = the first zero pivot
  * (1-based) for a singular matrix.  No reference counterpart in f2py: the
  * reference calls PETSc here. */
 int bcg_csr_band_lu_solve(int n, const int* indptr, const int* indices, const double* data, long long nnz,
