@@ -67,6 +67,7 @@ struct AdjCtx {
     if (i == 0) return 2.0 * g(1, j) - g(2, j);
     if (i == e.im + 1) return 2.0 * g(e.im, j) - g(e.im - 1, j);
     if (j == e.jm + 1) return 2.0 * g(i, e.jm) - g(i, e.jm - 1);
+    if (j == 0) return 2.0 * g(i, 1) - g(i, 2);  // no-wall j-faces at j = 1
     return g(i, j);
   }
   BCG_HD double NX(int i, int j, int d) const { return __ldg(nx + (size_t)(d - 1) * e.nn() + e.nidx(i, j)); }
@@ -352,7 +353,7 @@ BCG_HD void face_rev(const AdjCtx& a, int dir, int i, int j, double* __restrict_
   for (int k = 0; k < 4; ++k) put(R_SP + k, spb[k]);
   for (int k = 0; k < 8; ++k) put(R_SG + k, sgb[k]);
   // ---- viscous: h_e -= (fv nxloc + gv nyloc) sn, e = 2..5
-  const bool o2 = (dir == 1) ? (j <= 2) : (j == 2);
+  const bool o2 = a.c.wall && ((dir == 1) ? (j <= 2) : (j == 2));
   ViscPts vp;
   if (dir == 1) visc_points_i(a, i, j, o2, vp); else visc_points_j(a, i, j, o2, vp);
   double g8[8];
@@ -407,7 +408,7 @@ __global__ void __launch_bounds__(128) k_adj_faces(AdjCtx a) {
   const int i = 1 + t % nI, j = 1 + t / nI;
   if (j <= e.jm) face_rev(a, 1, i, j, a.rec1, a.nn, t);
   if (i <= e.im) {
-    if (j == 1) wall_rev(a, i, a.rec2, a.nn, t);
+    if (j == 1 && a.c.wall) wall_rev(a, i, a.rec2, a.nn, t);
     else face_rev(a, 2, i, j, a.rec2, a.nn, t);
   }
 }
@@ -490,7 +491,7 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
   for (int j = cj - 2; j <= cj + 2; ++j)
     for (int i = ci - 1; i <= ci + 2; ++i) {
       if (!g.ifx(i, j)) continue;
-      const bool o2 = j <= 2;
+      const bool o2 = c.wall && j <= 2;
       const int di = ci - i, dj = cj - j;  // cell offset from the face
       double wN, wS, wE, wO, wuu;
       if (!o2) {
@@ -518,33 +519,35 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
       mub += wuu * g.R1(R_VM + 3, i, j);
     }
   // ---- j-faces -------------------------------------------------------------
-  // Euler: generic faces j >= 4 over rows j-3..j+2; near-wall faces 2, 3 over rows 1..5
+  // Euler: generic faces j >= 4 over rows j-3..j+2; near-wall faces 2, 3 over
+  // rows 1..5 (without the wall: generic faces from j = 1)
+  const int jgen = c.wall ? 4 : 1, jfirst = c.wall ? 2 : 1;
   for (int s = -3; s <= 2; ++s) {
     const int j = cj - s;
-    if (j < 4 || !g.jfx(ci, j)) continue;
+    if (j < jgen || !g.jfx(ci, j)) continue;
     const double we = w_euler(c, s);
     for (int v = 0; v < 5; ++v) { fb[v] += we * g.R2(R_EA + v, ci, j); gb[v] += we * g.R2(R_EB + v, ci, j); }
   }
-  if (cj >= 1 && cj <= 5) {
+  if (c.wall && cj >= 1 && cj <= 5) {
     for (int j = 2; j <= 3; ++j) {
       if (!g.jfx(ci, j)) continue;
       const double we = (j == 3) ? c.c5[cj - 1] : c.c3w[cj - 1];
       for (int v = 0; v < 5; ++v) { fb[v] += we * g.R2(R_EA + v, ci, j); gb[v] += we * g.R2(R_EB + v, ci, j); }
     }
   }
-  // predictor: all j-faces j >= 2
+  // predictor: all j-faces j >= 2 (j >= 1 without the wall)
   for (int s = -3; s <= 2; ++s) {
     const int j = cj - s;
-    if (j < 2 || !g.jfx(ci, j)) continue;
+    if (j < jfirst || !g.jfx(ci, j)) continue;
     const double wp = w_pred(c, s);
     for (int v = 0; v < 5; ++v) wb[v] += wp * g.R2(R_PR + v, ci, j);
   }
-  if (cj >= 2 && g.jfx(ci, cj)) {
+  if (cj >= jfirst && g.jfx(ci, cj)) {
     for (int v = 0; v < 5; ++v) wb[v] += g.R2(R_DF + v, ci, cj);
     wb[0] += g.R2(R_ROE + 4, ci, cj); wb[1] += g.R2(R_ROE + 5, ci, cj); wb[2] += g.R2(R_ROE + 6, ci, cj);
     ub[3] += g.R2(R_ROE + 7, ci, cj);
   }
-  if (cj + 1 >= 2 && g.jfx(ci, cj + 1)) {
+  if (cj + 1 >= jfirst && g.jfx(ci, cj + 1)) {
     for (int v = 0; v < 5; ++v) wb[v] -= g.R2(R_DF + v, ci, cj + 1);
     wb[0] += g.R2(R_ROE + 0, ci, cj + 1); wb[1] += g.R2(R_ROE + 1, ci, cj + 1); wb[2] += g.R2(R_ROE + 2, ci, cj + 1);
     ub[3] += g.R2(R_ROE + 3, ci, cj + 1);
@@ -552,11 +555,11 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
   if (c.k2 != 0.0) {
     for (int k = 0; k < 4; ++k) {
       const int j = cj + 2 - k;
-      if (j >= 2 && g.jfx(ci, j)) pb += g.R2(R_SP + k, ci, j);
+      if (j >= jfirst && g.jfx(ci, j)) pb += g.R2(R_SP + k, ci, j);
     }
   }
   // wall faces (i, 1): p(i,1), p(i,2), mu(i,1), u v w (i,1)
-  if (g.jfx(ci, 1)) {
+  if (c.wall && g.jfx(ci, 1)) {
     if (cj == 1) {
       pb += g.R2(W_P1, ci, 1);
       mub += g.R2(W_MU, ci, 1);
@@ -568,8 +571,8 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
   // viscous j-faces (i, j) with i - ci in [-2, 2] and j - cj in [-1, 2]
   for (int j = cj - 1; j <= cj + 2; ++j)
     for (int i = ci - 2; i <= ci + 2; ++i) {
-      if (j < 2 || !g.jfx(i, j)) continue;
-      const bool o2 = (j == 2);
+      if (j < jfirst || !g.jfx(i, j)) continue;
+      const bool o2 = c.wall && (j == 2);
       const int di = ci - i, dj = cj - j;
       double wN, wS, wE, wO, wuu;
       if (!o2) {
@@ -610,8 +613,10 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
     if (ci == 2) addg(-1.0, nullptr, R_SG + 0, 1, cj, true);
     if (ci == e.im) addg(2.0, nullptr, R_SG + 4, e.im + 1, cj, true);       // ghost i = im+1
     if (ci == e.im - 1) addg(-1.0, nullptr, R_SG + 4, e.im + 1, cj, true);
-    if (cj >= 2) addg(1.0, nullptr, R_SG + 4, ci, cj, false);
-    if (cj + 1 <= e.jm + 1 && cj + 1 >= 2) addg(1.0, nullptr, R_SG + 0, ci, cj + 1, false);
+    if (cj >= jfirst) addg(1.0, nullptr, R_SG + 4, ci, cj, false);
+    if (cj + 1 <= e.jm + 1 && cj + 1 >= jfirst) addg(1.0, nullptr, R_SG + 0, ci, cj + 1, false);
+    if (!c.wall && cj == 1) addg(2.0, nullptr, R_SG + 0, ci, 1, false);   // ghost j = 0 extrapolated
+    if (!c.wall && cj == 2) addg(-1.0, nullptr, R_SG + 0, ci, 1, false);
     if (cj == e.jm) addg(2.0, nullptr, R_SG + 4, ci, e.jm + 1, false);     // ghost j = jm+1
     if (cj == e.jm - 1) addg(-1.0, nullptr, R_SG + 4, ci, e.jm + 1, false);
   }
@@ -717,7 +722,8 @@ size_t adjoint_scratch_doubles(int im, int jm, int gh) {
 
 cudaError_t run_adjoint(const AdjointArgs& a, cudaStream_t st) {
   const Ext e = make_ext(a.im, a.jm, a.gh);
-  const Coef c = make_coef(a.phys);
+  Coef c = make_coef(a.phys);
+  c.wall = a.nowall ? 0 : 1;
   const size_t nn = (size_t)(a.im + 1) * (a.jm + 1);
   double* pr = a.scratch;
   double* gr = pr + (size_t)F_NPRIM * e.np;

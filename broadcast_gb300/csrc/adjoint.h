@@ -17,6 +17,7 @@ struct AdjointArgs {
   double* rb;           // residub (ni, nj, 5): interior read, then zeroed
   double* wb;           // (ni, nj, 5): overwritten on every padded cell
   double* scratch;      // adjoint_scratch_doubles(im, jm, gh) doubles
+  int nowall;           // 1: flux_num_dnc5_nowall_2d_b (centred rows everywhere, no wall face)
 };
 
 size_t adjoint_scratch_doubles(int im, int jm, int gh);

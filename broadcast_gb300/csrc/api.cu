@@ -588,12 +588,39 @@ int bcg_coeffs_5p_dz2_dn(double* dz2_out, const double* w, const double* wd, int
 // ---- adjoint (srcfv/adjoint/flux_num_dnc5_b.f90:15) ------------------------
 // wb = (dR/dw)^T residub on every padded cell (wb overwritten); the interior
 // of residub is zeroed, as the Tapenade routine does.  residu is unused.
+namespace {
+int adjoint_call(double* residub, const double* w, double* wb, const double* nx, const double* ny, const double* vol,
+                 const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs,
+                 double muref, double tref, double s_suth, double k2, double k4, int im, int jm, int nowall);
+}
+
 int bcg_flux_num_dnc5_2d_b(double* residu, double* residub, const double* w, double* wb, const double* x0,
                            const double* y0, const double* nx, const double* ny, const double* xc, const double* yc,
                            const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
                            double gam, double rgaz, double cs, double muref, double tref, double s_suth, double k2,
                            double k4, int im, int jm) {
   (void)residu; (void)x0; (void)y0; (void)xc; (void)yc;
+  return adjoint_call(residub, w, wb, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2,
+                      k4, im, jm, 0);
+}
+
+// srcfv/adjoint/flux_num_dnc5_nowall_b.f90: the adjoint of the scheme without the wall rows
+int bcg_flux_num_dnc5_nowall_2d_b(double* residu, double* residub, const double* w, double* wb, const double* x0,
+                                  const double* y0, const double* nx, const double* ny, const double* xc,
+                                  const double* yc, const double* vol, const double* volf, int gh, double cp,
+                                  double cv, double prandtl, double gam, double rgaz, double cs, double muref,
+                                  double tref, double s_suth, double k2, double k4, int im, int jm) {
+  (void)residu; (void)x0; (void)y0; (void)xc; (void)yc;
+  return adjoint_call(residub, w, wb, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2,
+                      k4, im, jm, 1);
+}
+
+}  // extern "C"
+
+namespace {
+int adjoint_call(double* residub, const double* w, double* wb, const double* nx, const double* ny, const double* vol,
+                 const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs,
+                 double muref, double tref, double s_suth, double k2, double k4, int im, int jm, int nowall) {
   if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
   if (!dims_ok(im, jm, gh)) return fail_arg("flux_num_dnc5_2d_b: need gh == 3 and im, jm >= 6");
   const size_t np = ncell(im, jm, gh), nn = nnode(im, jm, gh);
@@ -610,12 +637,16 @@ int bcg_flux_num_dnc5_2d_b(double* residu, double* residub, const double* w, dou
   a.w = sg.dev<double>(hw); a.nx = sg.dev<double>(hnx); a.ny = sg.dev<double>(hny);
   a.vol = sg.dev<double>(hvol); a.volf = sg.dev<double>(hvolf);
   a.rb = sg.dev<double>(hrb); a.wb = sg.dev<double>(hwb);
+  a.nowall = nowall;
   a.scratch = (double*)pool_get(POOL_SCRATCH, adjoint_scratch_doubles(im, jm, gh) * 8);
   if (!a.scratch) return fail_arg("scratch allocation failed"), BCG_ERR_NOMEM;
   cudaError_t e = run_adjoint(a, st);
   if (e != cudaSuccess) return fail_cuda("flux_num_dnc5_2d_b", e);
   return sg.finish();
 }
+}  // namespace
+
+extern "C" {
 
 // ---- boundary conditions (srcfv/borders/*.F90, srcfv/tangent/bc_*_d.f90) ----
 int bcg_bc_wall_viscous_adia_2d(double* w, const char* loc, double gam, const int* interf, int gh, int im, int jm) {

@@ -3,6 +3,8 @@
 flux_num_dnc5_2d_b       : adjoint/flux_num_dnc5_b.f90:15 -- wb = (dR/dw)^T residub
                            on every padded cell (wb overwritten); the interior
                            of residub is zeroed.
+flux_num_dnc5_nowall_2d_b: adjoint/flux_num_dnc5_nowall_b.f90 -- the same for the
+                           scheme without the wall rows.
 bc_wall_viscous_adia_2d_b: adjoint/bc_wall_viscous_b.f90:11
 bc_no_reflexion_2d_b     : adjoint/bc_no_reflexion_b.f90:16
 bc_supandsubinlet_2d_b   : adjoint/bc_supandsubinlet_b.f90:11
@@ -25,6 +27,17 @@ def flux_num_dnc5_2d_b(residu, residub, w, wb, x0, y0, nx, ny, xc, yc, vol, volf
     call("bcg_flux_num_dnc5_2d_b", None, arr(residub, "residub", True), arr(w, "w"), arr(wb, "wb", True), None, None,
          arr(nx, "nx"), arr(ny, "ny"), None, None, arr(vol, "vol"), arr(volf, "volf"), gh, cp, cv, prandtl, gam, rgaz,
          cs, muref, tref, s_suth, k2, k4, int(im), int(jm))
+
+
+def flux_num_dnc5_nowall_2d_b(residu, residub, w, wb, x0, y0, nx, ny, xc, yc, vol, volf, gh, cp, cv, prandtl, gam,
+                              rgaz, cs, muref, tref, s_suth, k2, k4, im=None, jm=None):
+    """adjoint/flux_num_dnc5_nowall_b.f90: the adjoint of the scheme without the wall rows."""
+    gh = int(gh)
+    if im is None or jm is None:
+        im, jm = dims_from_cell(w, gh)
+    call("bcg_flux_num_dnc5_nowall_2d_b", None, arr(residub, "residub", True), arr(w, "w"), arr(wb, "wb", True), None,
+         None, arr(nx, "nx"), arr(ny, "ny"), None, None, arr(vol, "vol"), arr(volf, "volf"), gh, cp, cv, prandtl, gam,
+         rgaz, cs, muref, tref, s_suth, k2, k4, int(im), int(jm))
 
 
 def bc_wall_viscous_adia_2d_b(w, wb, loc, gam, interf, gh, im=None, jm=None):

@@ -84,6 +84,14 @@ int bcg_flux_num_dnc5_nowall_2d_d(double* residu, double* residud, const double*
                                   double cp, double cv, double prandtl, double gam, double rgaz, double cs,
                                   double muref, double tref, double s_suth, double k2, double k4, int im, int jm);
 
+/* srcfv/adjoint/flux_num_dnc5_nowall_b.f90: the adjoint of flux_num_dnc5_nowall_2d,
+ * with the arguments of flux_num_dnc5_2d_b. */
+int bcg_flux_num_dnc5_nowall_2d_b(double* residu, double* residub, const double* w, double* wb, const double* x0,
+                                  const double* y0, const double* nx, const double* ny, const double* xc,
+                                  const double* yc, const double* vol, const double* volf, int gh, double cp,
+                                  double cv, double prandtl, double gam, double rgaz, double cs, double muref,
+                                  double tref, double s_suth, double k2, double k4, int im, int jm);
+
 /* The schemes of order 3, 7 and 9 and their tangents, with the arguments of
  * flux_num_dnc5_2d / _d (gh >= (order+1)/2; im, jm >= 6, and >= 9 for DNC7 and
  * >= 11 for DNC9, whose wall rows read that many cell rows):

@@ -23,6 +23,7 @@ SIGS = {
     "orc_flux_num_dnc5_2d": [_P] * 6 + [_I] + _PHYS + [_I, _I],
     "orc_flux_num_dnc5_2d_d": [_P] * 4 + [_I] + [_P] * 4 + [_I] + _PHYS + [_I, _I],
     "orc_flux_num_dnc5_2d_b": [_P] * 3 + [_P] * 4 + [_I] + _PHYS + [_I, _I],
+    "orc_flux_num_dnc5_nowall_2d_b": [_P] * 3 + [_P] * 4 + [_I] + _PHYS + [_I, _I],
     "orc_flux_num_dnc5_nowall_2d": [_P] * 6 + [_I] + _PHYS + [_I, _I],
     "orc_flux_num_dnc5_nowall_2d_d": [_P] * 4 + [_I] + [_P] * 4 + [_I] + _PHYS + [_I, _I],
     "orc_flux_num_dnc5_2d_opcount": [_P] * 6 + [_I] + _PHYS + [_I, _I],
@@ -148,11 +149,12 @@ def impli_matrix_free(grid, ph, w, dw, dtcoef, cfl, lmax):
     return dwi
 
 
-def vjp(grid, ph, w, rb):
-    """wb = (dR/dw)^T rb over all padded cells (rb interior only)."""
+def vjp(grid, ph, w, rb, nowall=False):
+    """wb = (dR/dw)^T rb over all padded cells (rb interior only); nowall: the
+    scheme without the wall rows."""
     rb = np.array(rb, order="F", copy=True)
     wb = np.zeros_like(w, order="F")
-    lib().orc_flux_num_dnc5_2d_b(_p(rb), _p(_chk(w)), _p(wb), _p(grid["nx"]), _p(grid["ny"]), _p(grid["vol"]),
+    (lib().orc_flux_num_dnc5_nowall_2d_b if nowall else lib().orc_flux_num_dnc5_2d_b)(_p(rb), _p(_chk(w)), _p(wb), _p(grid["nx"]), _p(grid["ny"]), _p(grid["vol"]),
                                  _p(grid["volf"]), grid["gh"], *_phys(ph), grid["im"], grid["jm"])
     return wb
 

@@ -148,10 +148,31 @@ int orc_impli_matrix_free_2d(double* dwi, const double* nx, const double* ny, co
 // the padded grid: a residual cell depends on cells at most 4 rows/columns
 // away (3 in the interior; 4 through the near-wall j-fluxes of rows 2-3), so
 // every residual cell sees at most one seeded cell per colour.
+namespace {
+int vjp_impl(double* residub, const double* w, double* wb, const double* nx, const double* ny, const double* vol,
+             const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs,
+             double muref, double tref, double s_suth, double k2, double k4, int im, int jm, bool wall);
+}
 int orc_flux_num_dnc5_2d_b(double* residub, const double* w, double* wb, const double* nx, const double* ny,
                            const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
                            double gam, double rgaz, double cs, double muref, double tref, double s_suth, double k2,
                            double k4, int im, int jm) {
+  return vjp_impl(residub, w, wb, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4,
+                  im, jm, true);
+}
+// the same for the scheme without the wall rows (adjoint/flux_num_dnc5_nowall_b.f90)
+int orc_flux_num_dnc5_nowall_2d_b(double* residub, const double* w, double* wb, const double* nx, const double* ny,
+                                  const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
+                                  double gam, double rgaz, double cs, double muref, double tref, double s_suth,
+                                  double k2, double k4, int im, int jm) {
+  return vjp_impl(residub, w, wb, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4,
+                  im, jm, false);
+}
+}  // extern "C"
+namespace {
+int vjp_impl(double* residub, const double* w, double* wb, const double* nx, const double* ny, const double* vol,
+             const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs,
+             double muref, double tref, double s_suth, double k2, double k4, int im, int jm, bool wall) {
   const Consts c = mk(cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4);
   const int ni = im + 2 * gh, nj = jm + 2 * gh, lo = 1 - gh;
   const size_t n = (size_t)ni * nj * 5;
@@ -168,7 +189,7 @@ int orc_flux_num_dnc5_2d_b(double* residub, const double* w, double* wb, const d
         for (int i = lo; i <= im + gh; ++i)
           if (((i - lo) % P) == a && ((j - lo) % P) == b)
             for (int v = 1; v <= 5; ++v) wv(i, j, v).d[v - 1] = 1.0;
-      flux_num_dnc5_2d<Dual<5>>(rdual.data(), wdual.data(), nx, ny, vol, volf, gh, c, im, jm);
+      flux_num_dnc5_2d<Dual<5>>(rdual.data(), wdual.data(), nx, ny, vol, volf, gh, c, im, jm, wall);
       FArr<Dual<5>> rv(rdual.data(), ni, nj, lo);
       for (int j = lo; j <= jm + gh; ++j)
         for (int i = lo; i <= im + gh; ++i) {
@@ -187,6 +208,8 @@ int orc_flux_num_dnc5_2d_b(double* residub, const double* w, double* wb, const d
       for (int i = 1; i <= im; ++i) rb(i, j, e) = 0.0;
   return 0;
 }
+}  // namespace
+extern "C" {
 
 // Operation tallies of one residual evaluation by kind (OpKind in dual.hpp),
 // written to counts[OP_NKIND]; returns the total.

@@ -23,6 +23,7 @@ ROUTINES = [
     ("srcfv/tangent/flux_num_dnc5_nowall_d.f90", ["flux_num_dnc5_nowall_2d_d"]),
     ("srcfv/tangent/flux_num_dnc5_d.f90", ["flux_num_dnc5_2d_d"]),
     ("srcfv/adjoint/flux_num_dnc5_b.f90", ["flux_num_dnc5_2d_b"]),
+    ("srcfv/adjoint/flux_num_dnc5_nowall_b.f90", ["flux_num_dnc5_nowall_2d_b"]),
     ("srcfv/prepro/flux_num_dnc3.f90", ["flux_num_dnc3_2d"]),
     ("srcfv/prepro/flux_num_dnc3_nowall.f90", ["flux_num_dnc3_nowall_2d"]),
     ("srcfv/tangent/flux_num_dnc3_d.f90", ["flux_num_dnc3_2d_d"]),

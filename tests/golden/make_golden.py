@@ -278,6 +278,33 @@ def make_impli(kind, im, jm, seed, lmaxes=(1, 2, 10), dtcoef=1.0, cfl=5.0):
     return out
 
 
+def make_nowall_adjoint(kind, im, jm, seed):
+    """flux_num_dnc5_nowall_2d_b (the reference's Tapenade adjoint of the scheme
+    without the wall rows) for one random cotangent."""
+    c = cases.bl_case(im, jm, seed=seed, ops=RefOps) if kind == "bl" else cases.cyl_case(im, jm, seed=seed, ops=RefOps)
+    g, ph = c["grid"], c["phys"]
+    w = c["w"]
+    ref_bcs(c, w)
+    rng = np.random.default_rng(seed + 100)
+    rb = np.zeros_like(w)
+    rb[3:-3, 3:-3] = rng.standard_normal((im, jm, 5))
+    out = {"kind": kind, "im": im, "jm": jm, "gh": g["gh"], "w": w.copy(order="F"), "rb": rb.copy(order="F"),
+           "wbd": c["wbd"]}
+    if kind == "bl":
+        out["field"] = c["field"]
+    for k in ("x0", "y0", "nx", "ny", "xc", "yc", "vol", "volf"):
+        out[k] = g[k]
+    for k in PHYS:
+        out["phys_" + k] = ph[k]
+    wb = np.zeros_like(w)
+    ref.call("flux_num_dnc5_nowall_2d_b", np.zeros_like(w), rb.copy(order="F"), w, wb, *residual_args(c))
+    out["wb_nowall"] = wb
+    return out
+
+
+NOWALL_ADJ = {"adj_nowall_bl_16x12": ("bl", 16, 12, 12), "adj_nowall_cyl_16x12": ("cyl", 16, 12, 13)}
+
+
 IMPLI = {"impli_bl_16x10": ("bl", 16, 10, 5), "impli_cyl_14x8": ("cyl", 14, 8, 6)}
 
 
@@ -292,6 +319,8 @@ def main():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **make_scheme(order, kind))
     for name, args in IMPLI.items():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **make_impli(*args))
+    for name, args in NOWALL_ADJ.items():
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **make_nowall_adjoint(*args))
     print("written:", sorted(f for f in os.listdir(HERE) if f.endswith(".npz")))
 
 

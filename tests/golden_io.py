@@ -11,6 +11,8 @@ CASES = ["bl_14x10", "cyl_14x8", "bl_23x17"]
 SCHEME_CASES = ["dnc%d_%s_12x11" % (o, k) for o in (3, 7, 9) for k in ("bl", "cyl")]
 # impli_matrix_free_2d on the residual of a small case, lmax = 1, 2, 10
 IMPLI_CASES = ["impli_bl_16x10", "impli_cyl_14x8"]
+# flux_num_dnc5_nowall_2d_b on one cotangent (k2 = 1.01 on the boundary layer, 0 on the cylinder)
+NOWALL_ADJ_CASES = ["adj_nowall_bl_16x12", "adj_nowall_cyl_16x12"]
 
 
 def load(name):

@@ -68,6 +68,15 @@ def test_scheme_orders(name):
         assert H.rel_err(rd, d["resd" + sfx], sc, gh) < TOL_DERIV
 
 
+@pytest.mark.parametrize("name", G.NOWALL_ADJ_CASES)
+def test_nowall_adjoint(name):
+    d = G.load(name)
+    c = G.as_case(d)
+    wb = O.vjp(c["grid"], c["phys"], c["w"], d["rb"], nowall=True)
+    sc = np.abs(d["wb_nowall"]).reshape(-1, 5).max(0)
+    assert (np.abs(wb - d["wb_nowall"]).reshape(-1, 5).max(0) / sc).max() < TOL_DERIV
+
+
 @pytest.mark.parametrize("name", G.IMPLI_CASES)
 def test_impli_matrix_free(name):
     """impli_matrix_free_2d: the whole dwi array (interior increment, zero ghosts)."""

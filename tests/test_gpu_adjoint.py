@@ -94,3 +94,28 @@ def test_boundary_chain_adjoint_dot_product():
     assert np.abs(ty - oy).max() <= 1e-12 * np.abs(oy).max()
     lhs, rhs = float(np.vdot(tx, y)), float(np.vdot(x, ty))
     assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), np.abs(tx).max() * np.abs(y).sum())
+
+
+@pytest.mark.parametrize("kind,im,jm", [("bl", 40, 30), ("cyl", 28, 20)])
+def test_nowall_vjp_matches_oracle_and_tangent(kind, im, jm):
+    """flux_num_dnc5_nowall_2d_b: against the oracle, and <J v, u> = <v, J^T u>
+    with the GPU tangent of the same scheme (flux_num_dnc5_nowall_2d_d)."""
+    from broadcast_gb300.srcfv import f_adj, f_lin
+    c = H.bl_case(im, jm) if kind == "bl" else H.cyl_case(im, jm)
+    H.oracle_bcs(c, c["w"])
+    rng = np.random.default_rng(12)
+    u = np.zeros_like(c["w"])
+    u[3:-3, 3:-3] = rng.standard_normal((im, jm, 5))
+    ref = O.vjp(c["grid"], c["phys"], c["w"], u, nowall=True)
+    ub = u.copy(order="F")
+    wb = np.full_like(c["w"], 5.0)
+    f_adj.flux_num_dnc5_nowall_2d_b(None, ub, c["w"], wb, *_args(c))
+    assert np.all(ub[3:-3, 3:-3] == 0.0)
+    sc = np.abs(ref).reshape(-1, 5).max(0)
+    assert (np.abs(wb - ref).reshape(-1, 5).max(0) / sc).max() < TOL
+    v = np.asfortranarray(rng.standard_normal(c["w"].shape))
+    r, jv = np.zeros_like(c["w"]), np.zeros_like(c["w"])
+    f_lin.flux_num_dnc5_nowall_2d_d(r, jv, c["w"], v, *_args(c))
+    lhs = float(np.sum(H.interior(jv) * H.interior(u)))
+    rhs = float(np.sum(v * wb))
+    assert abs(lhs - rhs) <= 1e-11 * max(abs(lhs), abs(rhs))

@@ -67,6 +67,21 @@ def test_scheme_orders(name):
         assert H.rel_err(rd, d["resd" + sfx], sc, gh) < 1e-11
 
 
+@pytest.mark.parametrize("name", G.NOWALL_ADJ_CASES)
+def test_nowall_adjoint(name):
+    """flux_num_dnc5_nowall_2d_b through srcfv.f_adj: wb on every padded cell,
+    the interior of residub zeroed."""
+    from broadcast_gb300.srcfv import f_adj
+    d = G.load(name)
+    c = G.as_case(d)
+    rb = d["rb"].copy(order="F")
+    wb = np.full_like(c["w"], 7.0)
+    f_adj.flux_num_dnc5_nowall_2d_b(None, rb, c["w"], wb, *_args(c))
+    sc = np.abs(d["wb_nowall"]).reshape(-1, 5).max(0)
+    assert (np.abs(wb - d["wb_nowall"]).reshape(-1, 5).max(0) / sc).max() < 1e-11
+    assert np.abs(rb[3:-3, 3:-3]).max() == 0.0
+
+
 @pytest.mark.parametrize("name", G.IMPLI_CASES)
 def test_impli_matrix_free(name):
     """impli_matrix_free_2d through srcfv.f_lhs: the whole dwi array."""
