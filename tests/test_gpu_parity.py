@@ -299,3 +299,22 @@ def test_impli_matrix_free_edge_cases():
         f_lhs.impli_matrix_free_2d(dwi, g["nx"], g["ny"], c["w"], dw, g["vol"], g["volf"], 1.0, 5.0, ph["gam"],
                                    ph["rgaz"], ph["prandtl"], 2, g["gh"], ph["cv"], ph["cs"], ph["muref"], ph["tref"],
                                    ph["cs"], 24, 16, 4)
+
+
+@pytest.mark.parametrize("gh", [2, 4, 5])
+@pytest.mark.parametrize("kind", ["bl", "cyl"])
+def test_boundary_fills_any_ghost_width(kind, gh):
+    """The DNC3/7/9 drivers fill gh = 2, 4, 5 ghost layers with the same BC
+    routines: the library's sequences (primal and tangent) against the oracle's."""
+    c = H.bl_case(30, 20, gh=gh) if kind == "bl" else H.cyl_case(30, 20, gh=gh)
+    w_ref, w_lib = c["w"].copy(order="F"), c["w"].copy(order="F")
+    H.oracle_bcs(c, w_ref)
+    H.lib_bcs(c, w_lib)
+    assert np.abs(w_lib - w_ref).max() <= 1e-13 * np.abs(w_ref).max()
+    rng = np.random.default_rng(gh)
+    wd = np.asfortranarray(rng.standard_normal(c["w"].shape))
+    wd_ref, wd_lib = wd.copy(order="F"), wd.copy(order="F")
+    w2_ref, w2_lib = c["w"].copy(order="F"), c["w"].copy(order="F")
+    H.oracle_bcs(c, w2_ref, wd_ref)
+    H.lib_bcs(c, w2_lib, wd_lib)
+    assert np.abs(wd_lib - wd_ref).max() <= 1e-12 * np.abs(wd_ref).max()
