@@ -56,14 +56,7 @@ int copy_streams(CopyStreams* cs) {
 // device -> host copy of the interior of nplanes padded (ni, nj) planes
 cudaError_t copy_interior_d2h(double* host, const double* dev, int ni, int nj, int nplanes, int gh, int im, int jm,
                               cudaStream_t st) {
-  const size_t pitch = (size_t)ni * sizeof(double), plane = (size_t)ni * nj;
-  const size_t off0 = (size_t)gh + (size_t)gh * ni;
-  for (int pl = 0; pl < nplanes; ++pl) {
-    cudaError_t e = cudaMemcpy2DAsync(host + pl * plane + off0, pitch, dev + pl * plane + off0, pitch,
-                                      (size_t)im * sizeof(double), jm, cudaMemcpyDeviceToHost, st);
-    if (e != cudaSuccess) return e;
-  }
-  return cudaSuccess;
+  return copy_interior_planes(host, dev, ni, nj, nplanes, gh, im, jm, cudaMemcpyDeviceToHost, st);
 }
 
 // Host tangents and outputs of many directions: the directions run in up to

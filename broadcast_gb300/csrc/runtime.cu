@@ -92,21 +92,30 @@ int Stager::commit() {
   return BCG_OK;
 }
 
+// the interiors of nplanes padded (ni, nj) planes, as one pitched 3D copy
+// (rows of im doubles, jm rows per plane); the ghosts of dst stay untouched
+cudaError_t copy_interior_planes(double* dst, const double* src, int ni, int nj, int nplanes, int gh, int im, int jm,
+                                 cudaMemcpyKind kind, cudaStream_t st) {
+  cudaMemcpy3DParms p = {};
+  const size_t pitch = (size_t)ni * sizeof(double);
+  p.srcPtr = make_cudaPitchedPtr(const_cast<double*>(src), pitch, (size_t)ni, (size_t)nj);
+  p.dstPtr = make_cudaPitchedPtr(dst, pitch, (size_t)ni, (size_t)nj);
+  p.srcPos = make_cudaPos((size_t)gh * sizeof(double), (size_t)gh, 0);
+  p.dstPos = p.srcPos;
+  p.extent = make_cudaExtent((size_t)im * sizeof(double), (size_t)jm, (size_t)nplanes);
+  p.kind = kind;
+  return cudaMemcpy3DAsync(&p, st);
+}
+
 int Stager::finish() {
   if (nstaged_ == 0) return BCG_OK;
   for (size_t k = 0; k < items_.size(); ++k) {
     Item& it = items_[k];
     if (!it.staged || !it.outp) continue;
     if (it.nplanes > 0) {
-      const size_t pitch = (size_t)it.ni * sizeof(double), plane = (size_t)it.ni * it.nj * sizeof(double);
-      const size_t off0 = ((size_t)it.gh + (size_t)it.gh * it.ni) * sizeof(double);
-      for (int pl = 0; pl < it.nplanes; ++pl) {
-        char* dst = (char*)const_cast<void*>(it.host) + pl * plane + off0;
-        const char* src = (const char*)ptrs_[k] + pl * plane + off0;
-        cudaError_t e = cudaMemcpy2DAsync(dst, pitch, src, pitch, (size_t)it.im * sizeof(double), it.jm,
-                                          cudaMemcpyDeviceToHost, st_);
-        if (e != cudaSuccess) return fail_cuda("device to host copy", e);
-      }
+      cudaError_t e = copy_interior_planes((double*)const_cast<void*>(it.host), (const double*)ptrs_[k], it.ni, it.nj,
+                                           it.nplanes, it.gh, it.im, it.jm, cudaMemcpyDeviceToHost, st_);
+      if (e != cudaSuccess) return fail_cuda("device to host copy", e);
       d2h_ += (size_t)it.nplanes * it.im * it.jm * sizeof(double);
       continue;
     }

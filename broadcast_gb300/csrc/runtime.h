@@ -18,6 +18,9 @@ enum {
 };
 
 cudaStream_t current_stream();
+// the interiors of nplanes padded (ni, nj) planes in one pitched 3D copy
+cudaError_t copy_interior_planes(double* dst, const double* src, int ni, int nj, int nplanes, int gh, int im, int jm,
+                                 cudaMemcpyKind kind, cudaStream_t st);
 void set_stream(cudaStream_t s);
 int fail_cuda(const char* where, cudaError_t e);   // records and returns BCG_ERR_CUDA
 int fail_arg(const char* msg);                     // records and returns BCG_ERR_ARG
