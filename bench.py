@@ -699,18 +699,27 @@ def run_newton_workload(args):
     the coordinates are local Reynolds numbers up to 6e5), or 40 iterations."""
     import torch
     from broadcast_gb300 import cases
-    from broadcast_gb300.newton import BLNewton
-    im, jm = args.im or 400, args.jm or 150
-    c = cases.bl_case(im, jm, seed=0, ops=LibOps)
-    nt = BLNewton(c)
+    from broadcast_gb300.newton import BLNewton, CylNewton
+    if args.case == "cyl":  # cylinder.py:841-1068 on the 256 x 256 O-mesh, Newton (cfl 1e10)
+        im, jm = args.im or 256, args.jm or 256
+        c = cases.cyl_case(im, jm, ops=LibOps)
+        nt = CylNewton(c)
+    else:
+        im, jm = args.im or 400, args.jm or 150
+        c = cases.bl_case(im, jm, seed=0, ops=LibOps)
+        nt = BLNewton(c)
     w = c["w"].copy(order="F")
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    converged, norm0 = None, None
+    converged, norm0, bad = None, None, 0
     for it in range(1, 41):
-        norm, _ = nt.step(w, first=(it == 1))
+        norm, dw = nt.step(w, first=(it == 1))
         nmax = float(np.max(norm))
         norm0 = nmax if norm0 is None else norm0
+        bad = bad + 1 if not (np.all(np.isfinite(dw)) and np.isfinite(nmax)) else 0
+        if bad >= 3:  # the step-back (cfl halving) does not recover: stop
+            converged = "diverged (non-finite updates)"
+            break
         if nmax <= 1e-10:
             converged = "absolute 1e-10"
             break
@@ -720,8 +729,9 @@ def run_newton_workload(args):
     total = time.perf_counter() - t0
     hist = nt.history
     mean = lambda k: float(np.mean([h[k] for h in hist]))
+    what = "cylinder O-mesh" if args.case == "cyl" else "BL"
     line = {"workload": "newton",
-            "metric": "SER Newton time to max L2 norm <= 1e-10, or 1e-11 relative (BL %dx%d, cfl 1e10)" % (im, jm),
+            "metric": "SER Newton time to max L2 norm <= 1e-10, or 1e-11 relative (%s %dx%d, cfl 1e10)" % (what, im, jm),
             "unit": "s", "value": total, "higher_is_better": False, "dtype": "f64", "data": "synthetic",
             "iterations": len(hist), "converged": converged, "final_norm": float(np.max(hist[-1]["norm"])),
             "final_norm_relative": float(np.max(hist[-1]["norm"])) / norm0,
@@ -730,8 +740,10 @@ def run_newton_workload(args):
                                       "jacobian_245_seeds": mean("seconds_jacobian"),
                                       "band_lu_solve": mean("seconds_solve")},
             "jacobian_nnz": hist[-1]["nnz"],
-            "config": {"workload": "boundary layer %dx%d, Blasius polynomial state + U(-1e-4, 1e-4) noise (seed 0), "
-                                   "card cfl 1e10" % (im, jm)},
+            "config": {"workload": ("cylinder O-mesh %dx%d, uniform flow + U(-1e-3, 1e-3) noise (seed 1), Mach 0.1, "
+                                    "Re 47, band LU in the folded azimuthal order" % (im, jm)) if args.case == "cyl" else
+                                   ("boundary layer %dx%d, Blasius polynomial state + U(-1e-4, 1e-4) noise (seed 0), "
+                                    "card cfl 1e10" % (im, jm))},
             "cpu_baseline": {"value": None, "unit": "s", "kind": "port", "cores": 1,
                              "sample": "none at this size: the host sparse LU in the image (SuperLU) did not finish "
                                        "one factorisation of this Jacobian in 1500 s; the reference's MUMPS is absent"}}
@@ -772,6 +784,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--lmax", type=int, default=10, help="impli workload: Gauss-Seidel sweeps per call")
+    ap.add_argument("--case", default="bl", choices=["bl", "cyl"], help="newton workload: boundary layer or cylinder")
     ap.add_argument("--workload", default="residual-jvp", choices=["residual-jvp", "jacobian", "batch", "impli", "newton"],
                     help="residual-jvp: the 256x256 cylinder line (default); jacobian: the batched "
                          "Jacobian / Dz / Dzz / J(beta) assembly of the 1024x512 boundary layer; batch: "

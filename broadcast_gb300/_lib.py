@@ -30,7 +30,7 @@ SIGNATURES = {
     "bcg_flux_num_dnc5_nowall_2d": "pppppppppp" + "i" + "d" * 11 + "ii",
     "bcg_flux_num_dnc5_nowall_2d_d": "pppp" + "pppppppp" + "i" + "d" * 11 + "ii",
     "bcg_impli_matrix_free_2d": "ppppppp" + "ddddd" + "ii" + "ddddd" + "iii",
-    "bcg_csr_band_lu_solve": "ipppLppip",
+    "bcg_csr_band_lu_solve": "ipppLpppip",
     **{"bcg_flux_num_dnc%d%s_2d" % (o, v): "pppppppppp" + "i" + "d" * 11 + "ii" for o in (3, 7, 9) for v in ("", "_nowall")},
     **{"bcg_flux_num_dnc%d%s_2d_d" % (o, v): "pppp" + "pppppppp" + "i" + "d" * 11 + "ii"
        for o in (3, 7, 9) for v in ("", "_nowall")},

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <vector>
 #include "bc.h"
 #include "residual.h"
 #include "runtime.h"
@@ -431,18 +432,33 @@ BCG_DNC_ENTRIES(9)
 // block size (0: 256).  Returns BCG_ERR_SINGULAR with *info = first zero pivot
 // (1-based) for a singular matrix.
 int bcg_csr_band_lu_solve(int n, const int* indptr, const int* indices, const double* data, long long nnz,
-                          const double* b, double* x, int nb, int* info) {
+                          const int* perm, const double* b, double* x, int nb, int* info) {
   if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
   if (n < 1 || nnz < 0 || !indptr || !indices || !data || !b || !x) return fail_arg("csr_band_lu_solve: bad arguments");
   cudaStream_t st = current_stream();
+  if (perm) {  // the reordering indexes the band storage: check it is a permutation of 0..n-1
+    std::vector<int> q((size_t)n);
+    if (is_device_ptr(perm)) {
+      const cudaError_t e = cudaMemcpy(q.data(), perm, (size_t)n * 4, cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return fail_cuda("csr_band_lu_solve: reading perm", e);
+    } else {
+      std::copy(perm, perm + n, q.begin());
+    }
+    std::vector<char> seen((size_t)n, 0);
+    for (int k = 0; k < n; ++k) {
+      if (q[k] < 0 || q[k] >= n || seen[q[k]]) return fail_arg("csr_band_lu_solve: perm is not a permutation");
+      seen[q[k]] = 1;
+    }
+  }
   Stager sg(st);
   const int hp = sg.in(indptr, (size_t)(n + 1) * 4), hi = sg.in(indices, (size_t)nnz * 4);
   const int hd = sg.in(data, (size_t)nnz * 8), hb = sg.in(b, (size_t)n * 8), hx = sg.out(x, (size_t)n * 8);
+  const int hq = perm ? sg.in(perm, (size_t)n * 4) : -1;
   int rc = sg.commit();
   if (rc) return rc;
   BandLuInfo bi{};
-  const int r = band_lu_solve(n, sg.dev<int>(hp), sg.dev<int>(hi), sg.dev<double>(hd), sg.dev<double>(hb),
-                              sg.dev<double>(hx), nb > 0 ? nb : 256, st, &bi);
+  const int r = band_lu_solve(n, sg.dev<int>(hp), sg.dev<int>(hi), sg.dev<double>(hd), hq >= 0 ? sg.dev<int>(hq) : nullptr,
+                              sg.dev<double>(hb), sg.dev<double>(hx), nb > 0 ? nb : 256, st, &bi);
   if (info) *info = bi.info;
   if (r == 1) return fail_arg("csr_band_lu_solve: singular matrix"), BCG_ERR_SINGULAR;
   if (r != 0) return fail_arg(band_lu_error()), BCG_ERR_CUDA;

@@ -27,12 +27,16 @@
 namespace bcg {
 namespace {
 
-__global__ void k_bandwidth(int n, const int* __restrict__ indptr, const int* __restrict__ indices, int* klku) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n) return;
+// q: optional reordering, row/column k of A is row/column q[k] of the
+// factorised matrix (null: the identity)
+__global__ void k_bandwidth(int n, const int* __restrict__ indptr, const int* __restrict__ indices,
+                            const int* __restrict__ q, int* klku) {
+  const int r0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r0 >= n) return;
+  const int r = q ? q[r0] : r0;
   int lo = 0, hi = 0;
-  for (int p = indptr[r]; p < indptr[r + 1]; ++p) {
-    const int c = indices[p];
+  for (int p = indptr[r0]; p < indptr[r0 + 1]; ++p) {
+    const int c = q ? q[indices[p]] : indices[p];
     lo = max(lo, r - c);
     hi = max(hi, c - r);
   }
@@ -41,13 +45,23 @@ __global__ void k_bandwidth(int n, const int* __restrict__ indptr, const int* __
 }
 
 __global__ void k_fill_band(int n, const int* __restrict__ indptr, const int* __restrict__ indices,
-                            const double* __restrict__ data, double* __restrict__ ab, long long ldab, int U) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  for (int p = indptr[r]; p < indptr[r + 1]; ++p) {
-    const long long c = indices[p];
+                            const double* __restrict__ data, const int* __restrict__ q, double* __restrict__ ab,
+                            long long ldab, int U) {
+  const int r0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r0 >= n) return;
+  const long long r = q ? q[r0] : r0;
+  for (int p = indptr[r0]; p < indptr[r0 + 1]; ++p) {
+    const long long c = q ? q[indices[p]] : indices[p];
     ab[U + r - c + c * ldab] += data[p];  // duplicates add, as a COO -> CSR conversion does
   }
+}
+
+// y[q[k]] = x[k] (forward) or y[k] = x[q[k]] (back)
+__global__ void k_permute(int n, const int* __restrict__ q, const double* __restrict__ x, double* __restrict__ y,
+                          int back) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  if (back) y[k] = x[q[k]]; else y[q[k]] = x[k];
 }
 
 // row swaps of one panel (pivots ipiv[0..jb), 1-based within the panel) on
@@ -101,8 +115,8 @@ bool handles() {
 
 const char* band_lu_error() { return g_err; }
 
-int band_lu_solve(int n, const int* indptr, const int* indices, const double* data, const double* b, double* x,
-                  int nb, cudaStream_t st, BandLuInfo* out) {
+int band_lu_solve(int n, const int* indptr, const int* indices, const double* data, const int* q, const double* b,
+                  double* x, int nb, cudaStream_t st, BandLuInfo* out) {
   g_err = "";
   if (n < 1) { g_err = "empty system"; return -1; }
   if (!handles()) return -1;
@@ -117,13 +131,14 @@ int band_lu_solve(int n, const int* indptr, const int* indices, const double* da
   int* d_info = nullptr;
   double* ab = nullptr;
   double* work = nullptr;
+  double* xq = nullptr;  // the solution in the factorised order
   int rc = 0;
   auto fail = [&](const char* m) { g_err = m; rc = -1; };
   do {
     if (cudaMalloc(&d_klku, 4 * sizeof(int)) != cudaSuccess) { fail("allocation failed"); break; }
     cudaMemsetAsync(d_klku, 0, 4 * sizeof(int), st);
     const int B = 256;
-    k_bandwidth<<<(n + B - 1) / B, B, 0, st>>>(n, indptr, indices, d_klku);
+    k_bandwidth<<<(n + B - 1) / B, B, 0, st>>>(n, indptr, indices, q, d_klku);
     int klku[2] = {0, 0};
     if (cudaMemcpyAsync(klku, d_klku, 2 * sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess) { fail("bandwidth pass failed"); break; }
@@ -137,7 +152,7 @@ int band_lu_solve(int n, const int* indptr, const int* indices, const double* da
     if (cudaMalloc(&d_ipiv, (size_t)n * sizeof(int)) != cudaSuccess) { fail("allocation failed"); break; }
     if (cudaMalloc(&d_info, sizeof(int)) != cudaSuccess) { fail("allocation failed"); break; }
     cudaMemsetAsync(ab, 0, bytes, st);
-    k_fill_band<<<(n + B - 1) / B, B, 0, st>>>(n, indptr, indices, data, ab, ldab, U);
+    k_fill_band<<<(n + B - 1) / B, B, 0, st>>>(n, indptr, indices, data, q, ab, ldab, U);
     double* d0 = ab + U;  // dense view: D(i, j) = d0[i + j * ldd]
     auto D = [&](long long i, long long j) { return d0 + i + j * ldd; };
     int lwork = 0;
@@ -201,19 +216,23 @@ int band_lu_solve(int n, const int* indptr, const int* indices, const double* da
       rc = 1;
       break;
     }
-    // solve: x = b, then forward (pivots, L) and backward (U)
-    if (cudaMemcpyAsync(x, b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+    // solve: x = b (reordered), then forward (pivots, L) and backward (U)
+    if (q) {
+      if (cudaMalloc(&xq, (size_t)n * sizeof(double)) != cudaSuccess) { fail("allocation failed"); break; }
+      k_permute<<<(n + B - 1) / B, B, 0, st>>>(n, q, b, xq, 0);
+    } else if (cudaMemcpyAsync(x, b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
       fail("copy failed");
       break;
     }
+    double* const xf = q ? xq : x;
     for (int j0 = 0; j0 < n && rc == 0; j0 += nb) {
       const int jb = std::min(nb, n - j0);
       const int m = std::min(kl + jb, n - j0);
-      k_swap_vec<<<1, 1, 0, st>>>(x + j0, d_ipiv + j0, jb);
-      if (cublasDtrsv(g_h.blas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_UNIT, jb, D(j0, j0), (int)ldd, x + j0,
+      k_swap_vec<<<1, 1, 0, st>>>(xf + j0, d_ipiv + j0, jb);
+      if (cublasDtrsv(g_h.blas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_UNIT, jb, D(j0, j0), (int)ldd, xf + j0,
                       1) != CUBLAS_STATUS_SUCCESS) { fail("trsv failed"); break; }
-      if (m > jb && cublasDgemv(g_h.blas, CUBLAS_OP_N, m - jb, jb, &mone, D(j0 + jb, j0), (int)ldd, x + j0, 1, &one,
-                                x + j0 + jb, 1) != CUBLAS_STATUS_SUCCESS) { fail("gemv failed"); break; }
+      if (m > jb && cublasDgemv(g_h.blas, CUBLAS_OP_N, m - jb, jb, &mone, D(j0 + jb, j0), (int)ldd, xf + j0, 1, &one,
+                                xf + j0 + jb, 1) != CUBLAS_STATUS_SUCCESS) { fail("gemv failed"); break; }
     }
     if (rc) break;
     const int nblk = (n + nb - 1) / nb;
@@ -221,17 +240,19 @@ int band_lu_solve(int n, const int* indptr, const int* indices, const double* da
       const int j0 = k * nb;
       const int jb = std::min(nb, n - j0);
       const int ncol = std::min(n - j0 - jb, kl + ku);
-      if (ncol > 0 && cublasDgemv(g_h.blas, CUBLAS_OP_N, jb, ncol, &mone, D(j0, j0 + jb), (int)ldd, x + j0 + jb, 1, &one,
-                                  x + j0, 1) != CUBLAS_STATUS_SUCCESS) { fail("gemv failed"); break; }
+      if (ncol > 0 && cublasDgemv(g_h.blas, CUBLAS_OP_N, jb, ncol, &mone, D(j0, j0 + jb), (int)ldd, xf + j0 + jb, 1, &one,
+                                  xf + j0, 1) != CUBLAS_STATUS_SUCCESS) { fail("gemv failed"); break; }
       if (cublasDtrsv(g_h.blas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, jb, D(j0, j0), (int)ldd,
-                      x + j0, 1) != CUBLAS_STATUS_SUCCESS) { fail("trsv failed"); break; }
+                      xf + j0, 1) != CUBLAS_STATUS_SUCCESS) { fail("trsv failed"); break; }
     }
+    if (q) k_permute<<<(n + B - 1) / B, B, 0, st>>>(n, q, xq, x, 1);
     if (out) out->info = 0;
   } while (false);
   const cudaError_t e = cudaStreamSynchronize(st);
   if (e != cudaSuccess && rc == 0) { g_err = cudaGetErrorString(e); rc = -1; }
   if (ev_a) cudaEventDestroy(ev_a);
   if (ev_b) cudaEventDestroy(ev_b);
+  cudaFree(xq);
   cudaFree(work);
   cudaFree(d_info);
   cudaFree(d_ipiv);

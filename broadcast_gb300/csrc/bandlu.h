@@ -13,8 +13,10 @@ struct BandLuInfo {
 // x = A^-1 b for the n x n CSR matrix A (device arrays; duplicates summed);
 // returns 0, 1 for a singular matrix (out->info = first zero pivot), -1 on
 // another failure (band_lu_error() says which).  Synchronises the stream.
-int band_lu_solve(int n, const int* indptr, const int* indices, const double* data, const double* b, double* x,
-                  int nb, cudaStream_t st, BandLuInfo* out);
+// q (optional, device): row and column k of A become row and column q[k] of
+// the factorised matrix (a bandwidth-reducing order); must be a permutation.
+int band_lu_solve(int n, const int* indptr, const int* indices, const double* data, const int* q, const double* b,
+                  double* x, int nb, cudaStream_t st, BandLuInfo* out);
 const char* band_lu_error();
 
 }  // namespace bcg

@@ -16,10 +16,12 @@ import numpy as np
 from . import _lib
 
 
-def band_lu_solve(A, b, nb=256):
+def band_lu_solve(A, b, nb=256, perm=None):
     """x = A^-1 b for a scipy sparse matrix A (converted to CSR) and vector b.
 
-    Raises RuntimeError for a singular matrix (as scipy's splu does)."""
+    perm: optional bandwidth-reducing order (row/column k of A is factorised
+    as row/column perm[k]).  Raises RuntimeError for a singular matrix (as
+    scipy's splu does)."""
     A = A.tocsr()
     n = A.shape[0]
     indptr = np.ascontiguousarray(A.indptr, dtype=np.int32)
@@ -29,9 +31,21 @@ def band_lu_solve(A, b, nb=256):
     x = np.zeros(n)
     info = np.zeros(1, np.int32)
     try:
-        _lib.call("bcg_csr_band_lu_solve", n, indptr, indices, data, int(A.nnz), b, x, int(nb), info)
+        q = None if perm is None else np.ascontiguousarray(perm, dtype=np.int32)
+        _lib.call("bcg_csr_band_lu_solve", n, indptr, indices, data, int(A.nnz), q, b, x, int(nb), info)
     except _lib.BroadcastError as e:
         if "singular" in str(e):
             raise RuntimeError("singular matrix (zero pivot at row %d)" % int(info[0])) from e
         raise
     return x
+
+
+def folded_ring_order(im, jm, nvar=5):
+    """Bandwidth-reducing order for the periodic O-mesh Jacobian (rows (i, j, e)
+    with i slowest, i periodic): the azimuthal index folded (1, im, 2, im-1,
+    ...) so that the periodic neighbours are close, and the radial index j
+    slowest; returns perm with perm[row] = new position."""
+    i = np.arange(im)
+    fold = np.where(i < (im + 1) // 2, 2 * i, 2 * (im - 1 - i) + 1)  # 0, 2, 4, ..., 5, 3, 1
+    ii, jj, ee = np.meshgrid(i, np.arange(jm), np.arange(nvar), indexing="ij")
+    return (ee + nvar * fold[ii] + nvar * im * jj).ravel().astype(np.int32)

@@ -1,6 +1,7 @@
 """Pseudo-transient Newton (SER) iteration to a steady base flow: the
-'fixed_point' mode of the boundary-layer driver (BROADCAST_npz.py:985-1196),
-the immediate caller of the residual and Jacobian hot path.
+'fixed_point' mode of the boundary-layer driver (BROADCAST_npz.py:985-1196,
+BLNewton) and of the cylinder driver (cylinder.py:841-1068, CylNewton), the
+immediate callers of the residual and Jacobian hot path.
 
 Per iteration, as the reference:
   1. boundary fills (inlet Ilo, no-reflexion Jhi, extrapolation Ihi, wall Jlo);
@@ -21,7 +22,7 @@ import time
 import numpy as np
 
 from . import _lib
-from .linsolve import band_lu_solve
+from .linsolve import band_lu_solve, folded_ring_order
 
 PHYS = ("cp", "cv", "prandtl", "gam", "rgaz", "cs", "muref", "tref", "s_suth", "k2", "k4")
 
@@ -126,3 +127,53 @@ class BLNewton:
                 break
         self.fill(w)
         return w
+
+
+class CylNewton(BLNewton):
+    """SER Newton on the cylinder O-mesh (broadcast_gb300.cases.cyl_case layout),
+    cylinder.py:841-1068: boundary fills no-reflexion (Jhi), wall (Jlo) and
+    the two periodic joins in handleBC.applyBC's order; time step from the
+    radial spacing of the first cell, dt = cfl |xc(1,1) - xc(1,2)| / (1/M + 1)
+    (:842); relaxed Jacobian with the periodic column wrap
+    (computejacobianfromjv_relaxed_withjn[andcheck], :900-980) assembled on the
+    GPU; the linear solve by the GPU band LU in the folded azimuthal order,
+    which makes the periodic Jacobian banded (kl ~ 15 im + 35).  The cylinder
+    card runs cfl 0.9 (card_cyl2d.py:57); cfl 1e10 gives Newton's iteration."""
+
+    def __init__(self, case, cfl=1.0e10, mach=None, solver=None):
+        super().__init__(case, cfl=cfl, mach=mach, solver=solver or self._banded)
+        g = case["grid"]
+        gh = self.gh
+        self.dt = self.cfl * abs(g["xc"][gh, gh] - g["xc"][gh, gh + 1]) / (1.0 / self.mach + 1.0)
+        self.perm = folded_ring_order(self.im, self.jm)
+
+    def _banded(self, J, b):
+        return band_lu_solve(J, b, perm=self.perm)
+
+    def fill(self, w):
+        from .srcfv import f_bnd
+        c, g = self.c, self.c["grid"]
+        it, gam, gh, im, jm = c["interf"], self.c["phys"]["gam"], self.gh, self.im, self.jm
+        f_bnd.bc_no_reflexion_2d(w, c["wbd"], "Jhi", it["Jhi"], g["nx"], g["ny"], gam, gh, im, jm)
+        f_bnd.bc_wall_viscous_adia_2d(w, "Jlo", gam, it["Jlo"], gh, im, jm)
+        for _ in range(2):  # the joins of interf3 and interf4 each apply both copies
+            f_bnd.jn_match_2d(w, it["prr1"], gh, gh, gh, gh, im, jm, w, it["prd2"], gh, gh, gh, gh, im, jm, it["tr"])
+            f_bnd.jn_match_2d(w, it["prr2"], gh, gh, gh, gh, im, jm, w, it["prd1"], gh, gh, gh, gh, im, jm, it["tr"])
+
+    def jacobian(self, w, coefdiag):
+        import scipy.sparse as sp
+        from ._f2py import interf4
+        g, c = self.c["grid"], self.c
+        it = c["interf"]
+        nrow = 5 * self.im * self.jm
+        cap = nrow * 245
+        indptr, indices, data = np.zeros(nrow + 1, np.int32), np.zeros(cap, np.int32), np.zeros(cap)
+        nnz = np.zeros(1, np.int64)
+        _lib.call("bcg_jacobian_dnc5_cyl_csr", w, g["nx"], g["ny"], g["vol"], g["volf"], self.gh, *self.phys,
+                  self.im, self.jm, interf4(it["Jhi"]), interf4(it["Jlo"]), c["wbd"], c["wbd"].shape[0],
+                  interf4(it["prr1"]), interf4(it["prd1"]), interf4(it["prr2"]), interf4(it["prd2"]),
+                  np.ascontiguousarray(np.asarray(it["tr"], dtype=np.int32).ravel()), np.asfortranarray(coefdiag),
+                  2e-16, 0, indptr, indices, data, cap, nnz)
+        n = int(nnz[0])
+        return sp.csr_matrix((data[:n].copy(), indices[:n].copy(), indptr), shape=(nrow, nrow))
+

@@ -154,11 +154,14 @@ int bcg_flux_num_dnc9_nowall_2d_d(double* residu, double* residud, const double*
  * GPU (LAPACK's blocked dgbtrf/dgbtrs algorithm through cuSOLVER getrf panels
  * and cuBLAS trsm/gemm on views of the band storage, which takes
  * 8 n (3 kl + ku + 2 nb + 1) bytes of device memory for bandwidths kl, ku).
+ * perm (optional, may be null): row and column k of A are row and column perm[k]
+ * of the factorised matrix, a bandwidth-reducing order (e.g. the folded
+ * azimuthal order of a periodic O-mesh); must be a permutation of 0..n-1.
  * nb: block size (0: 256).  Returns -5 with *info = the first zero pivot
  * (1-based) for a singular matrix.  No reference counterpart in f2py: the
  * reference calls PETSc here. */
 int bcg_csr_band_lu_solve(int n, const int* indptr, const int* indices, const double* data, long long nnz,
-                          const double* b, double* x, int nb, int* info);
+                          const int* perm, const double* b, double* x, int nb, int* info);
 
 /* srcfv/lhs/impli_matrix_free.F90:7 (IMPLI_MATRIX_FREE_2D): the implicit phase
  * of the 'impli' time marching (BROADCAST_npz.py:911-941): lmax symmetric
