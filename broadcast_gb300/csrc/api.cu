@@ -34,9 +34,10 @@ int has_device() {
   return 1;
 }
 
-// Copy streams of the pipelined host-array path (one pair per device,
-// created on first use, never destroyed).
-struct CopyStreams { cudaStream_t in = nullptr, out = nullptr; };
+// Streams of the pipelined host-array path (per device, created on first
+// use, never destroyed): uploads, downloads, and two compute streams that
+// alternate over the chunks.
+struct CopyStreams { cudaStream_t in = nullptr, out = nullptr, comp[2] = {nullptr, nullptr}; };
 int copy_streams(CopyStreams* cs) {
   static std::mutex mu;
   static std::map<int, CopyStreams> per_dev;
@@ -48,6 +49,8 @@ int copy_streams(CopyStreams* cs) {
   if (!c.in) {
     e = cudaStreamCreateWithFlags(&c.in, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.out, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.comp[0], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.comp[1], cudaStreamNonBlocking);
     if (e != cudaSuccess) { c = CopyStreams{}; return fail_cuda("copy streams", e); }
   }
   *cs = c;
@@ -62,12 +65,13 @@ cudaError_t copy_interior_d2h(double* host, const double* dev, int ni, int nj, i
 
 // Host tangents and outputs of many directions: the directions run in up to
 // four chunks of whole 4-direction groups; chunk c's upload (copy stream in),
-// its residual passes (library stream) and its download (copy stream out)
-// overlap the other chunks'.  Only the first chunk's upload and the last
-// chunk's download are exposed, so more chunks shrink them, while each launch
-// still covers at least one group per chunk of the residual passes.  Uploads
-// start only after the library stream's earlier work, since the pool buffers
-// they fill may still be in use.
+// its residual passes (compute stream c mod 2, with its own scratch) and its
+// download (copy stream out) overlap the other chunks'.  Only the first
+// chunk's upload and the last chunk's download are exposed, so more chunks
+// shrink them; the two compute streams let a chunk's kernels fill the SMs the
+// previous chunk's last partial waves leave idle.  Everything starts only after
+// the library stream's earlier work, since the pool buffers may still be in
+// use, and the library stream waits for the last download.
 int residual_pipelined(ResidualArgs a, double* res, double* residud, const double* wd, int nd, cudaStream_t st) {
   const int im = a.im, jm = a.jm, gh = a.gh, ni = im + 2 * gh, nj = jm + 2 * gh;
   const size_t plane5 = (size_t)ni * nj * 5;
@@ -85,7 +89,8 @@ int residual_pipelined(ResidualArgs a, double* res, double* residud, const doubl
   double* wd_dev = (double*)pool_get(POOL_AUX, plane5 * nd * sizeof(double));
   double* rd_dev = (double*)pool_get(POOL_STAGE_OUT, plane5 * nd * sizeof(double));
   const size_t s4 = residual_scratch_doubles(im, jm, gh, 4);
-  double* scr = (double*)pool_get(POOL_SCRATCH, s4 * 8 * (size_t)std::max(gmax, 1) + residual_scratch_doubles(im, jm, gh, 2) * 8);
+  const size_t scr_each = s4 * (size_t)std::max(gmax, 1) + residual_scratch_doubles(im, jm, gh, 2);
+  double* scr = (double*)pool_get(POOL_SCRATCH, 2 * scr_each * 8);
   if (!wd_dev || !rd_dev || !scr) return fail_arg("scratch allocation failed"), BCG_ERR_NOMEM;
   constexpr int kEv = 2 * kMaxChunk + 2;
   cudaEvent_t ev[kEv] = {};  // 0: start; 1 + c: chunk c uploaded; 1 + nch + c: chunk c computed; last: downloads done
@@ -94,14 +99,17 @@ int residual_pipelined(ResidualArgs a, double* res, double* residud, const doubl
   struct Guard { cudaEvent_t* e; ~Guard() { for (int k = 0; k < kEv; ++k) if (e[k]) cudaEventDestroy(e[k]); } } guard{ev};
   cudaError_t e = cudaEventRecord(ev[0], st);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(cs.in, ev[0], 0);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(cs.comp[0], ev[0], 0);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(cs.comp[1], ev[0], 0);
   if (e != cudaSuccess) return fail_cuda("pipelined residual", e);
   for (int c = 0; c < nch; ++c) {
     const int d0 = bounds[c], d1 = bounds[c + 1];
     if (d1 <= d0) continue;
+    cudaStream_t cst = cs.comp[c & 1];
     e = cudaMemcpyAsync(wd_dev + plane5 * d0, wd + plane5 * d0, plane5 * (d1 - d0) * sizeof(double),
                         cudaMemcpyHostToDevice, cs.in);
     if (e == cudaSuccess) e = cudaEventRecord(ev[1 + c], cs.in);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev[1 + c], 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cst, ev[1 + c], 0);
     if (e != cudaSuccess) return fail_cuda("pipelined residual: upload", e);
     for (int k0 = d0; k0 < d1;) {
       const int left = d1 - k0;
@@ -109,12 +117,12 @@ int residual_pipelined(ResidualArgs a, double* res, double* residud, const doubl
       a.ndir = kk; a.ngroup = left >= 4 ? left / 4 : 1;
       a.wd = wd_dev + plane5 * k0; a.resd = rd_dev + plane5 * k0;
       a.res = (k0 == 0) ? res : nullptr;
-      a.scratch = scr;
-      e = run_residual(a, st);
+      a.scratch = scr + (size_t)(c & 1) * scr_each;
+      e = run_residual(a, cst);
       if (e != cudaSuccess) return fail_cuda("flux_num_dnc5_2d_d", e);
       k0 += kk * a.ngroup;
     }
-    e = cudaEventRecord(ev[1 + nch + c], st);
+    e = cudaEventRecord(ev[1 + nch + c], cst);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(cs.out, ev[1 + nch + c], 0);
     if (e == cudaSuccess)
       e = copy_interior_d2h(residud + plane5 * d0, rd_dev + plane5 * d0, ni, nj, 5 * (d1 - d0), gh, im, jm, cs.out);
