@@ -188,23 +188,51 @@ int residual_call(double* residu, double* residud, const double* w, const double
     const double* wdd = sg.dev<double>(hwd);
     double* rdd = sg.dev<double>(hresd);
     // full groups of 4 directions run as one launch per pass (blockIdx.y =
-    // group), as many groups at a time as fit a 2 GiB scratch budget; the
-    // remaining 1-3 directions run as 2 + 1
+    // group), as many groups at a time as fit a 2 GiB scratch budget, split
+    // in two halves on two streams (each with its own part of the scratch)
+    // so that one half's kernels fill the SMs the other's last partial waves
+    // leave idle; the remaining 1-3 directions run as 2 + 1
     const size_t s4 = residual_scratch_doubles(im, jm, gh, 4);
     const int gmax = (int)std::max<size_t>(1, ((size_t)2 << 30) / (s4 * 8));
+    CopyStreams cs;
+    rc = copy_streams(&cs);
+    if (rc) return rc;
+    cudaEvent_t ev[3] = {};
+    struct Guard { cudaEvent_t* e; ~Guard() { for (int k = 0; k < 3; ++k) if (e[k]) cudaEventDestroy(e[k]); } } guard{ev};
+    for (auto& x : ev)
+      if (cudaEventCreateWithFlags(&x, cudaEventDisableTiming) != cudaSuccess) return fail_cuda("events", cudaGetLastError());
     int off = 0;
     while (off < nd) {
       const int left = nd - off;
       int kk, ng;
       if (left >= 4) { kk = 4; ng = std::min(left / 4, gmax); }
       else { kk = left >= 2 ? 2 : 1; ng = 1; }
-      a.ndir = kk; a.ngroup = ng;
+      double* scr = (double*)pool_get(POOL_SCRATCH, residual_scratch_doubles(im, jm, gh, kk) * 8 * (size_t)ng);
+      if (!scr) return fail_arg("scratch allocation failed"), BCG_ERR_NOMEM;
+      a.ndir = kk;
       a.wd = wdd + (size_t)off * np * 5;
       a.resd = rdd + (size_t)off * np * 5;
       a.res = (off == 0) ? res : nullptr;
-      a.scratch = (double*)pool_get(POOL_SCRATCH, residual_scratch_doubles(im, jm, gh, kk) * 8 * (size_t)ng);
-      if (!a.scratch) return fail_arg("scratch allocation failed"), BCG_ERR_NOMEM;
-      cudaError_t e = run_residual(a, st);
+      cudaError_t e = cudaSuccess;
+      if (kk == 4 && ng >= 2) {
+        const int h0 = (ng + 1) / 2;
+        e = cudaEventRecord(ev[0], st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(cs.comp[0], ev[0], 0);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(cs.comp[1], ev[0], 0);
+        ResidualArgs b = a;
+        a.ngroup = h0; a.scratch = scr;
+        b.ngroup = ng - h0; b.scratch = scr + s4 * (size_t)h0; b.res = nullptr;
+        b.wd = a.wd + (size_t)4 * h0 * np * 5; b.resd = a.resd + (size_t)4 * h0 * np * 5;
+        if (e == cudaSuccess) e = run_residual(a, cs.comp[0]);
+        if (e == cudaSuccess) e = run_residual(b, cs.comp[1]);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[1], cs.comp[0]);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[2], cs.comp[1]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev[1], 0);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev[2], 0);
+      } else {
+        a.ngroup = ng; a.scratch = scr;
+        e = run_residual(a, st);
+      }
       if (e != cudaSuccess) return fail_cuda("flux_num_dnc5_2d_d", e);
       off += kk * ng;
     }
