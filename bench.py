@@ -764,6 +764,73 @@ def run_newton_workload(args):
     return 0
 
 
+def run_warmstart_workload(args):
+    """Learned warm start of the cylinder base flow (Re in [40, 200], Mach in
+    [0.05, 0.3]): base flows at --ntrain seeded (Re, Mach) points (seed 5) by
+    continuation with the GPU Newton iteration, the conditioned MLP trained on
+    them by the BF16 kernels, then every one of --nheld held-out points (seed
+    6) solved to max L2 norm <= 1e-10 from the network's guess (plain start as
+    fallback) and from the nearest training base flow (plain continuation);
+    value = mean time from the learned guess, beside the plain mean."""
+    import torch
+    from broadcast_gb300 import warmstart as WS
+    im, jm = args.im or 56, args.jm or 42
+    ratio = 1.05 ** 0.5
+    logs = []
+    log = lambda msg: (logs.append(msg), print(msg, file=sys.stderr, flush=True))
+    train = WS.sample_parameters(args.ntrain, seed=5)
+    held = WS.sample_parameters(args.nheld, seed=6)
+    t0 = time.perf_counter()
+    states, recs = WS.solve_baseflows(train, im, jm, ratio=ratio, log=log)
+    t_data = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    ev0.record()
+    model, fit_log = WS.train_on_baseflows(train, states, im, jm, ratio=ratio, steps=args.train_steps,
+                                           batch=args.batch, log_every=max(1, args.train_steps // 10))
+    ev1.record()
+    torch.cuda.synchronize()
+    t_fit = time.perf_counter() - t0
+    fit_ms = ev0.elapsed_time(ev1)
+    d = WS.DIMS
+    flops_step = 3 * 2 * args.batch * sum(d[i] * d[i + 1] for i in range(4))  # forward, data and weight gradients
+    out = WS.compare_starts(model, train, states, held, im, jm, ratio=ratio, log=log)
+    conv = [r for r in out if r["plain"]["converged"] and r["learned"]["converged"]]
+    mean = lambda arm, k: float(np.mean([r[arm][k] for r in conv])) if conv else None
+    line = {"workload": "warmstart",
+            "metric": "baseflow time to max L2 norm <= 1e-10 from the learned guess (cylinder O-mesh %dx%d, "
+                      "mean over %d held-out (Re, Mach))" % (im, jm, len(held)),
+            "unit": "s", "value": mean("learned", "seconds"), "higher_is_better": False, "dtype": "f64 solver, bf16/f32 network",
+            "data": "synthetic (solver-generated base flows)",
+            "plain_continuation": {"seconds": mean("plain", "seconds"), "iterations": mean("plain", "iterations"),
+                                   "first_norm": mean("plain", "first_norm")},
+            "learned": {"seconds": mean("learned", "seconds"), "iterations": mean("learned", "iterations"),
+                        "first_norm": mean("learned", "first_norm"),
+                        "guess_seconds": mean("learned", "guess_seconds"),
+                        "fallbacks": int(sum(r["learned"]["fallback"] for r in out))},
+            "speedup_vs_plain": (mean("plain", "seconds") / mean("learned", "seconds")) if conv else None,
+            "converged_both": len(conv), "held_out": len(out),
+            "training_set": {"points": len(train), "converged": int(sum(s is not None for s in states)),
+                             "seconds": t_data,
+                             "newton_iterations_mean": float(np.mean([r["iterations"] for r in recs if r]))},
+            "network": {"train_seconds": t_fit, "train_steps": args.train_steps, "batch": args.batch,
+                        "loss_first": fit_log[0][1], "loss_last": fit_log[-1][1],
+                        "gemm_tflops_bf16": flops_step * args.train_steps / (fit_ms / 1e3) / 1e12,
+                        "note": "whole training loop (features, 4 forward, 3 backward-data, 4 weight-gradient "
+                                "GEMMs, column sums, Adam) per step; TFLOP/s counts the GEMM flops only"},
+            "per_point": [{"re": r["re"], "mach": r["mach"],
+                           "plain": {k: r["plain"][k] for k in ("iterations", "seconds", "first_norm")},
+                           "learned": {k: r["learned"][k] for k in ("iterations", "seconds", "first_norm", "fallback")}}
+                          for r in out],
+            "config": {"workload": "cylinder O-mesh %dx%d (r 0.5..50 D, radial ratio %.4f), Re U(40, 200), Mach "
+                                   "U(0.05, 0.3); %d training points (seed 5), %d held out (seed 6); Newton cfl 1e10, "
+                                   "GPU Jacobian and band LU" % (im, jm, ratio, len(train), len(held))},
+            "cpu_baseline": None}
+    print(json.dumps(line))
+    return 0
+
+
 def _hbm_peak():
     try:
         return float(json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")))["hbm_gbs"])
@@ -798,7 +865,12 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--lmax", type=int, default=10, help="impli workload: Gauss-Seidel sweeps per call")
     ap.add_argument("--case", default="bl", choices=["bl", "cyl"], help="newton workload: boundary layer or cylinder")
-    ap.add_argument("--workload", default="residual-jvp", choices=["residual-jvp", "jacobian", "batch", "impli", "newton"],
+    ap.add_argument("--ntrain", type=int, default=200, help="warmstart workload: training base flows")
+    ap.add_argument("--nheld", type=int, default=20, help="warmstart workload: held-out (Re, Mach) points")
+    ap.add_argument("--train-steps", type=int, default=3000, help="warmstart workload: Adam steps")
+    ap.add_argument("--batch", type=int, default=16384, help="warmstart workload: samples per Adam step")
+    ap.add_argument("--workload", default="residual-jvp",
+                    choices=["residual-jvp", "jacobian", "batch", "impli", "newton", "warmstart"],
                     help="residual-jvp: the 256x256 cylinder line (default); jacobian: the batched "
                          "Jacobian / Dz / Dzz / J(beta) assembly of the 1024x512 boundary layer; batch: "
                          "residual + JVP of 64 uneven boundary-layer grids in one graph")
@@ -814,6 +886,8 @@ def main():
         return run_newton_workload(args)
     if args.workload == "batch":
         return run_batch_workload(args)
+    if args.workload == "warmstart":
+        return run_warmstart_workload(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -12,9 +12,9 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libbroadcast_gb300.so")
 
-P, I, D, S, L, Z = "p", "i", "d", "s", "L", "z"
+P, I, D, S, L, Z, F = "p", "i", "d", "s", "L", "z", "f"
 _CT = {P: ctypes.c_void_p, I: ctypes.c_int, D: ctypes.c_double, S: ctypes.c_char_p, L: ctypes.c_longlong,
-       Z: ctypes.c_size_t}
+       Z: ctypes.c_size_t, F: ctypes.c_float}
 
 # name -> argument kinds (every function returns int unless listed in _RESTYPE)
 SIGNATURES = {
@@ -81,6 +81,13 @@ SIGNATURES = {
     "bcg_batch_destroy": "L",
     "bcg_csr_spanwise_beta": "i" + "ppp" * 3 + "ip" + "ppp" + "L" + "p",
     "bcg_jacobian_dnc5_cyl_csr": "ppppp" + "i" + "d" * 11 + "ii" + "pp" + "pi" + "ppppp" + "pdi" + "ppp" + "L" + "p",
+    "bcg_mlp_gemm_nn": "i" + "pppppppp" + "iiiii" + "f",
+    "bcg_mlp_gemm_tn": "pppiiii",
+    "bcg_mlp_colsum": "piiip",
+    "bcg_mlp_adam": "pipiii" + "pppppppp" + "ffff" + "p",
+    "bcg_mlp_cast_weights": "piipp",
+    "bcg_mlp_features": "ppipipiLiiipp",
+    "bcg_mlp_sum": "pip",
     "bcg_jacobian_dz_bl_csr": "ppppp" + "i" + "d" * 9 + "ii" + "pppp" + "pipi" + "id" + "ppp" + "L" + "p",
 }
 _RESTYPE = {"bcg_get_stream": ctypes.c_void_p, "bcg_last_error_string": ctypes.c_char_p,

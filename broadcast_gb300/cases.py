@@ -65,6 +65,11 @@ def _alloc(im, jm, gh=GH):
 
 
 def _geom(g, ops):
+    if ops is None:  # the library's host geometry (srcfv/geom/computegeom.F90)
+        from .srcfv import f_geom
+        f_geom.computegeom_2d(g["x0"], g["y0"], g["nx"], g["ny"], g["xc"], g["yc"], g["vol"], g["volf"], g["im"],
+                              g["jm"], g["gh"])
+        return
     ops.computegeom(g["x0"], g["y0"], g["nx"], g["ny"], g["xc"], g["yc"], g["vol"], g["volf"], g["im"], g["jm"],
                     g["gh"])
 

@@ -85,12 +85,18 @@ class BLNewton:
         n = int(nnz[0])
         return sp.csr_matrix((data[:n].copy(), indices[:n].copy(), indptr), shape=(nrow, nrow))
 
-    def step(self, w, first=False):
-        """One SER Newton iteration on w (Fortran-ordered, updated in place)."""
+    def step(self, w, first=False, tol=None):
+        """One SER Newton iteration on w (Fortran-ordered, updated in place).
+        With tol given, a state whose max L2 residual norm is already <= tol
+        is left as it is (no Jacobian, no solve) and dw is None."""
         t0 = time.perf_counter()
         self.fill(w)
         res, norm, ninf = self.residual(w)
         t1 = time.perf_counter()
+        if tol is not None and norm.max() <= tol:
+            self.history.append(dict(norm=norm.tolist(), cflm1=0.0, nnz=0, seconds=t1 - t0, seconds_residual=t1 - t0,
+                                     seconds_jacobian=0.0, seconds_solve=0.0))
+            return norm, None
         if first:
             self.norm0m1 = 1.0 / np.maximum(norm, 1e-15)
             self.ninf0m1 = 1.0 / np.maximum(ninf, 1e-15)
@@ -122,8 +128,8 @@ class BLNewton:
     def solve(self, w, ite=50, tol=1e-10):
         """Iterate until max L2 residual norm <= tol (absolute) or ite steps."""
         for it in range(1, ite + 1):
-            norm, _ = self.step(w, first=(it == 1))
-            if norm.max() <= tol:
+            norm, dw = self.step(w, first=(it == 1), tol=tol)
+            if dw is None:
                 break
         self.fill(w)
         return w

@@ -389,6 +389,47 @@ int bcg_flux_num_dnc5_2d_noalloc(double* residu, const double* w, const double* 
                                  double gam, double rgaz, double cs, double muref, double tref, double s_suth,
                                  double k2, double k4, int im, int jm);
 
+/* ---- learned warm start (no reference counterpart) ----------------------------- */
+/* Kernels of the conditioned MLP that gives the cylinder base-flow Newton
+ * iteration (cylinder.py:841-1068) its initial state for a new (Re, Mach),
+ * in place of the restart from the nearest converged neighbour
+ * (cylinder.py:776-792).  BF16 operands (uint16 bit patterns), FP32
+ * accumulation, row-major device arrays only; queued on the library stream.
+ * GEMM  C[m x n] = A[m x k] B[n x k]^T (+ bias[n]), m and n multiples of 128,
+ * k a multiple of 64, with the epilogue epi:
+ *   0  out_bf = bf16(tanh(C))
+ *   1  out_bf = bf16(C * (1 - yprev^2))              (backward through tanh)
+ *   2  out_f32[m x nout] = C[:, :nout] (if given); with target [m x nout]:
+ *      out_bf = bf16(gscale (C - target)) on the first nout columns of the
+ *      first m_valid rows, 0 elsewhere, and loss_part[one per CTA] = the sum
+ *      of squares of (C - target) there. */
+int bcg_mlp_gemm_nn(int epi, const void* a, const void* b, const float* bias, const void* yprev, const float* target,
+                    void* out_bf, float* out_f32, float* loss_part, int m, int n, int k, int nout, int m_valid,
+                    float gscale);
+/* part[z][n1 x n2] = sum over the rows of chunk z (m / nsplit rows, a multiple
+ * of 64) of dz[row][n1] x[row][n2]; n1, n2 multiples of 128. */
+int bcg_mlp_gemm_tn(const void* dz, const void* x, float* part, int m, int n1, int n2, int nsplit);
+/* part[z][col] = sum of dz[row][col] over the rows of chunk z (ceil(m / nsplit) rows). */
+int bcg_mlp_colsum(const void* dz, int m, int n, int nsplit, float* part);
+/* gradient = fixed-order sum of the partials (weights n1 x n2, then bias n1),
+ * written to grad_out if given; lr != 0: one Adam step on the FP32 master
+ * weights and moments (lr carrying the bias corrections), refreshing the BF16
+ * weights wbf [n1 x n2] and their transpose wtbf [n2 x n1]. */
+int bcg_mlp_adam(const float* wpart, int nsplit, const float* bpart, int bsplit, int n1, int n2, float* w, float* mw,
+                 float* vw, float* b, float* mb, float* vb, void* wbf, void* wtbf, float lr, float beta1, float beta2,
+                 float eps, float* grad_out);
+/* wbf = bf16(w) and wtbf its transpose. */
+int bcg_mlp_cast_weights(const float* w, int n1, int n2, void* wbf, void* wtbf);
+/* 128 BF16 input features per row of x [m x 128] from the cell's azimuth and
+ * normalised log radius and the normalised (Re, Mach) of its parameter set.
+ * seed >= 0: row r samples (set, cell) by a hash of (seed, r) and gathers its
+ * targets [nset x ncell x nout] into t; seed < 0: row r is cell r of `set`.
+ * Rows >= m_valid are zero. */
+int bcg_mlp_features(const float* theta, const float* rho, int ncell, const float* params, int nset,
+                     const float* targets, int nout, long long seed, int set, int m, int m_valid, void* x, float* t);
+/* *out = sum of x[0..n) (one CTA, fixed order). */
+int bcg_mlp_sum(const float* x, int n, float* out);
+
 /* ---- calibration (no reference counterpart) ------------------------------------ */
 /* FP64 FMA throughput of the current GPU in TFLOP/s (FMA = 2 flops): the
  * denominator of the FP64 roofline that bounds the residual kernels. */
