@@ -64,7 +64,7 @@ cudaError_t copy_interior_d2h(double* host, const double* dev, int ni, int nj, i
 }
 
 // Host tangents and outputs of many directions: the directions run in up to
-// four chunks of whole 4-direction groups; chunk c's upload (copy stream in),
+// eight chunks of whole 4-direction groups; chunk c's upload (copy stream in),
 // its residual passes (compute stream c mod 2, with its own scratch) and its
 // download (copy stream out) overlap the other chunks'.  Only the first
 // chunk's upload and the last chunk's download are exposed, so more chunks
@@ -78,7 +78,7 @@ int residual_pipelined(ResidualArgs a, double* res, double* residud, const doubl
   CopyStreams cs;
   int rc = copy_streams(&cs);
   if (rc) return rc;
-  constexpr int kMaxChunk = 4;
+  constexpr int kMaxChunk = 8;
   const int ng = nd / 4;
   const int nch = std::max(1, std::min(kMaxChunk, ng));
   int bounds[kMaxChunk + 1];
