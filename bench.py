@@ -826,7 +826,9 @@ def run_warmstart_workload(args):
             "config": {"workload": "cylinder O-mesh %dx%d (r 0.5..50 D, radial ratio %.4f), Re U(40, 200), Mach "
                                    "U(0.05, 0.3); %d training points (seed 5), %d held out (seed 6); Newton cfl 1e10, "
                                    "GPU Jacobian and band LU" % (im, jm, ratio, len(train), len(held))},
-            "cpu_baseline": None}
+            "cpu_baseline": {"value": None, "unit": "s", "kind": "port", "cores": 0,
+                             "sample": "none: both arms run the same GPU Newton iteration and differ only in "
+                                       "the initial state; the comparison is learned vs plain start"}}
     print(json.dumps(line))
     return 0
 

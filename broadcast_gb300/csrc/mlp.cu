@@ -428,13 +428,16 @@ constexpr size_t kSmemTN = (size_t)2 * 2 * BK * PT * 2;
 cudaError_t mlp_gemm_nn(int epi, const void* a, const void* b, const float* bias, const void* yprev,
                         const float* target, void* out_bf, float* out_f32, float* loss_part, int m, int n, int k,
                         int nout, int m_valid, float gscale, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_gemm_nn<MLP_EPI_TANH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNN);
-    cudaFuncSetAttribute(k_gemm_nn<MLP_EPI_DTANH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNN);
-    cudaFuncSetAttribute(k_gemm_nn<MLP_EPI_LOSS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNN);
-    attr = true;
-  }
+  static const cudaError_t attr = [] {  // once per process (thread-safe static initialisation)
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_nn<MLP_EPI_TANH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kSmemNN);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_gemm_nn<MLP_EPI_DTANH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNN);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_gemm_nn<MLP_EPI_LOSS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNN);
+    return e;
+  }();
+  if (attr != cudaSuccess) return attr;
   NNArgs p{};
   p.a = (const __nv_bfloat16*)a; p.b = (const __nv_bfloat16*)b; p.bias = bias;
   p.yprev = (const __nv_bfloat16*)yprev; p.target = target; p.out_bf = (__nv_bfloat16*)out_bf;
@@ -451,11 +454,9 @@ cudaError_t mlp_gemm_nn(int epi, const void* a, const void* b, const float* bias
 
 cudaError_t mlp_gemm_tn(const void* a, const void* b, float* part, int m, int n1, int n2, int nsplit,
                         cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTN);
-    attr = true;
-  }
+  static const cudaError_t attr =
+      cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTN);
+  if (attr != cudaSuccess) return attr;
   TNArgs p{(const __nv_bfloat16*)a, (const __nv_bfloat16*)b, part, m, n1, n2, m / nsplit};
   k_gemm_tn<<<dim3(n2 / BN, n1 / BM, nsplit), NT, kSmemTN, st>>>(p);
   return cudaGetLastError();
