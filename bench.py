@@ -329,8 +329,22 @@ def run_ours(args):
         b_ev.record(stream)
         torch.cuda.synchronize()
         vms = a_ev.elapsed_time(b_ev) / nv
+        # NDIR cotangents in one call (bcg_flux_num_dnc5_2d_bn)
+        rbs = torch.zeros((NDIR,) + tuple(res.shape), dtype=res.dtype, device=res.device)
+        rbs[:, :, 3:-3, 3:-3] = 1.0
+        wbs = op.vjp(w_dev, rbs)
+        torch.cuda.synchronize()
+        a_ev.record(stream)
+        for _ in range(2):
+            op.vjp(w_dev, rbs, wbs)
+        b_ev.record(stream)
+        torch.cuda.synchronize()
+        bms = a_ev.elapsed_time(b_ev) / 2
         vjp = {"value": IM * JM / (vms / 1e3) / 1e6, "unit": UNIT, "ms_per_vjp": vms,
-               "note": "flux_num_dnc5_2d_b (residual VJP, one cotangent) per call, device arrays, not L2-flushed"}
+               "note": "flux_num_dnc5_2d_b (residual VJP, one cotangent) per call, device arrays, not L2-flushed",
+               "batched": {"value": IM * JM * NDIR / (bms / 1e3) / 1e6, "unit": UNIT, "cotangents_per_call": NDIR,
+                           "ms_per_call": bms,
+                           "note": "bcg_flux_num_dnc5_2d_bn: %d cotangents per call, device arrays" % NDIR}}
 
     # end to end through the C ABI with pinned host buffers
     e2e = None

@@ -35,6 +35,7 @@ SIGNATURES = {
     **{"bcg_flux_num_dnc%d%s_2d_d" % (o, v): "pppp" + "pppppppp" + "i" + "d" * 11 + "ii"
        for o in (3, 7, 9) for v in ("", "_nowall")},
     "bcg_flux_num_dnc5_2d_b": "pppp" + "pppppppp" + "i" + "d" * 11 + "ii",
+    "bcg_flux_num_dnc5_2d_bn": "ppppi" + "pppppppp" + "i" + "d" * 11 + "ii",
     "bcg_flux_num_dnc5_nowall_2d_b": "pppp" + "pppppppp" + "i" + "d" * 11 + "ii",
     "bcg_bc_wall_viscous_adia_2d": "psdpiii",
     "bcg_bc_wall_viscous_adia_2d_d": "ppsdpiii",

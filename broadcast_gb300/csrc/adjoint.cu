@@ -45,6 +45,17 @@ enum CellAdj {
   NCADJ
 };
 
+// cotangent of a batched call: blockIdx.y (every kernel below runs one
+// cotangent per grid row; its residub / wb planes are cstride doubles apart,
+// its records and gathered adjoints kstride doubles apart in the scratch)
+BCG_HD size_t ycot() {
+#ifdef __CUDA_ARCH__
+  return blockIdx.y;
+#else
+  return 0;
+#endif
+}
+
 struct AdjCtx {
   Ext e;
   Coef c;
@@ -59,6 +70,8 @@ struct AdjCtx {
   double* __restrict__ rec1;       // i-face records NREC x nn
   double* __restrict__ rec2;       // j-face records
   size_t nn;                       // (im+1)(jm+1)
+  size_t cstride;                  // doubles between the residub planes of consecutive cotangents
+  size_t kstride;                  // doubles between the scratch blocks of consecutive cotangents
 
   BCG_HD double W(int i, int j, int v) const { return __ldg(w + (size_t)e.cidx(i, j) + (size_t)(v - 1) * e.np); }
   BCG_HD double P(int f, int i, int j) const { return __ldg(pr + (size_t)f * e.np + e.cidx(i, j)); }
@@ -76,7 +89,7 @@ struct AdjCtx {
   BCG_HD double VOLF(int i, int j, int d) const { return __ldg(volf + (size_t)(d - 1) * e.np + e.cidx(i, j)); }
   BCG_HD double RB(int i, int j, int v) const {
     if (i < 1 || i > e.im || j < 1 || j > e.jm) return 0.0;
-    return __ldg(rb + (size_t)e.cidx(i, j) + (size_t)(v - 1) * e.np);
+    return __ldg(rb + ycot() * cstride + (size_t)e.cidx(i, j) + (size_t)(v - 1) * e.np);
   }
   BCG_HD static double q4(double a, double b, double cc, double d) { return -a + 9.0 * b + 9.0 * cc - d; }
 };
@@ -406,10 +419,12 @@ __global__ void __launch_bounds__(128) k_adj_faces(AdjCtx a) {
   const int nI = e.im + 1;
   if (t >= nI * (e.jm + 1)) return;
   const int i = 1 + t % nI, j = 1 + t / nI;
-  if (j <= e.jm) face_rev(a, 1, i, j, a.rec1, a.nn, t);
+  double* rec1 = a.rec1 + ycot() * a.kstride;
+  double* rec2 = a.rec2 + ycot() * a.kstride;
+  if (j <= e.jm) face_rev(a, 1, i, j, rec1, a.nn, t);
   if (i <= e.im) {
-    if (j == 1 && a.c.wall) wall_rev(a, i, a.rec2, a.nn, t);
-    else face_rev(a, 2, i, j, a.rec2, a.nn, t);
+    if (j == 1 && a.c.wall) wall_rev(a, i, rec2, a.nn, t);
+    else face_rev(a, 2, i, j, rec2, a.nn, t);
   }
 }
 
@@ -426,10 +441,9 @@ struct GatherCtx {
   const double* __restrict__ ny;
   const double* __restrict__ vol;
   double* __restrict__ cadj;  // NCADJ x np
+  size_t kstride;             // doubles between the scratch blocks of consecutive cotangents
   BCG_HD bool ifx(int i, int j) const { return i >= 1 && i <= e.im + 1 && j >= 1 && j <= e.jm; }
   BCG_HD bool jfx(int i, int j) const { return i >= 1 && i <= e.im && j >= 1 && j <= e.jm + 1; }
-  BCG_HD double R1(int f, int i, int j) const { return __ldg(rec1 + (size_t)f * nn + (i - 1) + (size_t)(j - 1) * (e.im + 1)); }
-  BCG_HD double R2(int f, int i, int j) const { return __ldg(rec2 + (size_t)f * nn + (i - 1) + (size_t)(j - 1) * (e.im + 1)); }
 };
 
 // weights of the line stencils, indexed by (cell - face) offset s in [-3, 2]
@@ -449,6 +463,11 @@ BCG_HD double w_row(int s) {  // -1 7 7 -1 over offsets 0..3 from the first row
 }
 
 __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
+  // this cotangent's records
+  const double* __restrict__ rec1 = g.rec1 + ycot() * g.kstride;
+  const double* __restrict__ rec2 = g.rec2 + ycot() * g.kstride;
+  auto R1 = [&](int f, int i, int j) { return __ldg(rec1 + (size_t)f * g.nn + (i - 1) + (size_t)(j - 1) * (g.e.im + 1)); };
+  auto R2 = [&](int f, int i, int j) { return __ldg(rec2 + (size_t)f * g.nn + (i - 1) + (size_t)(j - 1) * (g.e.im + 1)); };
   const Ext& e = g.e;
   const Coef& c = g.c;
   const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -465,26 +484,26 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
     if (!g.ifx(i, cj)) continue;
     const double we = w_euler(c, s), wp = w_pred(c, s);
     for (int v = 0; v < 5; ++v) {
-      fb[v] += we * g.R1(R_EA + v, i, cj);
-      gb[v] += we * g.R1(R_EB + v, i, cj);
-      wb[v] += wp * g.R1(R_PR + v, i, cj);
+      fb[v] += we * R1(R_EA + v, i, cj);
+      gb[v] += we * R1(R_EB + v, i, cj);
+      wb[v] += wp * R1(R_PR + v, i, cj);
     }
   }
   // differences, Roe average, sensor pressure: faces (ci, cj) [cell = R] and (ci+1, cj) [cell = L]
   if (g.ifx(ci, cj)) {
-    for (int v = 0; v < 5; ++v) wb[v] += g.R1(R_DF + v, ci, cj);
-    wb[0] += g.R1(R_ROE + 4, ci, cj); wb[1] += g.R1(R_ROE + 5, ci, cj); wb[2] += g.R1(R_ROE + 6, ci, cj);
-    ub[3] += g.R1(R_ROE + 7, ci, cj);
+    for (int v = 0; v < 5; ++v) wb[v] += R1(R_DF + v, ci, cj);
+    wb[0] += R1(R_ROE + 4, ci, cj); wb[1] += R1(R_ROE + 5, ci, cj); wb[2] += R1(R_ROE + 6, ci, cj);
+    ub[3] += R1(R_ROE + 7, ci, cj);
   }
   if (g.ifx(ci + 1, cj)) {
-    for (int v = 0; v < 5; ++v) wb[v] -= g.R1(R_DF + v, ci + 1, cj);
-    wb[0] += g.R1(R_ROE + 0, ci + 1, cj); wb[1] += g.R1(R_ROE + 1, ci + 1, cj); wb[2] += g.R1(R_ROE + 2, ci + 1, cj);
-    ub[3] += g.R1(R_ROE + 3, ci + 1, cj);
+    for (int v = 0; v < 5; ++v) wb[v] -= R1(R_DF + v, ci + 1, cj);
+    wb[0] += R1(R_ROE + 0, ci + 1, cj); wb[1] += R1(R_ROE + 1, ci + 1, cj); wb[2] += R1(R_ROE + 2, ci + 1, cj);
+    ub[3] += R1(R_ROE + 3, ci + 1, cj);
   }
   if (c.k2 != 0.0) {  // pressure of the sensor: face i uses LL=i-2, L=i-1, R=i, RR=i+1
     for (int k = 0; k < 4; ++k) {
       const int i = ci + 2 - k;  // cell = i-2+k
-      if (g.ifx(i, cj)) pb += g.R1(R_SP + k, i, cj);
+      if (g.ifx(i, cj)) pb += R1(R_SP + k, i, cj);
     }
   }
   // viscous: i-faces (i, j) with i - ci in [-1, 2] and j - cj in [-2, 2]
@@ -511,12 +530,12 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
       }
       if (wN == 0.0 && wS == 0.0 && wE == 0.0 && wO == 0.0 && wuu == 0.0) continue;
       for (int v = 0; v < 4; ++v)
-        ub[v] += wN * g.R1(R_VS + 4 * v + 0, i, j) + wS * g.R1(R_VS + 4 * v + 1, i, j) +
-                 wE * g.R1(R_VS + 4 * v + 2, i, j) + wO * g.R1(R_VS + 4 * v + 3, i, j);
-      ub[0] += wuu * g.R1(R_VM + 0, i, j);
-      ub[1] += wuu * g.R1(R_VM + 1, i, j);
-      ub[2] += wuu * g.R1(R_VM + 2, i, j);
-      mub += wuu * g.R1(R_VM + 3, i, j);
+        ub[v] += wN * R1(R_VS + 4 * v + 0, i, j) + wS * R1(R_VS + 4 * v + 1, i, j) +
+                 wE * R1(R_VS + 4 * v + 2, i, j) + wO * R1(R_VS + 4 * v + 3, i, j);
+      ub[0] += wuu * R1(R_VM + 0, i, j);
+      ub[1] += wuu * R1(R_VM + 1, i, j);
+      ub[2] += wuu * R1(R_VM + 2, i, j);
+      mub += wuu * R1(R_VM + 3, i, j);
     }
   // ---- j-faces -------------------------------------------------------------
   // Euler: generic faces j >= 4 over rows j-3..j+2; near-wall faces 2, 3 over
@@ -526,13 +545,13 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
     const int j = cj - s;
     if (j < jgen || !g.jfx(ci, j)) continue;
     const double we = w_euler(c, s);
-    for (int v = 0; v < 5; ++v) { fb[v] += we * g.R2(R_EA + v, ci, j); gb[v] += we * g.R2(R_EB + v, ci, j); }
+    for (int v = 0; v < 5; ++v) { fb[v] += we * R2(R_EA + v, ci, j); gb[v] += we * R2(R_EB + v, ci, j); }
   }
   if (c.wall && cj >= 1 && cj <= 5) {
     for (int j = 2; j <= 3; ++j) {
       if (!g.jfx(ci, j)) continue;
       const double we = (j == 3) ? c.c5[cj - 1] : c.c3w[cj - 1];
-      for (int v = 0; v < 5; ++v) { fb[v] += we * g.R2(R_EA + v, ci, j); gb[v] += we * g.R2(R_EB + v, ci, j); }
+      for (int v = 0; v < 5; ++v) { fb[v] += we * R2(R_EA + v, ci, j); gb[v] += we * R2(R_EB + v, ci, j); }
     }
   }
   // predictor: all j-faces j >= 2 (j >= 1 without the wall)
@@ -540,32 +559,32 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
     const int j = cj - s;
     if (j < jfirst || !g.jfx(ci, j)) continue;
     const double wp = w_pred(c, s);
-    for (int v = 0; v < 5; ++v) wb[v] += wp * g.R2(R_PR + v, ci, j);
+    for (int v = 0; v < 5; ++v) wb[v] += wp * R2(R_PR + v, ci, j);
   }
   if (cj >= jfirst && g.jfx(ci, cj)) {
-    for (int v = 0; v < 5; ++v) wb[v] += g.R2(R_DF + v, ci, cj);
-    wb[0] += g.R2(R_ROE + 4, ci, cj); wb[1] += g.R2(R_ROE + 5, ci, cj); wb[2] += g.R2(R_ROE + 6, ci, cj);
-    ub[3] += g.R2(R_ROE + 7, ci, cj);
+    for (int v = 0; v < 5; ++v) wb[v] += R2(R_DF + v, ci, cj);
+    wb[0] += R2(R_ROE + 4, ci, cj); wb[1] += R2(R_ROE + 5, ci, cj); wb[2] += R2(R_ROE + 6, ci, cj);
+    ub[3] += R2(R_ROE + 7, ci, cj);
   }
   if (cj + 1 >= jfirst && g.jfx(ci, cj + 1)) {
-    for (int v = 0; v < 5; ++v) wb[v] -= g.R2(R_DF + v, ci, cj + 1);
-    wb[0] += g.R2(R_ROE + 0, ci, cj + 1); wb[1] += g.R2(R_ROE + 1, ci, cj + 1); wb[2] += g.R2(R_ROE + 2, ci, cj + 1);
-    ub[3] += g.R2(R_ROE + 3, ci, cj + 1);
+    for (int v = 0; v < 5; ++v) wb[v] -= R2(R_DF + v, ci, cj + 1);
+    wb[0] += R2(R_ROE + 0, ci, cj + 1); wb[1] += R2(R_ROE + 1, ci, cj + 1); wb[2] += R2(R_ROE + 2, ci, cj + 1);
+    ub[3] += R2(R_ROE + 3, ci, cj + 1);
   }
   if (c.k2 != 0.0) {
     for (int k = 0; k < 4; ++k) {
       const int j = cj + 2 - k;
-      if (j >= jfirst && g.jfx(ci, j)) pb += g.R2(R_SP + k, ci, j);
+      if (j >= jfirst && g.jfx(ci, j)) pb += R2(R_SP + k, ci, j);
     }
   }
   // wall faces (i, 1): p(i,1), p(i,2), mu(i,1), u v w (i,1)
   if (c.wall && g.jfx(ci, 1)) {
     if (cj == 1) {
-      pb += g.R2(W_P1, ci, 1);
-      mub += g.R2(W_MU, ci, 1);
-      ub[0] += g.R2(W_U, ci, 1); ub[1] += g.R2(W_V, ci, 1); ub[2] += g.R2(W_W, ci, 1);
+      pb += R2(W_P1, ci, 1);
+      mub += R2(W_MU, ci, 1);
+      ub[0] += R2(W_U, ci, 1); ub[1] += R2(W_V, ci, 1); ub[2] += R2(W_W, ci, 1);
     } else if (cj == 2) {
-      pb += g.R2(W_P2, ci, 1);
+      pb += R2(W_P2, ci, 1);
     }
   }
   // viscous j-faces (i, j) with i - ci in [-2, 2] and j - cj in [-1, 2]
@@ -593,18 +612,18 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
       }
       if (wN == 0.0 && wS == 0.0 && wE == 0.0 && wO == 0.0 && wuu == 0.0) continue;
       for (int v = 0; v < 4; ++v)
-        ub[v] += wN * g.R2(R_VS + 4 * v + 0, i, j) + wS * g.R2(R_VS + 4 * v + 1, i, j) +
-                 wE * g.R2(R_VS + 4 * v + 2, i, j) + wO * g.R2(R_VS + 4 * v + 3, i, j);
-      ub[0] += wuu * g.R2(R_VM + 0, i, j);
-      ub[1] += wuu * g.R2(R_VM + 1, i, j);
-      ub[2] += wuu * g.R2(R_VM + 2, i, j);
-      mub += wuu * g.R2(R_VM + 3, i, j);
+        ub[v] += wN * R2(R_VS + 4 * v + 0, i, j) + wS * R2(R_VS + 4 * v + 1, i, j) +
+                 wE * R2(R_VS + 4 * v + 2, i, j) + wO * R2(R_VS + 4 * v + 3, i, j);
+      ub[0] += wuu * R2(R_VM + 0, i, j);
+      ub[1] += wuu * R2(R_VM + 1, i, j);
+      ub[2] += wuu * R2(R_VM + 2, i, j);
+      mub += wuu * R2(R_VM + 3, i, j);
     }
   // ---- gradient adjoints (interior cells, sensor only) ----------------------
   double gsb[4] = {0, 0, 0, 0};  // ux, uy, vx, vy
   if (c.k2 != 0.0 && ci >= 1 && ci <= e.im && cj >= 1 && cj <= e.jm) {
     auto addg = [&](double s, const double* base, int f0, int i, int j, bool i_face) {
-      for (int k = 0; k < 4; ++k) gsb[k] += s * (i_face ? g.R1(f0 + k, i, j) : g.R2(f0 + k, i, j));
+      for (int k = 0; k < 4; ++k) gsb[k] += s * (i_face ? R1(f0 + k, i, j) : R2(f0 + k, i, j));
       (void)base;
     };
     if (g.ifx(ci, cj)) addg(1.0, nullptr, R_SG + 4, ci, cj, true);        // as R
@@ -621,7 +640,7 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
     if (cj == e.jm - 1) addg(-1.0, nullptr, R_SG + 4, ci, e.jm + 1, false);
   }
   // store
-  double* o = g.cadj;
+  double* o = g.cadj + ycot() * g.kstride;
   const size_t np = e.np;
   o[A_U * np + q] = ub[0]; o[A_V * np + q] = ub[1]; o[A_W * np + q] = ub[2]; o[A_T * np + q] = ub[3];
   o[A_P * np + q] = pb; o[A_MU * np + q] = mub;
@@ -650,10 +669,13 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
 
 // Final: transposed gradient stencil, reverse of the primitive map, zero rb.
 __global__ void __launch_bounds__(256) k_adj_final(Ext e, Coef c, const double* __restrict__ w,
-                                                   const double* __restrict__ cadj, double* __restrict__ wbo,
-                                                   double* __restrict__ rb) {
+                                                   const double* __restrict__ cadj0, double* __restrict__ wbo0,
+                                                   double* __restrict__ rb0, size_t cstride, size_t kstride) {
   const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= e.np) return;
+  const double* __restrict__ cadj = cadj0 + blockIdx.y * kstride;
+  double* __restrict__ wbo = wbo0 + blockIdx.y * cstride;
+  double* __restrict__ rb = rb0 + blockIdx.y * cstride;
   const size_t np = e.np;
   auto A = [&](int f, long long qq) { return __ldg(cadj + (size_t)f * np + (size_t)qq); };
   const int ci = (int)(q % e.ni) + 1 - e.gh, cj = (int)(q / e.ni) + 1 - e.gh;
@@ -714,10 +736,15 @@ __global__ void __launch_bounds__(256) k_adj_final(Ext e, Coef c, const double* 
     for (int k = 0; k < 5; ++k) rb[q + (size_t)k * np] = 0.0;
 }
 
-size_t adjoint_scratch_doubles(int im, int jm, int gh) {
+size_t adjoint_cotangent_doubles(int im, int jm, int gh) {
   const Ext e = make_ext(im, jm, gh);
   const size_t nn = (size_t)(im + 1) * (jm + 1);
-  return (size_t)(F_NPRIM + G_NGRAD + NCADJ) * e.np + 2 * (size_t)NREC * nn;
+  return (size_t)NCADJ * e.np + 2 * (size_t)NREC * nn;
+}
+
+size_t adjoint_scratch_doubles(int im, int jm, int gh, int ncot) {
+  const Ext e = make_ext(im, jm, gh);
+  return (size_t)(F_NPRIM + G_NGRAD) * e.np + (size_t)(ncot > 1 ? ncot : 1) * adjoint_cotangent_doubles(im, jm, gh);
 }
 
 cudaError_t run_adjoint(const AdjointArgs& a, cudaStream_t st) {
@@ -731,13 +758,16 @@ cudaError_t run_adjoint(const AdjointArgs& a, cudaStream_t st) {
   double* rec1 = cadj + (size_t)NCADJ * e.np;
   double* rec2 = rec1 + (size_t)NREC * nn;
   const int B = 256;
-  launch_primal_passes(e, c, a.w, pr, gr, a.nx, a.ny, a.vol, st);
-  AdjCtx ac{e, c, a.w, pr, gr, a.nx, a.ny, a.vol, a.volf, a.rb, rec1, rec2, nn};
+  const unsigned ncot = a.ncot > 1 ? (unsigned)a.ncot : 1u;
+  const size_t cstride = a.cstride ? a.cstride : (size_t)5 * e.np;
+  const size_t kstride = adjoint_cotangent_doubles(a.im, a.jm, a.gh);
+  launch_primal_passes(e, c, a.w, pr, gr, a.nx, a.ny, a.vol, st);  // shared by the cotangents
+  AdjCtx ac{e, c, a.w, pr, gr, a.nx, a.ny, a.vol, a.volf, a.rb, rec1, rec2, nn, cstride, kstride};
   const int BF = 128;
-  k_adj_faces<<<(unsigned)((nn + BF - 1) / BF), BF, 0, st>>>(ac);
-  GatherCtx gc{e, c, rec1, rec2, nn, a.nx, a.ny, a.vol, cadj};
-  k_adj_gather<<<(unsigned)((e.np + BF - 1) / BF), BF, 0, st>>>(gc);
-  k_adj_final<<<(unsigned)((e.np + B - 1) / B), B, 0, st>>>(e, c, a.w, cadj, a.wb, a.rb);
+  k_adj_faces<<<dim3((unsigned)((nn + BF - 1) / BF), ncot), BF, 0, st>>>(ac);
+  GatherCtx gc{e, c, rec1, rec2, nn, a.nx, a.ny, a.vol, cadj, kstride};
+  k_adj_gather<<<dim3((unsigned)((e.np + BF - 1) / BF), ncot), BF, 0, st>>>(gc);
+  k_adj_final<<<dim3((unsigned)((e.np + B - 1) / B), ncot), B, 0, st>>>(e, c, a.w, cadj, a.wb, a.rb, cstride, kstride);
   return cudaGetLastError();
 }
 

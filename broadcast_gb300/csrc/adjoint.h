@@ -18,9 +18,14 @@ struct AdjointArgs {
   double* wb;           // (ni, nj, 5): overwritten on every padded cell
   double* scratch;      // adjoint_scratch_doubles(im, jm, gh) doubles
   int nowall;           // 1: flux_num_dnc5_nowall_2d_b (centred rows everywhere, no wall face)
+  int ncot;             // cotangents in this call (0 or 1: one); rb and wb hold ncot blocks
+  size_t cstride;       // doubles between consecutive cotangents' rb / wb blocks (0: 5 * padded cells)
 };
 
-size_t adjoint_scratch_doubles(int im, int jm, int gh);
+// scratch of one call: primitives and gradients once, then per cotangent its
+// gathered adjoints and face records
+size_t adjoint_scratch_doubles(int im, int jm, int gh, int ncot = 1);
+size_t adjoint_cotangent_doubles(int im, int jm, int gh);
 cudaError_t run_adjoint(const AdjointArgs& a, cudaStream_t st);
 
 }  // namespace bcg

@@ -636,7 +636,8 @@ int bcg_coeffs_5p_dz2_dn(double* dz2_out, const double* w, const double* wd, int
 namespace {
 int adjoint_call(double* residub, const double* w, double* wb, const double* nx, const double* ny, const double* vol,
                  const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs,
-                 double muref, double tref, double s_suth, double k2, double k4, int im, int jm, int nowall);
+                 double muref, double tref, double s_suth, double k2, double k4, int im, int jm, int nowall,
+                 int nd = 1);
 }
 
 int bcg_flux_num_dnc5_2d_b(double* residu, double* residub, const double* w, double* wb, const double* x0,
@@ -660,20 +661,39 @@ int bcg_flux_num_dnc5_nowall_2d_b(double* residu, double* residub, const double*
                       k4, im, jm, 1);
 }
 
+// nd cotangents in one call (no reference counterpart: the drivers call
+// flux_num_dnc5_2d_b once per seed, cylinder.py:1116-1159): residub and wb
+// hold nd consecutive (ni, nj, 5) blocks; the primal passes run once per
+// launch and every cotangent's face records, gather and primitive reverse
+// run as one grid row of the same kernels.
+int bcg_flux_num_dnc5_2d_bn(double* residu, double* residub, const double* w, double* wb, int nd, const double* x0,
+                            const double* y0, const double* nx, const double* ny, const double* xc, const double* yc,
+                            const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
+                            double gam, double rgaz, double cs, double muref, double tref, double s_suth, double k2,
+                            double k4, int im, int jm) {
+  (void)residu; (void)x0; (void)y0; (void)xc; (void)yc;
+  if (nd < 0) return fail_arg("flux_num_dnc5_2d_bn: negative cotangent count");
+  if (nd == 0) return BCG_OK;
+  return adjoint_call(residub, w, wb, nx, ny, vol, volf, gh, cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2,
+                      k4, im, jm, 0, nd);
+}
+
 }  // extern "C"
 
 namespace {
 int adjoint_call(double* residub, const double* w, double* wb, const double* nx, const double* ny, const double* vol,
                  const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz, double cs,
-                 double muref, double tref, double s_suth, double k2, double k4, int im, int jm, int nowall) {
+                 double muref, double tref, double s_suth, double k2, double k4, int im, int jm, int nowall,
+                 int nd) {
   if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
   if (!dims_ok(im, jm, gh)) return fail_arg("flux_num_dnc5_2d_b: need gh == 3 and im, jm >= 6");
+  if (!residub || !w || !wb) return fail_arg("flux_num_dnc5_2d_b: residub, w and wb are required");
   const size_t np = ncell(im, jm, gh), nn = nnode(im, jm, gh);
   cudaStream_t st = current_stream();
   Stager sg(st);
   const int hw = sg.in(w, np * 5 * 8), hnx = sg.in(nx, nn * 2 * 8), hny = sg.in(ny, nn * 2 * 8);
   const int hvol = sg.in(vol, np * 8), hvolf = sg.in(volf, np * 2 * 8);
-  const int hrb = sg.inout(residub, np * 5 * 8), hwb = sg.out(wb, np * 5 * 8);
+  const int hrb = sg.inout(residub, np * 5 * 8 * (size_t)nd), hwb = sg.out(wb, np * 5 * 8 * (size_t)nd);
   int rc = sg.commit();
   if (rc) return rc;
   AdjointArgs a{};
@@ -681,12 +701,24 @@ int adjoint_call(double* residub, const double* w, double* wb, const double* nx,
   a.phys = Phys{cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4};
   a.w = sg.dev<double>(hw); a.nx = sg.dev<double>(hnx); a.ny = sg.dev<double>(hny);
   a.vol = sg.dev<double>(hvol); a.volf = sg.dev<double>(hvolf);
-  a.rb = sg.dev<double>(hrb); a.wb = sg.dev<double>(hwb);
   a.nowall = nowall;
-  a.scratch = (double*)pool_get(POOL_SCRATCH, adjoint_scratch_doubles(im, jm, gh) * 8);
-  if (!a.scratch) return fail_arg("scratch allocation failed"), BCG_ERR_NOMEM;
-  cudaError_t e = run_adjoint(a, st);
-  if (e != cudaSuccess) return fail_cuda("flux_num_dnc5_2d_b", e);
+  a.cstride = np * 5;
+  double* rb = sg.dev<double>(hrb);
+  double* wbd = sg.dev<double>(hwb);
+  // as many cotangents per launch as fit a 2 GiB scratch budget
+  const size_t per = adjoint_cotangent_doubles(im, jm, gh);
+  const int cmax = (int)std::max<size_t>(1, ((size_t)2 << 30) / (per * 8));
+  for (int off = 0; off < nd;) {
+    const int n = std::min(nd - off, cmax);
+    a.ncot = n;
+    a.rb = rb + (size_t)off * np * 5;
+    a.wb = wbd + (size_t)off * np * 5;
+    a.scratch = (double*)pool_get(POOL_SCRATCH, adjoint_scratch_doubles(im, jm, gh, n) * 8);
+    if (!a.scratch) return fail_arg("scratch allocation failed"), BCG_ERR_NOMEM;
+    cudaError_t e = run_adjoint(a, st);
+    if (e != cudaSuccess) return fail_cuda("flux_num_dnc5_2d_b", e);
+    off += n;
+  }
   return sg.finish();
 }
 }  // namespace

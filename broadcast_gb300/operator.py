@@ -74,8 +74,16 @@ class Dnc5Operator:
         return res, (resd[0] if single else resd)
 
     def vjp(self, w, rb, wb=None):
-        """wb = (dR/dw)^T rb over every padded cell (rb: interior cotangent,
-        left unchanged here; the library consumes a copy)."""
+        """wb = (dR/dw)^T rb over every padded cell; rb is one interior
+        cotangent (5, nj, ni) or K of them (K, 5, nj, ni), all K in one call;
+        rb is left unchanged here (the library consumes a copy)."""
+        if rb.dim() == 4:
+            k = rb.shape[0]
+            wb = self.new_state(k) if wb is None else wb
+            rbc = rb.detach().clone().contiguous()
+            _lib.call("bcg_flux_num_dnc5_2d_bn", None, rbc, w, wb, k, None, None, self.nx, self.ny, None, None,
+                      self.vol, self.volf, self.gh, *self.phys, self.im, self.jm)
+            return wb
         wb = self.new_state() if wb is None else wb
         rbc = rb.detach().clone().contiguous()
         _lib.call("bcg_flux_num_dnc5_2d_b", None, rbc, w, wb, None, None, self.nx, self.ny, None, None, self.vol,

@@ -182,6 +182,15 @@ int bcg_flux_num_dnc5_2d_b(double* residu, double* residub, const double* w, dou
                            const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
                            double gam, double rgaz, double cs, double muref, double tref, double s_suth, double k2,
                            double k4, int im, int jm);
+/* nd cotangents at once (no reference counterpart; the drivers loop over
+ * flux_num_dnc5_2d_b, cylinder.py:1116-1159): residub and wb hold nd
+ * consecutive (ni, nj, 5) blocks; same result as nd calls of
+ * bcg_flux_num_dnc5_2d_b, bit for bit. */
+int bcg_flux_num_dnc5_2d_bn(double* residu, double* residub, const double* w, double* wb, int nd, const double* x0,
+                            const double* y0, const double* nx, const double* ny, const double* xc, const double* yc,
+                            const double* vol, const double* volf, int gh, double cp, double cv, double prandtl,
+                            double gam, double rgaz, double cs, double muref, double tref, double s_suth, double k2,
+                            double k4, int im, int jm);
 
 /* ---- boundary conditions ---------------------------------------------------- */
 /* srcfv/borders/bc_wall_viscous.F90:2 ; tangent/bc_wall_viscous_d.f90:11 */

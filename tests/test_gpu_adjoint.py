@@ -119,3 +119,50 @@ def test_nowall_vjp_matches_oracle_and_tangent(kind, im, jm):
     lhs = float(np.sum(H.interior(jv) * H.interior(u)))
     rhs = float(np.sum(v * wb))
     assert abs(lhs - rhs) <= 1e-11 * max(abs(lhs), abs(rhs))
+
+
+@pytest.mark.parametrize("nd", [1, 3])
+def test_batched_vjp_equals_single_calls(nd):
+    """bcg_flux_num_dnc5_2d_bn: nd cotangents in one call (host arrays), bit
+    for bit the results of nd calls of flux_num_dnc5_2d_b, every residub
+    interior consumed."""
+    from broadcast_gb300 import _lib
+    from broadcast_gb300.srcfv import f_adj
+    c = H.cyl_case(40, 24)
+    H.oracle_bcs(c, c["w"])
+    rng = np.random.default_rng(31)
+    rbs = np.zeros(c["w"].shape + (nd,), order="F")
+    rbs[3:-3, 3:-3] = rng.standard_normal((40, 24, 5, nd))
+    rb_in = rbs.copy(order="F")
+    wbs = np.full_like(rbs, 7.0)
+    _lib.call("bcg_flux_num_dnc5_2d_bn", None, rbs, c["w"], wbs, nd, *_args(c), 40, 24)
+    assert np.all(rbs[3:-3, 3:-3] == 0.0)
+    for k in range(nd):
+        wb = np.zeros_like(c["w"])
+        f_adj.flux_num_dnc5_2d_b(None, rb_in[..., k].copy(order="F"), c["w"], wb, *_args(c))
+        assert np.array_equal(wbs[..., k], wb), k
+
+
+def test_batched_vjp_device_arrays():
+    """The operator's batched VJP (device arrays, K cotangents in one call)
+    equals K single-cotangent calls bit for bit, and matches the oracle."""
+    import torch
+    from broadcast_gb300.operator import Dnc5Operator, to_device, to_host
+    c = H.cyl_case(32, 20)
+    H.oracle_bcs(c, c["w"])
+    op = Dnc5Operator(c["grid"], c["phys"])
+    w = to_device(c["w"])
+    rng = np.random.default_rng(32)
+    k = 5
+    rbs = torch.zeros((k,) + tuple(op.state_shape), dtype=torch.float64, device="cuda")
+    rbs[:, :, 3:-3, 3:-3] = torch.from_numpy(rng.standard_normal((k, 5, 20, 32))).cuda()
+    wbs = op.vjp(w, rbs)
+    torch.cuda.synchronize()
+    for i in range(k):
+        wb1 = op.vjp(w, rbs[i])
+        assert torch.equal(wbs[i], wb1), i
+    rb0 = to_host(rbs[2], c["w"].shape)
+    ref = O.vjp(c["grid"], c["phys"], c["w"], rb0)
+    got = to_host(wbs[2], c["w"].shape)
+    sc = np.abs(ref).reshape(-1, 5).max(0)
+    assert (np.abs(got - ref).reshape(-1, 5).max(0) / sc).max() < TOL
