@@ -2,7 +2,7 @@
 own Fortran routines (translated to C by oracle/ref_translate.py, compiled by
 gcc with -ffp-contract=off).
 
-Runs only where the reference checkout is present (this build container):
+Runs only where the reference checkout is present:
     python oracle/ref_build.py [reference_root]
 Outputs go to oracle/_ref/ (git-ignored): libref.c, libref.so, signatures.json.
 """

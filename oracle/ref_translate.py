@@ -1,6 +1,6 @@
 """Test infrastructure only: translate the reference's Fortran routines into C.
 
-There is no Fortran compiler in this build environment, so to run the
+No Fortran compiler is available, so to run the
 reference's own code (the parity pin for the C++ restatement in
 broadcast_oracle.hpp) its source files are translated mechanically into C by
 this script and compiled with gcc (oracle/ref_build.py).  The translator

@@ -1,7 +1,7 @@
 """Parity of the CUDA path (libbroadcast_gb300.so through its f2py-style
 modules and the device operator API) against the CPU oracle.
 
-Tolerances (spec criteria): residual within 1e-12 of the face-flux
+Tolerances: residual within 1e-12 of the face-flux
 magnitude (max-norm per variable); tangent outputs within 1e-11 of the same
 scale times the tangent magnitude; boundary fills within 1e-13 relative;
 integer index work bit-exact.

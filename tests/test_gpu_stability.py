@@ -2,7 +2,7 @@
 the reference's per-seed loop run through the oracle (BROADCAST_npz.py:
 1068-1137, 1206-1210, 1221-1249): J/vol, Dz and Dzz of a small boundary
 layer, J(beta) = J - beta^2 Dzz + i beta Dz (biglobal.py:82), ten eigenvalues
-nearest a target by shift-invert.  Spec bar: 1e-8 relative.  PETSc /
+nearest a target by shift-invert.  Bar: 1e-8 relative.  PETSc /
 SLEPc are absent, so both sides use scipy's ARPACK + SuperLU: this pins the
 matrices handed to the eigen stage, not PETSc itself."""
 import numpy as np
