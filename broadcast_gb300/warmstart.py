@@ -114,8 +114,9 @@ class SurrogateMLP:
         self.nsplit = max(1, min(64, m // 256))
         while m % (64 * self.nsplit):
             self.nsplit -= 1
+        self.bsplit = m // 64  # column sums in chunks of 64 rows
         self.wpart = t.empty(self.nsplit * 256 * 256, dtype=t.float32, device=self.dev)
-        self.bpart = t.empty(self.nsplit * 256, dtype=t.float32, device=self.dev)
+        self.bpart = t.empty(self.bsplit * 256, dtype=t.float32, device=self.dev)
         self.lsum = t.empty(1, dtype=t.float32, device=self.dev)
         self._m = m
 
@@ -141,8 +142,8 @@ class SurrogateMLP:
             xin = self.x if li == 0 else self.y[li - 1]
             n1, n2 = DIMS[li + 1], DIMS[li]
             L("bcg_mlp_gemm_tn", self.dz[li], xin, self.wpart, m, n1, n2, self.nsplit)
-            L("bcg_mlp_colsum", self.dz[li], m, n1, self.nsplit, self.bpart)
-            L("bcg_mlp_adam", self.wpart, self.nsplit, self.bpart, self.nsplit, n1, n2, self.w[li], self.mw[li],
+            L("bcg_mlp_colsum", self.dz[li], m, n1, self.bsplit, self.bpart)
+            L("bcg_mlp_adam", self.wpart, self.nsplit, self.bpart, self.bsplit, n1, n2, self.w[li], self.mw[li],
               self.vw[li], self.b[li], self.mb[li], self.vb[li], self.wbf[li], self.wtbf[li], float(lr), beta1, beta2,
               eps, grads[li] if grads is not None else None)
 
