@@ -1,20 +1,27 @@
 """Benchmark of the FP64 DNC5 residual + JVP hot path on GB300.
 
-Workload (the reference's second configuration): 2-D cylinder O-mesh,
-256 (azimuth, periodic) x 256 (radial) cells, outer radius 50 D, radial
-stretching 1.05, Mach 0.1, Re 47, seeded uniform-flow state plus 1e-3 noise,
-32 seeded Gaussian direction vectors.  One step = the residual R(w) and the 32
-Jacobian-vector products dR/dw . v_k, i.e. 256*256*32 cell evaluations of
-residual + JVP.  The metric is Mcells/s = interior cells x directions / s.
+Default workload (the largest residual + JVP configuration that fits one GPU):
+64 independent laminar boundary layers of uneven size, nx ~ U{200..1200},
+ny ~ U{80..300}, Mach ~ U(0.3, 0.8) (default_rng(4), 9.59M interior cells),
+Blasius state plus seeded 1e-4 noise, one seeded Gaussian direction per grid.
+One step = the residual and one Jacobian-vector product of every grid, run
+as one CUDA graph of persistent launches over the tiles of all grids.  The
+metric is Mcells/s = interior cells / s (one residual + one JVP per cell).
 
   value : kernels only, inputs resident in HBM, L2 flushed between steps
-  e2e   : through the C ABI (bcg_flux_num_dnc5_2d_dn) with pinned host arrays,
-          host->device and device->host copies inside the timed region
+  e2e   : through the C ABI (bcg_batch_run_host) with pinned host arrays:
+          state, direction and metrics uploaded and the residual and tangent
+          interiors downloaded inside the timed region, every step
+
+The 256x256 cylinder line (residual + 32 directions, VJP) rides along as the
+key "cylinder_256" (or alone with --workload cylinder); the other workloads
+(jacobian, impli, newton, warmstart) print their own lines.
 
 python bench.py [--gpus N --steps K --warmup W] [--impl reference]
-Under torchrun each rank runs its own 32 directions (weak scaling); rank 0
+Under torchrun each rank runs its own copy of the batch (weak scaling); rank 0
 prints one JSON line.  --impl reference times the reference path's CPU
-restatement (the oracle port, OpenMP on all host cores) on the same workload.
+restatement (the oracle port, OpenMP on all host cores) on the same grids,
+states and directions.
 """
 import argparse
 import json
@@ -252,17 +259,27 @@ def run_reference(args):
     return 0
 
 
-def run_ours(args):
+# FP64 lane instructions (DFMA + DADD + DMUL) and DRAM bytes per cell and
+# direction of the passes of the 256x256 cylinder line (residual + 32
+# directions in groups of 4), from one ncu capture of that command:
+#   ncu --clock-control none -k regex:"k_(prim|qrows|vpts|faces|balance)" --metrics
+#       smsp__sass_thread_inst_executed_op_dfma_pred_on.sum,
+#       smsp__sass_thread_inst_executed_op_dadd_pred_on.sum,
+#       smsp__sass_thread_inst_executed_op_dmul_pred_on.sum,
+#       dram__bytes_read.sum,dram__bytes_write.sum
+#       python bench.py --workload cylinder --steps 1 --warmup 1 --no-extras
+# divided by cells x directions.
+CYL_NCU = None
+
+
+def cylinder_measure(args, dev, extras_only=False, ws=1, rank=0):
+    """Residual + JVP for NDIR directions on the 256x256 cylinder: kernel time
+    (CUDA events, L2 flushed between steps), e2e through
+    bcg_flux_num_dnc5_2d_dn with pinned host arrays, and the VJP with one and
+    with NDIR cotangents per call."""
     import torch
-    ws, rank, local = _dist()
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", init_method="env://")
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
     from broadcast_gb300 import _lib
     from broadcast_gb300.operator import Dnc5Operator, to_device
-
     c, wds = build_workload()
     op = Dnc5Operator(c["grid"], c["phys"], device=dev)
     w_dev = to_device(c["w"], dev)
@@ -271,157 +288,151 @@ def run_ours(args):
     resd = op.new_state(NDIR)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
     stream = torch.cuda.current_stream(dev)
+    steps = args.steps if not extras_only else min(args.steps, 10)
 
     def step():
-        # one call: each pass of the kernel runs the 8 groups of 4 directions
-        # as two launches of 4 groups (blockIdx.y = group) on two streams
+        # one call: each pass runs the 8 groups of 4 directions as two
+        # launches of 4 groups (blockIdx.y = group) on two streams
         op.jvp(w_dev, wd_dev, res=res, resd=resd)
 
     for _ in range(max(args.warmup, 1)):
         step()
     torch.cuda.synchronize()
-    sampler = ClockSampler(local)
-    if rank == 0:
+    sampler = ClockSampler(dev.index or 0)
+    if rank == 0 and not extras_only:
         sampler.start()
-    # untimed steps right before the timed region, so that the clock samples
-    # (one per 100 ms) see the GPU under this load
     t0 = time.perf_counter()
     while time.perf_counter() - t0 < 0.3:
         step()
         torch.cuda.synchronize()
     if ws > 1:
+        import torch.distributed as dist
         dist.barrier()
     torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    for s in range(args.steps):
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for s_ in range(steps):
         flush.add_(1.0)
-        ev[s][0].record(stream)
+        ev[s_][0].record(stream)
         step()
-        ev[s][1].record(stream)
+        ev[s_][1].record(stream)
     torch.cuda.synchronize()
     if ws > 1:
         dist.barrier()
-    clocks = sampler.stop() if rank == 0 else None
+    clocks = sampler.stop() if (rank == 0 and not extras_only) else None
     if clocks:
         clocks["window"] = "0.3 s of the same step untimed, then the timed region"
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    tot_ms = sum(step_ms)
+    tot_ms = sum(a.elapsed_time(b) for a, b in ev)
     if ws > 1:
         t = torch.tensor([tot_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         tot_ms = float(t.item())
-    units = IM * JM * NDIR * args.steps * ws
-    value = units / (tot_ms / 1e3) / 1e6
-
-    # adjoint (VJP) throughput on the same grid, device arrays, one cotangent per call
-    vjp = None
-    if rank == 0:
-        rb = torch.zeros_like(res)
-        rb[:, 3:-3, 3:-3] = 1.0
-        wb = op.new_state()
+    out = {"value": IM * JM * NDIR * ws * steps / (tot_ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": tot_ms / steps,
+           "steps": steps, "clocks": clocks,
+           "workload": "cylinder O-mesh %dx%d (r 0.5..50 D, stretch 1.05), Mach 0.1, Re 47; residual + JVP for %d "
+                       "seeded Gaussian directions per step, L2 flushed between steps" % (IM, JM, NDIR)}
+    if rank != 0:
+        return out
+    # VJP on the same grid, device arrays: one cotangent per call, then NDIR in one call
+    rb = torch.zeros_like(res)
+    rb[:, 3:-3, 3:-3] = 1.0
+    wb = op.new_state()
+    op.vjp(w_dev, rb, wb)
+    torch.cuda.synchronize()
+    a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nv = 8
+    a_ev.record(stream)
+    for _ in range(nv):
         op.vjp(w_dev, rb, wb)
-        torch.cuda.synchronize()
-        a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        nv = 8
-        a_ev.record(stream)
-        for _ in range(nv):
-            op.vjp(w_dev, rb, wb)
-        b_ev.record(stream)
-        torch.cuda.synchronize()
-        vms = a_ev.elapsed_time(b_ev) / nv
-        # NDIR cotangents in one call (bcg_flux_num_dnc5_2d_bn)
-        rbs = torch.zeros((NDIR,) + tuple(res.shape), dtype=res.dtype, device=res.device)
-        rbs[:, :, 3:-3, 3:-3] = 1.0
-        wbs = op.vjp(w_dev, rbs)
-        torch.cuda.synchronize()
-        a_ev.record(stream)
-        for _ in range(2):
-            op.vjp(w_dev, rbs, wbs)
-        b_ev.record(stream)
-        torch.cuda.synchronize()
-        bms = a_ev.elapsed_time(b_ev) / 2
-        vjp = {"value": IM * JM / (vms / 1e3) / 1e6, "unit": UNIT, "ms_per_vjp": vms,
-               "note": "flux_num_dnc5_2d_b (residual VJP, one cotangent) per call, device arrays, not L2-flushed",
-               "batched": {"value": IM * JM * NDIR / (bms / 1e3) / 1e6, "unit": UNIT, "cotangents_per_call": NDIR,
-                           "ms_per_call": bms,
-                           "note": "bcg_flux_num_dnc5_2d_bn: %d cotangents per call, device arrays" % NDIR}}
-
+    b_ev.record(stream)
+    torch.cuda.synchronize()
+    vms = a_ev.elapsed_time(b_ev) / nv
+    rbs = torch.zeros((NDIR,) + tuple(res.shape), dtype=res.dtype, device=res.device)
+    rbs[:, :, 3:-3, 3:-3] = 1.0
+    wbs = op.vjp(w_dev, rbs)
+    torch.cuda.synchronize()
+    a_ev.record(stream)
+    for _ in range(2):
+        op.vjp(w_dev, rbs, wbs)
+    b_ev.record(stream)
+    torch.cuda.synchronize()
+    bms = a_ev.elapsed_time(b_ev) / 2
+    out["vjp"] = {"value": IM * JM / (vms / 1e3) / 1e6, "unit": UNIT, "ms_per_vjp": vms,
+                  "note": "flux_num_dnc5_2d_b (residual VJP, one cotangent) per call, device arrays, not L2-flushed",
+                  "batched": {"value": IM * JM * NDIR / (bms / 1e3) / 1e6, "unit": UNIT, "cotangents_per_call": NDIR,
+                              "ms_per_call": bms,
+                              "note": "bcg_flux_num_dnc5_2d_bn: %d cotangents per call, device arrays" % NDIR}}
     # end to end through the C ABI with pinned host buffers
-    e2e = None
+    pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    w_h = pin(c["w"].size)
+    w_h[:] = np.ravel(c["w"], order="F")
+    wd_h = pin(c["w"].size * NDIR)
+    for k in range(NDIR):
+        wd_h[k * c["w"].size:(k + 1) * c["w"].size] = np.ravel(wds[k], order="F")
+    g = c["grid"]
+    geo = {k: pin(g[k].size) for k in ("nx", "ny", "vol", "volf")}
+    for k in geo:
+        geo[k][:] = np.ravel(g[k], order="F")
+    res_h, resd_h = pin(c["w"].size), pin(c["w"].size * NDIR)
+    ph = [float(c["phys"][k]) for k in Dnc5Operator.PHYS_KEYS]
+
+    def e2e_step():
+        _lib.call("bcg_flux_num_dnc5_2d_dn", res_h, resd_h, w_h, wd_h, NDIR, None, None, geo["nx"], geo["ny"],
+                  None, None, geo["vol"], geo["volf"], 3, *ph, IM, JM)
+
+    for _ in range(max(args.warmup, 1)):
+        e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        e2e_step()
+    el = time.perf_counter() - t0
+    np_, nn = (IM + 6) * (JM + 6), (IM + 7) * (JM + 7)
+    h2d = 8 * (5 * np_ * (1 + NDIR) + 4 * nn + 3 * np_)
+    d2h = 8 * 5 * IM * JM * (1 + NDIR)
+    out["e2e"] = {"value": IM * JM * NDIR * steps / el / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                  "d2h_bytes_per_step": d2h, "ms_per_step": el / steps * 1e3}
+    group_ms = tot_ms / steps / (NDIR // GROUP)
+    nb = algorithmic_bytes(IM, JM, 3, GROUP)
+    hbm_peak = _hbm_peak()
+    roof = {"bound": "fp64", "unit": "G FP64 inst/s", "achieved": None, "frac": None, "traffic": None,
+            "kernel": "fused residual+JVP pass (prim, qrows, vpts, faces, balance) per group of %d directions"
+                      % GROUP,
+            "hbm": {"achieved": nb / (group_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": nb / (group_ms / 1e3) / 1e9 / hbm_peak, "algorithmic_bytes_per_group": nb}}
+    if CYL_NCU:
+        props = torch.cuda.get_device_properties(dev)
+        mhz = (clocks or {}).get("sm_mhz") or 2070.0
+        peak = 2.0 * props.multi_processor_count * mhz * 1e6 / 1e9
+        inst = CYL_NCU["fp64_inst_per_cell_dir"] * IM * JM * NDIR
+        roof.update(peak=peak, achieved=inst / (tot_ms / steps / 1e3) / 1e9)
+        roof["frac"] = roof["achieved"] / peak
+        roof["traffic"] = CYL_NCU["dram_bytes_per_cell_dir"] * IM * JM * GROUP
+        roof["ncu_source"] = CYL_NCU["source"]
+    out["roofline"] = roof
+    out["gpu_launches"] = 5 * 2 * steps  # prim, qrows, vpts, faces, balance; two stream halves
+    return out
+
+
+def run_cylinder(args):
+    """--workload cylinder: the 256x256 cylinder residual + 32-direction JVP line."""
+    import torch
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    m = cylinder_measure(args, dev, ws=ws, rank=rank)
     if rank == 0:
-        pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
-        w_h = pin(c["w"].size)
-        w_h[:] = np.ravel(c["w"], order="F")
-        wd_h = pin(c["w"].size * NDIR)
-        for k in range(NDIR):
-            wd_h[k * c["w"].size:(k + 1) * c["w"].size] = np.ravel(wds[k], order="F")
-        g = c["grid"]
-        geo = {k: pin(g[k].size) for k in ("nx", "ny", "vol", "volf")}
-        for k in geo:
-            geo[k][:] = np.ravel(g[k], order="F")
-        res_h, resd_h = pin(c["w"].size), pin(c["w"].size * NDIR)
-        ph = [float(c["phys"][k]) for k in Dnc5Operator.PHYS_KEYS]
-
-        def e2e_step():
-            _lib.call("bcg_flux_num_dnc5_2d_dn", res_h, resd_h, w_h, wd_h, NDIR, None, None, geo["nx"], geo["ny"],
-                      None, None, geo["vol"], geo["volf"], 3, *ph, IM, JM)
-
-        for _ in range(max(args.warmup, 1)):
-            e2e_step()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            e2e_step()
-        el = time.perf_counter() - t0
-        np_, nn = (IM + 6) * (JM + 6), (IM + 7) * (JM + 7)
-        h2d = 8 * (5 * np_ * (1 + NDIR) + 4 * nn + 3 * np_)
-        d2h = 8 * 5 * IM * JM * (1 + NDIR)
-        e2e = {"value": IM * JM * NDIR * args.steps / el / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": el / args.steps * 1e3}
-
-    if rank == 0:
-        peak_fp64 = ctypes_double()
-        _lib.call("bcg_fp64_peak_tflops", peak_fp64)
-        peak_fp64 = peak_fp64[0]
-        primal, tangent = flop_counts(c)
-        per_group_ms = tot_ms / args.steps / (NDIR // GROUP)  # per GPU: every rank runs its own 8 groups
-        flops_group = primal + GROUP * tangent
-        bytes_group = algorithmic_bytes(IM, JM, 3, GROUP)
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-        hbm_peak = peaks.get("hbm_gbs", 6800.0)
-        ach_gbs = bytes_group / (per_group_ms / 1e3) / 1e9
-        ach_tf = flops_group / (per_group_ms / 1e3) / 1e12
-        traffic = _profiled_traffic()
+        c, wds = build_workload()
         cpu = cpu_baseline(c, wds[:4], seconds=args.cpu_seconds)
-        # prim, [grad,] qrows, vpts, faces, balance; twice when the groups split over two streams
-        launches_per_step = (5 + (1 if c["phys"]["k2"] != 0 else 0)) * (2 if NDIR // GROUP >= 2 else 1)
-        line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": tot_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "cylinder O-mesh %dx%d (r 0.5..50 D, stretch 1.05), Mach 0.1, Re 47; residual + "
-                                   "JVP for %d seeded Gaussian directions per step" % (IM, JM, NDIR),
-                       "cells": IM * JM, "directions_per_step": NDIR, "directions_per_launch_group": GROUP,
-                       "l2": "flushed between steps (256 MB write)", "parallelism": "replicas" if ws > 1 else "single"},
-            "roofline": {"bound": "hbm", "achieved": ach_gbs, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": ach_gbs / hbm_peak, "traffic": traffic,
-                         "kernel": "fused residual+JVP pass (prim, qrows, vpts, faces, balance), figures per group of "
-                                   "%d directions; each pass runs the %d groups as two launches on two streams"
-                                   % (GROUP, NDIR // GROUP),
-                         "fp64": {"achieved": ach_tf, "peak": peak_fp64, "unit": "TFLOP/s",
-                                  "frac": ach_tf / peak_fp64, "flops_per_group": flops_group,
-                                  "peak_source": "bcg_fp64_peak_tflops (FMA chains, measured in this run)",
-                                  "note": "flops of the reference's algorithm (the oracle's operation tally); the "
-                                          "kernels execute fewer FP64 operations than that algorithm (shared "
-                                          "point values, folded constants, Roe average from sqrt(rho) products), "
-                                          "so the fraction can exceed 1; the FP64-pipe busy share measured by ncu "
-                                          "is in profiles/dnc5_jvp_cylinder256.md"}},
-            "cpu_baseline": cpu,
-            "e2e": e2e,
-            "vjp": vjp,
-            "gpu_launches": launches_per_step * args.steps,
-            "clocks": clocks,
-        }
+        line = {"workload": "cylinder", "metric": METRIC, "value": m["value"], "unit": UNIT, "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": m["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic",
+                "config": {"workload": m["workload"], "cells": IM * JM, "directions_per_step": NDIR,
+                           "directions_per_launch_group": GROUP, "parallelism": "replicas" if ws > 1 else "single"},
+                "roofline": m["roofline"], "cpu_baseline": cpu, "e2e": m["e2e"], "vjp": m["vjp"],
+                "gpu_launches": m["gpu_launches"], "clocks": m["clocks"]}
         print(json.dumps(line))
     if ws > 1:
         dist.barrier()
@@ -550,82 +561,336 @@ def _flux_scale(c):
     return (np.abs(f) + np.abs(h)).reshape(-1, 5).max(0) * np.sqrt(g["nx"] ** 2 + g["ny"] ** 2).max()
 
 
-def run_batch_workload(args):
-    """Uneven batch (the reference's fourth configuration): 64 boundary-layer
-    instances, nx ~ U{200..1200}, ny ~ U{80..300}, Mach ~ U(0.3, 0.8)
-    (default_rng(4)); residual + one JVP direction of every instance in one
-    set of persistent launches replayed from a CUDA graph, tile shapes from
-    the autotuner; per-instance error against the single-grid kernels and
-    against the oracle."""
-    import torch
+# FP64 lane instructions (DFMA + DADD + DMUL, predicated on) and DRAM bytes
+# per interior cell of each pass of one uneven-batch evaluation (residual + one
+# JVP direction, boundary-layer grids), from one ncu capture of the first 6
+# grids of the uneven batch (1.34M cells):
+#   ncu --clock-control none -k regex:k_batch --metrics
+#       smsp__sass_thread_inst_executed_op_dfma_pred_on.sum,
+#       smsp__sass_thread_inst_executed_op_dadd_pred_on.sum,
+#       smsp__sass_thread_inst_executed_op_dmul_pred_on.sum,
+#       dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
+#       python bench.py --grids 6 --steps 1 --warmup 1 --no-extras
+# divided by the capture's cells; the full batch's figures scale with its cells.
+BATCH_NCU = None
+BATCH_PASSES = ("prim", "grad", "qrows", "vpts", "faces", "balance")
+
+
+def batch_inputs(n, ops, bcs):
+    """The uneven batch (nx ~ U{200..1200}, ny ~ U{80..300}, Mach ~ U(0.3, 0.8),
+    default_rng(4)): the first n grids with their boundary fills and one
+    seeded N(0, 1) direction each."""
     from broadcast_gb300 import cases
-    from broadcast_gb300.batch import GridBatch
-    from broadcast_gb300.operator import Dnc5Operator, to_device, to_host
-    n = args.grids or 64
-    rng = np.random.default_rng(4)
-    spec = [(int(rng.integers(200, 1201)), int(rng.integers(80, 301)), float(rng.uniform(0.3, 0.8))) for _ in range(n)]
     cs, wds = [], []
-    for k, (im, jm, mach) in enumerate(spec):
-        c = cases.bl_case(im, jm, mach=mach, seed=100 + k, ops=LibOps)
-        bl_bcs(c, c["w"])
-        wd = np.zeros_like(c["w"])
-        wd[3:-3, 3:-3] = rng.standard_normal((im, jm, 5))
+    for _, c, wd in cases.uneven_bl_batch(n, ops=ops):
+        bcs(c, c["w"])
         cs.append(c)
         wds.append(wd)
-    dev = torch.device("cuda", 0)
+    return cs, wds
+
+
+def oracle_bl_bcs(c, w):
+    from oracle import oracle as O
+    g, ph, it = c["grid"], c["phys"], c["interf"]
+    im, jm, gh = g["im"], g["jm"], g["gh"]
+    O.bc_inlet(w, "Ilo", it["Ilo"], c["field"], g["nx"], g["ny"], ph["gam"], im, jm, gh)
+    O.bc_noref(w, c["wbd"], "Jhi", it["Jhi"], g["nx"], g["ny"], ph["gam"], gh, im, jm)
+    O.bc_extrap(w, "Ihi", it["Ihi"], im, jm, gh)
+    O.bc_wall(w, "Jlo", ph["gam"], it["Jlo"], gh, im, jm)
+
+
+class OracleOps:
+    @staticmethod
+    def computegeom(*a):
+        from oracle import oracle as O
+        O.computegeom(*a)
+
+    @staticmethod
+    def initblfv(*a):
+        from oracle import oracle as O
+        O.initblfv(*a)
+
+    @staticmethod
+    def set_bndbl(*a):
+        from oracle import oracle as O
+        O.set_bndbl(*a)
+
+
+def oracle_jvp_batch(cs, wds, outs=None):
+    """Residual + JVP of every grid through the oracle with OpenMP on all host
+    cores (orc_flux_num_dnc5_2d_d); returns [(res, resd)]."""
+    from oracle import oracle as O
+    lib = O.lib(openmp=True)
+    out = []
+    for k, (c, wd) in enumerate(zip(cs, wds)):
+        g, ph = c["grid"], c["phys"]
+        r, rd = outs[k] if outs else (np.zeros_like(c["w"], order="F"), np.zeros_like(c["w"], order="F"))
+        lib.orc_flux_num_dnc5_2d_d(O._p(r), O._p(rd), O._p(c["w"]), O._p(wd), 1, O._p(g["nx"]), O._p(g["ny"]),
+                                   O._p(g["vol"]), O._p(g["volf"]), g["gh"], *O._phys(ph), g["im"], g["jm"])
+        out.append((r, rd))
+    return out
+
+
+def batch_config(n, cells):
+    return {"workload": "uneven batch of %d laminar boundary layers (grids %s of nx U{200..1200} x ny U{80..300}, "
+                        "Mach U(0.3, 0.8), default_rng(4); Blasius + 1e-4 noise), residual + one JVP direction "
+                        "per grid" % (n, "1-%d" % n), "grids": n, "cells": cells,
+            "unit_of_work": "one residual plus one JVP of one interior cell"}
+
+
+def batch_cpu_baseline(cs, wds, seconds):
+    """The oracle port on all host cores over the grids of the batch, repeated
+    for about `seconds`."""
+    outs = [(np.zeros_like(c["w"], order="F"), np.zeros_like(c["w"], order="F")) for c in cs]
+    cells, n, t0 = 0, 0, time.perf_counter()
+    while True:
+        k = n % len(cs)
+        oracle_jvp_batch([cs[k]], [wds[k]], [outs[k]])
+        cells += cs[k]["grid"]["im"] * cs[k]["grid"]["jm"]
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds and n >= 2:
+            break
+    return {"value": cells / el / 1e6, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": "%d grid evaluations (residual + 1 JVP direction, %d cells) of the uneven batch in grid order, "
+                      "%.1f s, OpenMP over j-rows" % (n, cells, el)}
+
+
+def run_batch_reference(args):
+    """Reference arm of the default line: the oracle port (C++ restatement of
+    the reference Fortran, OpenMP on all host cores) on the same grids, inputs
+    and directions; one step = every grid's residual + JVP."""
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    n = args.grids or 64
+    cs, wds = batch_inputs(n, OracleOps, oracle_bl_bcs)
+    cells = sum(c["grid"]["im"] * c["grid"]["jm"] for c in cs)
+    outs = [(np.zeros_like(c["w"], order="F"), np.zeros_like(c["w"], order="F")) for c in cs]
+    for _ in range(args.warmup):
+        oracle_jvp_batch(cs, wds, outs)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle_jvp_batch(cs, wds, outs)
+    el = time.perf_counter() - t0
+    v = cells * args.steps / el / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": batch_config(n, cells), "same_config": True,
+            "inputs_sha": inputs_digest(cs, wds),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                             "sample": "every step: all %d grids (%d cells), residual + 1 JVP direction each, "
+                                       "OpenMP over j-rows" % (n, cells)},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def inputs_digest(cs, wds):
+    """Digest of the grids' metrics, states and directions, rounded to 13
+    significant digits (the two arms fill the ghost cells with different
+    boundary-fill code, equal to ~1e-15)."""
+    import hashlib
+    h = hashlib.sha256()
+    for c, wd in zip(cs, wds):
+        for a in (c["grid"]["nx"], c["grid"]["ny"], c["grid"]["vol"], c["grid"]["volf"], c["w"], wd):
+            h.update(np.array([float("%.12e" % x) for x in np.ravel(a)[::97]]).tobytes())
+    return h.hexdigest()[:16]
+
+
+def run_batch(args):
+    """Default line: the uneven batch of 64 boundary layers (residual + one JVP
+    per grid) as one CUDA graph of persistent launches; value from CUDA events
+    with the inputs resident in HBM, e2e through bcg_batch_run_host with pinned
+    host arrays."""
+    import torch
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from broadcast_gb300.batch import GridBatch
+    from broadcast_gb300.operator import to_device, to_host
+    n = args.grids or 64
+    cs, wds = batch_inputs(n, LibOps, bl_bcs)
+    cells = sum(c["grid"]["im"] * c["grid"]["jm"] for c in cs)
     gb = GridBatch([c["grid"] for c in cs], [c["phys"] for c in cs], ndir=1, device=dev)
     gb.set_states([to_device(c["w"], dev) for c in cs], [to_device(wd, dev) for wd in wds])
-    tune = gb.autotune(repeats=3, use_cache=False)
-    gb.run(use_graph=True)
-    torch.cuda.synchronize()
+    if args.tile:  # fixed tile shapes (faces threads, cell threads, face CTAs per SM), no autotuning
+        gb.configure(*[int(x) for x in args.tile.split(",")])
+        tune = {"config": list(gb.config)}
+    else:
+        tune = gb.autotune(repeats=3, use_cache=False)
     stream = torch.cuda.current_stream(dev)
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    for _ in range(max(args.warmup, 1)):
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+
+    def step():
         gb.run(use_graph=True)
+
+    for _ in range(max(args.warmup, 1)):
+        step()
     torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    if rank == 0:
+        sampler.start()
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < 0.3:  # the clock samples see the GPU under this load
+        step()
+        torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for s in range(args.steps):
         flush.add_(1.0)
         ev[s][0].record(stream)
-        gb.run(use_graph=True)
+        step()
         ev[s][1].record(stream)
     torch.cuda.synchronize()
-    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
-    # per-instance errors: single-grid kernels, oracle
-    from oracle import oracle as O
-    err_single, err_res, err_tan, kink_cells = [], [], [], 0
-    for g, c in enumerate(cs):
-        r, rd = to_host(gb.res[g]), to_host(gb.resd[g])
-        op = Dnc5Operator(c["grid"], c["phys"], device=dev)
-        r1, rd1 = op.jvp(to_device(c["w"], dev), to_device(wds[g], dev))
-        err_single.append(float(max(np.abs(r - to_host(r1)).max(), np.abs(rd - to_host(rd1)).max())))
-        ref, refd = O.jvp(c["grid"], c["phys"], c["w"], wds[g])
-        sc = _flux_scale(c)  # residual: relative to the face-flux magnitude
-        scd = np.abs(refd[3:-3, 3:-3]).reshape(-1, 5).max(0)
-        et = np.abs(rd - refd)[3:-3, 3:-3] / scd
-        err_res.append(float((np.abs(r - ref)[3:-3, 3:-3].reshape(-1, 5).max(0) / sc).max()))
-        err_tan.append(float(et.max()))
-        kink_cells += int((et.max(axis=2) > 1e-11).sum())
-    cells = gb.cells
-    line = {"workload": "batch", "metric": "FP64 residual+JVP Mcells/s, 64 uneven grids", "unit": "Mcells/s",
-            "value": cells / (ms / 1e3) / 1e6, "ms_per_step": ms, "higher_is_better": True, "dtype": "f64",
-            "data": "synthetic",
-            "config": {"grids": n, "cells": cells, "sizes": "nx U{200..1200}, ny U{80..300}, Mach U(0.3, 0.8), "
-                                                             "default_rng(4)", "graph": True,
-                       "tile": {"faces": tune["config"][0], "cells": tune["config"][1],
-                                "ctas_per_sm": tune["config"][2]},
-                       "l2": "flushed between steps (256 MB write)"},
-            "per_instance_error": {"vs_single_grid_max_abs": max(err_single),
-                                   "residual_vs_oracle_max": max(err_res),
-                                   "tangent_vs_oracle_max": max(err_tan),
-                                   "tangent_cells_above_1e-11": kink_cells,
-                                   "note": "residual relative to the face-flux magnitude, tangent to max|R'v| per "
-                                           "variable; cells above 1e-11 sit on an abs() kink of the pressure "
-                                           "sensor (second difference ~ 0 next to the extrapolated outflow)"},
-            "autotune_ms": {"%d/%d/%d" % tuple(c): t for c, t in tune["timings"]},
-            "gpu_launches": 6 * args.steps}  # prim, grad, qrows, vpts, faces, balance
-    print(json.dumps(line))
+    if ws > 1:
+        dist.barrier()
+    clocks = sampler.stop() if rank == 0 else None
+    if clocks:
+        clocks["window"] = "0.3 s of the same step untimed, then the timed region"
+    tot_ms = sum(a.elapsed_time(b) for a, b in ev)
+    if ws > 1:
+        t = torch.tensor([tot_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_ms = float(t.item())
+    value = cells * ws * args.steps / (tot_ms / 1e3) / 1e6
+    line = None
+    if rank == 0:
+        # each pass alone (events around one launch, L2 flushed before each)
+        pass_ms = []
+        for k in range(len(BATCH_PASSES)):
+            a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            tk = 0.0
+            for _ in range(3):
+                for q in range(k):  # the earlier passes produce this pass's inputs
+                    gb.run_pass(q)
+                flush.add_(1.0)
+                a_ev.record(stream)
+                gb.run_pass(k)
+                b_ev.record(stream)
+                torch.cuda.synchronize()
+                tk += a_ev.elapsed_time(b_ev)
+            pass_ms.append(tk / 3)
+        # end to end: pinned host arrays through bcg_batch_run_host
+        pin = lambda a: _pinned_copy(torch, a)
+        w_h, wd_h = [pin(c["w"]) for c in cs], [pin(wd) for wd in wds]
+        geo_h = [{k: pin(c["grid"][k]) for k in ("nx", "ny", "vol", "volf")} for c in cs]
+        res_h, resd_h = [pin(np.zeros_like(c["w"], order="F")) for c in cs], [pin(np.zeros_like(c["w"], order="F")) for c in cs]
+        nchunk = 8
+        for _ in range(max(args.warmup, 1)):
+            gb.run_host(w_h, wd_h, res_h, resd_h, geo_h, nchunk=nchunk)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            gb.run_host(w_h, wd_h, res_h, resd_h, geo_h, nchunk=nchunk)
+        el = time.perf_counter() - t0
+        nps = [(c["grid"]["im"] + 6) * (c["grid"]["jm"] + 6) for c in cs]
+        nns = [(c["grid"]["im"] + 7) * (c["grid"]["jm"] + 7) for c in cs]
+        h2d = sum(8 * (13 * a + 4 * b) for a, b in zip(nps, nns))
+        d2h = 8 * 10 * cells
+        e2e = {"value": cells * args.steps / el / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": el / args.steps * 1e3, "chunks": nchunk,
+               "call": "bcg_batch_run_host (GridBatch.run_host): state, direction and metrics of every grid "
+                       "uploaded, residual and tangent interiors downloaded, every step"}
+        # parity of this run's outputs (device run and host-array run) with the oracle
+        ref = oracle_jvp_batch(cs, wds)
+        err_res, err_tan, above, host_dev = 0.0, 0.0, 0, 0.0
+        for g, c in enumerate(cs):
+            r, rd = to_host(gb.res[g]), to_host(gb.resd[g])
+            host_dev = max(host_dev, float(np.abs(H_int(res_h[g]) - H_int(r)).max()),
+                           float(np.abs(H_int(resd_h[g]) - H_int(rd)).max()))
+            rr, rrd = ref[g]
+            sc = _flux_scale(c)
+            scd = np.abs(H_int(rrd)).reshape(-1, 5).max(0)
+            err_res = max(err_res, float((np.abs(H_int(r) - H_int(rr)).reshape(-1, 5).max(0) / sc).max()))
+            et = (np.abs(H_int(rd) - H_int(rrd)) / scd).max(axis=2)
+            err_tan = max(err_tan, float(et.max()))
+            above += int((et > 1e-11).sum())
+        cpu = batch_cpu_baseline(cs, wds, args.cpu_seconds)
+        roof = batch_roofline([(c["grid"]["im"], c["grid"]["jm"]) for c in cs], tot_ms / args.steps, pass_ms, clocks)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": tot_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": dict(batch_config(n, cells), parallelism="replicas" if ws > 1 else "single", graph=True,
+                           l2="flushed between steps (256 MB write); the batch's arrays (~%.1f GB) exceed L2 anyway"
+                              % (cells * 8 * 23 / 1e9),
+                           tile={"faces": tune["config"][0], "cells": tune["config"][1],
+                                 "ctas_per_sm": tune["config"][2]}),
+            "roofline": roof,
+            "pass_ms": dict(zip(BATCH_PASSES, pass_ms)),
+            "parity": {"residual_vs_oracle_max": err_res, "tangent_vs_oracle_max": err_tan,
+                       "tangent_cells_above_1e-11": above, "host_run_vs_device_run_max_abs": host_dev,
+                       "note": "residual relative to the face-flux magnitude, tangent to max|R'v| per variable"},
+            "inputs_sha": inputs_digest(cs, wds),
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": 6 * args.steps,
+            "clocks": clocks,
+        }
+    if not args.no_extras and rank == 0:
+        del gb
+        torch.cuda.empty_cache()
+        line["cylinder_256"] = cylinder_measure(args, dev, extras_only=True)
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
     return 0
+
+
+def H_int(a):
+    return a[3:-3, 3:-3]
+
+
+def _pinned_copy(torch, a):
+    t = torch.empty(a.size, dtype=torch.float64, pin_memory=True).numpy()
+    t[:] = np.ravel(a, order="F")
+    return t.reshape(a.shape, order="F")
+
+
+def batch_roofline(dims, step_ms, pass_ms, clocks):
+    """FP64-bound roofline of the evaluation and of its dominant pass (faces):
+    executed FP64 lane instructions (ncu counts per cell, scaled to the batch's
+    cells) over the FP64 issue peak of 2 lane instructions per clock per SM at
+    the clock sampled during the timed region; DRAM traffic likewise from ncu
+    per cell; the HBM fraction of the algorithmic bytes beside it."""
+    import torch
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    nsm = props.multi_processor_count
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    peak = 2.0 * nsm * mhz * 1e6 / 1e9  # G FP64 lane instructions / s
+    hbm_peak = _hbm_peak()
+    faces_ms = pass_ms[BATCH_PASSES.index("faces")]
+    out = {"bound": "fp64", "unit": "G FP64 inst/s", "peak": peak,
+           "peak_source": "2 FP64 lane instructions per clock per SM x %d SMs x %.0f MHz (median SM clock sampled "
+                          "in the timed region); GB300's FP64 FMA rate measured with FMA chains matches it" % (nsm, mhz),
+           "kernel": "k_batch<DK<1>, faces> (face fluxes of all grids, one persistent launch), %.1f%% of the sum of "
+                     "the passes timed alone" % (100 * faces_ms / sum(pass_ms)),
+           "achieved": None, "frac": None, "traffic": None}
+    cells = sum(i * j for i, j in dims)
+    nb = sum(algorithmic_bytes(i, j, 3, 1) for i, j in dims)
+    out["hbm"] = {"achieved": nb / (step_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                  "frac": nb / (step_ms / 1e3) / 1e9 / hbm_peak,
+                  "algorithmic_bytes_per_step": nb, "peak_source": "MEASURED_PEAKS.json hbm_gbs"}
+    if BATCH_NCU:
+        inst = {k: v * cells for k, v in BATCH_NCU["fp64_inst_per_cell"].items()}
+        dram = {k: v * cells for k, v in BATCH_NCU["dram_bytes_per_cell"].items()}
+        out["achieved"] = inst["faces"] / (faces_ms / 1e3) / 1e9
+        out["frac"] = out["achieved"] / peak
+        out["traffic"] = dram["faces"]
+        out["algorithmic_fp64_inst_per_launch"] = inst["faces"]
+        tot = sum(inst.values())
+        out["whole_step"] = {"achieved": tot / (step_ms / 1e3) / 1e9, "frac": tot / (step_ms / 1e3) / 1e9 / peak,
+                             "fp64_inst_per_step": tot, "traffic_per_step": sum(dram.values())}
+        out["ncu_source"] = BATCH_NCU["source"]
+    return out
 
 
 def run_impli_workload(args):
@@ -848,28 +1113,11 @@ def run_warmstart_workload(args):
 
 
 def _hbm_peak():
+    """Measured HBM copy bandwidth (GB/s) of this GPU pool, else the fallback figure."""
     try:
-        return float(json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")))["hbm_gbs"])
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
     except (OSError, KeyError, ValueError):
         return 6800.0
-
-
-def ctypes_double():
-    return np.zeros(1)
-
-
-def _profiled_traffic():
-    """DRAM bytes per launch group from the committed ncu summary, if present."""
-    p = os.path.join(ROOT, "profiles", "dnc5_jvp_cylinder256.md")
-    if not os.path.exists(p):
-        return None
-    for ln in open(p):
-        if ln.startswith("traffic_bytes_per_group:"):
-            try:
-                return float(ln.split(":", 1)[1])
-            except ValueError:
-                return None
-    return None
 
 
 def main():
@@ -879,18 +1127,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-extras", action="store_true", help="default line without the cylinder extra key")
     ap.add_argument("--lmax", type=int, default=10, help="impli workload: Gauss-Seidel sweeps per call")
     ap.add_argument("--case", default="bl", choices=["bl", "cyl"], help="newton workload: boundary layer or cylinder")
     ap.add_argument("--ntrain", type=int, default=200, help="warmstart workload: training base flows")
     ap.add_argument("--nheld", type=int, default=20, help="warmstart workload: held-out (Re, Mach) points")
     ap.add_argument("--train-steps", type=int, default=3000, help="warmstart workload: Adam steps")
     ap.add_argument("--batch", type=int, default=16384, help="warmstart workload: samples per Adam step")
-    ap.add_argument("--workload", default="residual-jvp",
-                    choices=["residual-jvp", "jacobian", "batch", "impli", "newton", "warmstart"],
-                    help="residual-jvp: the 256x256 cylinder line (default); jacobian: the batched "
-                         "Jacobian / Dz / Dzz / J(beta) assembly of the 1024x512 boundary layer; batch: "
-                         "residual + JVP of 64 uneven boundary-layer grids in one graph")
-    ap.add_argument("--grids", type=int, default=0)
+    ap.add_argument("--workload", default="batch",
+                    choices=["batch", "cylinder", "jacobian", "impli", "newton", "warmstart"],
+                    help="batch (default): residual + JVP of the 64 uneven boundary-layer grids in one graph; "
+                         "cylinder: the 256x256 cylinder residual + 32-direction JVP line; jacobian: the batched "
+                         "Jacobian / Dz / Dzz / J(beta) assembly of the 1024x512 boundary layer")
+    ap.add_argument("--grids", type=int, default=0, help="batch workload: the first N grids of the 64")
+    ap.add_argument("--tile", default="", help="batch workload: fixed tile shapes F,C,N instead of the autotuner")
     ap.add_argument("--im", type=int, default=0)
     ap.add_argument("--jm", type=int, default=0)
     args = ap.parse_args()
@@ -900,13 +1150,11 @@ def main():
         return run_impli_workload(args)
     if args.workload == "newton":
         return run_newton_workload(args)
-    if args.workload == "batch":
-        return run_batch_workload(args)
     if args.workload == "warmstart":
         return run_warmstart_workload(args)
-    if args.impl == "reference":
-        return run_reference(args)
-    return run_ours(args)
+    if args.workload == "cylinder":
+        return run_reference(args) if args.impl == "reference" else run_cylinder(args)
+    return run_batch_reference(args) if args.impl == "reference" else run_batch(args)
 
 
 if __name__ == "__main__":

@@ -78,6 +78,8 @@ SIGNATURES = {
     "bcg_batch_set_arrays": "L" + "p" * 8,
     "bcg_batch_configure": "Liii",
     "bcg_batch_run": "Li",
+    "bcg_batch_run_pass": "Li",
+    "bcg_batch_run_host": "Li" + "p" * 8,
     "bcg_batch_device_bytes": "Lp",
     "bcg_batch_destroy": "L",
     "bcg_csr_spanwise_beta": "i" + "ppp" * 3 + "ip" + "ppp" + "L" + "p",

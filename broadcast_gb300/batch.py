@@ -6,6 +6,7 @@ in one set of persistent launches, optionally replayed from a CUDA graph
     gb.set_states(ws, wds)              # torch tensors, operator layout (5, nj, ni)
     gb.run(use_graph=True)              # queued on torch's current stream
     gb.res[g], gb.resd[g]               # residual / tangent of grid g
+    gb.run_host(ws_h, wds_h, res_h, resd_h, geo_h)  # host arrays, copies overlapped
     gb.autotune()                       # times the tile candidates, keeps the best
 
 The autotuner measures every candidate on the plan's own grids with CUDA
@@ -87,6 +88,26 @@ class GridBatch:
 
     def run(self, use_graph=True):
         _lib.call("bcg_batch_run", self.plan, 1 if use_graph else 0)
+
+    def run_pass(self, k):
+        """Queue pass k (0 primitives .. 4 faces, 5 balance) alone, for timing."""
+        _lib.call("bcg_batch_run_pass", self.plan, int(k))
+
+    def run_host(self, ws, wds, res, resd, geo, nchunk=8):
+        """One evaluation with host arrays (bcg_batch_run_host): lists of
+        Fortran-ordered float64 numpy arrays per grid (pinned memory copies
+        fastest); geo is a list of dicts with nx, ny, vol, volf.  The grids'
+        uploads, graph replays and interior downloads overlap in nchunk
+        chunks; returns when res / resd hold the results."""
+        addr = lambda arrs: _u64([a.ctypes.data for a in arrs])
+        for a in list(ws) + list(res) + ([] if not self.ndir else list(wds) + list(resd)):
+            if not (a.flags.f_contiguous and a.dtype == np.float64):
+                raise ValueError("run_host: Fortran-ordered float64 arrays expected")
+        wd = addr(wds) if self.ndir else addr(ws)
+        rd = addr(resd) if self.ndir else addr(res)
+        _lib.call("bcg_batch_run_host", self.plan, int(nchunk), addr(ws), wd, addr([g["nx"] for g in geo]),
+                  addr([g["ny"] for g in geo]), addr([g["vol"] for g in geo]), addr([g["volf"] for g in geo]),
+                  addr(res), rd)
 
     def signature(self):
         key = "%d|%s" % (self.ndir, ",".join("%dx%d" % (i, j) for i, j in zip(self.im, self.jm)))

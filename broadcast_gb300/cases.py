@@ -174,3 +174,29 @@ def cyl_case(im=256, jm=256, mach=0.1, reynolds=47.0, noise=1.0e-3, seed=1, r_ou
 
 def interior(a, gh=GH):
     return a[gh:-gh, gh:-gh, ...]
+
+
+def uneven_bl_spec(n=64, seed=4):
+    """Sizes and Mach numbers of the uneven batch of boundary layers:
+    nx ~ U{200..1200}, ny ~ U{80..300}, Mach ~ U(0.3, 0.8), drawn in that
+    order per grid from default_rng(seed).  Returns the list of (im, jm, mach)
+    and the generator, whose next draws are the grids' tangent directions."""
+    rng = np.random.default_rng(seed)
+    spec = [(int(rng.integers(200, 1201)), int(rng.integers(80, 301)), float(rng.uniform(0.3, 0.8))) for _ in range(n)]
+    return spec, rng
+
+
+def uneven_bl_batch(n=64, seed=4, ops=None, only=None):
+    """Yield (k, case, wd) for the grids of uneven_bl_spec: grid k is
+    bl_case(im, jm, mach, seed=100 + k) and its direction wd is N(0, 1) on the
+    interior cells (zero ghosts), drawn in grid order from the same generator.
+    `only`: the grid indices to build (the others' directions are still drawn)."""
+    spec, rng = uneven_bl_spec(n, seed)
+    for k, (im, jm, mach) in enumerate(spec):
+        d = rng.standard_normal((im, jm, 5))
+        if only is not None and k not in only:
+            continue
+        c = bl_case(im, jm, mach=mach, seed=100 + k, ops=ops)
+        wd = np.zeros_like(c["w"])
+        wd[GH:GH + im, GH:GH + jm] = d
+        yield k, c, wd

@@ -1234,6 +1234,22 @@ extern "C" int bcg_batch_run(long long plan, int use_graph) {
   return batch_run(p, use_graph, current_stream());
 }
 
+extern "C" int bcg_batch_run_pass(long long plan, int pass) {
+  BatchPlan* p = batch_of(plan);
+  if (!p) return fail_arg("batch: unknown plan");
+  return batch_run_pass(p, pass, current_stream());
+}
+
+extern "C" int bcg_batch_run_host(long long plan, int nchunk, const unsigned long long* w,
+                                  const unsigned long long* wd, const unsigned long long* nx,
+                                  const unsigned long long* ny, const unsigned long long* vol,
+                                  const unsigned long long* volf, const unsigned long long* res,
+                                  const unsigned long long* resd) {
+  BatchPlan* p = batch_of(plan);
+  if (!p) return fail_arg("batch: unknown plan");
+  return batch_run_host(p, nchunk, w, wd, nx, ny, vol, volf, res, resd, current_stream());
+}
+
 extern "C" int bcg_batch_device_bytes(long long plan, long long* bytes) {
   BatchPlan* p = batch_of(plan);
   if (!p || !bytes) return fail_arg("batch: unknown plan");

@@ -132,6 +132,16 @@ struct BatchPlan {
   bool any_grad = false;
   cudaStream_t cap = nullptr;  // capture stream (the caller's may be the legacy default stream)
   cudaGraphExec_t exec = nullptr;
+  bool owns_scratch = true;
+  // host-array runs (batch_run_host): device mirrors of every grid's arrays,
+  // and the grids split into contiguous chunks, each a child plan over the
+  // mirrors that shares this plan's scratch
+  double* mirror = nullptr;
+  std::vector<size_t> moff;          // per grid: offset of its mirrors (MIR_* order)
+  std::vector<BatchPlan*> chunks;
+  std::vector<int> chunk_lo;         // first grid of each chunk, then ngrid
+  cudaStream_t hs[4] = {nullptr, nullptr, nullptr, nullptr};  // upload, download, two compute streams
+  std::vector<cudaEvent_t> hev;      // start, per chunk uploaded, per chunk computed, downloads done
 };
 
 static long long pass_count(const Ext& e, int pass, bool grad) {
@@ -219,6 +229,10 @@ int batch_configure(BatchPlan* p, int tile_faces, int tile_cells, int ctas_per_s
   if (ctas_per_sm < 1 || ctas_per_sm > 8) return fail_arg("batch: ctas_per_sm must be 1..8");
   p->tile_faces = tile_faces; p->tile_cells = tile_cells; p->ctas = ctas_per_sm;
   if (p->exec) { cudaGraphExecDestroy(p->exec); p->exec = nullptr; }
+  for (BatchPlan* c : p->chunks) {
+    const int rc = batch_configure(c, tile_faces, tile_cells, ctas_per_sm);
+    if (rc) return rc;
+  }
   return upload_starts(p);
 }
 
@@ -259,6 +273,29 @@ static cudaError_t launch_all(const BatchPlan* p, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+int batch_run_pass(BatchPlan* p, int pass, cudaStream_t st) {
+  if (pass < 0 || pass >= NPASS) return fail_arg("batch: pass must be 0..5");
+  if (!p->h.empty() && !p->h[0].w) return fail_arg("batch: arrays not set");
+  auto one = [&](auto tag) {
+    using S = decltype(tag);
+    if (pass == P_GRAD && !p->any_grad) return;
+    if (pass == P_FACES) {
+      switch (p->tile_faces) {
+        case 64: launch_pass<S, P_FACES, 64>(p, p->ctas, st); break;
+        case 128: launch_pass<S, P_FACES, 128>(p, p->ctas, st); break;
+        default: launch_pass<S, P_FACES, 256>(p, p->ctas, st); break;
+      }
+    } else if (p->tile_cells == 128) {
+      launch_cells<S, 128>(p, pass, st);
+    } else {
+      launch_cells<S, 256>(p, pass, st);
+    }
+  };
+  if (p->K) one(DK<1>{}); else one(0.0);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? BCG_OK : fail_cuda("batch: pass launch", e);
+}
+
 int batch_run(BatchPlan* p, int use_graph, cudaStream_t st) {
   if (!p->h.empty() && !p->h[0].w) return fail_arg("batch: arrays not set");
   auto launch = [&](cudaStream_t s) { return p->K ? launch_all<DK<1>>(p, s) : launch_all<double>(p, s); };
@@ -292,16 +329,178 @@ int batch_run(BatchPlan* p, int use_graph, cudaStream_t st) {
 
 void batch_destroy(BatchPlan* p) {
   if (!p) return;
+  for (BatchPlan* c : p->chunks) batch_destroy(c);
+  for (cudaEvent_t ev : p->hev) cudaEventDestroy(ev);
+  for (cudaStream_t s : p->hs)
+    if (s) cudaStreamDestroy(s);
+  if (p->mirror) cudaFree(p->mirror);
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->cap) cudaStreamDestroy(p->cap);
-  if (p->scratch) cudaFree(p->scratch);
+  if (p->scratch && p->owns_scratch) cudaFree(p->scratch);
   if (p->d) cudaFree(p->d);
   if (p->dstarts) cudaFree(p->dstarts);
   delete p;
 }
 
 size_t batch_device_bytes(const BatchPlan* p) {
-  return p->scratch_doubles * sizeof(double) + sizeof(GridDesc) * p->ngrid + sizeof(long long) * NPASS * (p->ngrid + 1);
+  size_t b = sizeof(GridDesc) * p->ngrid + sizeof(long long) * NPASS * (p->ngrid + 1);
+  if (p->owns_scratch) b += p->scratch_doubles * sizeof(double);
+  if (p->mirror) b += p->moff.back() * sizeof(double);
+  for (const BatchPlan* c : p->chunks) b += batch_device_bytes(c);
+  return b;
+}
+
+// ---------------------------------------------------------------------------
+// Host-array runs.  Mirrors per grid, in this order: w, wd, nx, ny, vol, volf,
+// res, resd (wd and resd only with a tangent); each starts on a 256-byte
+// boundary.
+namespace {
+enum { MIR_W = 0, MIR_WD, MIR_NX, MIR_NY, MIR_VOL, MIR_VOLF, MIR_RES, MIR_RESD, MIR_N };
+
+void mirror_sizes(const Ext& e, int K, size_t sz[MIR_N]) {
+  const size_t np = e.np, nn = (size_t)(e.ni + 1) * (e.nj + 1);
+  sz[MIR_W] = 5 * np; sz[MIR_WD] = K ? 5 * np : 0; sz[MIR_NX] = 2 * nn; sz[MIR_NY] = 2 * nn;
+  sz[MIR_VOL] = np; sz[MIR_VOLF] = 2 * np; sz[MIR_RES] = 5 * np; sz[MIR_RESD] = K ? 5 * np : 0;
+}
+inline size_t al32(size_t n) { return (n + 31) & ~(size_t)31; }
+
+// child plan over grids [g0, g1) of p: the parent's descriptors (with its
+// scratch), arrays on the parent's mirrors, the parent's tile shapes
+int make_chunk(BatchPlan* p, int g0, int g1, BatchPlan** out) {
+  BatchPlan* c = new BatchPlan();
+  c->ngrid = g1 - g0; c->K = p->K; c->nsm = p->nsm; c->any_grad = false;
+  c->owns_scratch = false; c->scratch = p->scratch;
+  c->tile_faces = p->tile_faces; c->tile_cells = p->tile_cells; c->ctas = p->ctas;
+  c->h.assign(p->h.begin() + g0, p->h.begin() + g1);
+  for (int g = 0; g < c->ngrid; ++g) {
+    GridDesc& G = c->h[g];
+    c->any_grad = c->any_grad || G.grad;
+    double* m = p->mirror + p->moff[g0 + g];
+    size_t sz[MIR_N];
+    mirror_sizes(G.e, p->K, sz);
+    double* at[MIR_N];
+    for (int k = 0; k < MIR_N; ++k) { at[k] = m; m += al32(sz[k]); }
+    G.w = at[MIR_W]; G.wd = p->K ? at[MIR_WD] : nullptr; G.nx = at[MIR_NX]; G.ny = at[MIR_NY];
+    G.vol = at[MIR_VOL]; G.volf = at[MIR_VOLF]; G.res = at[MIR_RES]; G.resd = p->K ? at[MIR_RESD] : nullptr;
+  }
+  cudaError_t e = cudaMalloc(&c->d, sizeof(GridDesc) * c->ngrid);
+  if (e == cudaSuccess) e = cudaMalloc(&c->dstarts, sizeof(long long) * NPASS * (c->ngrid + 1));
+  if (e == cudaSuccess) e = cudaMemcpy(c->d, c->h.data(), sizeof(GridDesc) * c->ngrid, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { batch_destroy(c); return fail_cuda("batch: chunk plan", e), BCG_ERR_NOMEM; }
+  const int rc = upload_starts(c);
+  if (rc) { batch_destroy(c); return rc; }
+  *out = c;
+  return BCG_OK;
+}
+
+// mirrors, chunk plans, streams and events for nchunk chunks (kept until the
+// count changes or the plan is destroyed)
+int prepare_host(BatchPlan* p, int nchunk) {
+  if (!p->mirror) {
+    p->moff.assign(p->ngrid + 1, 0);
+    for (int g = 0; g < p->ngrid; ++g) {
+      size_t sz[MIR_N], n = 0;
+      mirror_sizes(p->h[g].e, p->K, sz);
+      for (size_t x : sz) n += al32(x);
+      p->moff[g + 1] = p->moff[g] + n;
+    }
+    cudaError_t e = cudaMalloc(&p->mirror, p->moff.back() * sizeof(double));
+    if (e != cudaSuccess) { p->mirror = nullptr; return fail_cuda("batch: host-run mirrors", e), BCG_ERR_NOMEM; }
+    for (cudaStream_t& s : p->hs) {
+      e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+      if (e != cudaSuccess) { s = nullptr; return fail_cuda("batch: host-run streams", e); }
+    }
+  }
+  if ((int)p->chunks.size() == nchunk) return BCG_OK;
+  for (BatchPlan* c : p->chunks) batch_destroy(c);
+  p->chunks.clear();
+  for (cudaEvent_t ev : p->hev) cudaEventDestroy(ev);
+  p->hev.clear();
+  // contiguous ranges of about equal cell counts
+  double tot = 0;
+  for (const GridDesc& G : p->h) tot += (double)G.e.im * G.e.jm;
+  p->chunk_lo.assign(1, 0);
+  double acc = 0;
+  for (int g = 0; g < p->ngrid; ++g) {
+    acc += (double)p->h[g].e.im * p->h[g].e.jm;
+    const int have = (int)p->chunk_lo.size();
+    if (have < nchunk && g + 1 < p->ngrid && acc >= tot * have / nchunk) p->chunk_lo.push_back(g + 1);
+  }
+  p->chunk_lo.push_back(p->ngrid);
+  const int nc = (int)p->chunk_lo.size() - 1;
+  for (int c = 0; c < nc; ++c) {
+    BatchPlan* ch = nullptr;
+    const int rc = make_chunk(p, p->chunk_lo[c], p->chunk_lo[c + 1], &ch);
+    if (rc) return rc;
+    p->chunks.push_back(ch);
+  }
+  p->hev.assign(2 * nc + 2, nullptr);
+  for (cudaEvent_t& ev : p->hev) {
+    cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) { ev = nullptr; return fail_cuda("batch: host-run events", e); }
+  }
+  return BCG_OK;
+}
+}  // namespace
+
+int batch_run_host(BatchPlan* p, int nchunk, const unsigned long long* w, const unsigned long long* wd,
+                   const unsigned long long* nx, const unsigned long long* ny, const unsigned long long* vol,
+                   const unsigned long long* volf, const unsigned long long* res, const unsigned long long* resd,
+                   cudaStream_t st) {
+  if (nchunk < 1 || nchunk > 16) return fail_arg("batch: nchunk must be 1..16");
+  if (!w || !nx || !ny || !vol || !volf || !res || (p->K && (!wd || !resd))) return fail_arg("batch: null array table");
+  for (int g = 0; g < p->ngrid; ++g) {
+    const void* ptrs[8] = {(const void*)w[g], (const void*)nx[g], (const void*)ny[g], (const void*)vol[g],
+                           (const void*)volf[g], (const void*)res[g], p->K ? (const void*)wd[g] : (const void*)w[g],
+                           p->K ? (const void*)resd[g] : (const void*)res[g]};
+    for (const void* q : ptrs)
+      if (!q || is_device_ptr(q)) return fail_arg("batch: every array of a host run must be a host pointer");
+  }
+  int rc = prepare_host(p, std::min(nchunk, p->ngrid));
+  if (rc) return rc;
+  const int nc = (int)p->chunks.size();
+  cudaStream_t up = p->hs[0], down = p->hs[1];
+  cudaEvent_t* ev = p->hev.data();  // 0 start, 1 + c uploaded, 1 + nc + c computed, 1 + 2 nc downloads done
+  // everything starts after the caller's earlier work on the library stream
+  cudaError_t e = cudaEventRecord(ev[0], st);
+  for (cudaStream_t s : p->hs)
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev[0], 0);
+  if (e != cudaSuccess) return fail_cuda("batch: host run", e);
+  const unsigned long long* src[6] = {w, p->K ? wd : nullptr, nx, ny, vol, volf};
+  for (int c = 0; c < nc; ++c) {
+    BatchPlan* ch = p->chunks[c];
+    const int g0 = p->chunk_lo[c];
+    for (int g = 0; g < ch->ngrid && e == cudaSuccess; ++g) {
+      const GridDesc& G = ch->h[g];
+      size_t sz[MIR_N];
+      mirror_sizes(G.e, p->K, sz);
+      double* dst[6] = {(double*)G.w, (double*)G.wd, (double*)G.nx, (double*)G.ny, (double*)G.vol, (double*)G.volf};
+      for (int k = 0; k < 6 && e == cudaSuccess; ++k)
+        if (sz[k]) e = cudaMemcpyAsync(dst[k], (const void*)src[k][g0 + g], sz[k] * sizeof(double),
+                                       cudaMemcpyHostToDevice, up);
+    }
+    cudaStream_t comp = p->hs[2 + (c & 1)];
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1 + c], up);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(comp, ev[1 + c], 0);
+    if (e != cudaSuccess) return fail_cuda("batch: host run upload", e);
+    rc = batch_run(ch, 1, comp);
+    if (rc) return rc;
+    e = cudaEventRecord(ev[1 + nc + c], comp);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(down, ev[1 + nc + c], 0);
+    for (int g = 0; g < ch->ngrid && e == cudaSuccess; ++g) {
+      const GridDesc& G = ch->h[g];
+      const Ext& x = G.e;
+      e = copy_interior_planes((double*)res[g0 + g], G.res, x.ni, x.nj, 5, 3, x.im, x.jm, cudaMemcpyDeviceToHost, down);
+      if (e == cudaSuccess && p->K)
+        e = copy_interior_planes((double*)resd[g0 + g], G.resd, x.ni, x.nj, 5, 3, x.im, x.jm, cudaMemcpyDeviceToHost,
+                                 down);
+    }
+    if (e != cudaSuccess) return fail_cuda("batch: host run download", e);
+  }
+  e = cudaEventRecord(ev[1 + 2 * nc], down);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev[1 + 2 * nc], 0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? BCG_OK : fail_cuda("batch: host run", e);
 }
 
 }  // namespace bcg

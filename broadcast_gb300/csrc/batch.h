@@ -21,6 +21,16 @@ int batch_set_arrays(BatchPlan* p, const unsigned long long* w, const unsigned l
 // per SM of the persistent grids; drops a captured graph
 int batch_configure(BatchPlan* p, int tile_faces, int tile_cells, int ctas_per_sm);
 int batch_run(BatchPlan* p, int use_graph, cudaStream_t st);
+// one pass alone (0 primitives, 1 gradients, 2 interpolation rows, 3 viscous
+// point values, 4 faces, 5 balance), for timing each kernel of a run
+int batch_run_pass(BatchPlan* p, int pass, cudaStream_t st);
+// one evaluation with host arrays: uploads, graph replays and interior
+// downloads of nchunk chunks of grids overlap; returns when the outputs are
+// in the host arrays
+int batch_run_host(BatchPlan* p, int nchunk, const unsigned long long* w, const unsigned long long* wd,
+                   const unsigned long long* nx, const unsigned long long* ny, const unsigned long long* vol,
+                   const unsigned long long* volf, const unsigned long long* res, const unsigned long long* resd,
+                   cudaStream_t st);
 void batch_destroy(BatchPlan* p);
 size_t batch_device_bytes(const BatchPlan* p);
 

@@ -100,6 +100,34 @@ template <int K> BCG_HD DK<K> pow_t(const DK<K>& a, double y) { DK<K> r; r.v = p
   for (int k = 0; k < K; ++k) r.d[k] = s * a.d[k]; return r; }
 BCG_HD double pow_t(double a, double y) { return pow(a, y); }
 template <class S> BCG_HD S fmax_t(const S& a, const S& b) { return (a < b) ? b : a; }
+
+// Operations whose value is rounded as the separate IEEE operation, never
+// contracted into a fused multiply-add, and a correctly rounded division.
+// The pressure and the pressure sensor are formed with them in the
+// reference's order: next to an extrapolated boundary the sensor's two
+// ratios can agree to ~1e-7, so MAX(ks1, ks2) and with it the tangent's
+// branch follow the last bits of the pressure (phys/Primitives.F,
+// rhs/ducrosfordnc_i.F).
+BCG_HD double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+BCG_HD double add_rn(double a, double b) { return __dadd_rn(a, b); }
+BCG_HD double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+BCG_HD double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+template <int K> BCG_HD DK<K> mul_rn(const DK<K>& a, const DK<K>& b) { DK<K> r; r.v = __dmul_rn(a.v, b.v);
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = fma(a.d[k], b.v, a.v * b.d[k]); return r; }
+template <int K> BCG_HD DK<K> mul_rn(double a, const DK<K>& b) { DK<K> r; r.v = __dmul_rn(a, b.v);
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = a * b.d[k]; return r; }
+template <int K> BCG_HD DK<K> add_rn(const DK<K>& a, const DK<K>& b) { DK<K> r; r.v = __dadd_rn(a.v, b.v);
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = a.d[k] + b.d[k]; return r; }
+template <int K> BCG_HD DK<K> sub_rn(const DK<K>& a, const DK<K>& b) { DK<K> r; r.v = __dsub_rn(a.v, b.v);
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = a.d[k] - b.d[k]; return r; }
+template <int K> BCG_HD DK<K> div_rn(const DK<K>& a, const DK<K>& b) {
+  DK<K> r; r.v = __ddiv_rn(a.v, b.v); const double inv = rcp_rn(b.v);
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = fma(-r.v, b.d[k], a.d[k]) * inv; return r; }
 BCG_HD double fsign(double a, double b) { return (b >= 0.0) ? fabs(a) : -fabs(a); }
 template <int K> BCG_HD double fsign(double a, const DK<K>& b) { return fsign(a, b.v); }
 

@@ -18,10 +18,12 @@ BCG_HD void prim_cell(const Ext& e, const Coef& c, const State<S>& w, const Scra
   const S ro = w(q), ru = w(q + n), rv = w(q + 2 * n), rw = w(q + 3 * n), re = w(q + 4 * n);
   const S rom1 = 1.0 / ro;
   const S u = ru * rom1, v = rv * rom1, ww = rw * rom1;
-  const S ec = 0.5 * (u * u + v * v + ww * ww);
-  const S eloc = (re - ec * ro) * rom1;
+  // energies and pressure rounded operation by operation in the reference's
+  // order: the pressure sensor's MAX/abs branches follow the pressure's bits
+  const S ec = 0.5 * add_rn(add_rn(mul_rn(u, u), mul_rn(v, v)), mul_rn(ww, ww));
+  const S eloc = mul_rn(sub_rn(re, mul_rn(ec, ro)), rom1);
   const S t = eloc * c.cvm1;
-  const S p = c.gam1 * ro * eloc;
+  const S p = mul_rn(mul_rn(c.gam1, ro), eloc);
   const S htot = (re + p) * rom1;
   pr.st(F_U, q, u); pr.st(F_V, q, v); pr.st(F_W, q, ww); pr.st(F_T, q, t); pr.st(F_P, q, p);
   pr.st(F_F2, q, ru * u + p); pr.st(F_F3, q, ru * v); pr.st(F_F4, q, ru * ww); pr.st(F_F5, q, ru * htot);
@@ -307,8 +309,9 @@ struct FaceCtx {
     {
       const S c2r = c.c2fac * P(F_T, iR, jR), c2l = c.c2fac * P(F_T, iL, jL);
       const S pL = P(F_P, iL, jL), pR = P(F_P, iR, jR), pLL = P(F_P, iLL, jLL), pRR = P(F_P, iRR, jRR);
-      const S ks1 = fabs_t(pL - 2.0 * pR + pRR) / fabs_t(pL + 2.0 * pR + pRR);
-      const S ks2 = fabs_t(pLL - 2.0 * pL + pR) / fabs_t(pLL + 2.0 * pL + pR);
+      const S pR2 = 2.0 * pR, pL2 = 2.0 * pL;  // exact
+      const S ks1 = div_rn(fabs_t(add_rn(sub_rn(pL, pR2), pRR)), fabs_t(add_rn(add_rn(pL, pR2), pRR)));
+      const S ks2 = div_rn(fabs_t(add_rn(sub_rn(pLL, pL2), pR)), fabs_t(add_rn(add_rn(pLL, pL2), pR)));
       S divu = G(G_UX, iR, jR) + G(G_VY, iR, jR);
       S divu2 = divu * divu;
       S vo = G(G_VX, iR, jR) - G(G_UY, iR, jR);

@@ -377,6 +377,22 @@ int bcg_batch_configure(long long plan, int tile_faces, int tile_cells, int ctas
 /* Queue one evaluation on the library stream; use_graph = 1 captures the
  * launches into a CUDA graph on first use and replays it afterwards. */
 int bcg_batch_run(long long plan, int use_graph);
+/* Queue one pass of an evaluation alone, outside any graph (0 primitives,
+ * 1 Ducros gradients, 2 interpolation rows, 3 viscous point values, 4 faces,
+ * 5 balance; run in that order they equal bcg_batch_run): for timing each
+ * kernel of the evaluation with events on the library stream. */
+int bcg_batch_run_pass(long long plan, int pass);
+/* One evaluation with HOST arrays (tables of host addresses in the order of
+ * bcg_batch_set_arrays; pinned memory copies fastest): the grids are split
+ * into nchunk (1..16) contiguous chunks of about equal cell counts, and each
+ * chunk's uploads (state, tangent, metrics), its graph replay and the
+ * interior-only downloads of its residual and tangent overlap the other
+ * chunks'.  The caller's ghost values of residu / residud stay untouched.
+ * Returns when the outputs are in the host arrays.  The plan keeps device
+ * mirrors of every grid's arrays after the first such call. */
+int bcg_batch_run_host(long long plan, int nchunk, const unsigned long long* w, const unsigned long long* wd,
+                       const unsigned long long* nx, const unsigned long long* ny, const unsigned long long* vol,
+                       const unsigned long long* volf, const unsigned long long* res, const unsigned long long* resd);
 int bcg_batch_device_bytes(long long plan, long long* bytes);
 int bcg_batch_destroy(long long plan);
 

@@ -96,3 +96,60 @@ def test_residual_only_batch_and_autotune_cache(tmp_path):
     for g, (c, _) in enumerate(cases):
         ref = O.residual(c["grid"], c["phys"], c["w"])
         assert H.rel_err(to_host(gb.res[g]), ref, H.flux_scale(c, c["w"])) < 1e-12
+
+
+def test_full_size_uneven_grids_at_the_sensor_tie():
+    """Two full-size grids of the 64-grid uneven batch (933x294 and 353x294)
+    whose outflow column i = im holds a face where the pressure sensor's two
+    ratios agree to ~1e-7 (second differences ~8e-10 of p ~ 1.2 next to the
+    linearly extrapolated ghosts): MAX(ks1, ks2) there follows the pressure's
+    last bits.  Every interior cell of the tangent, i = im included, within
+    1e-11 of max|R'v| of the oracle, through the single-grid operator and the
+    batch."""
+    import torch
+    from broadcast_gb300 import cases
+    from broadcast_gb300.batch import GridBatch
+    from broadcast_gb300.operator import Dnc5Operator, to_device, to_host
+    sel = []
+    for k, c, wd in cases.uneven_bl_batch(only=(8, 29), ops=H.OracleOps):
+        H.oracle_bcs(c, c["w"])
+        sel.append((c, wd))
+    assert [c["grid"]["im"] for c, _ in sel] == [933, 353]
+    gb = GridBatch([c["grid"] for c, _ in sel], [c["phys"] for c, _ in sel], ndir=1)
+    gb.set_states([to_device(c["w"]) for c, _ in sel], [to_device(wd) for _, wd in sel])
+    gb.run(use_graph=True)
+    torch.cuda.synchronize()
+    for g, (c, wd) in enumerate(sel):
+        ref, refd = O.jvp(c["grid"], c["phys"], c["w"], wd)
+        scd = np.abs(H.interior(refd)).reshape(-1, 5).max(0)
+        op = Dnc5Operator(c["grid"], c["phys"])
+        r1, rd1 = op.jvp(to_device(c["w"]), to_device(wd))
+        for rd in (to_host(rd1), to_host(gb.resd[g])):
+            cell = (np.abs(H.interior(rd) - H.interior(refd)) / scd).max(axis=2)
+            assert cell.max() < 1e-11, (g, cell.max(), np.unravel_index(cell.argmax(), cell.shape))
+        assert H.rel_err(to_host(r1), ref, H.flux_scale(c, c["w"])) < 1e-12
+
+
+@pytest.mark.parametrize("nchunk", [1, 3, 16])
+def test_host_array_run_matches_device_run(nchunk):
+    """bcg_batch_run_host: host arrays in, overlapped chunk uploads / graph
+    replays / interior downloads, the same results as the device-array run
+    bit for bit, and the caller's ghost values of residu and residud kept."""
+    import torch
+    from broadcast_gb300.operator import to_host
+    cases = _cases(6, seed=11)
+    gb = _batch(cases)
+    gb.run(use_graph=True)
+    torch.cuda.synchronize()
+    ref = [(to_host(r).copy(), to_host(rd).copy()) for r, rd in zip(gb.res, gb.resd)]
+    res = [np.full_like(c["w"], 7.0) for c, _ in cases]
+    resd = [np.full_like(c["w"], -3.0) for c, _ in cases]
+    for _ in range(2):  # the second call reuses the plan's mirrors and chunk graphs
+        gb.run_host([c["w"] for c, _ in cases], [wd for _, wd in cases], res, resd, [c["grid"] for c, _ in cases],
+                    nchunk=nchunk)
+        for g in range(len(cases)):
+            assert np.array_equal(H.interior(res[g]), H.interior(ref[g][0]))
+            assert np.array_equal(H.interior(resd[g]), H.interior(ref[g][1]))
+            ghost = np.ones(res[g].shape, bool)
+            ghost[3:-3, 3:-3] = False
+            assert (res[g][ghost] == 7.0).all() and (resd[g][ghost] == -3.0).all()
