@@ -259,17 +259,17 @@ def run_reference(args):
     return 0
 
 
-# FP64 lane instructions (DFMA + DADD + DMUL) and DRAM bytes per cell and
-# direction of the passes of the 256x256 cylinder line (residual + 32
-# directions in groups of 4), from one ncu capture of that command:
-#   ncu --clock-control none -k regex:"k_(prim|qrows|vpts|faces|balance)" --metrics
-#       smsp__sass_thread_inst_executed_op_dfma_pred_on.sum,
-#       smsp__sass_thread_inst_executed_op_dadd_pred_on.sum,
-#       smsp__sass_thread_inst_executed_op_dmul_pred_on.sum,
-#       dram__bytes_read.sum,dram__bytes_write.sum
-#       python bench.py --workload cylinder --steps 1 --warmup 1 --no-extras
+# FP64 lane instructions (warp instructions of the FP64 pipe x 32) and DRAM
+# bytes per cell and direction of the passes of the 256x256 cylinder line
+# (residual + 32 directions in groups of 4), from one ncu capture of that
+# command:
+#   ncu --clock-control none -k regex:"k_(prim|qrows|vpts|faces|balance)" -c 10
+#       --metrics sm__inst_executed_pipe_fp64.sum,dram__bytes_read.sum,dram__bytes_write.sum
+#       python bench.py --workload cylinder --steps 1 --warmup 1 --cpu-seconds 1
 # divided by cells x directions.
-CYL_NCU = None
+CYL_NCU = {"fp64_inst_per_cell_dir": 664.9, "dram_bytes_per_cell_dir": 1381.8,
+           "source": "ncu sm__inst_executed_pipe_fp64.sum x 32 lanes and DRAM bytes of the five passes of one "
+                     "launch half (16 directions), per cell and direction, cold caches"}
 
 
 def cylinder_measure(args, dev, extras_only=False, ws=1, rank=0):
@@ -561,18 +561,27 @@ def _flux_scale(c):
     return (np.abs(f) + np.abs(h)).reshape(-1, 5).max(0) * np.sqrt(g["nx"] ** 2 + g["ny"] ** 2).max()
 
 
-# FP64 lane instructions (DFMA + DADD + DMUL, predicated on) and DRAM bytes
-# per interior cell of each pass of one uneven-batch evaluation (residual + one
+# FP64 lane instructions (warp instructions issued to the FP64 pipe x 32: the
+# DFMA, DADD and DMUL that make up 97 % of them and the compares and
+# conversions) and DRAM bytes per interior cell of each pass of one uneven-batch evaluation (residual + one
 # JVP direction, boundary-layer grids), from one ncu capture of the first 6
 # grids of the uneven batch (1.34M cells):
-#   ncu --clock-control none -k regex:k_batch --metrics
-#       smsp__sass_thread_inst_executed_op_dfma_pred_on.sum,
-#       smsp__sass_thread_inst_executed_op_dadd_pred_on.sum,
-#       smsp__sass_thread_inst_executed_op_dmul_pred_on.sum,
+#   ncu --clock-control none -k regex:k_batch -c 6 --metrics
+#       sm__inst_executed_pipe_fp64.sum,
+#       sm__sass_thread_inst_executed_ops_dadd_dmul_dfma_pred_on.sum,
+#       sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active,
 #       dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
-#       python bench.py --grids 6 --steps 1 --warmup 1 --no-extras
+#       python bench.py --grids 6 --steps 1 --warmup 1 --no-extras --tile 128,128,3 --cpu-seconds 1
 # divided by the capture's cells; the full batch's figures scale with its cells.
-BATCH_NCU = None
+BATCH_NCU = {
+    "fp64_inst_per_cell": {"prim": 139.0, "grad": 65.0, "qrows": 93.3, "vpts": 48.5, "faces": 1404.0,
+                           "balance": 30.0},
+    "dram_bytes_per_cell": {"prim": 334.2, "grad": 108.2, "qrows": 338.3, "vpts": 231.5, "faces": 1003.3,
+                            "balance": 219.4},
+    "source": "ncu sm__inst_executed_pipe_fp64.sum x 32 lanes and dram__bytes_read.sum + dram__bytes_write.sum "
+              "per k_batch launch, first 6 grids (1,344,226 cells), cold caches; per cell, scaled to this run's "
+              "cells",
+}
 BATCH_PASSES = ("prim", "grad", "qrows", "vpts", "faces", "balance")
 
 
@@ -688,15 +697,30 @@ def run_batch_reference(args):
 
 
 def inputs_digest(cs, wds):
-    """Digest of the grids' metrics, states and directions, rounded to 13
-    significant digits (the two arms fill the ghost cells with different
-    boundary-fill code, equal to ~1e-15)."""
+    """Digest of what both arms build bit-identically (host pre-processing
+    through the library and through the oracle agree bit for bit): the
+    grids' metrics, the interior states and the directions.  The ghost cells
+    are filled by each arm's own boundary-fill code (library kernels, oracle)
+    and compared numerically (parity.ghost_fill_vs_oracle_max_rel)."""
     import hashlib
     h = hashlib.sha256()
     for c, wd in zip(cs, wds):
-        for a in (c["grid"]["nx"], c["grid"]["ny"], c["grid"]["vol"], c["grid"]["volf"], c["w"], wd):
-            h.update(np.array([float("%.12e" % x) for x in np.ravel(a)[::97]]).tobytes())
+        for a in (c["grid"]["nx"], c["grid"]["ny"], c["grid"]["vol"], c["grid"]["volf"], H_int(c["w"]), wd):
+            h.update(np.ascontiguousarray(a).tobytes())
     return h.hexdigest()[:16]
+
+
+def ghost_fill_difference(cs):
+    """Largest difference, relative to the state's magnitude per variable,
+    between the ghost cells the library filled and the oracle's fills of the
+    same interior states."""
+    worst = 0.0
+    for c in cs:
+        w = c["w"].copy(order="F")
+        oracle_bl_bcs(c, w)
+        sc = np.abs(w).reshape(-1, 5).max(0)
+        worst = max(worst, float((np.abs(w - c["w"]).reshape(-1, 5) / sc).max()))
+    return worst
 
 
 def run_batch(args):
@@ -826,6 +850,7 @@ def run_batch(args):
             "pass_ms": dict(zip(BATCH_PASSES, pass_ms)),
             "parity": {"residual_vs_oracle_max": err_res, "tangent_vs_oracle_max": err_tan,
                        "tangent_cells_above_1e-11": above, "host_run_vs_device_run_max_abs": host_dev,
+                       "ghost_fill_vs_oracle_max_rel": ghost_fill_difference(cs),
                        "note": "residual relative to the face-flux magnitude, tangent to max|R'v| per variable"},
             "inputs_sha": inputs_digest(cs, wds),
             "cpu_baseline": cpu,

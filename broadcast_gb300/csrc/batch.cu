@@ -38,7 +38,7 @@ struct GridDesc {
   double* res;
   double* resd;
   double* scratch;  // residual_scratch_doubles(im, jm, 3, K) doubles
-  int grad;         // k2 != 0: the Ducros gradients are needed
+  int grad;         // k2 != 0: the sensor pass is needed
 };
 
 template <class S>
@@ -53,8 +53,8 @@ BCG_HD Fields<S> fields_of(const GridDesc& G) {
   Fields<S> f;
   f.pr = Scratch<S>{G.scratch, e.np};
   f.gr = Scratch<S>{G.scratch + (size_t)F_NPRIM * NP * e.np, e.np};
-  f.qr = Scratch<S>{G.scratch + (size_t)(F_NPRIM + G_NGRAD) * NP * e.np, e.np};
-  f.hn = Scratch<S>{G.scratch + (size_t)(F_NPRIM + G_NGRAD + Q_NQ) * NP * e.np, nn};
+  f.qr = Scratch<S>{G.scratch + (size_t)(F_NPRIM + S_NSENS) * NP * e.np, e.np};
+  f.hn = Scratch<S>{G.scratch + (size_t)(F_NPRIM + S_NSENS + Q_NQ) * NP * e.np, nn};
   return f;
 }
 template <class S> BCG_HD State<S> state_of(const GridDesc& G);
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(BT) k_batch(const GridDesc* __restrict__ descs
       } else if constexpr (PASS == P_VPTS) {
         if (el < (long long)e.np) vpts_cell<S>(e, f.qr, (size_t)el);
       } else if constexpr (PASS == P_GRAD) {
-        if (el < (long long)e.im * e.jm) grad_cell<S>(e, G.c, f.pr, f.gr, G.nx, G.ny, G.vol, (int)el);
+        if (el < (long long)(e.im + 2) * (e.jm + 2)) sensor_cell<S>(e, G.c, f.pr, f.gr, G.nx, G.ny, G.vol, (int)el);
       } else {
         if (el < (long long)e.im * e.jm) balance_cell<S>(e, f.hn, G.res, G.resd, G.dstride, (int)el);
       }
@@ -147,7 +147,7 @@ struct BatchPlan {
 static long long pass_count(const Ext& e, int pass, bool grad) {
   switch (pass) {
     case P_PRIM: case P_QROWS: case P_VPTS: return (long long)e.np;
-    case P_GRAD: return grad ? (long long)e.im * e.jm : 0;
+    case P_GRAD: return grad ? (long long)(e.im + 2) * (e.jm + 2) : 0;
     case P_FACES: return (long long)(e.im + 1) * (e.jm + 1);
     default: return (long long)e.im * e.jm;
   }

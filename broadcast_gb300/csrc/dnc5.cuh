@@ -10,7 +10,9 @@
 // The kernels work in three passes over HBM-resident scratch:
 //   pass 1  cell primitives (u, v, w, T, p, mu, Euler fluxes f2..f5, g2..g5)
 //           on every padded cell, once per cell;
-//   pass 2  cell gradients of u and v (Ducros sensor), once per interior cell;
+//   pass 2  the sensor's cell quantities (pressure ratios, Ducros ratio from
+//           the u and v gradients), once per cell of the interior and its
+//           one-cell ghost ring;
 //   pass 3  every face flux once (i- and j-faces of node (i,j)), then the
 //           balance differences them into the residual.
 #pragma once
@@ -168,8 +170,12 @@ enum PField {
 // gradients, each shared by two faces: C (3-point along i), D (3-point along
 // j), EI (4-point across i-face rows), NJ (4-point across j-face columns)
 enum QField { Q_I = 0, Q_J = 5, V_C = 10, V_D = 14, V_EI = 18, V_NJ = 22, Q_NQ = 26 };
-// Fields of the gradient scratch (pass 2)
+// Fields of the gradient scratch of the adjoint's forward pass
 enum GField { G_UX = 0, G_UY, G_VX, G_VY, G_NGRAD };
+// Fields of the sensor scratch of the residual pass 2 (k2 != 0), per cell of
+// the interior and its one-cell ghost ring: the pressure sensor along i and
+// along j, the Ducros ratio, 10 vol div(u) and the sound speed
+enum SField { S_KSI = 0, S_KSJ, S_DUC, S_ARG, S_CS, S_NSENS };
 
 // State accessor: value array plus K tangent arrays (stride dstride).
 template <class S> struct State;

@@ -12,7 +12,7 @@
 //
 // Limits and sharing rules:
 //  - the scratch holds kNoAllocScratchDoubles doubles (32 MiB); a grid needs
-//    48*(im+2gh)*(jm+2gh) + 10*(im+1)*(jm+1) of them (e.g. 256 x 256 or
+//    49*(im+2gh)*(jm+2gh) + 10*(im+1)*(jm+1) of them (e.g. 256 x 256 or
 //    400 x 150 fit), larger grids are rejected with BCG_ERR_ARG;
 //  - every call on a device uses the same array, which keeps the previous
 //    call's contents.  The residual kernels write every scratch entry they
@@ -70,7 +70,7 @@ int bcg_flux_num_dnc5_2d_noalloc(double* residu, const double* w, const double* 
   const size_t need = residual_scratch_doubles(im, jm, gh, 0);
   if (need > kNoAllocScratchDoubles)
     return fail_arg("flux_num_dnc5_2d_noalloc: grid too large for the fixed 32 MiB scratch "
-                    "(needs 48*(im+6)*(jm+6) + 10*(im+1)*(jm+1) <= 4194304 doubles)");
+                    "(needs 49*(im+6)*(jm+6) + 10*(im+1)*(jm+1) <= 4194304 doubles)");
   const void* arrays[] = {residu, w, nx, ny, vol, volf};
   for (const void* a : arrays)
     if (!is_device_ptr(a)) return fail_arg("flux_num_dnc5_2d_noalloc: every array must be a device pointer");

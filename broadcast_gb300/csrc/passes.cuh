@@ -128,6 +128,84 @@ BCG_HD void grad_cell(const Ext& e, const Coef& c, const Scratch<S>& pr, const S
 }
 
 // ---------------------------------------------------------------------------
+// pass 2 of the residual (k2 != 0): the cell quantities of the pressure/Ducros
+// sensor (rhs/ducrosfordnc_i.F, _j.F), once per cell instead of once per face
+// that reads them, on element t of the (im+2) x (jm+2) cells i in [0, im+1],
+// j in [0, jm+1] without the corners (the cells the faces' sensor reads):
+//   KSI, KSJ  |p(c-1) - 2 p(c) + p(c+1)| / |p(c-1) + 2 p(c) + p(c+1)| along i
+//             (rows 1..jm) and along j (columns 1..im), rounded operation by
+//             operation in the reference's order, so MAX(ks1, ks2) of a face
+//             compares the reference's values
+//   DUC       div(u)^2 / (div(u)^2 + rot(u)^2 + 1e-15)
+//   ARG       10 vol div(u), CS sqrt(gam R T): the face's tanh argument is
+//             2.5 + ARG / (CS |n| + 1e-15)
+// The u, v gradients are the 4th-order cell gradients (rhs/gradop_5pi.F,
+// gradop_5pj.F, gradient.F; 3p, 7p, 9p for R = 2, 4, 5), on the ghost ring
+// extrapolated from the two nearest interior cells (rhs/gradveloingh.F).
+template <class S, int R = 3>
+BCG_HD void cell_gradient(const Ext& e, const Coef& c, const Scratch<S>& pr, const double* __restrict__ nx,
+                          const double* __restrict__ ny, const double* __restrict__ vol, int i, int j, S g[4]) {
+  const size_t q = e.cidx(i, j);
+  const int di = 1, dj = e.ni;
+  auto g4 = [&](int f, int s) {
+    S x = c.bb[0] * (pr.ld(f, q + s) - pr.ld(f, q - s));
+#pragma unroll
+    for (int n = 2; n < R; ++n) x = x + c.bb[n - 1] * (pr.ld(f, q + n * s) - pr.ld(f, q - n * s));
+    return x;
+  };
+  const S gui = g4(F_U, di), gvi = g4(F_V, di), guj = g4(F_U, dj), gvj = g4(F_V, dj);
+  const size_t nn = e.nn();
+  const int a = e.nidx(i, j);
+  const double volm1 = 1.0 / __ldg(vol + q);
+  const double dxm1 = 0.5 * (__ldg(nx + a) + __ldg(nx + a + 1)) * volm1;
+  const double dxm2 = 0.5 * (__ldg(nx + nn + a) + __ldg(nx + nn + a + e.ni + 1)) * volm1;
+  const double dym1 = 0.5 * (__ldg(ny + a) + __ldg(ny + a + 1)) * volm1;
+  const double dym2 = 0.5 * (__ldg(ny + nn + a) + __ldg(ny + nn + a + e.ni + 1)) * volm1;
+  g[G_UX] = dxm1 * gui + dxm2 * guj;
+  g[G_VX] = dxm1 * gvi + dxm2 * gvj;
+  g[G_UY] = dym1 * gui + dym2 * guj;
+  g[G_VY] = dym1 * gvi + dym2 * gvj;
+}
+
+template <class S>
+BCG_HD S pressure_ratio(const S& pm, const S& p0, const S& pp) {
+  const S p02 = 2.0 * p0;  // exact
+  return div_rn(fabs_t(add_rn(sub_rn(pm, p02), pp)), fabs_t(add_rn(add_rn(pm, p02), pp)));
+}
+
+template <class S, int R = 3>
+BCG_HD void sensor_cell(const Ext& e, const Coef& c, const Scratch<S>& pr, const Scratch<S>& sg,
+                        const double* __restrict__ nx, const double* __restrict__ ny, const double* __restrict__ vol,
+                        int t) {
+  const int i = t % (e.im + 2), j = t / (e.im + 2);
+  const bool iring = (i == 0 || i == e.im + 1), jring = (j == 0 || j == e.jm + 1);
+  if (iring && jring) return;
+  S g[4];
+  if (!iring && !jring) {
+    cell_gradient<S, R>(e, c, pr, nx, ny, vol, i, j, g);
+  } else {
+    // ghost ring: 2 g(nearest interior) - g(next interior), as the faces' gradients
+    int i1 = i, j1 = j, i2 = i, j2 = j;
+    if (i == 0) { i1 = 1; i2 = 2; } else if (i == e.im + 1) { i1 = e.im; i2 = e.im - 1; }
+    else if (j == e.jm + 1) { j1 = e.jm; j2 = e.jm - 1; } else { j1 = 1; j2 = 2; }
+    S g1[4], g2[4];
+    cell_gradient<S, R>(e, c, pr, nx, ny, vol, i1, j1, g1);
+    cell_gradient<S, R>(e, c, pr, nx, ny, vol, i2, j2, g2);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) g[k] = 2.0 * g1[k] - g2[k];
+  }
+  const size_t q = e.cidx(i, j);
+  const S divu = g[G_UX] + g[G_VY], vo = g[G_VX] - g[G_UY];
+  const S divu2 = divu * divu, vort2 = vo * vo;
+  sg.st(S_DUC, q, divu2 / (divu2 + vort2 + 1e-15));
+  sg.st(S_ARG, q, (10.0 * __ldg(vol + q)) * divu);
+  sg.st(S_CS, q, sqrt_t(c.c2fac * pr.ld(F_T, q)));
+  if (!jring) sg.st(S_KSI, q, pressure_ratio(pr.ld(F_P, q - 1), pr.ld(F_P, q), pr.ld(F_P, q + 1)));
+  if (!iring)
+    sg.st(S_KSJ, q, pressure_ratio(pr.ld(F_P, q - e.ni), pr.ld(F_P, q), pr.ld(F_P, q + e.ni)));
+}
+
+// ---------------------------------------------------------------------------
 // pass 3: face fluxes of the DNC scheme with R point pairs (R = 3: DNC5)
 template <class S, int R = 3>
 struct FaceCtx {
@@ -154,14 +232,8 @@ struct FaceCtx {
   BCG_HD double NY(int i, int j, int d) const { return __ldg(ny + (size_t)(d - 1) * e.nn() + e.nidx(i, j)); }
   BCG_HD double VOL(int i, int j) const { return __ldg(vol + e.cidx(i, j)); }
   BCG_HD double VOLF(int i, int j, int d) const { return __ldg(volf + (size_t)(d - 1) * e.np + e.cidx(i, j)); }
-  // gradients, with the ghost lines the faces need (rhs/gradveloingh.F)
-  BCG_HD S G(int f, int i, int j) const {
-    if (i == 0) return 2.0 * gr.ld(f, e.cidx(1, j)) - gr.ld(f, e.cidx(2, j));
-    if (i == e.im + 1) return 2.0 * gr.ld(f, e.cidx(e.im, j)) - gr.ld(f, e.cidx(e.im - 1, j));
-    if (j == e.jm + 1) return 2.0 * gr.ld(f, e.cidx(i, e.jm)) - gr.ld(f, e.cidx(i, e.jm - 1));
-    if (j == 0) return 2.0 * gr.ld(f, e.cidx(i, 1)) - gr.ld(f, e.cidx(i, 2));  // no-wall j-faces at j = 1
-    return gr.ld(f, e.cidx(i, j));
-  }
+  // sensor quantities of pass 2 (cells of the interior and its ghost ring)
+  BCG_HD S SG(int f, int i, int j) const { return gr.ld(f, e.cidx(i, j)); }
   BCG_HD static S q4(const S& a, const S& b, const S& cc, const S& d) { return -a + 9.0 * b + 9.0 * cc - d; }
 
   // Normal viscous flux fv * snx + gv * sny (the only combination the face
@@ -286,9 +358,10 @@ struct FaceCtx {
 
   // spectral radius, Ducros/pressure sensor and dissipation through the face
   // between cells L and R (rhs/spectralradius_i.F, ducrosfordnc_i.F,
-  // dissipation_ducros_i.F); LL/RR extend the pressure stencil.
-  BCG_HD void dissipation(int iL, int jL, int iR, int jR, int iLL, int jLL, int iRR, int jRR, double fnx, double fny,
-                          const S pred[5], S diss[5]) const {
+  // dissipation_ducros_i.F); ksf: the pressure-sensor field of the face's
+  // direction (S_KSI or S_KSJ).
+  BCG_HD void dissipation(int iL, int jL, int iR, int jR, int ksf, double fnx, double fny, const S pred[5],
+                          S diss[5]) const {
     // Roe average: rr = sqrt(rhoL)/(sqrt(rhoL)+sqrt(rhoR)), so
     // u = (sL uL + sR uR)/(sL + sR), and likewise v and c^2
     const S inv = 1.0 / (P(F_SR, iL, jL) + P(F_SR, iR, jR));
@@ -307,24 +380,27 @@ struct FaceCtx {
     }
     S eps2, eps4;
     {
-      const S c2r = c.c2fac * P(F_T, iR, jR), c2l = c.c2fac * P(F_T, iL, jL);
-      const S pL = P(F_P, iL, jL), pR = P(F_P, iR, jR), pLL = P(F_P, iLL, jLL), pRR = P(F_P, iRR, jRR);
-      const S pR2 = 2.0 * pR, pL2 = 2.0 * pL;  // exact
-      const S ks1 = div_rn(fabs_t(add_rn(sub_rn(pL, pR2), pRR)), fabs_t(add_rn(add_rn(pL, pR2), pRR)));
-      const S ks2 = div_rn(fabs_t(add_rn(sub_rn(pLL, pL2), pR)), fabs_t(add_rn(add_rn(pLL, pL2), pR)));
-      S divu = G(G_UX, iR, jR) + G(G_VY, iR, jR);
-      S divu2 = divu * divu;
-      S vo = G(G_VX, iR, jR) - G(G_UY, iR, jR);
-      S vort2 = vo * vo;
-      const S ducros1 = divu2 / (divu2 + vort2 + 1e-15);
-      const S dxm1 = 0.5 * (1.0 - tanh_t(2.5 + 10.0 * VOL(iR, jR) / (sqrt_t(c2r * nx2) + 1e-15) * divu));
-      divu = G(G_UX, iL, jL) + G(G_VY, iL, jL);
-      divu2 = divu * divu;
-      vo = G(G_VX, iL, jL) - G(G_UY, iL, jL);
-      vort2 = vo * vo;
-      const S ducros2 = divu2 / (divu2 + vort2 + 1e-15);
-      const S dxm2 = 0.5 * (1.0 - tanh_t(2.5 + 10.0 * VOL(iL, jL) / (sqrt_t(c2l * nx2) + 1e-15) * divu));
-      const S coef = fmax_t(ks1, ks2) * fmax_t(ducros1, ducros2) * fmax_t(dxm1, dxm2);
+      // sensor of cells R (1) and L (2): ks and Ducros from pass 2
+      const S ks1 = SG(ksf, iR, jR), ks2 = SG(ksf, iL, jL);
+      const S ducros1 = SG(S_DUC, iR, jR), ducros2 = SG(S_DUC, iL, jL);
+      // dxm = (1 - tanh(arg)) / 2, arg = 2.5 + 10 vol div(u) / (c |n| + 1e-15),
+      // decreases with arg: MAX(dxm1, dxm2) is the dxm of the smaller
+      // argument.  Arguments closer than rounding could order differently take
+      // both tanh and the reference's rule (MAX keeps its first argument unless
+      // it is strictly smaller).
+      const double nabs = sqrt(nx2);
+      const S arg1 = 2.5 + SG(S_ARG, iR, jR) / (SG(S_CS, iR, jR) * nabs + 1e-15);
+      const S arg2 = 2.5 + SG(S_ARG, iL, jL) / (SG(S_CS, iL, jL) * nabs + 1e-15);
+      const double gap = val(arg1) - val(arg2), tol = 1e-12 * (fabs(val(arg1)) + 1.0);
+      S dxm;
+      if (gap > tol) {
+        dxm = 0.5 * (1.0 - tanh_t(arg2));
+      } else if (gap < -tol) {
+        dxm = 0.5 * (1.0 - tanh_t(arg1));
+      } else {
+        dxm = fmax_t(0.5 * (1.0 - tanh_t(arg1)), 0.5 * (1.0 - tanh_t(arg2)));
+      }
+      const S coef = fmax_t(ks1, ks2) * fmax_t(ducros1, ducros2) * dxm;
       eps2 = c.k2 * coef;
       eps4 = fmax_t(Planes<S>::c(0.0), c.k4 - eps2 * 12.0);
     }
@@ -386,7 +462,7 @@ struct FaceCtx {
       pred[v5 - 1] = predictor(v5, i, j, 1, 0);
     }
     visc_i(i, j, ALL_O2 || (c.wall && j <= 2), fnx, fny, fn);
-    dissipation(i - 1, j, i, j, i - 2, j, i + 1, j, fnx, fny, pred, diss);
+    dissipation(i - 1, j, i, j, S_KSI, fnx, fny, pred, diss);
     assemble(fx, diss, fn, h);
   }
 
@@ -415,7 +491,7 @@ struct FaceCtx {
       pred[v5 - 1] = predictor(v5, i, j, 0, 1);
     }
     visc_j(i, j, ALL_O2 || (c.wall && j == 2), fnx, fny, fn);
-    dissipation(i, j - 1, i, j, i, j - 2, i, j + 1, fnx, fny, pred, diss);
+    dissipation(i, j - 1, i, j, S_KSJ, fnx, fny, pred, diss);
     assemble(fx, diss, fn, h);
   }
 

@@ -24,7 +24,7 @@ void launch_primal_passes(const Ext& e, const Coef& c, const double* w, double* 
 size_t residual_scratch_doubles(int im, int jm, int gh, int ndir) {
   const Ext e = make_ext(im, jm, gh);
   const size_t nn = (size_t)(im + 1) * (jm + 1);
-  return (size_t)(ndir + 1) * ((size_t)(F_NPRIM + G_NGRAD + Q_NQ) * e.np + 10 * nn);
+  return (size_t)(ndir + 1) * ((size_t)(F_NPRIM + S_NSENS + Q_NQ) * e.np + 10 * nn);
 }
 
 cudaError_t run_residual(const ResidualArgs& a, cudaStream_t st) {

@@ -62,6 +62,17 @@ __global__ void __launch_bounds__(256) k_grad(Ext e, Coef c, Scratch<S> pr, Scra
 }
 
 template <class S, int R = 3>
+__global__ void __launch_bounds__(256) k_sensor(Ext e, Coef c, Scratch<S> pr, Scratch<S> sg,
+                                                const double* __restrict__ nx, const double* __restrict__ ny,
+                                                const double* __restrict__ vol, GroupStride gs) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (e.im + 2) * (e.jm + 2)) return;
+  shift_scratch(pr, blockIdx.y * gs.scratch);
+  shift_scratch(sg, blockIdx.y * gs.scratch);
+  sensor_cell<S, R>(e, c, pr, sg, nx, ny, vol, t);
+}
+
+template <class S, int R = 3>
 __global__ void __launch_bounds__(128) k_faces(FaceCtx<S, R> fc0, Scratch<S> hn, GroupStride gs) {
   const Ext& e = fc0.e;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -96,8 +107,8 @@ static cudaError_t run_residual_t(const ResidualArgs& a, cudaStream_t st) {
   const size_t nn = (size_t)(a.im + 1) * (a.jm + 1);
   Scratch<S> pr{a.scratch, e.np};
   Scratch<S> gr{a.scratch + (size_t)F_NPRIM * NP * e.np, e.np};
-  Scratch<S> qr{a.scratch + (size_t)(F_NPRIM + G_NGRAD) * NP * e.np, e.np};
-  Scratch<S> hn{a.scratch + (size_t)(F_NPRIM + G_NGRAD + Q_NQ) * NP * e.np, nn};
+  Scratch<S> qr{a.scratch + (size_t)(F_NPRIM + S_NSENS) * NP * e.np, e.np};
+  Scratch<S> hn{a.scratch + (size_t)(F_NPRIM + S_NSENS + Q_NQ) * NP * e.np, nn};
   State<S> w;
   if constexpr (NP == 1) w = State<S>{a.w};
   else w = State<S>{a.w, a.wd, a.dstride};
@@ -107,7 +118,8 @@ static cudaError_t run_residual_t(const ResidualArgs& a, cudaStream_t st) {
   const int B = 256;
   k_prim<S><<<dim3((unsigned)((e.np + B - 1) / B), ng), B, 0, st>>>(e, c, w, pr, gs);
   if (c.k2 != 0.0)
-    k_grad<S, R><<<dim3((unsigned)((a.im * a.jm + B - 1) / B), ng), B, 0, st>>>(e, c, pr, gr, a.nx, a.ny, a.vol, gs);
+    k_sensor<S, R><<<dim3((unsigned)(((a.im + 2) * (a.jm + 2) + B - 1) / B), ng), B, 0, st>>>(e, c, pr, gr, a.nx,
+                                                                                            a.ny, a.vol, gs);
   if (!FaceCtx<S, R>::ALL_O2) {  // the 4th-order viscous fluxes' interpolation rows
     k_qrows<S><<<dim3((unsigned)((e.np + B - 1) / B), ng), B, 0, st>>>(e, pr, qr, gs);
     k_vpts<S><<<dim3((unsigned)((e.np + B - 1) / B), ng), B, 0, st>>>(e, qr, gs);

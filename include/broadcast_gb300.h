@@ -403,7 +403,7 @@ int bcg_batch_destroy(long long plan);
  * arguments and result as bcg_flux_num_dnc5_2d, but every array must be a
  * device pointer and the working storage is a fixed 32 MiB static device
  * array (held by every GPU that loads the library until the process exits):
- * grids need 48*(im+6)*(jm+6) + 10*(im+1)*(jm+1) <= 4194304 doubles (256 x 256
+ * grids need 49*(im+6)*(jm+6) + 10*(im+1)*(jm+1) <= 4194304 doubles (256 x 256
  * and 400 x 150 fit); larger ones return -1.  All calls share that array:
  * calls that overlap on the GPU race, so serialise them.  The first call on a
  * device looks up the array's address for that device; make it before any

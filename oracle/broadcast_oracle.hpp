@@ -1186,42 +1186,69 @@ enum JacMode {
   JAC_WITHJN = 3,         // computejacobianfromjv_withjn     (:929-999)
   JAC_DZ = 4,             // computejacobianfromdz            (:708-779)
 };
-inline void computejacobian(int mode, double* jac, int* ia, int* ja, const double* resd_, int m, int l, int k,
-                            int gh, int im, int jm, const double* coefdiag) {
-  FArr<const double> resd(resd_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+// One COO slot of seed (m, l, k) for output (i, j, e): row, column and value,
+// or the reference's invalid-slot marker (row 5*im*jm-1, or -2 for the _withjn
+// variants; column 0, value 0).
+inline void jacobian_slot(int mode, const FArr<const double>& resd, int i, int j, int e, int m, int l, int k, int gh,
+                          int im, int jm, const double* coefdiag, int* ia_out, int* ja_out, double* val_out) {
   const int step = 1 + 2 * gh;
   const bool jn = (mode == JAC_RELAXED_WITHJN || mode == JAC_WITHJN);
   const bool relaxed = (mode == JAC_RELAXED || mode == JAC_RELAXED_WITHJN);
   const int bad = jn ? 5 * im * jm - 2 : 5 * im * jm - 1;
+  const int ia = e - 1 + (j - 1) * 5 + (i - 1) * jm * 5;
+  int valj, vali;
+  if (mode == JAC_DZ) {
+    if (k <= gh) valj = (j <= k + 1 + gh) ? k : (j - (k + 1) + gh) / step * step + k;
+    else valj = (j <= k - gh) ? jm + 1 : (j - (k + 1) + gh) / step * step + k;
+  } else {
+    valj = (j <= k + 1 + gh) ? k : (j - gh - (k + 1) + 2 * gh) / step * step + k;
+  }
+  if (valj >= jm) { *ia_out = bad; *ja_out = 0; *val_out = 0.0; return; }
+  if (l <= gh) vali = (i <= l + 1 + gh) ? l : (i - (l + 1) + gh) / step * step + l;
+  else {
+    if (i <= l - gh) vali = jn ? im - 1 - 2 * gh + l : im + 1;
+    else vali = (i - (l + 1) + gh) / step * step + l;
+  }
+  if (vali >= im) {
+    if (jn && vali - im <= gh - 1) vali = l;
+    else { *ia_out = bad; *ja_out = 0; *val_out = 0.0; return; }
+  }
+  const int ja = m + valj * 5 + vali * jm * 5;
+  const double r = resd(i, j, e);
+  *ia_out = ia;
+  *ja_out = ja;
+  if (mode == JAC_DZ) *val_out = r;
+  else if (relaxed && ia == ja) *val_out = coefdiag[(i - 1) + (size_t)(j - 1) * im] - r;
+  else *val_out = -r;
+}
+
+inline void computejacobian(int mode, double* jac, int* ia, int* ja, const double* resd_, int m, int l, int k,
+                            int gh, int im, int jm, const double* coefdiag) {
+  FArr<const double> resd(resd_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  const int step = 1 + 2 * gh;
   for (int e = 1; e <= 5; ++e)
     for (int j = 1; j <= jm; ++j)
       for (int i = 1; i <= im; ++i) {
         const long long cur = (long long)(i - 1) + (long long)(j - 1) * im + (long long)(e - 1) * im * jm +
                               (long long)k * im * jm * 5 + (long long)l * im * jm * 5 * step +
                               (long long)m * im * jm * 5 * step * step;
-        ia[cur] = e - 1 + (j - 1) * 5 + (i - 1) * jm * 5;
-        int valj, vali;
-        if (mode == JAC_DZ) {
-          if (k <= gh) valj = (j <= k + 1 + gh) ? k : (j - (k + 1) + gh) / step * step + k;
-          else valj = (j <= k - gh) ? jm + 1 : (j - (k + 1) + gh) / step * step + k;
-        } else {
-          valj = (j <= k + 1 + gh) ? k : (j - gh - (k + 1) + 2 * gh) / step * step + k;
-        }
-        if (valj >= jm) { ia[cur] = bad; ja[cur] = 0; jac[cur] = 0.0; continue; }
-        if (l <= gh) vali = (i <= l + 1 + gh) ? l : (i - (l + 1) + gh) / step * step + l;
-        else {
-          if (i <= l - gh) vali = jn ? im - 1 - 2 * gh + l : im + 1;
-          else vali = (i - (l + 1) + gh) / step * step + l;
-        }
-        if (vali >= im) {
-          if (jn && vali - im <= gh - 1) vali = l;
-          else { ia[cur] = bad; ja[cur] = 0; jac[cur] = 0.0; continue; }
-        }
-        ja[cur] = m + valj * 5 + vali * jm * 5;
-        const double r = resd(i, j, e);
-        if (mode == JAC_DZ) jac[cur] = r;
-        else if (relaxed && ia[cur] == ja[cur]) jac[cur] = coefdiag[(i - 1) + (size_t)(j - 1) * im] - r;
-        else jac[cur] = -r;
+        jacobian_slot(mode, resd, i, j, e, m, l, k, gh, im, jm, coefdiag, ia + cur, ja + cur, jac + cur);
+      }
+}
+
+// The slots of one seed for the outputs of columns i0..i1 only, in a
+// band-local layout: slot (i - i0) + (j - 1) nb + (e - 1) nb jm with
+// nb = i1 - i0 + 1 (test infrastructure: the full COO of a large grid does not
+// fit in memory, the slots of one seed and a band of rows do).
+inline void computejacobian_band(int mode, double* jac, int* ia, int* ja, const double* resd_, int m, int l, int k,
+                                 int gh, int im, int jm, const double* coefdiag, int i0, int i1) {
+  FArr<const double> resd(resd_, im + 2 * gh, jm + 2 * gh, 1 - gh);
+  const long long nb = i1 - i0 + 1;
+  for (int e = 1; e <= 5; ++e)
+    for (int j = 1; j <= jm; ++j)
+      for (int i = i0; i <= i1; ++i) {
+        const long long cur = (long long)(i - i0) + (long long)(j - 1) * nb + (long long)(e - 1) * nb * jm;
+        jacobian_slot(mode, resd, i, j, e, m, l, k, gh, im, jm, coefdiag, ia + cur, ja + cur, jac + cur);
       }
 }
 

@@ -49,6 +49,7 @@ SIGS = {
     "orc_testvector_partial": [_P] + [_I] * 10,
     "orc_computejacobian": [_I, _P, _P, _P, _P] + [_I] * 6 + [_P],
     "orc_computejacobian_withjnandcheck": [_P, _P, _P, _P] + [_I] * 6 + [_P, _D, _I],
+    "orc_computejacobian_band": [_I, _P, _P, _P, _P] + [_I] * 6 + [_P, _I, _I],
     "orc_coeffs_5p_dz": [_P] * 3 + [_I] + [_P] * 3 + [_I] + [_D] * 9 + [_I] * 3,
     "orc_bc_b": [_I, _P, _P, _P, _I, _S, _P, _P, _P, _D, _I, _I, _I, _I],
 }
@@ -114,8 +115,9 @@ def residual(grid, ph, w, nowall=False, order=5):
     return res
 
 
-def jvp(grid, ph, w, wd, nowall=False, order=5):
-    """wd: one padded state or a stack (nd, ...) of them; returns (res, resd)."""
+def jvp(grid, ph, w, wd, nowall=False, order=5, openmp=False):
+    """wd: one padded state or a stack (nd, ...) of them; returns (res, resd).
+    openmp: the OpenMP build (all host cores over j-rows)."""
     wd = np.asarray(wd)
     single = wd.ndim == 3
     wds = wd[None] if single else wd
@@ -126,11 +128,12 @@ def jvp(grid, ph, w, wd, nowall=False, order=5):
     res = np.zeros_like(w, order="F")
     args = (_p(res), _p(out), _p(_chk(w)), _p(buf), nd, _p(grid["nx"]), _p(grid["ny"]), _p(grid["vol"]),
             _p(grid["volf"]), grid["gh"], *_phys(ph), grid["im"], grid["jm"])
+    L = lib(openmp=openmp)
     if order != 5:
-        if lib().orc_flux_num_dnc_2d_d(order, 0 if nowall else 1, *args):
+        if L.orc_flux_num_dnc_2d_d(order, 0 if nowall else 1, *args):
             raise ValueError("flux_num_dnc%d_2d_d: bad order or ghost width" % order)
     else:
-        fn = lib().orc_flux_num_dnc5_nowall_2d_d if nowall else lib().orc_flux_num_dnc5_2d_d
+        fn = L.orc_flux_num_dnc5_nowall_2d_d if nowall else L.orc_flux_num_dnc5_2d_d
         fn(*args)
     n = w.size
     resd = [np.reshape(out[k * n:(k + 1) * n], w.shape, order="F") for k in range(nd)]
@@ -311,6 +314,20 @@ JAC_PLAIN, JAC_RELAXED, JAC_RELAXED_WITHJN, JAC_WITHJN, JAC_DZ = 0, 1, 2, 3, 4
 def computejacobian(mode, jac, ia, ja, resd, m, l, k, gh, im, jm, coefdiag=None):
     cd = None if coefdiag is None else np.asfortranarray(coefdiag, dtype=np.float64)
     lib().orc_computejacobian(mode, _p(jac), _p(ia), _p(ja), _p(resd), m, l, k, gh, im, jm, _p(cd))
+
+
+def computejacobian_band(mode, resd, m, l, k, gh, im, jm, coefdiag=None, i0=1, i1=None):
+    """The COO slots of seed (m, l, k) for the outputs of columns i0..i1
+    (1-based, inclusive): (ia, ja, jac) arrays of 5 jm (i1 - i0 + 1) slots in
+    the order (i, j, e) with i fastest; invalid slots carry the reference's
+    marker row."""
+    i1 = im if i1 is None else i1
+    n = 5 * jm * (i1 - i0 + 1)
+    jac, ia, ja = np.zeros(n), np.zeros(n, np.int32), np.zeros(n, np.int32)
+    cd = None if coefdiag is None else np.asfortranarray(coefdiag, dtype=np.float64)
+    if lib().orc_computejacobian_band(mode, _p(jac), _p(ia), _p(ja), _p(resd), m, l, k, gh, im, jm, _p(cd), i0, i1):
+        raise ValueError("computejacobian_band: bad column range")
+    return ia, ja, jac
 
 
 def computejacobian_withjnandcheck(jac, ia, ja, resd, m, l, k, gh, im, jm, coefdiag, mini, n):

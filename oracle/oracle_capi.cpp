@@ -379,6 +379,13 @@ int orc_computejacobian(int mode, double* jac, int* ia, int* ja, const double* r
   computejacobian(mode, jac, ia, ja, resd, m, l, k, gh, im, jm, coefdiag);
   return 0;
 }
+int orc_computejacobian_band(int mode, double* jac, int* ia, int* ja, const double* resd, int m, int l, int k,
+                              int gh, int im, int jm, const double* coefdiag, int i0, int i1) {
+  if (i0 < 1 || i1 > im || i1 < i0) return -1;
+  computejacobian_band(mode, jac, ia, ja, resd, m, l, k, gh, im, jm, coefdiag, i0, i1);
+  return 0;
+}
+
 int orc_computejacobian_withjnandcheck(double* jac, int* ia, int* ja, const double* resd, int m, int l, int k, int gh,
                                        int im, int jm, const double* coefdiag, double mini, int n) {
   computejacobian_withjnandcheck(jac, ia, ja, resd, m, l, k, gh, im, jm, coefdiag, mini, n);
