@@ -574,15 +574,15 @@ def _flux_scale(c):
 #       python bench.py --grids 6 --steps 1 --warmup 1 --no-extras --tile 128,128,3 --cpu-seconds 1
 # divided by the capture's cells; the full batch's figures scale with its cells.
 BATCH_NCU = {
-    "fp64_inst_per_cell": {"prim": 139.0, "grad": 65.0, "qrows": 93.3, "vpts": 48.5, "faces": 1404.0,
+    "fp64_inst_per_cell": {"prim": 139.0, "sensor": 175.9, "qrows": 93.3, "vpts": 48.5, "faces": 1134.4,
                            "balance": 30.0},
-    "dram_bytes_per_cell": {"prim": 334.2, "grad": 108.2, "qrows": 338.3, "vpts": 231.5, "faces": 1003.3,
-                            "balance": 219.4},
+    "dram_bytes_per_cell": {"prim": 334.2, "sensor": 161.2, "qrows": 338.5, "vpts": 232.3, "faces": 980.6,
+                            "balance": 219.7},
     "source": "ncu sm__inst_executed_pipe_fp64.sum x 32 lanes and dram__bytes_read.sum + dram__bytes_write.sum "
               "per k_batch launch, first 6 grids (1,344,226 cells), cold caches; per cell, scaled to this run's "
               "cells",
 }
-BATCH_PASSES = ("prim", "grad", "qrows", "vpts", "faces", "balance")
+BATCH_PASSES = ("prim", "sensor", "qrows", "vpts", "faces", "balance")
 
 
 def batch_inputs(n, ops, bcs):
