@@ -1020,11 +1020,11 @@ def run_newton_workload(args):
     if args.case == "cyl":  # cylinder.py:841-1068 on the 256 x 256 O-mesh, Newton (cfl 1e10)
         im, jm = args.im or 256, args.jm or 256
         c = cases.cyl_case(im, jm, ops=LibOps)
-        nt = CylNewton(c)
+        nt = CylNewton(c, solver=None if args.solver == "band" else "krylov")
     else:
         im, jm = args.im or 400, args.jm or 150
         c = cases.bl_case(im, jm, seed=0, ops=LibOps)
-        nt = BLNewton(c)
+        nt = BLNewton(c) if args.solver == "band" else BLNewton(c, solver="krylov")
     w = c["w"].copy(order="F")
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -1055,7 +1055,10 @@ def run_newton_workload(args):
             "norms": [float(np.max(h["norm"])) for h in hist],
             "seconds_per_iteration": {"total": mean("seconds"), "fills_residual_norms": mean("seconds_residual"),
                                       "jacobian_245_seeds": mean("seconds_jacobian"),
-                                      "band_lu_solve": mean("seconds_solve")},
+                                      "linear_solve": mean("seconds_solve")},
+            "linear_solver": ("FP64 band LU (cuSOLVER getrf panels, cuBLAS trsm/gemm)" if args.solver == "band" else
+                              "FP64 GMRES, FP32 band LU preconditioner reused across iterations"),
+            "krylov": getattr(nt.solver, "log", None),
             "jacobian_nnz": hist[-1]["nnz"],
             "config": {"workload": ("cylinder O-mesh %dx%d, uniform flow + U(-1e-3, 1e-3) noise (seed 1), Mach 0.1, "
                                     "Re 47, band LU in the folded azimuthal order" % (im, jm)) if args.case == "cyl" else
@@ -1155,6 +1158,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="default line without the cylinder extra key")
     ap.add_argument("--lmax", type=int, default=10, help="impli workload: Gauss-Seidel sweeps per call")
     ap.add_argument("--case", default="bl", choices=["bl", "cyl"], help="newton workload: boundary layer or cylinder")
+    ap.add_argument("--solver", default="band", choices=["band", "krylov"],
+                    help="newton workload: FP64 band LU, or FP64 GMRES with an FP32 band LU preconditioner")
     ap.add_argument("--ntrain", type=int, default=200, help="warmstart workload: training base flows")
     ap.add_argument("--nheld", type=int, default=20, help="warmstart workload: held-out (Re, Mach) points")
     ap.add_argument("--train-steps", type=int, default=3000, help="warmstart workload: Adam steps")

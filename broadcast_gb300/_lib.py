@@ -31,6 +31,11 @@ SIGNATURES = {
     "bcg_flux_num_dnc5_nowall_2d_d": "pppp" + "pppppppp" + "i" + "d" * 11 + "ii",
     "bcg_impli_matrix_free_2d": "ppppppp" + "ddddd" + "ii" + "ddddd" + "iii",
     "bcg_csr_band_lu_solve": "ipppLpppip",
+    "bcg_band32_factor": "ipppppipp",
+    "bcg_band32_solve": "Lpp",
+    "bcg_band32_dims": "Lp",
+    "bcg_band32_destroy": "L",
+    "bcg_gmres_solve": "Lipppppiidpp",
     **{"bcg_flux_num_dnc%d%s_2d" % (o, v): "pppppppppp" + "i" + "d" * 11 + "ii" for o in (3, 7, 9) for v in ("", "_nowall")},
     **{"bcg_flux_num_dnc%d%s_2d_d" % (o, v): "pppp" + "pppppppp" + "i" + "d" * 11 + "ii"
        for o in (3, 7, 9) for v in ("", "_nowall")},

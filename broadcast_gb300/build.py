@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libbroadcast_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CU_SOURCES = ["residual.cu", "bc.cu", "assembly.cu", "runtime.cu", "api.cu", "calib.cu", "noalloc.cu", "adjoint.cu", "jacobian.cu", "span.cu", "batch.cu", "schemes.cu", "impli.cu", "bandlu.cu", "mlp.cu"]
+CU_SOURCES = ["residual.cu", "bc.cu", "assembly.cu", "runtime.cu", "api.cu", "calib.cu", "noalloc.cu", "adjoint.cu", "jacobian.cu", "span.cu", "batch.cu", "schemes.cu", "impli.cu", "bandlu.cu", "krylov.cu", "mlp.cu"]
 CPP_SOURCES = ["host.cpp"]
 
 

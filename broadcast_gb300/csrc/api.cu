@@ -20,6 +20,7 @@
 #include "batch.h"
 #include "impli.h"
 #include "bandlu.h"
+#include "krylov.h"
 
 using namespace bcg;
 
@@ -1269,4 +1270,35 @@ extern "C" int bcg_batch_destroy(long long plan) {
   cudaError_t e = cudaStreamSynchronize(current_stream());
   batch_destroy(p);
   return e == cudaSuccess ? BCG_OK : fail_cuda("batch_destroy", e);
+}
+
+// ===========================================================================
+// Newton-Krylov solves (krylov.cu): FP32 band LU preconditioner, FP64 GMRES
+// ===========================================================================
+extern "C" int bcg_band32_factor(int n, const int* indptr, const int* indices, const double* data, const int* perm,
+                                 int nb, long long* handle, int* info) {
+  if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
+  const void* arrs[3] = {indptr, indices, data};
+  for (const void* a : arrs)
+    if (!a || !is_device_ptr(a)) return fail_arg("band32_factor: CSR arrays must be device pointers");
+  if (perm && !is_device_ptr(perm)) return fail_arg("band32_factor: perm must be a device pointer");
+  return band32_factor(n, indptr, indices, data, perm, nb, current_stream(), handle, info);
+}
+
+extern "C" int bcg_band32_solve(long long handle, const double* b, double* x) {
+  if (!b || !x || !is_device_ptr(b) || !is_device_ptr(x)) return fail_arg("band32_solve: device vectors expected");
+  return band32_solve(handle, b, x, current_stream());
+}
+
+extern "C" int bcg_band32_dims(long long handle, int* klku_nb) { return band32_dims(handle, klku_nb); }
+
+extern "C" int bcg_band32_destroy(long long handle) { return band32_destroy(handle); }
+
+extern "C" int bcg_gmres_solve(long long handle, int n, const int* indptr, const int* indices, const double* data,
+                               const double* b, double* x, int restart, int maxit, double rtol, int* iters,
+                               double* relres) {
+  const void* arrs[5] = {indptr, indices, data, b, x};
+  for (const void* a : arrs)
+    if (!a || !is_device_ptr(a)) return fail_arg("gmres_solve: every array must be a device pointer");
+  return gmres_solve(handle, n, indptr, indices, data, b, x, restart, maxit, rtol, current_stream(), iters, relres);
 }

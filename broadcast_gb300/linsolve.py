@@ -1,5 +1,9 @@
 """Linear solves of the Newton iteration on the GPU.
 
+Two solvers: `band_lu_solve` (FP64 band LU, direct) and `KrylovSolver` (FP64
+GMRES preconditioned by an FP32 band LU kept on the device and reused while it
+keeps GMRES short; the large O-meshes, where FP64 factorisations cost minutes).
+
 The reference factorises the Newton matrix with PETSc/MUMPS on the host
 (BROADCAST_npz.py:1146-1158, misc/PETSc_func.py:137-152).  `band_lu_solve`
 factorises it on the GPU instead: the boundary-layer Jacobian rows are ordered
@@ -49,3 +53,87 @@ def folded_ring_order(im, jm, nvar=5):
     fold = np.where(i < (im + 1) // 2, 2 * i, 2 * (im - 1 - i) + 1)  # 0, 2, 4, ..., 5, 3, 1
     ii, jj, ee = np.meshgrid(i, np.arange(jm), np.arange(nvar), indexing="ij")
     return (ee + nvar * fold[ii] + nvar * im * jj).ravel().astype(np.int32)
+
+
+class KrylovSolver:
+    """Newton-system solves on the GPU by FP64 GMRES (bcg_gmres_solve), right-
+    preconditioned by an FP32 band LU of a recent Newton matrix
+    (bcg_band32_factor: the row-equilibrated matrix in FP32, factorised in the
+    bandwidth-reducing order perm).  The factor is reused for later systems
+    (the next Newton steps, neighbouring base flows) and rebuilt from the
+    current matrix when GMRES needs more than `refactor_after` iterations or
+    does not reach `rtol`.
+
+    solve(indptr, indices, data, b) takes device tensors (torch, CSR int32 /
+    float64) and returns x as a device tensor."""
+
+    device_csr = True
+
+    def __init__(self, perm=None, nb=256, restart=60, maxit=240, rtol=1e-10, refactor_after=40):
+        _lib.load()
+        self.perm = None if perm is None else np.ascontiguousarray(perm, dtype=np.int32)
+        self.nb, self.restart, self.maxit, self.rtol = int(nb), int(restart), int(maxit), float(rtol)
+        self.refactor_after = int(refactor_after)
+        self.handle = None
+        self.n = None
+        self.log = []
+        self._perm_dev = None
+
+    def close(self):
+        if self.handle is not None:
+            try:
+                _lib.call("bcg_band32_destroy", self.handle)
+            finally:
+                self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def factor(self, indptr, indices, data):
+        import torch
+        self.close()
+        n = int(indptr.numel()) - 1
+        if self.perm is not None and self._perm_dev is None:
+            self._perm_dev = torch.from_numpy(self.perm).to(indptr.device)
+        h, info = np.zeros(1, np.int64), np.zeros(1, np.int32)
+        try:
+            _lib.call("bcg_band32_factor", n, indptr, indices, data, self._perm_dev, self.nb, h, info)
+        except _lib.BroadcastError as e:
+            if "singular" in str(e):
+                raise RuntimeError("singular FP32 factor (zero pivot at row %d)" % int(info[0])) from e
+            raise
+        self.handle, self.n = int(h[0]), n
+
+    def gmres(self, indptr, indices, data, b, x):
+        it, rr = np.zeros(1, np.int32), np.zeros(1)
+        _lib.call("bcg_gmres_solve", self.handle, self.n, indptr, indices, data, b, x, self.restart, self.maxit,
+                  self.rtol, it, rr)
+        return int(it[0]), float(rr[0])
+
+    def solve(self, indptr, indices, data, b):
+        import time
+        import torch
+        x = torch.empty_like(b)
+        n = int(indptr.numel()) - 1
+        t0 = time.perf_counter()
+        refactored = False
+        if self.handle is None or self.n != n:
+            self.factor(indptr, indices, data)
+            refactored = True
+        t1 = time.perf_counter()
+        it, rr = self.gmres(indptr, indices, data, b, x)
+        if not refactored and (rr > self.rtol or it > self.refactor_after):
+            self.factor(indptr, indices, data)
+            refactored = True
+            t1 = time.perf_counter()
+            it2, rr = self.gmres(indptr, indices, data, b, x)
+            it += it2
+        t2 = time.perf_counter()
+        self.log.append(dict(iterations=it, relres=rr, refactored=refactored, seconds_factor=t1 - t0,
+                             seconds_gmres=t2 - t1))
+        if not (rr <= self.rtol * 10) or not torch.isfinite(x).all():
+            raise RuntimeError("GMRES did not converge: relative residual %.2e after %d iterations" % (rr, it))
+        return x

@@ -14,7 +14,9 @@ Per iteration, as the reference:
      stepping back and halving cfl when dw is not finite (:1167-1172).
 Steps 1, 2 and 4 run on the GPU through the library; step 5 calls `solver`,
 by default the GPU band LU (broadcast_gb300.linsolve.band_lu_solve: the
-Jacobian is banded with bandwidth ~15 jm in its (i, j, e) row order);
+Jacobian is banded with bandwidth ~15 jm in its (i, j, e) row order); a
+linsolve.KrylovSolver (FP64 GMRES preconditioned by a reused FP32 band LU,
+the matrix assembled straight into device memory) for large grids;
 `superlu_solve` (scipy, host) or a PETSc/MUMPS solve can be passed instead.
 """
 import time
@@ -46,6 +48,9 @@ class BLNewton:
         self.phys = [float(ph[k]) for k in PHYS]
         self.mach = float(mach if mach is not None else ph.get("mach", 0.5))
         self.cfl = float(cfl)
+        if solver == "krylov":  # FP64 GMRES with a reused FP32 band LU preconditioner
+            from .linsolve import KrylovSolver
+            solver = KrylovSolver()
         self.solver = solver
         it = case["interf"]
         self.interf = [interf4(it[k]) for k in ("Ilo", "Jhi", "Ihi", "Jlo")]
@@ -72,18 +77,40 @@ class BLNewton:
         norm, ninf = f_norm.compute_norml2inf(res, self.im, self.jm, self.gh)
         return res, np.asarray(norm), np.asarray(ninf)
 
+    def _jac_args(self, w, coefdiag):
+        g, c = self.c["grid"], self.c
+        return ("bcg_jacobian_dnc5_bl_csr", (w, g["nx"], g["ny"], g["vol"], g["volf"], self.gh, *self.phys, self.im,
+                                             self.jm, *self.interf, c["field"], c["field"].shape[0], c["wbd"],
+                                             c["wbd"].shape[0], np.asfortranarray(coefdiag), 2e-16, 0))
+
     def jacobian(self, w, coefdiag):
         import scipy.sparse as sp
-        g, c = self.c["grid"], self.c
         nrow = 5 * self.im * self.jm
         cap = nrow * 245
         indptr, indices, data = np.zeros(nrow + 1, np.int32), np.zeros(cap, np.int32), np.zeros(cap)
         nnz = np.zeros(1, np.int64)
-        _lib.call("bcg_jacobian_dnc5_bl_csr", w, g["nx"], g["ny"], g["vol"], g["volf"], self.gh, *self.phys,
-                  self.im, self.jm, *self.interf, c["field"], c["field"].shape[0], c["wbd"], c["wbd"].shape[0],
-                  np.asfortranarray(coefdiag), 2e-16, 0, indptr, indices, data, cap, nnz)
+        name, args = self._jac_args(w, coefdiag)
+        _lib.call(name, *args, indptr, indices, data, cap, nnz)
         n = int(nnz[0])
         return sp.csr_matrix((data[:n].copy(), indices[:n].copy(), indptr), shape=(nrow, nrow))
+
+    def jacobian_device(self, w, coefdiag):
+        """The same CSR matrix in device tensors (indptr, indices, data)."""
+        import torch
+        nrow = 5 * self.im * self.jm
+        cap = nrow * 245
+        dev = torch.device("cuda", torch.cuda.current_device())
+        if getattr(self, "_jbuf", None) is None or self._jbuf[1].numel() != cap:
+            self._jbuf = (torch.empty(nrow + 1, dtype=torch.int32, device=dev),
+                          torch.empty(cap, dtype=torch.int32, device=dev),
+                          torch.empty(cap, dtype=torch.float64, device=dev))
+        indptr, indices, data = self._jbuf
+        nnz = np.zeros(1, np.int64)
+        _lib.call("bcg_set_stream", torch.cuda.current_stream(dev).cuda_stream)
+        name, args = self._jac_args(w, coefdiag)
+        _lib.call(name, *args, indptr, indices, data, cap, nnz)
+        n = int(nnz[0])
+        return indptr, indices[:n], data[:n]
 
     def step(self, w, first=False, tol=None):
         """One SER Newton iteration on w (Fortran-ordered, updated in place).
@@ -104,12 +131,25 @@ class BLNewton:
         cflm1 = r / self.dt
         gh = self.gh
         coefdiag = cflm1 * self.c["grid"]["vol"][gh:-gh, gh:-gh]
-        J = self.jacobian(w, coefdiag)
-        t2 = time.perf_counter()
-        try:
-            dw = np.reshape(self.solver(J, np.ravel(res[gh:-gh, gh:-gh, :])), (self.im, self.jm, 5))
-        except RuntimeError:  # singular factorisation: treated like a non-finite update
-            dw = np.full((self.im, self.jm, 5), np.nan)
+        rhs = np.ravel(res[gh:-gh, gh:-gh, :])
+        if getattr(self.solver, "device_csr", False):  # GPU matrix and solve (KrylovSolver)
+            import torch
+            J = self.jacobian_device(w, coefdiag)
+            t2 = time.perf_counter()
+            try:
+                x = self.solver.solve(*J, torch.from_numpy(rhs).to(J[0].device))
+                dw = np.reshape(x.cpu().numpy(), (self.im, self.jm, 5))
+            except RuntimeError:  # singular factor or no convergence: treated like a non-finite update
+                dw = np.full((self.im, self.jm, 5), np.nan)
+            nnz = int(J[2].numel())
+        else:
+            J = self.jacobian(w, coefdiag)
+            t2 = time.perf_counter()
+            try:
+                dw = np.reshape(self.solver(J, rhs), (self.im, self.jm, 5))
+            except RuntimeError:  # singular factorisation: treated like a non-finite update
+                dw = np.full((self.im, self.jm, 5), np.nan)
+            nnz = int(J.nnz)
         if np.all(np.isfinite(dw)):
             w[gh:-gh, gh:-gh, :] += dw
             self.dw_old = dw
@@ -121,7 +161,7 @@ class BLNewton:
             self.cfl /= 2.0
             self.dt /= 2.0
         t3 = time.perf_counter()
-        self.history.append(dict(norm=norm.tolist(), cflm1=float(cflm1), nnz=int(J.nnz), seconds=t3 - t0,
+        self.history.append(dict(norm=norm.tolist(), cflm1=float(cflm1), nnz=nnz, seconds=t3 - t0,
                                  seconds_residual=t1 - t0, seconds_jacobian=t2 - t1, seconds_solve=t3 - t2))
         return norm, dw
 
@@ -147,11 +187,14 @@ class CylNewton(BLNewton):
     card runs cfl 0.9 (card_cyl2d.py:57); cfl 1e10 gives Newton's iteration."""
 
     def __init__(self, case, cfl=1.0e10, mach=None, solver=None):
-        super().__init__(case, cfl=cfl, mach=mach, solver=solver or self._banded)
         g = case["grid"]
+        self.perm = folded_ring_order(int(g["im"]), int(g["jm"]))
+        if solver == "krylov":  # FP64 GMRES, FP32 band LU preconditioner in the folded order
+            from .linsolve import KrylovSolver
+            solver = KrylovSolver(perm=self.perm)
+        super().__init__(case, cfl=cfl, mach=mach, solver=solver or self._banded)
         gh = self.gh
         self.dt = self.cfl * abs(g["xc"][gh, gh] - g["xc"][gh, gh + 1]) / (1.0 / self.mach + 1.0)
-        self.perm = folded_ring_order(self.im, self.jm)
 
     def _banded(self, J, b):
         return band_lu_solve(J, b, perm=self.perm)
@@ -166,20 +209,13 @@ class CylNewton(BLNewton):
             f_bnd.jn_match_2d(w, it["prr1"], gh, gh, gh, gh, im, jm, w, it["prd2"], gh, gh, gh, gh, im, jm, it["tr"])
             f_bnd.jn_match_2d(w, it["prr2"], gh, gh, gh, gh, im, jm, w, it["prd1"], gh, gh, gh, gh, im, jm, it["tr"])
 
-    def jacobian(self, w, coefdiag):
-        import scipy.sparse as sp
+    def _jac_args(self, w, coefdiag):
         from ._f2py import interf4
         g, c = self.c["grid"], self.c
         it = c["interf"]
-        nrow = 5 * self.im * self.jm
-        cap = nrow * 245
-        indptr, indices, data = np.zeros(nrow + 1, np.int32), np.zeros(cap, np.int32), np.zeros(cap)
-        nnz = np.zeros(1, np.int64)
-        _lib.call("bcg_jacobian_dnc5_cyl_csr", w, g["nx"], g["ny"], g["vol"], g["volf"], self.gh, *self.phys,
-                  self.im, self.jm, interf4(it["Jhi"]), interf4(it["Jlo"]), c["wbd"], c["wbd"].shape[0],
-                  interf4(it["prr1"]), interf4(it["prd1"]), interf4(it["prr2"]), interf4(it["prd2"]),
-                  np.ascontiguousarray(np.asarray(it["tr"], dtype=np.int32).ravel()), np.asfortranarray(coefdiag),
-                  2e-16, 0, indptr, indices, data, cap, nnz)
-        n = int(nnz[0])
-        return sp.csr_matrix((data[:n].copy(), indices[:n].copy(), indptr), shape=(nrow, nrow))
-
+        return ("bcg_jacobian_dnc5_cyl_csr", (w, g["nx"], g["ny"], g["vol"], g["volf"], self.gh, *self.phys, self.im,
+                                              self.jm, interf4(it["Jhi"]), interf4(it["Jlo"]), c["wbd"],
+                                              c["wbd"].shape[0], interf4(it["prr1"]), interf4(it["prd1"]),
+                                              interf4(it["prr2"]), interf4(it["prd2"]),
+                                              np.ascontiguousarray(np.asarray(it["tr"], dtype=np.int32).ravel()),
+                                              np.asfortranarray(coefdiag), 2e-16, 0))
