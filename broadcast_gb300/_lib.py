@@ -31,7 +31,7 @@ SIGNATURES = {
     "bcg_flux_num_dnc5_nowall_2d_d": "pppp" + "pppppppp" + "i" + "d" * 11 + "ii",
     "bcg_impli_matrix_free_2d": "ppppppp" + "ddddd" + "ii" + "ddddd" + "iii",
     "bcg_csr_band_lu_solve": "ipppLpppip",
-    "bcg_band32_factor": "ipppppipp",
+    "bcg_band32_factor": "ippppipp",
     "bcg_band32_solve": "Lpp",
     "bcg_band32_dims": "Lp",
     "bcg_band32_destroy": "L",

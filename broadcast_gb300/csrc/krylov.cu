@@ -82,27 +82,76 @@ __global__ void k_note_info32(const int* __restrict__ info, int* __restrict__ fi
   if (threadIdx.x == 0 && blockIdx.x == 0 && *first == 0 && *info > 0) *first = j0 + *info;
 }
 
-__global__ void k_swap_vec32(float* __restrict__ b, const int* __restrict__ ipiv, int jb) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// gather index of each block's row swaps: after the swaps ipiv[0..jb) of a
+// panel, row t of its m-row window holds the former row perm[t]
+__global__ void k_block_perms(int n, int nb, int kl, const int* __restrict__ ipiv, const long long* __restrict__ off,
+                              int* __restrict__ perm) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j0 = k * nb;
+  if (j0 >= n) return;
+  const int jb = min(nb, n - j0), m = min(kl + jb, n - j0);
+  int* p = perm + off[k];
+  for (int t = 0; t < m; ++t) p[t] = t;
   for (int t = 0; t < jb; ++t) {
-    const int p = ipiv[t] - 1;
-    if (p != t) { const float x = b[t]; b[t] = b[p]; b[p] = x; }
+    const int q = ipiv[j0 + t] - 1;
+    if (q != t) { const int x = p[t]; p[t] = p[q]; p[q] = x; }
   }
 }
 
-// xf[q[k]] = s[k] v[k] in FP32 (q null: the identity)
-__global__ void k_scale_in(int n, const int* __restrict__ q, const double* __restrict__ s, const double* __restrict__ v,
-                           float* __restrict__ xf) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  xf[q ? q[k] : k] = (float)(s[k] * v[k]);
+// identity matrices of size jb x jb (ld nb) for every block
+__global__ void k_identity_blocks(int n, int nb, float* __restrict__ a) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)n * nb) return;
+  const int k = (int)(e / ((long long)nb * nb));
+  const long long r = e - (long long)k * nb * nb;
+  const int i = (int)(r % nb), j = (int)(r / nb);
+  a[e] = (i == j && k * nb + i < n) ? 1.0f : 0.0f;
 }
 
-// z[k] = xf[q[k]]
-__global__ void k_permute_out(int n, const int* __restrict__ q, const float* __restrict__ xf, double* __restrict__ z) {
+// pointers of one apply (read by the captured graph's first and last kernels)
+struct ApplyArgs { const double* v; double* z; };
+
+__global__ void k_scale_in_args(int n, const int* __restrict__ q, const double* __restrict__ s,
+                                const ApplyArgs* __restrict__ args, float* __restrict__ xf) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  z[k] = (double)xf[q ? q[k] : k];
+  xf[q ? q[k] : k] = (float)(s[k] * args->v[k]);
+}
+
+__global__ void k_permute_out_args(int n, const int* __restrict__ q, const float* __restrict__ xf,
+                                   const ApplyArgs* __restrict__ args) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  args->z[k] = (double)xf[q ? q[k] : k];
+}
+
+// forward step of block k (one CTA): the panel's row swaps on the m-row window
+// of w (through shared memory), and y_k = L_kk^-1 (swapped w_k)
+__global__ void __launch_bounds__(256) k_fwd_diag(float* __restrict__ w, float* __restrict__ y,
+                                                  const int* __restrict__ perm, int m, int jb,
+                                                  const float* __restrict__ linv, int ld) {
+  extern __shared__ float seg[];
+  for (int t = threadIdx.x; t < m; t += blockDim.x) seg[t] = w[t];
+  __syncthreads();
+  for (int t = threadIdx.x + jb; t < m; t += blockDim.x) w[t] = seg[perm[t]];
+  for (int i = threadIdx.x; i < jb; i += blockDim.x) {
+    float acc = 0.0f;
+    for (int j = 0; j < jb; ++j) acc = fmaf(linv[i + (long long)j * ld], seg[perm[j]], acc);
+    y[i] = acc;
+  }
+}
+
+// backward step of block k (one CTA): z_k = U_kk^-1 y_k
+__global__ void __launch_bounds__(256) k_bwd_diag(const float* __restrict__ y, float* __restrict__ z, int jb,
+                                                  const float* __restrict__ uinv, int ld) {
+  __shared__ float yk[1024];
+  for (int t = threadIdx.x; t < jb; t += blockDim.x) yk[t] = y[t];
+  __syncthreads();
+  for (int i = threadIdx.x; i < jb; i += blockDim.x) {
+    float acc = 0.0f;
+    for (int j = 0; j < jb; ++j) acc = fmaf(uinv[i + (long long)j * ld], yk[j], acc);
+    z[i] = acc;
+  }
 }
 
 // y = A x (or y = b - A x with b given), FP64 CSR, one warp per row
@@ -120,13 +169,22 @@ __global__ void __launch_bounds__(256) k_spmv(int n, const int* __restrict__ ind
 }
 
 struct Band32 {
-  int n = 0, kl = 0, ku = 0, nb = 0;
+  int n = 0, kl = 0, ku = 0, nb = 0, nblk = 0;
   long long ldab = 0, ldd = 0;
   float* ab = nullptr;
   int* ipiv = nullptr;
   int* q = nullptr;
   double* rs = nullptr;
-  float* xf = nullptr;
+  float* xf = nullptr;        // forward working vector (swapped and updated right-hand side)
+  float* yf = nullptr;        // forward result, then the backward right-hand side
+  float* zf = nullptr;        // backward result
+  float* linv = nullptr;      // per block: L_kk^-1 (nb x nb, unit lower)
+  float* uinv = nullptr;      // per block: U_kk^-1 (nb x nb, upper)
+  int* perms = nullptr;       // per block: gather index of its row swaps (m_k entries)
+  std::vector<long long> poff;  // per block: offset of its gather index
+  ApplyArgs* args = nullptr;  // device copy of the current apply's pointers
+  cudaStream_t gs = nullptr;  // capture stream
+  cudaGraphExec_t graph = nullptr;
   int dev = 0;
 };
 
@@ -153,12 +211,18 @@ int handles_for(int dev, KHandles** out) {
 
 void free_band(Band32* f) {
   if (!f) return;
+  if (f->graph) cudaGraphExecDestroy(f->graph);
+  if (f->gs) cudaStreamDestroy(f->gs);
   cudaFree(f->ab); cudaFree(f->ipiv); cudaFree(f->q); cudaFree(f->rs); cudaFree(f->xf);
+  cudaFree(f->yf); cudaFree(f->zf); cudaFree(f->linv); cudaFree(f->uinv); cudaFree(f->perms); cudaFree(f->args);
   delete f;
 }
 
-// M^-1 v into z (device FP64 vectors) on stream st
-int band32_apply(const Band32* f, KHandles* h, const double* v, double* z, cudaStream_t st) {
+// the launches of one apply of M^-1 (pointers from f->args) on stream st:
+// scale and permute in, per block forward (swaps + L_kk^-1 on one CTA, the
+// L21 product by cuBLAS), per block backward (U12 product by cuBLAS, U_kk^-1
+// on one CTA), permute out
+int band32_launch(const Band32* f, KHandles* h, cudaStream_t st) {
   const int n = f->n, nb = f->nb, kl = f->kl, ku = f->ku;
   const long long ldd = f->ldd;
   const int U = kl + ku + nb;
@@ -168,30 +232,51 @@ int band32_apply(const Band32* f, KHandles* h, const double* v, double* z, cudaS
   cublasSetStream(h->blas, st);
   cublasSetPointerMode(h->blas, CUBLAS_POINTER_MODE_HOST);
   const int B = 256;
-  k_scale_in<<<(n + B - 1) / B, B, 0, st>>>(n, f->q, f->rs, v, f->xf);
-  float* xf = f->xf;
-  for (int j0 = 0; j0 < n; j0 += nb) {
-    const int jb = std::min(nb, n - j0);
-    const int m = std::min(kl + jb, n - j0);
-    k_swap_vec32<<<1, 1, 0, st>>>(xf + j0, f->ipiv + j0, jb);
-    if (cublasStrsv(h->blas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_UNIT, jb, D(j0, j0), (int)ldd, xf + j0, 1) !=
-        CUBLAS_STATUS_SUCCESS) return fail_arg("band32: trsv failed");
-    if (m > jb && cublasSgemv(h->blas, CUBLAS_OP_N, m - jb, jb, &mone, D(j0 + jb, j0), (int)ldd, xf + j0, 1, &one,
-                              xf + j0 + jb, 1) != CUBLAS_STATUS_SUCCESS) return fail_arg("band32: gemv failed");
+  k_scale_in_args<<<(n + B - 1) / B, B, 0, st>>>(n, f->q, f->rs, f->args, f->xf);
+  for (int k = 0; k < f->nblk; ++k) {
+    const int j0 = k * nb, jb = std::min(nb, n - j0), m = std::min(kl + jb, n - j0);
+    k_fwd_diag<<<1, 256, (size_t)m * sizeof(float), st>>>(f->xf + j0, f->yf + j0, f->perms + f->poff[k], m, jb,
+                                                          f->linv + (size_t)k * nb * nb, nb);
+    if (m > jb && cublasSgemv(h->blas, CUBLAS_OP_N, m - jb, jb, &mone, D(j0 + jb, j0), (int)ldd, f->yf + j0, 1, &one,
+                              f->xf + j0 + jb, 1) != CUBLAS_STATUS_SUCCESS) return fail_arg("band32: gemv failed");
   }
-  const int nblk = (n + nb - 1) / nb;
-  for (int k = nblk - 1; k >= 0; --k) {
-    const int j0 = k * nb;
-    const int jb = std::min(nb, n - j0);
-    const int ncol = std::min(n - j0 - jb, kl + ku);
-    if (ncol > 0 && cublasSgemv(h->blas, CUBLAS_OP_N, jb, ncol, &mone, D(j0, j0 + jb), (int)ldd, xf + j0 + jb, 1, &one,
-                                xf + j0, 1) != CUBLAS_STATUS_SUCCESS) return fail_arg("band32: gemv failed");
-    if (cublasStrsv(h->blas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, jb, D(j0, j0), (int)ldd, xf + j0,
-                    1) != CUBLAS_STATUS_SUCCESS) return fail_arg("band32: trsv failed");
+  for (int k = f->nblk - 1; k >= 0; --k) {
+    const int j0 = k * nb, jb = std::min(nb, n - j0), ncol = std::min(n - j0 - jb, kl + ku);
+    if (ncol > 0 && cublasSgemv(h->blas, CUBLAS_OP_N, jb, ncol, &mone, D(j0, j0 + jb), (int)ldd, f->zf + j0 + jb, 1,
+                                &one, f->yf + j0, 1) != CUBLAS_STATUS_SUCCESS) return fail_arg("band32: gemv failed");
+    k_bwd_diag<<<1, 256, 0, st>>>(f->yf + j0, f->zf + j0, jb, f->uinv + (size_t)k * nb * nb, nb);
   }
-  k_permute_out<<<(n + B - 1) / B, B, 0, st>>>(n, f->q, xf, z);
+  k_permute_out_args<<<(n + B - 1) / B, B, 0, st>>>(n, f->q, f->zf, f->args);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? BCG_OK : fail_cuda("band32 apply", e);
+}
+
+// M^-1 v into z (device FP64 vectors) on stream st: the launches replayed from
+// a CUDA graph captured on the factor's first apply (or queued directly when
+// capture is not possible)
+int band32_apply(Band32* f, KHandles* h, const double* v, double* z, cudaStream_t st) {
+  const ApplyArgs a{v, z};
+  cudaError_t e = cudaMemcpyAsync(f->args, &a, sizeof(a), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return fail_cuda("band32 apply: arguments", e);
+  if (!f->graph && !f->gs) {
+    if (cudaStreamCreateWithFlags(&f->gs, cudaStreamNonBlocking) == cudaSuccess) {
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(f->gs, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        const int rc = band32_launch(f, h, f->gs);
+        const cudaError_t ec = cudaStreamEndCapture(f->gs, &g);
+        if (rc == BCG_OK && ec == cudaSuccess && g && cudaGraphInstantiate(&f->graph, g, 0) != cudaSuccess)
+          f->graph = nullptr;
+        if (g) cudaGraphDestroy(g);
+      }
+      cudaGetLastError();  // a failed capture falls back to direct launches
+    }
+    cublasSetStream(h->blas, st);  // the handle is shared with the caller's stream work
+  }
+  if (f->graph) {
+    e = cudaGraphLaunch(f->graph, st);
+    return e == cudaSuccess ? BCG_OK : fail_cuda("band32 apply: graph launch", e);
+  }
+  return band32_launch(f, h, st);
 }
 
 Band32* factor_of(long long hnd) {
@@ -234,9 +319,17 @@ int band32_factor(int n, const int* indptr, const int* indices, const double* da
     if (cudaMemcpyAsync(klku, d_klku, 2 * sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess) { bad(fail_cuda("band32: bandwidth", cudaGetLastError())); break; }
     const int kl = klku[0], ku = klku[1];
-    nb = std::max(1, std::min(nb, n));
+    nb = std::max(1, std::min(std::min(nb, 1024), n));
     const int L = kl + nb, U = kl + ku + nb;
     f->kl = kl; f->ku = ku; f->nb = nb;
+    // the forward solve holds a panel's window (kl + nb rows) in shared memory
+    const size_t seg = (size_t)(kl + nb) * sizeof(float);
+    if (seg > 227 * 1024) { bad(fail_arg("band32: lower bandwidth too large (kl + nb > 58112)")); break; }
+    if (seg > 48 * 1024 &&
+        cudaFuncSetAttribute(k_fwd_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)seg) != cudaSuccess) {
+      bad(fail_cuda("band32: shared memory", cudaGetLastError()));
+      break;
+    }
     f->ldab = (long long)L + U + 1;
     f->ldd = f->ldab - 1;
     const size_t bytes = (size_t)f->ldab * (size_t)n * sizeof(float);
@@ -303,6 +396,43 @@ int band32_factor(int n, const int* indptr, const int* indices, const double* da
         cudaStreamSynchronize(st) != cudaSuccess) { bad(fail_cuda("band32: factorisation", cudaGetLastError())); break; }
     if (info) *info = first;
     if (first) { bad(fail_arg("band32: singular matrix (zero pivot)")); rc = BCG_ERR_SINGULAR; break; }
+    // for the solves: each block's swaps as a gather index, the inverses of
+    // the diagonal blocks of L and U, work vectors
+    f->nblk = (n + nb - 1) / nb;
+    f->poff.assign(f->nblk + 1, 0);
+    for (int k = 0; k < f->nblk; ++k) {
+      const int j0 = k * nb, jb = std::min(nb, n - j0);
+      f->poff[k + 1] = f->poff[k] + std::min(kl + jb, n - j0);
+    }
+    const size_t inv = (size_t)f->nblk * nb * nb;
+    long long* d_off = nullptr;
+    if (cudaMalloc(&f->perms, (size_t)f->poff.back() * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&d_off, (size_t)(f->nblk + 1) * sizeof(long long)) != cudaSuccess ||
+        cudaMalloc(&f->linv, inv * sizeof(float)) != cudaSuccess || cudaMalloc(&f->uinv, inv * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&f->yf, (size_t)n * sizeof(float)) != cudaSuccess || cudaMalloc(&f->zf, (size_t)n * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&f->args, sizeof(ApplyArgs)) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(d_off);
+      bad(fail_arg("band32: allocation of the solve data failed"));
+      break;
+    }
+    cudaMemcpyAsync(d_off, f->poff.data(), (size_t)(f->nblk + 1) * sizeof(long long), cudaMemcpyHostToDevice, st);
+    k_block_perms<<<(f->nblk + 127) / 128, 128, 0, st>>>(n, nb, kl, f->ipiv, d_off, f->perms);
+    const long long nall = (long long)f->nblk * nb * nb;
+    k_identity_blocks<<<(unsigned)((nall + 255) / 256), 256, 0, st>>>(f->nblk * nb, nb, f->linv);
+    k_identity_blocks<<<(unsigned)((nall + 255) / 256), 256, 0, st>>>(f->nblk * nb, nb, f->uinv);
+    for (int k = 0; k < f->nblk && rc == BCG_OK; ++k) {
+      const int j0 = k * nb, jb = std::min(nb, n - j0);
+      float* li = f->linv + (size_t)k * nb * nb;
+      float* ui = f->uinv + (size_t)k * nb * nb;
+      if (cublasStrsm(h->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_UNIT, jb, jb, &one,
+                      D(j0, j0), (int)ldd, li, nb) != CUBLAS_STATUS_SUCCESS ||
+          cublasStrsm(h->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, jb, jb, &one,
+                      D(j0, j0), (int)ldd, ui, nb) != CUBLAS_STATUS_SUCCESS) bad(fail_arg("band32: block inverse failed"));
+    }
+    cudaStreamSynchronize(st);
+    cudaFree(d_off);
+    if (rc) break;
   } while (false);
   cudaStreamSynchronize(st);
   if (ev_a) cudaEventDestroy(ev_a);

@@ -14,6 +14,8 @@ remove_zero_jac with |a| > 2e-16 (BROADCAST_npz.py:129-135), Jac/vol
   by seed and keeps, per row, the counts of the structural and of the filtered
   pattern (= the whole indptr of both), and every entry of three bands of rows
   (inlet, middle, outflow); and J v against the oracle's JVP for random v.
+  Filter decisions on cancellation residues near 2e-16 may differ between the
+  two computations; they are bounded and counted.
 Entries near the filter threshold (where a rounding difference could flip the
 pattern) are counted and reported."""
 import numpy as np
@@ -124,6 +126,15 @@ def test_relaxed_jacobian_400x150_whole_csr():
 
 
 def test_stability_jacobian_1024x512_indptr_bands_and_products():
+    """J/vol of the 1024x512 boundary layer.  The structural pattern (every
+    valid slot, before the |a| > 2e-16 filter) must be exact in every row, and
+    on three bands of rows (inlet, middle, outflow) every entry's value within
+    1e-11 of the largest.  After the filter, the row counts may differ only
+    through entries that are cancellation residues -- exact zeros of the
+    derivative rounded to ~1e-16 by each computation's own operation order,
+    which the threshold 2e-16 (BROADCAST_npz.py:129-135) cuts through: each
+    such flip is checked to be below 1e-13 of its row's largest entry in both
+    computations, and the flips are counted."""
     import torch
     im, jm = 1024, 512
     c = H.bl_case(im, jm, seed=3)
@@ -133,40 +144,82 @@ def test_stability_jacobian_1024x512_indptr_bands_and_products():
     bad = nrow - 1
     bands = [(1, 8), (509, 516), (1017, 1024)]
     band_rows = [(5 * jm * (i0 - 1), 5 * jm * i1) for i0, i1 in bands]
+    # the library: J/vol after the filter, and every valid slot (raw J) before it
+    indptr, indices, data, nnz = _gpu_csr(c, None, MINI, True, nrow * 245)
+    got_ptr = indptr.cpu().numpy().astype(np.int64)
+    sptr_d, sidx_d, sdat_d, snnz = _gpu_csr(c, None, -1.0, False, nrow * 245)
+    sptr = sptr_d.cpu().numpy().astype(np.int64)
     struct = np.zeros(nrow, np.int64)
     post = np.zeros(nrow, np.int64)
+    csum = np.zeros(nrow)   # per row: sum of the kept columns and of their squares
+    csq = np.zeros(nrow)
     picks = [([], [], []) for _ in bands]
-    near = []
+    near = [0]
 
     def visit(ia, ja, jac):
         valid = _valid(ia, ja, jac, bad)
         struct[:] += np.bincount(ia[valid], minlength=nrow)
         keep = valid & (np.abs(jac) > MINI)
         post[:] += np.bincount(ia[keep], minlength=nrow)
-        nb = valid & (np.abs(jac) > MINI / 4) & (np.abs(jac) < MINI * 4)
-        near.extend(zip(ia[nb].tolist(), ja[nb].tolist(), jac[nb].tolist()))
+        colk = ja[keep].astype(np.float64)
+        csum[:] += np.bincount(ia[keep], weights=colk, minlength=nrow)
+        csq[:] += np.bincount(ia[keep], weights=colk * colk, minlength=nrow)
+        near[0] += int((valid & (np.abs(jac) > MINI / 4) & (np.abs(jac) < MINI * 4)).sum())
         for (r0, r1), (pr, pc, pv) in zip(band_rows, picks):
-            sel = keep & (ia >= r0) & (ia < r1)
-            pr.append(ia[sel]); pc.append(ja[sel]); pv.append(jac[sel] / _row_volume(c, ia[sel]))
+            sel = valid & (ia >= r0) & (ia < r1)
+            pr.append(ia[sel]); pc.append(ja[sel]); pv.append(jac[sel])
 
     _seed_sweep(c, O.JAC_PLAIN, None, visit)
-    indptr, indices, data, nnz = _gpu_csr(c, None, MINI, True, nrow * 245)
-    got_ptr = indptr.cpu().numpy().astype(np.int64)
-    assert np.array_equal(np.diff(got_ptr), post), "filtered pattern: row counts differ"
-    # every entry of the three bands
-    scale = 0.0
-    errs = []
+    # structural pattern: exact in every row
+    assert snnz == int(struct.sum())
+    assert np.array_equal(np.diff(sptr), struct)
+    # every entry of the three bands, before the filter
+    scale, errs = 0.0, []
     for (r0, r1), (pr, pc, pv) in zip(band_rows, picks):
         ref = sp.csr_matrix((np.concatenate(pv), (np.concatenate(pr) - r0, np.concatenate(pc))), shape=(r1 - r0, nrow))
         ref.sum_duplicates()
         ref.sort_indices()
-        a, b = int(got_ptr[r0]), int(got_ptr[r1])
-        assert np.array_equal(got_ptr[r0:r1 + 1] - a, ref.indptr)
-        assert np.array_equal(indices[a:b].cpu().numpy(), ref.indices)
+        a, b = int(sptr[r0]), int(sptr[r1])
+        assert np.array_equal(sptr[r0:r1 + 1] - a, ref.indptr)
+        assert np.array_equal(sidx_d[a:b].cpu().numpy(), ref.indices)
         scale = max(scale, np.abs(ref.data).max())
-        errs.append(np.abs(data[a:b].cpu().numpy() - ref.data).max())
+        errs.append(np.abs(sdat_d[a:b].cpu().numpy() - ref.data).max())
     band_err = max(errs) / scale
     assert band_err <= 1e-11, band_err
+    # the filtered pattern: rows whose kept columns differ (count, sum, sum of
+    # squares) hold only residue flips
+    rid = torch.repeat_interleave(torch.arange(nrow, device=indptr.device), torch.diff(indptr.long()))
+    colf = indices[:nnz].double()
+    gsum = torch.zeros(nrow, dtype=torch.float64, device=indptr.device).index_add_(0, rid, colf).cpu().numpy()
+    gsq = torch.zeros(nrow, dtype=torch.float64, device=indptr.device).index_add_(0, rid, colf * colf).cpu().numpy()
+    del rid, colf
+    rows = np.nonzero((np.diff(got_ptr) != post) | (gsum != csum) | (gsq != csq))[0]
+    flips = []
+    if rows.size:
+        assert rows.size < 1e-4 * nrow, rows.size
+        want = {int(r): {} for r in rows}
+        rset = np.asarray(sorted(want))
+
+        def collect(ia, ja, jac):
+            sel = np.isin(ia, rset) & _valid(ia, ja, jac, bad)
+            for r, col, v in zip(ia[sel].tolist(), ja[sel].tolist(), jac[sel].tolist()):
+                want[r][col] = v
+
+        _seed_sweep(c, O.JAC_PLAIN, None, collect)
+        for r, ora in want.items():
+            a, b = int(sptr[r]), int(sptr[r + 1])
+            mine = dict(zip(sidx_d[a:b].cpu().numpy().tolist(), sdat_d[a:b].cpu().numpy().tolist()))
+            assert set(mine) == set(ora)
+            rowmax = max(abs(v) for v in ora.values())
+            kept_lib = set(indices[int(got_ptr[r]):int(got_ptr[r + 1])].cpu().numpy().tolist())
+            assert kept_lib == {col for col, v in mine.items() if abs(v) > MINI}
+            for col, v in ora.items():
+                if (abs(v) > MINI) != (abs(mine[col]) > MINI):
+                    assert max(abs(v), abs(mine[col])) <= 1e-13 * rowmax, (r, col, v, mine[col], rowmax)
+                    flips.append((r, col, v, mine[col]))
+        assert len(flips) >= 1
+    del sidx_d, sdat_d
+    torch.cuda.empty_cache()
     # J v against the oracle's tangent (the same linearised boundary chain)
     J = sp.csr_matrix((data[:nnz].cpu().numpy(), indices[:nnz].cpu().numpy(), got_ptr), shape=(nrow, nrow))
     rng = np.random.default_rng(12)
@@ -176,14 +229,9 @@ def test_stability_jacobian_1024x512_indptr_bands_and_products():
         wd[3:-3, 3:-3] = v
         H.oracle_bcs(c, c["w"].copy(order="F"), wd)
         _, rd = O.jvp(g, ph, c["w"], wd, openmp=True)
-        want = (-H.interior(rd) / H.interior(g["vol"])[:, :, None]).reshape(-1)  # (i, j, e) C order = row order
-        got = J @ v.reshape(-1)
-        err = np.abs(got - want).max() / np.abs(want).max()
+        want_v = (-H.interior(rd) / H.interior(g["vol"])[:, :, None]).reshape(-1)  # (i, j, e) C order = row order
+        err = np.abs(J @ v.reshape(-1) - want_v).max() / np.abs(want_v).max()
         assert err <= 1e-11, err
-    del J
-    torch.cuda.empty_cache()
-    sptr, _, _, snnz = _gpu_csr(c, None, -1.0, True, nrow * 245)
-    assert snnz == int(struct.sum())
-    assert np.array_equal(np.diff(sptr.cpu().numpy()), struct)
-    print("1024x512 J/vol: nnz %d (structural %d), band max rel err %.2e, J v max rel err %.2e, "
-          "entries within 4x of 2e-16: %d %s" % (nnz, snnz, band_err, err, len(near), near[:10]))
+    print("1024x512 J/vol: nnz %d (structural %d), band max rel err %.2e, J v max rel err %.2e, entries within 4x of "
+          "2e-16: %d, filter flips (residues < 1e-13 of the row): %d %s"
+          % (nnz, snnz, band_err, err, near[0], len(flips), flips[:6]))

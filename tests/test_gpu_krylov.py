@@ -71,7 +71,10 @@ def test_cylinder_newton_matrix_and_factor_reuse():
     dims = np.zeros(3, np.int32)
     from broadcast_gb300 import _lib
     _lib.call("bcg_band32_dims", ks.handle, dims)
-    assert dims[0] <= 15 * 28 + 35 and dims[1] <= 15 * 28 + 35   # the folded order's band
+    coo = J.tocoo()
+    pr, pc = nt.perm[coo.row], nt.perm[coo.col]
+    assert (dims[0], dims[1]) == (int((pr - pc).max()), int((pc - pr).max()))   # the folded order's band
+    assert dims[0] + dims[1] < 5 * 28 * 21 // 4
 
 
 def test_newton_with_krylov_converges_as_direct():
