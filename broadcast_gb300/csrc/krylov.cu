@@ -125,33 +125,13 @@ __global__ void k_permute_out_args(int n, const int* __restrict__ q, const float
   args->z[k] = (double)xf[q ? q[k] : k];
 }
 
-// forward step of block k (one CTA): the panel's row swaps on the m-row window
-// of w (through shared memory), and y_k = L_kk^-1 (swapped w_k)
-__global__ void __launch_bounds__(256) k_fwd_diag(float* __restrict__ w, float* __restrict__ y,
-                                                  const int* __restrict__ perm, int m, int jb,
-                                                  const float* __restrict__ linv, int ld) {
+// a panel's row swaps on its m-row window of w, as one gather through shared
+// memory (one CTA)
+__global__ void __launch_bounds__(1024) k_gather_window(float* __restrict__ w, const int* __restrict__ perm, int m) {
   extern __shared__ float seg[];
   for (int t = threadIdx.x; t < m; t += blockDim.x) seg[t] = w[t];
   __syncthreads();
-  for (int t = threadIdx.x + jb; t < m; t += blockDim.x) w[t] = seg[perm[t]];
-  for (int i = threadIdx.x; i < jb; i += blockDim.x) {
-    float acc = 0.0f;
-    for (int j = 0; j < jb; ++j) acc = fmaf(linv[i + (long long)j * ld], seg[perm[j]], acc);
-    y[i] = acc;
-  }
-}
-
-// backward step of block k (one CTA): z_k = U_kk^-1 y_k
-__global__ void __launch_bounds__(256) k_bwd_diag(const float* __restrict__ y, float* __restrict__ z, int jb,
-                                                  const float* __restrict__ uinv, int ld) {
-  __shared__ float yk[1024];
-  for (int t = threadIdx.x; t < jb; t += blockDim.x) yk[t] = y[t];
-  __syncthreads();
-  for (int i = threadIdx.x; i < jb; i += blockDim.x) {
-    float acc = 0.0f;
-    for (int j = 0; j < jb; ++j) acc = fmaf(uinv[i + (long long)j * ld], yk[j], acc);
-    z[i] = acc;
-  }
+  for (int t = threadIdx.x; t < m; t += blockDim.x) w[t] = seg[perm[t]];
 }
 
 // y = A x (or y = b - A x with b given), FP64 CSR, one warp per row
@@ -219,24 +199,25 @@ void free_band(Band32* f) {
 }
 
 // the launches of one apply of M^-1 (pointers from f->args) on stream st:
-// scale and permute in, per block forward (swaps + L_kk^-1 on one CTA, the
-// L21 product by cuBLAS), per block backward (U12 product by cuBLAS, U_kk^-1
-// on one CTA), permute out
+// scale and permute in; per block forward: the panel's swaps (one CTA), then
+// L_kk^-1 and L21 products (cuBLAS gemv); per block backward: U12 and U_kk^-1
+// products; permute out
 int band32_launch(const Band32* f, KHandles* h, cudaStream_t st) {
   const int n = f->n, nb = f->nb, kl = f->kl, ku = f->ku;
   const long long ldd = f->ldd;
   const int U = kl + ku + nb;
   float* dv = f->ab + U;
   auto D = [&](long long i, long long j) { return dv + i + j * ldd; };
-  const float one = 1.0f, mone = -1.0f;
+  const float one = 1.0f, zero = 0.0f, mone = -1.0f;
   cublasSetStream(h->blas, st);
   cublasSetPointerMode(h->blas, CUBLAS_POINTER_MODE_HOST);
   const int B = 256;
   k_scale_in_args<<<(n + B - 1) / B, B, 0, st>>>(n, f->q, f->rs, f->args, f->xf);
   for (int k = 0; k < f->nblk; ++k) {
     const int j0 = k * nb, jb = std::min(nb, n - j0), m = std::min(kl + jb, n - j0);
-    k_fwd_diag<<<1, 256, (size_t)m * sizeof(float), st>>>(f->xf + j0, f->yf + j0, f->perms + f->poff[k], m, jb,
-                                                          f->linv + (size_t)k * nb * nb, nb);
+    k_gather_window<<<1, 1024, (size_t)m * sizeof(float), st>>>(f->xf + j0, f->perms + f->poff[k], m);
+    if (cublasSgemv(h->blas, CUBLAS_OP_N, jb, jb, &one, f->linv + (size_t)k * nb * nb, nb, f->xf + j0, 1, &zero,
+                    f->yf + j0, 1) != CUBLAS_STATUS_SUCCESS) return fail_arg("band32: gemv failed");
     if (m > jb && cublasSgemv(h->blas, CUBLAS_OP_N, m - jb, jb, &mone, D(j0 + jb, j0), (int)ldd, f->yf + j0, 1, &one,
                               f->xf + j0 + jb, 1) != CUBLAS_STATUS_SUCCESS) return fail_arg("band32: gemv failed");
   }
@@ -244,7 +225,8 @@ int band32_launch(const Band32* f, KHandles* h, cudaStream_t st) {
     const int j0 = k * nb, jb = std::min(nb, n - j0), ncol = std::min(n - j0 - jb, kl + ku);
     if (ncol > 0 && cublasSgemv(h->blas, CUBLAS_OP_N, jb, ncol, &mone, D(j0, j0 + jb), (int)ldd, f->zf + j0 + jb, 1,
                                 &one, f->yf + j0, 1) != CUBLAS_STATUS_SUCCESS) return fail_arg("band32: gemv failed");
-    k_bwd_diag<<<1, 256, 0, st>>>(f->yf + j0, f->zf + j0, jb, f->uinv + (size_t)k * nb * nb, nb);
+    if (cublasSgemv(h->blas, CUBLAS_OP_N, jb, jb, &one, f->uinv + (size_t)k * nb * nb, nb, f->yf + j0, 1, &zero,
+                    f->zf + j0, 1) != CUBLAS_STATUS_SUCCESS) return fail_arg("band32: gemv failed");
   }
   k_permute_out_args<<<(n + B - 1) / B, B, 0, st>>>(n, f->q, f->zf, f->args);
   const cudaError_t e = cudaGetLastError();
@@ -326,7 +308,7 @@ int band32_factor(int n, const int* indptr, const int* indices, const double* da
     const size_t seg = (size_t)(kl + nb) * sizeof(float);
     if (seg > 227 * 1024) { bad(fail_arg("band32: lower bandwidth too large (kl + nb > 58112)")); break; }
     if (seg > 48 * 1024 &&
-        cudaFuncSetAttribute(k_fwd_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)seg) != cudaSuccess) {
+        cudaFuncSetAttribute(k_gather_window, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)seg) != cudaSuccess) {
       bad(fail_cuda("band32: shared memory", cudaGetLastError()));
       break;
     }

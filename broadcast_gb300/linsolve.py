@@ -69,7 +69,7 @@ class KrylovSolver:
 
     device_csr = True
 
-    def __init__(self, perm=None, nb=256, restart=60, maxit=240, rtol=1e-10, refactor_after=40):
+    def __init__(self, perm=None, nb=1024, restart=60, maxit=240, rtol=1e-10, refactor_after=40):
         _lib.load()
         self.perm = None if perm is None else np.ascontiguousarray(perm, dtype=np.int32)
         self.nb, self.restart, self.maxit, self.rtol = int(nb), int(restart), int(maxit), float(rtol)
