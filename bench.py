@@ -1020,11 +1020,11 @@ def run_newton_workload(args):
     if args.case == "cyl":  # cylinder.py:841-1068 on the 256 x 256 O-mesh, Newton (cfl 1e10)
         im, jm = args.im or 256, args.jm or 256
         c = cases.cyl_case(im, jm, ops=LibOps)
-        nt = CylNewton(c, solver=None if args.solver == "band" else "krylov")
+        nt = CylNewton(c, solver="krylov" if args.solver == "krylov" else None)
     else:
         im, jm = args.im or 400, args.jm or 150
         c = cases.bl_case(im, jm, seed=0, ops=LibOps)
-        nt = BLNewton(c) if args.solver == "band" else BLNewton(c, solver="krylov")
+        nt = BLNewton(c, solver="krylov") if args.solver == "krylov" else BLNewton(c)
     w = c["w"].copy(order="F")
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -1056,7 +1056,7 @@ def run_newton_workload(args):
             "seconds_per_iteration": {"total": mean("seconds"), "fills_residual_norms": mean("seconds_residual"),
                                       "jacobian_245_seeds": mean("seconds_jacobian"),
                                       "linear_solve": mean("seconds_solve")},
-            "linear_solver": ("FP64 band LU (cuSOLVER getrf panels, cuBLAS trsm/gemm)" if args.solver == "band" else
+            "linear_solver": ("FP64 band LU (cuSOLVER getrf panels, cuBLAS trsm/gemm)" if args.solver != "krylov" else
                               "FP64 GMRES, FP32 band LU preconditioner reused across iterations"),
             "krylov": getattr(nt.solver, "log", None),
             "jacobian_nnz": hist[-1]["nnz"],
@@ -1081,14 +1081,18 @@ def run_warmstart_workload(args):
     value = mean time from the learned guess, beside the plain mean."""
     import torch
     from broadcast_gb300 import warmstart as WS
-    im, jm = args.im or 56, args.jm or 42
-    ratio = 1.05 ** 0.5
+    im, jm = args.im or 512, args.jm or 256
+    ratio = WS.radial_ratio(jm)
+    solver = None
+    if args.solver == "krylov" or (args.solver == "auto" and im * jm > 20000):
+        from broadcast_gb300.linsolve import KrylovSolver, folded_ring_order
+        solver = KrylovSolver(perm=folded_ring_order(im, jm))
     logs = []
     log = lambda msg: (logs.append(msg), print(msg, file=sys.stderr, flush=True))
     train = WS.sample_parameters(args.ntrain, seed=5)
     held = WS.sample_parameters(args.nheld, seed=6)
     t0 = time.perf_counter()
-    states, recs = WS.solve_baseflows(train, im, jm, ratio=ratio, log=log)
+    states, recs = WS.solve_baseflows(train, im, jm, ratio=ratio, log=log, solver=solver)
     t_data = time.perf_counter() - t0
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -1102,7 +1106,7 @@ def run_warmstart_workload(args):
     fit_ms = ev0.elapsed_time(ev1)
     d = WS.DIMS
     flops_step = 3 * 2 * args.batch * sum(d[i] * d[i + 1] for i in range(4))  # forward, data and weight gradients
-    out = WS.compare_starts(model, train, states, held, im, jm, ratio=ratio, log=log)
+    out = WS.compare_starts(model, train, states, held, im, jm, ratio=ratio, log=log, solver=solver)
     conv = [r for r in out if r["plain"]["converged"] and r["learned"]["converged"]]
     mean = lambda arm, k: float(np.mean([r[arm][k] for r in conv])) if conv else None
     line = {"workload": "warmstart",
@@ -1132,7 +1136,15 @@ def run_warmstart_workload(args):
                           for r in out],
             "config": {"workload": "cylinder O-mesh %dx%d (r 0.5..50 D, radial ratio %.4f), Re U(40, 200), Mach "
                                    "U(0.05, 0.3); %d training points (seed 5), %d held out (seed 6); Newton cfl 1e10, "
-                                   "GPU Jacobian and band LU" % (im, jm, ratio, len(train), len(held))},
+                                   "GPU Jacobian, %s; the first base flow by grid sequencing %s" % (
+                                       im, jm, ratio, len(train), len(held),
+                                       "FP64 GMRES with a reused FP32 band LU preconditioner" if solver is not None
+                                       else "FP64 band LU", " -> ".join("%dx%d" % lv for lv in WS.sequence_levels(im, jm)))},
+            "linear_solves": None if solver is None else {
+                "count": len(solver.log), "factorisations": int(sum(k["refactored"] for k in solver.log)),
+                "gmres_iterations_mean": float(np.mean([k["iterations"] for k in solver.log])),
+                "seconds_factor_total": float(sum(k["seconds_factor"] for k in solver.log)),
+                "seconds_gmres_total": float(sum(k["seconds_gmres"] for k in solver.log))},
             "cpu_baseline": {"value": None, "unit": "s", "kind": "port", "cores": 0,
                              "sample": "none: both arms run the same GPU Newton iteration and differ only in "
                                        "the initial state; the comparison is learned vs plain start"}}
@@ -1158,8 +1170,9 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="default line without the cylinder extra key")
     ap.add_argument("--lmax", type=int, default=10, help="impli workload: Gauss-Seidel sweeps per call")
     ap.add_argument("--case", default="bl", choices=["bl", "cyl"], help="newton workload: boundary layer or cylinder")
-    ap.add_argument("--solver", default="band", choices=["band", "krylov"],
-                    help="newton workload: FP64 band LU, or FP64 GMRES with an FP32 band LU preconditioner")
+    ap.add_argument("--solver", default="auto", choices=["auto", "band", "krylov"],
+                    help="newton / warmstart workloads: FP64 band LU, or FP64 GMRES with an FP32 band LU "
+                         "preconditioner (auto: band for the newton workload, krylov above 20000 cells for warmstart)")
     ap.add_argument("--ntrain", type=int, default=200, help="warmstart workload: training base flows")
     ap.add_argument("--nheld", type=int, default=20, help="warmstart workload: held-out (Re, Mach) points")
     ap.add_argument("--train-steps", type=int, default=3000, help="warmstart workload: Adam steps")

@@ -6,7 +6,7 @@ itself produces (broadcast_gb300.newton.CylNewton, the GPU Newton iteration
 of cylinder.py:841-1068) and gives the Newton iteration its initial state for
 a new (Re, Mach); the plain method it is compared with is the reference's
 practice of restarting from the nearest converged neighbour
-(restart_init.read_init + interpgrid, cylinder.py:776-792,
+(restart_init.read_init + interpgrid, cylinder.py:560-589,
 BROADCAST_npz.py:1062-1067), which is also the fallback when the learned
 guess does not converge.
 
@@ -200,12 +200,22 @@ class SurrogateMLP:
 # ---------------------------------------------------------------------------
 # base flows and the time-to-tolerance comparison
 
-def newton_to_tol(case, w0, tol=1e-10, maxit=12, diverge=1e3):
+def radial_ratio(jm):
+    """Radial stretching of the O-meshes here: one family of grids from r = 0.5
+    to 50 D whose jm-cell member stretches by 1.05^(21/jm) per cell (1.05^0.5
+    at jm = 42), so that doubling jm halves each cell; 512 x 256 has a first
+    cell of 0.11 D."""
+    return 1.05 ** (21.0 / jm)
+
+
+def newton_to_tol(case, w0, tol=1e-10, maxit=12, diverge=1e3, solver=None):
     """Newton's iteration (CylNewton, cfl 1e10) from w0 until the max L2
     residual norm is <= tol; stops early when the norm is not finite or grows
-    `diverge` times above its first value.  Returns the state and a record."""
+    `diverge` times above its first value.  solver: None (the FP64 band LU)
+    or a linsolve.KrylovSolver shared between calls.  Returns the state and a
+    record."""
     from .newton import CylNewton
-    nt = CylNewton(case)
+    nt = CylNewton(case, solver=solver)
     w = np.array(w0, dtype=np.float64, order="F", copy=True)
     t0 = time.perf_counter()
     n0 = None
@@ -222,6 +232,81 @@ def newton_to_tol(case, w0, tol=1e-10, maxit=12, diverge=1e3):
                       final_norm=nmax)
 
 
+def interpolate_state(grid_to, grid_from, w_from):
+    """Interior state on O-mesh grid_from (im', jm', 5) onto grid_to: bilinear
+    in the azimuth (periodic) and the logarithm of the radius of the cell
+    centres; returns (im, jm, 5)."""
+    def polar(g):
+        gh = int(g["gh"])
+        xc, yc = g["xc"][gh:-gh, gh:-gh], g["yc"][gh:-gh, gh:-gh]
+        return np.arctan2(yc[:, 0], xc[:, 0]), np.log(np.hypot(xc[0, :], yc[0, :]))
+    th_f, lr_f = polar(grid_from)
+    th_t, lr_t = polar(grid_to)
+    imf, jmf = len(th_f), len(lr_f)
+    # azimuth falls with i (clockwise from the upstream point): fractional source index
+    fi = np.mod((th_f[0] - th_t) / (2.0 * np.pi / imf), imf)
+    i0 = np.floor(fi).astype(int)
+    ai = (fi - i0)[:, None, None]
+    i1 = (i0 + 1) % imf
+    i0 %= imf
+    fj = np.interp(lr_t, lr_f, np.arange(jmf))
+    j0 = np.minimum(np.floor(fj).astype(int), jmf - 2)
+    aj = (fj - j0)[None, :, None]
+    j1 = j0 + 1
+    W = np.asarray(w_from)
+    return ((1 - ai) * ((1 - aj) * W[i0][:, j0] + aj * W[i0][:, j1]) +
+            ai * ((1 - aj) * W[i1][:, j0] + aj * W[i1][:, j1]))
+
+
+def sequence_levels(im, jm, coarsest=(56, 42)):
+    """Grids of a sequence from the coarsest member of the family to (im, jm):
+    the coarsest doubled in both directions while that stays within (im, jm),
+    then (im, jm) itself; a grid not finer than the coarsest is its own
+    sequence."""
+    if im <= coarsest[0] or jm <= coarsest[1]:
+        return [(im, jm)]
+    levels = [tuple(coarsest)]
+    while 2 * levels[-1][0] <= im and 2 * levels[-1][1] <= jm:
+        levels.append((2 * levels[-1][0], 2 * levels[-1][1]))
+    if levels[-1] != (im, jm):
+        levels.append((im, jm))
+    return levels
+
+
+def sequenced_baseflow(re, mach, im, jm, tol=1e-10, maxit=12, solver=None, log=None):
+    """A base flow without a converged neighbour: Newton's iteration from the
+    uniform flow on the coarsest grid of the family (56 x 42), then on each
+    finer grid of sequence_levels from the previous grid's solution
+    interpolated (grid sequencing); the finest level uses `solver`, the others
+    above 20000 cells a Krylov solver of their own.  Returns the finest
+    level's state (or None) and a record."""
+    t0 = time.perf_counter()
+    prev, w_int, iters = None, None, []
+    levels = sequence_levels(im, jm)
+    for k, (a, b) in enumerate(levels):
+        case = cyl_case(a, b, mach=float(mach), reynolds=float(re), noise=0.0, ratio=radial_ratio(b))
+        w0 = case["w"] if prev is None else _full_state(case, interpolate_state(case["grid"], prev["grid"], w_int))
+        if k == len(levels) - 1:
+            lsolve = solver
+        elif a * b > 20000:  # an intermediate level of its own size: FP64 GMRES, FP32 band LU
+            from .linsolve import KrylovSolver, folded_ring_order
+            lsolve = KrylovSolver(perm=folded_ring_order(a, b))
+        else:
+            lsolve = None
+        w, rec = newton_to_tol(case, w0, tol=tol, maxit=maxit, solver=lsolve)
+        iters.append(rec["iterations"])
+        if log:
+            log("  sequence level %dx%d: %s in %d iterations" % (a, b, "converged" if w is not None else "FAILED",
+                                                                rec["iterations"]))
+        if w is None:
+            return None, dict(converged=False, iterations=sum(iters), seconds=time.perf_counter() - t0,
+                              first_norm=rec["first_norm"], final_norm=rec["final_norm"], levels=levels)
+        gh = int(case["grid"]["gh"])
+        prev, w_int = case, w[gh:-gh, gh:-gh, :].copy(order="F")
+    return w, dict(converged=True, iterations=sum(iters), seconds=time.perf_counter() - t0, first_norm=None,
+                   final_norm=None, levels=levels, level_iterations=iters)
+
+
 def _full_state(case, w_int):
     gh = int(case["grid"]["gh"])
     w = case["w"].copy(order="F")
@@ -234,12 +319,16 @@ def sample_parameters(n, seed):
     return np.stack([rng.uniform(*RE_RANGE, size=n), rng.uniform(*MACH_RANGE, size=n)], axis=1)
 
 
-def solve_baseflows(params, im, jm, ratio=1.05 ** 0.5, tol=1e-10, maxit=12, log=None):
+def solve_baseflows(params, im, jm, ratio=None, tol=1e-10, maxit=12, log=None, solver=None):
     """Converged base flows at every (Re, Mach) of params by continuation:
-    the first from the uniform flow, each next one (the unsolved point
-    nearest to a solved one) from its nearest solved neighbour, retried from
-    the uniform flow if that does not converge.  Returns the interior states
-    (None where both failed) and the per-point records."""
+    the first by grid sequencing from the uniform flow on the coarsest grid
+    of the family, each next one (the unsolved point nearest to a solved one)
+    from its nearest solved neighbour, retried by grid sequencing if that does
+    not converge.  solver: the linear solve of the (im, jm) Newton iterations
+    (None: the FP64 band LU; a linsolve.KrylovSolver is shared by all of them,
+    its FP32 factor reused from one base flow to the next).  Returns the
+    interior states (None where both failed) and the per-point records."""
+    ratio = radial_ratio(jm) if ratio is None else ratio
     n = len(params)
     a, b = normalise(params[:, 0], params[:, 1])
     p = np.stack([a, b], axis=1)
@@ -256,14 +345,18 @@ def solve_baseflows(params, im, jm, ratio=1.05 ** 0.5, tol=1e-10, maxit=12, log=
         todo.remove(u)
         case = cyl_case(im, jm, mach=float(params[u, 1]), reynolds=float(params[u, 0]), noise=0.0, ratio=ratio)
         gh = int(case["grid"]["gh"])
-        w0 = case["w"] if src is None else _full_state(case, states[src])
-        w, rec = newton_to_tol(case, w0, tol=tol, maxit=maxit)
-        rec["start"] = "uniform" if src is None else "neighbour"
-        if w is None and src is not None:
-            w, rec2 = newton_to_tol(case, case["w"], tol=tol, maxit=maxit)
-            rec2["start"] = "uniform after neighbour failed"
-            rec2["seconds"] += rec["seconds"]
-            rec = rec2
+        if src is None:
+            w, rec = sequenced_baseflow(params[u, 0], params[u, 1], im, jm, tol=tol, maxit=maxit, solver=solver, log=log)
+            rec["start"] = "grid sequencing from the uniform flow"
+        else:
+            w, rec = newton_to_tol(case, _full_state(case, states[src]), tol=tol, maxit=maxit, solver=solver)
+            rec["start"] = "neighbour"
+            if w is None:
+                w, rec2 = sequenced_baseflow(params[u, 0], params[u, 1], im, jm, tol=tol, maxit=maxit, solver=solver,
+                                             log=log)
+                rec2["start"] = "grid sequencing after the neighbour failed"
+                rec2["seconds"] += rec["seconds"]
+                rec = rec2
         recs[u] = rec
         if w is not None:
             states[u] = w[gh:-gh, gh:-gh, :].copy(order="F")
@@ -275,11 +368,13 @@ def solve_baseflows(params, im, jm, ratio=1.05 ** 0.5, tol=1e-10, maxit=12, log=
     return states, recs
 
 
-def compare_starts(model, train_params, train_states, held_params, im, jm, ratio=1.05 ** 0.5, tol=1e-10, maxit=12,
-                   log=None):
+def compare_starts(model, train_params, train_states, held_params, im, jm, ratio=None, tol=1e-10, maxit=12,
+                   log=None, solver=None):
     """Time to tol for every held-out (Re, Mach): from the nearest training
     base flow (plain continuation) and from the network's guess (with the
-    plain start as fallback).  Returns per-point records."""
+    plain start as fallback), both with the same linear `solver`.  Returns
+    per-point records."""
+    ratio = radial_ratio(jm) if ratio is None else ratio
     ok = [i for i, s in enumerate(train_states) if s is not None]
     ta, tb = normalise(train_params[ok, 0], train_params[ok, 1])
     tp = np.stack([ta, tb], axis=1)
@@ -291,22 +386,24 @@ def compare_starts(model, train_params, train_states, held_params, im, jm, ratio
         nn = ok[int(np.argmin(np.linalg.norm(tp - np.array([a, b])[None, :], axis=1)))]
         t0 = time.perf_counter()
         w_plain0 = _full_state(case, train_states[nn])
-        _, plain = newton_to_tol(case, w_plain0, tol=tol, maxit=maxit)
+        _, plain = newton_to_tol(case, w_plain0, tol=tol, maxit=maxit, solver=solver)
         plain["fallback"] = False
-        if not plain["converged"]:  # as the base-flow generation: restart from the uniform flow
-            _, fb = newton_to_tol(case, case["w"], tol=tol, maxit=maxit)
+        if not plain["converged"]:  # as the base-flow generation: grid sequencing
+            _, fb = sequenced_baseflow(re, mach, im, jm, tol=tol, maxit=maxit, solver=solver)
             plain.update(fallback=True, converged=fb["converged"], iterations=plain["iterations"] + fb["iterations"])
         plain["seconds"] = time.perf_counter() - t0
         t0 = time.perf_counter()
         guess = decode(model.predict(theta, rho, re, mach), case["phys"], im, jm)
         t_guess = time.perf_counter() - t0
-        _, learned = newton_to_tol(case, _full_state(case, guess), tol=tol, maxit=maxit)
+        _, learned = newton_to_tol(case, _full_state(case, guess), tol=tol, maxit=maxit, solver=solver)
         learned["seconds"] += t_guess
         learned["guess_seconds"] = t_guess
         learned["fallback"] = False
         if not learned["converged"]:  # the plain start as fallback
-            _, fb = newton_to_tol(case, w_plain0 if plain["iterations"] and not plain["fallback"] else case["w"],
-                                  tol=tol, maxit=maxit)
+            if plain["iterations"] and not plain["fallback"]:
+                _, fb = newton_to_tol(case, w_plain0, tol=tol, maxit=maxit, solver=solver)
+            else:
+                _, fb = sequenced_baseflow(re, mach, im, jm, tol=tol, maxit=maxit, solver=solver)
             learned.update(fallback=True, converged=fb["converged"], seconds=learned["seconds"] + fb["seconds"],
                            iterations=learned["iterations"] + fb["iterations"])
         rec = dict(re=float(re), mach=float(mach), plain=plain, learned=learned)
@@ -319,8 +416,9 @@ def compare_starts(model, train_params, train_states, held_params, im, jm, ratio
     return out
 
 
-def train_on_baseflows(train_params, train_states, im, jm, ratio=1.05 ** 0.5, seed=0, **fit_kw):
+def train_on_baseflows(train_params, train_states, im, jm, ratio=None, seed=0, **fit_kw):
     """Network trained on the converged base flows (None entries skipped)."""
+    ratio = radial_ratio(jm) if ratio is None else ratio
     ok = [i for i, s in enumerate(train_states) if s is not None]
     case = cyl_case(im, jm, noise=0.0, ratio=ratio)
     theta, rho = cell_coordinates(case["grid"])

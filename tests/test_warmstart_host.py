@@ -1,7 +1,8 @@
 """CPU checks of the learned warm start's host logic with a stand-in for the
 GPU Newton iteration: the continuation order of the base-flow generation,
-its retry from the uniform flow, and the plain / learned comparison with its
-fallbacks."""
+its retry by grid sequencing from the uniform flow, the plain / learned
+comparison with its fallbacks, and the grid sequence's levels and state
+interpolation between O-meshes."""
 import numpy as np
 import pytest
 
@@ -24,7 +25,7 @@ class FakeNewton:
     def __init__(self, reach=np.inf, refuse=()):
         self.reach, self.refuse, self.calls = reach, set(refuse), []
 
-    def __call__(self, case, w0, tol=1e-10, maxit=12, diverge=1e3):
+    def __call__(self, case, w0, tol=1e-10, maxit=12, diverge=1e3, solver=None):
         re, mach = case["phys"]["re_key"]
         gh = 3
         start = np.array(w0[gh:-gh, gh:-gh, :])
@@ -60,7 +61,7 @@ def test_continuation_order_and_neighbour_starts(patched):
     patched.setattr(WS, "newton_to_tol", fake)
     states, recs = WS.solve_baseflows(params, IM, JM)
     assert all(s is not None for s in states)
-    assert recs[0]["start"] == "uniform" and fake.calls[0]["uniform"]
+    assert recs[0]["start"] == "grid sequencing from the uniform flow" and fake.calls[0]["uniform"]
     a, b = WS.normalise(params[:, 0], params[:, 1])
     p = np.stack([a, b], 1)
     solved = [0]
@@ -84,7 +85,7 @@ def test_failed_neighbour_start_retries_from_uniform(patched):
     fake = FakeNewton(refuse=[(50.0, 0.06)])
     patched.setattr(WS, "newton_to_tol", fake)
     states, recs = WS.solve_baseflows(params, IM, JM)
-    assert states[1] is not None and recs[1]["start"] == "uniform after neighbour failed"
+    assert states[1] is not None and recs[1]["start"] == "grid sequencing after the neighbour failed"
     assert [c["uniform"] for c in fake.calls] == [True, False, True]
 
 
@@ -130,3 +131,31 @@ def test_compare_starts_fallbacks(patched):
     assert r["learned"]["iterations"] == fake_iterations(fake, 2) + 8  # both attempts counted
     starts = [c["uniform"] for c in fake.calls]
     assert starts == [False, True, False, True]
+
+
+def test_sequence_levels():
+    assert WS.sequence_levels(512, 256) == [(56, 42), (112, 84), (224, 168), (512, 256)]
+    assert WS.sequence_levels(112, 84) == [(56, 42), (112, 84)]
+    assert WS.sequence_levels(56, 42) == [(56, 42)]
+    assert WS.sequence_levels(28, 21) == [(28, 21)]
+    assert WS.radial_ratio(42) == 1.05 ** 0.5
+
+
+def test_interpolate_state_between_o_meshes():
+    """A smooth field of (azimuth, log radius) interpolated from one O-mesh of
+    the family to a finer one is close to the field itself, and the identity
+    on the same grid; the azimuth is periodic."""
+    def field(g):
+        gh = 3
+        xc, yc = g["xc"][gh:-gh, gh:-gh], g["yc"][gh:-gh, gh:-gh]
+        th, lr = np.arctan2(yc, xc), np.log(np.hypot(xc, yc))
+        return np.stack([np.cos(th) + lr, np.sin(2 * th) * lr, lr ** 2, np.cos(th) * np.sin(th), 1.0 + 0 * lr], -1)
+    from tests import helpers as H
+    coarse = WS.cyl_case(56, 42, ratio=WS.radial_ratio(42), noise=0.0, ops=H.OracleOps)["grid"]
+    fine = WS.cyl_case(112, 84, ratio=WS.radial_ratio(84), noise=0.0, ops=H.OracleOps)["grid"]
+    fc = field(coarse)
+    assert np.allclose(WS.interpolate_state(coarse, coarse, fc), fc, atol=1e-12)
+    got = WS.interpolate_state(fine, coarse, fc)
+    want = field(fine)
+    inner = slice(1, -1)  # the last radial cells lie past the coarse centres (clamped)
+    assert np.abs(got[:, inner] - want[:, inner]).max() < 0.02 * np.abs(want).max()
