@@ -1001,7 +1001,7 @@ int jacobian_outputs(JacobianArgs& a, Stager& sg, int* indptr, int* indices, dou
   const int im = a.im, jm = a.jm, gh = a.gh, nrow = 5 * im * jm;
   cudaStream_t st = current_stream();
   int rc = 0;
-  a.scratch = (double*)pool_get(POOL_SCRATCH, jacobian_scratch_doubles(im, jm, gh) * 8);
+  a.scratch = (double*)pool_get(POOL_SCRATCH, jacobian_scratch_doubles(im, jm, gh, a.nzone == 2 ? 2 : 1) * 8);
   if (!a.scratch) return fail_arg("jacobian: scratch allocation failed"), BCG_ERR_NOMEM;
   a.iscratch = (int*)pool_get(POOL_AUX, jacobian_iscratch_ints(im, jm) * 4);
   if (!a.iscratch) return fail_arg("jacobian: scratch allocation failed"), BCG_ERR_NOMEM;
@@ -1077,6 +1077,11 @@ extern "C" int bcg_jacobian_dnc5_cyl_csr(const double* w, const double* nx, cons
   a.w = sg.dev<double>(hw); a.nx = sg.dev<double>(hnx); a.ny = sg.dev<double>(hny);
   a.vol = sg.dev<double>(hvol); a.volf = sg.dev<double>(hvolf);
   a.op = 0; a.withjn = 1;
+  // im not a multiple of the colour step: the driver's two azimuthal zones
+  // (cylinder.py:899-938, Nzones), so that no colour has two seeds within a
+  // stencil of each other across the periodic join
+  if (im % (2 * gh + 1) != 0) { a.nzone = 2; a.imid = im / 2 / (2 * gh + 1) * (2 * gh + 1); }
+  else a.nzone = 1;
   a.relaxed = coefdiag ? 1 : 0;
   a.coefdiag = hc >= 0 ? sg.dev<double>(hc) : nullptr;
   a.mini = mini; a.divide_by_vol = divide_by_vol; a.capacity = capacity; a.nnz = nnz;

@@ -28,8 +28,11 @@ namespace bcg {
 
 namespace {
 
-// 4 seeds into 4 stacked padded tangent states (testvector for each)
-__global__ void k_seed4(double* __restrict__ wd, int nseed, const int* __restrict__ seeds, int gh, int im, int jm) {
+// seeded tangent states (testvector, or testvector_partial within the seed's
+// zone: 0-based columns [0, imid) for zone 0, [imid, im) for zone 1); the
+// seed table holds (m, l, k, zone) per seed
+__global__ void k_seed4(double* __restrict__ wd, int nseed, const int* __restrict__ seeds, int gh, int im, int jm,
+                        int imid) {
   const int ni = im + 2 * gh, nj = jm + 2 * gh;
   const size_t ns = (size_t)ni * nj * 5;
   const int step = 1 + 2 * gh;
@@ -37,9 +40,10 @@ __global__ void k_seed4(double* __restrict__ wd, int nseed, const int* __restric
     const int s = (int)(q / ns);
     const size_t r = q % ns;
     const int i = (int)(r % ni) + 1 - gh, j = (int)((r / ni) % nj) + 1 - gh, v = (int)(r / ((size_t)ni * nj));
-    const int m = seeds[3 * s], l = seeds[3 * s + 1], k = seeds[3 * s + 2];
-    const bool on = (v == m) && j >= k + 1 && j <= jm && (j - k - 1) % step == 0 && i >= l + 1 && i <= im &&
-                    (i - l - 1) % step == 0;
+    const int m = seeds[4 * s], l = seeds[4 * s + 1], k = seeds[4 * s + 2], z = seeds[4 * s + 3];
+    const int i0 = z ? imid : 0, i1 = z ? im : imid;  // zone columns [i0, i1), 0-based
+    const bool on = (v == m) && j >= k + 1 && j <= jm && (j - k - 1) % step == 0 && i - 1 >= i0 && i - 1 < i1 &&
+                    (i - 1 - i0 - l) % step == 0 && i - 1 - i0 - l >= 0;
     wd[q] = on ? 1.0 : 0.0;
   }
 }
@@ -49,8 +53,9 @@ __global__ void k_seed4(double* __restrict__ wd, int nseed, const int* __restric
 // op 0 stores -resd (+coefdiag on the diagonal when relaxed), the fill of
 // computejacobianfromjv(_relaxed) (ComputeJacobian.f90:292-355, 503-570);
 // op != 0 stores +dz with the row window of computejacobianfromdz (:708-779).
-__global__ void __launch_bounds__(128) k_csr_rows(int pass, int op, int withjn, const double* __restrict__ resd_all, int gh,
-                                                  int im, int jm, int relaxed, const double* __restrict__ coefdiag, double mini,
+__global__ void __launch_bounds__(128) k_csr_rows(int pass, int op, int withjn, int nzone, const double* __restrict__ resd_all,
+                                                  int gh, int im, int jm, int relaxed,
+                                                  const double* __restrict__ coefdiag, double mini,
                                                   const double* __restrict__ vol, int* __restrict__ count,
                                                   const long long* __restrict__ rowptr, int* __restrict__ indices,
                                                   double* __restrict__ data) {
@@ -64,23 +69,38 @@ __global__ void __launch_bounds__(128) k_csr_rows(int pass, int op, int withjn, 
   const size_t cell = (size_t)(i + gh - 1) + (size_t)(j + gh - 1) * ni;
   const double cd = relaxed ? coefdiag[(i - 1) + (size_t)(j - 1) * im] : 0.0;
   const double vinv = vol ? 1.0 / vol[cell] : 1.0;
-  // per l and per k, the seed cell index (0-based) or -1; sort l and k by it
-  int li[7], lv[7], ki[7], kv[7];
+  // per (l, zone): the seed cell index (0-based) or -1; sorted by it
+  constexpr int NC = 14;
+  const int nc = 7 * nzone;
+  int li[NC], lv[NC], ki[7], kv[7];
   const int step = 1 + 2 * gh;
-  for (int l = 0; l < 7; ++l) {
-    li[l] = l;
+  for (int c = 0; c < nc; ++c) {
+    const int l = c % 7, z = c / 7;
+    li[c] = c;
     int vali;
-    if (!withjn) {
+    if (nzone == 2) {
+      // computejacobianfromjv_relaxed_withjnandcheck (ComputeJacobian.f90:1095-1204): zone 0 wraps the
+      // columns past im - 2gh back to l, zone 1 those up to 2gh to the last seed of colour l
+      if (l <= gh) vali = (i <= l + 1 + gh) ? l : (i - (l + 1) + gh) / step * step + l;
+      else vali = (i <= l - gh) ? l : (i - (l + 1) + gh) / step * step + l;
+      if (z == 0) {
+        if (vali >= im - 2 * gh) vali = l;
+      } else if (vali <= 2 * gh) {
+        vali = im - (im % step) + l;
+        if (vali > im - 1) vali -= step;
+      }
+      lv[c] = vali;
+    } else if (!withjn) {
       if (l <= gh) vali = (i <= l + 1 + gh) ? l : (i - (l + 1) + gh) / step * step + l;
       else vali = (i <= l - gh) ? im + 1 : (i - (l + 1) + gh) / step * step + l;
-      lv[l] = vali < im ? vali : -1;
+      lv[c] = vali < im ? vali : -1;
     } else {
       // periodic in i (ComputeJacobian.f90:876-897): the seeded column left of
       // the first ones wraps to im-1-2gh+l, the one past im back to l
       if (l <= gh) vali = (i <= l + 1 + gh) ? l : (i - (l + 1) + gh) / step * step + l;
       else vali = (i <= l - gh) ? im - 1 - 2 * gh + l : (i - (l + 1) + gh) / step * step + l;
       if (vali >= im) vali = (vali - im <= gh - 1) ? l : -1;
-      lv[l] = vali;
+      lv[c] = vali;
     }
   }
   for (int k = 0; k < 7; ++k) {
@@ -90,19 +110,20 @@ __global__ void __launch_bounds__(128) k_csr_rows(int pass, int op, int withjn, 
     else valj = (j <= k - gh) ? jm + 1 : (j - (k + 1) + gh) / step * step + k;
     kv[k] = valj < jm ? valj : -1;
   }
-  // insertion sorts (7 elements)
-  for (int a = 1; a < 7; ++a)
+  // insertion sorts
+  for (int a = 1; a < nc; ++a)
     for (int b = a; b > 0 && lv[b - 1] > lv[b]; --b) { int t = lv[b]; lv[b] = lv[b - 1]; lv[b - 1] = t; t = li[b]; li[b] = li[b - 1]; li[b - 1] = t; }
   for (int a = 1; a < 7; ++a)
     for (int b = a; b > 0 && kv[b - 1] > kv[b]; --b) { int t = kv[b]; kv[b] = kv[b - 1]; kv[b - 1] = t; t = ki[b]; ki[b] = ki[b - 1]; ki[b - 1] = t; }
   long long out = pass ? rowptr[row] : 0;
   int n = 0;
-  for (int a = 0; a < 7;) {
-    // run of seeds l with the same column (only with the periodic wrap when
-    // im is not a multiple of 7): their slots are duplicates, summed as the
-    // COO -> CSR conversion does, each slot filtered on its own first
+  for (int a = 0; a < nc;) {
+    // run of (l, zone) candidates with the same column (the periodic wrap when
+    // im is not a multiple of 7, or the two zones): their slots are
+    // duplicates, summed as the COO -> CSR conversion does, each slot
+    // filtered on its own first
     int a2 = a + 1;
-    while (a2 < 7 && lv[a2] == lv[a]) ++a2;
+    while (a2 < nc && lv[a2] == lv[a]) ++a2;
     if (lv[a] < 0) { a = a2; continue; }
     for (int b = 0; b < 7; ++b) {
       if (kv[b] < 0) continue;
@@ -112,7 +133,8 @@ __global__ void __launch_bounds__(128) k_csr_rows(int pass, int op, int withjn, 
         double sum = 0.0;
         bool kept = false;
         for (int q = a; q < a2; ++q) {
-          const int seed = k + 7 * li[q] + 49 * m;  // the reference's slot order
+          const int l = li[q] % 7, z = li[q] / 7;
+          const int seed = z * 245 + k + 7 * l + 49 * m;  // the reference's slot order, zone by zone
           const double r = resd_all[(size_t)seed * np * 5 + (size_t)e * np + cell];
           const double v = op ? r : ((relaxed && col == row) ? cd - r : -r);
           if (!(fabs(v) > mini)) continue;
@@ -174,10 +196,10 @@ static int jacobian_groups(int im, int jm, int gh) {
   return (int)std::max<size_t>(1, std::min<size_t>(61, g));
 }
 
-size_t jacobian_scratch_doubles(int im, int jm, int gh) {
+size_t jacobian_scratch_doubles(int im, int jm, int gh, int nzone) {
   const size_t np = (size_t)(im + 2 * gh) * (jm + 2 * gh);
   const size_t G = (size_t)jacobian_groups(im, jm, gh);
-  return 245 * np * 5      // tangent outputs of every seed
+  return 245 * (size_t)nzone * np * 5  // tangent outputs of every seed (per zone)
          + 4 * G * np * 5  // seeded tangent states of G groups
          + np * 5          // state copy written by the linearised boundary fills
          + G * residual_scratch_doubles(im, jm, gh, 4);
@@ -186,22 +208,25 @@ size_t jacobian_scratch_doubles(int im, int jm, int gh) {
 int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
   const int im = a.im, jm = a.jm, gh = a.gh;
   const size_t np = (size_t)(im + 2 * gh) * (jm + 2 * gh);
+  const int nzone = a.nzone == 2 ? 2 : 1, nseed = 245 * nzone;
   double* resd_all = a.scratch;
-  double* wd4 = resd_all + 245 * np * 5;
+  double* wd4 = resd_all + (size_t)nseed * np * 5;
   double* wcopy = wd4 + 4 * (size_t)jacobian_groups(im, jm, gh) * np * 5;
   double* rscr = wcopy + np * 5;
-  int* seeds_dev = a.iscratch;                        // 245 x 3
-  long long* rowptr = (long long*)(a.iscratch + 1024);  // nrow + 1 (8-byte aligned offset)
+  int* seeds_dev = a.iscratch;                        // 2 x 245 x 4
+  long long* rowptr = (long long*)(a.iscratch + 2048);  // nrow + 1 (8-byte aligned offset)
   const int nrow = 5 * im * jm;
   long long* bsum = rowptr + nrow + 2;
   const int nb = (nrow + kScanBlock - 1) / kScanBlock;
   long long* total = bsum + nb + 1;
   int* count = (int*)(total + 2);
-  // seed table in the reference's loop order: m, then l, then k
-  std::vector<int> seeds(245 * 3);
-  for (int m = 0, s = 0; m < 5; ++m)
-    for (int l = 0; l < 7; ++l)
-      for (int k = 0; k < 7; ++k, ++s) { seeds[3 * s] = m; seeds[3 * s + 1] = l; seeds[3 * s + 2] = k; }
+  // seed table in the reference's loop order: zone, then m, then l, then k
+  std::vector<int> seeds((size_t)nseed * 4);
+  for (int z = 0, s = 0; z < nzone; ++z)
+    for (int m = 0; m < 5; ++m)
+      for (int l = 0; l < 7; ++l)
+        for (int k = 0; k < 7; ++k, ++s) { seeds[4 * s] = m; seeds[4 * s + 1] = l; seeds[4 * s + 2] = k; seeds[4 * s + 3] = z; }
+  const int imid = nzone == 2 ? a.imid : im;
   cudaError_t e = cudaMemcpyAsync(seeds_dev, seeds.data(), seeds.size() * sizeof(int), cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return fail_cuda("jacobian: seed table", e);
   e = cudaMemcpyAsync(wcopy, a.w, np * 5 * sizeof(double), cudaMemcpyDeviceToDevice, st);
@@ -211,15 +236,15 @@ int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
   ra.vol = a.vol; ra.volf = a.volf; ra.dstride = np * 5; ra.scratch = rscr; ra.res = nullptr;
   // chunks of G groups of 4 seeds: seed, linearised boundary chain per group,
   // then one tangent launch per pass over the whole chunk (blockIdx.y = group);
-  // the last seed (245 = 61 * 4 + 1) runs as a 1-direction chunk
+  // the last seeds (245 = 61 * 4 + 1, 490 = 122 * 4 + 2) run as 1-direction chunks
   const int G = jacobian_groups(im, jm, gh);
   ra.ndir = 4;
-  for (int s0 = 0; s0 < 245;) {
-    const int left = 245 - s0;
+  for (int s0 = 0; s0 < nseed;) {
+    const int left = nseed - s0;
     const int kk = left >= 4 ? 4 : 1;
     const int ng = left >= 4 ? std::min(G, left / 4) : 1;
     const int ns = kk * ng;
-    k_seed4<<<1024, 256, 0, st>>>(wd4, ns, seeds_dev + 3 * s0, gh, im, jm);
+    k_seed4<<<1024, 256, 0, st>>>(wd4, ns, seeds_dev + 4 * s0, gh, im, jm, imid);
     for (int g = 0; g < ng; ++g)
       for (const BcArgs& b0 : a.bcs) {
         BcArgs b = b0;
@@ -256,8 +281,8 @@ int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
   }
   // CSR: count, scan, fill
   const int B = 128;
-  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(0, a.op, a.withjn, resd_all, gh, im, jm, a.relaxed, a.coefdiag, a.mini,
-                                             a.divide_by_vol ? a.vol : nullptr, count, nullptr, nullptr, nullptr);
+  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(0, a.op, a.withjn, nzone, resd_all, gh, im, jm, a.relaxed, a.coefdiag,
+                                             a.mini, a.divide_by_vol ? a.vol : nullptr, count, nullptr, nullptr, nullptr);
   k_scan_block<<<nb, kScanBlock, 0, st>>>(count, rowptr, bsum, nrow);
   k_scan_sums<<<1, 1, 0, st>>>(bsum, nb, total);
   k_scan_add<<<(nrow + 1 + 255) / 256, 256, 0, st>>>(rowptr, bsum, nrow, total);
@@ -269,8 +294,8 @@ int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
   if (nnz > a.capacity) return fail_arg("jacobian: CSR capacity too small (see nnz)");
   if (nnz >= (1LL << 31)) return fail_arg("jacobian: nnz exceeds 32-bit CSR indices");
   k_ptr_to_int<<<(nrow + 1 + 255) / 256, 256, 0, st>>>(rowptr, a.indptr, nrow);
-  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(1, a.op, a.withjn, resd_all, gh, im, jm, a.relaxed, a.coefdiag, a.mini,
-                                             a.divide_by_vol ? a.vol : nullptr, count, rowptr, a.indices, a.data);
+  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(1, a.op, a.withjn, nzone, resd_all, gh, im, jm, a.relaxed, a.coefdiag,
+                                             a.mini, a.divide_by_vol ? a.vol : nullptr, count, rowptr, a.indices, a.data);
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail_cuda("jacobian: csr", e);
   return BCG_OK;
@@ -351,7 +376,7 @@ size_t csr_beta_iscratch_ints(int nrow) {
 size_t jacobian_iscratch_ints(int im, int jm) {
   const size_t nrow = 5 * (size_t)im * jm;
   const size_t nb = (nrow + kScanBlock - 1) / kScanBlock;
-  return 1024 + 2 * (nrow + 2 + nb + 1 + 2) + nrow + 64;
+  return 2048 + 2 * (nrow + 2 + nb + 1 + 2) + nrow + 64;
 }
 
 }  // namespace bcg

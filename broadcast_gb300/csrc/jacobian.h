@@ -19,6 +19,9 @@ struct JacobianArgs {
   std::vector<BcArgs> bcs;  // linearised boundary chain, in the drivers' order
   std::vector<JnArgs> joins;  // periodic joins applied to each tangent after the fills (wr = wd = the tangent)
   int withjn;               // 1: columns wrap periodically in i (computejacobianfromjv[_relaxed]_withjn)
+  int nzone;                // 2: seeds in the two azimuthal zones i < imid, i >= imid (testvector_partial)
+                            //    with computejacobianfromjv_relaxed_withjnandcheck's columns; else 1
+  int imid;                 // first 0-based column of the second zone (a multiple of 7)
   int op;                   // 0: residual tangent (Jacobian); SPAN_DZ / SPAN_DZZ: spanwise operators
   int relaxed;              // 1: coefdiag added on the diagonal (computejacobianfromjv_relaxed)
   const double* coefdiag;   // (im, jm)
@@ -52,7 +55,7 @@ struct CsrBetaArgs {
 int run_csr_beta(const CsrBetaArgs& a, cudaStream_t st);
 size_t csr_beta_iscratch_ints(int nrow);
 
-size_t jacobian_scratch_doubles(int im, int jm, int gh);
+size_t jacobian_scratch_doubles(int im, int jm, int gh, int nzone = 1);
 size_t jacobian_iscratch_ints(int im, int jm);
 int run_jacobian(const JacobianArgs& a, cudaStream_t st);
 

@@ -219,17 +219,20 @@ def newton_to_tol(case, w0, tol=1e-10, maxit=12, diverge=1e3, solver=None):
     w = np.array(w0, dtype=np.float64, order="F", copy=True)
     t0 = time.perf_counter()
     n0 = None
+    norms = []
+    nlog = len(getattr(solver, "log", []))
     for it in range(1, maxit + 1):
         norm, dw = nt.step(w, first=(it == 1), tol=tol)
         nmax = float(np.max(norm))
+        norms.append(nmax)
         n0 = nmax if n0 is None else n0
         if dw is None:
             return w, dict(converged=True, iterations=it, seconds=time.perf_counter() - t0, first_norm=n0,
-                           final_norm=nmax)
+                           final_norm=nmax, norms=norms, solves=getattr(solver, "log", [])[nlog:])
         if not np.isfinite(nmax) or nmax > diverge * max(n0, 1.0):
             break
     return None, dict(converged=False, iterations=it, seconds=time.perf_counter() - t0, first_norm=n0,
-                      final_norm=nmax)
+                      final_norm=nmax, norms=norms, solves=getattr(solver, "log", [])[nlog:])
 
 
 def interpolate_state(grid_to, grid_from, w_from):
@@ -261,15 +264,16 @@ def interpolate_state(grid_to, grid_from, w_from):
 def sequence_levels(im, jm, coarsest=(56, 42)):
     """Grids of a sequence from the coarsest member of the family to (im, jm):
     the coarsest doubled in both directions while that stays within (im, jm),
-    then (im, jm) itself; a grid not finer than the coarsest is its own
-    sequence."""
+    then steps of at most twice each extent up to (im, jm); a grid not finer
+    than the coarsest is its own sequence."""
     if im <= coarsest[0] or jm <= coarsest[1]:
         return [(im, jm)]
     levels = [tuple(coarsest)]
     while 2 * levels[-1][0] <= im and 2 * levels[-1][1] <= jm:
         levels.append((2 * levels[-1][0], 2 * levels[-1][1]))
-    if levels[-1] != (im, jm):
-        levels.append((im, jm))
+    while levels[-1] != (im, jm):
+        a, b = levels[-1]
+        levels.append((min(2 * a, im), min(2 * b, jm)))
     return levels
 
 
@@ -296,8 +300,11 @@ def sequenced_baseflow(re, mach, im, jm, tol=1e-10, maxit=12, solver=None, log=N
         w, rec = newton_to_tol(case, w0, tol=tol, maxit=maxit, solver=lsolve)
         iters.append(rec["iterations"])
         if log:
-            log("  sequence level %dx%d: %s in %d iterations" % (a, b, "converged" if w is not None else "FAILED",
-                                                                rec["iterations"]))
+            log("  sequence level %dx%d: %s in %d iterations, %.1f s, norms %s%s" % (
+                a, b, "converged" if w is not None else "FAILED", rec["iterations"], rec["seconds"],
+                " ".join("%.1e" % x for x in rec["norms"]),
+                "" if not rec["solves"] else "; GMRES iterations %s, factorisations %d" % (
+                    [k["iterations"] for k in rec["solves"]], sum(k["refactored"] for k in rec["solves"]))))
         if w is None:
             return None, dict(converged=False, iterations=sum(iters), seconds=time.perf_counter() - t0,
                               first_norm=rec["first_norm"], final_norm=rec["final_norm"], levels=levels)

@@ -284,8 +284,12 @@ int bcg_jacobian_dnc5_bl_csr(const double* w, const double* nx, const double* ny
  * chain of handleBC.applyBC (no-reflexion Jhi, wall Jlo, the joins prr1 <- prd2
  * and prr2 <- prd1 twice, as jn_match_2d_d), flux_num_dnc5_2d_d and
  * computejacobianfromjv[_relaxed]_withjn, whose columns wrap periodically in
- * i; where the wrap maps two seeds to one column (im not a multiple of 7) the
- * slots are summed, as the COO -> CSR conversion does. */
+ * i.  When im is not a multiple of 7 the seeds of one colour would meet
+ * within a stencil across the periodic join, so, as the driver does
+ * (cylinder.py:899-938), the seeds run in two azimuthal zones (columns below
+ * and from im/2/7*7, testvector_partial, 490 seeds) with the columns of
+ * computejacobianfromjv_relaxed_withjnandcheck; slots that land on one
+ * column are summed, as the COO -> CSR conversion does. */
 int bcg_jacobian_dnc5_cyl_csr(const double* w, const double* nx, const double* ny, const double* vol,
                               const double* volf, int gh, double cp, double cv, double prandtl, double gam,
                               double rgaz, double cs, double muref, double tref, double s_suth, double k2, double k4,

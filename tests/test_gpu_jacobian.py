@@ -89,18 +89,34 @@ def test_batched_jacobian_columns_against_dense_jvp():
 
 
 def _reference_cyl_csr(c, coefdiag, mini=2e-16):
+    """The cylinder driver's loop (cylinder.py:899-980): for im a multiple of
+    7, testvector and computejacobianfromjv[_relaxed]_withjn; otherwise two
+    azimuthal zones (Nzones: columns below and from im/2/7*7), testvector_partial
+    and computejacobianfromjv_relaxed_withjnandcheck per zone (its plain form
+    with a zero coefdiag)."""
     g = c["grid"]
     im, jm, gh = g["im"], g["jm"], g["gh"]
-    nb = im * jm * 49 * 25
+    zoned = im % 7 != 0
+    nb = im * jm * 49 * 25 * (2 if zoned else 1)
     jac, ia, ja = np.zeros(nb), np.zeros(nb, np.int32), np.zeros(nb, np.int32)
     mode = O.JAC_RELAXED_WITHJN if coefdiag is not None else O.JAC_WITHJN
-    for m in range(5):
-        for l in range(7):
-            for k in range(7):
-                wd = O.testvector(m, l, k, gh, im, jm)
-                H.oracle_bcs(c, c["w"].copy(order="F"), wd)
-                _, resd = O.jvp(g, c["phys"], c["w"], wd)
-                O.computejacobian(mode, jac, ia, ja, resd, m, l, k, gh, im, jm, coefdiag)
+    imid = im // 2 // 7 * 7
+    zones = [(0, imid - 1), (imid, im - 1)] if zoned else [None]
+    cd = coefdiag if coefdiag is not None else np.zeros((im, jm), order="F")
+    for n, zone in enumerate(zones):
+        for m in range(5):
+            for l in range(7):
+                for k in range(7):
+                    if zone is None:
+                        wd = O.testvector(m, l, k, gh, im, jm)
+                    else:
+                        wd = O.testvector_partial(m, l, k, gh, im, jm, zone[0], zone[1], 0, jm - 1)
+                    H.oracle_bcs(c, c["w"].copy(order="F"), wd)
+                    _, resd = O.jvp(g, c["phys"], c["w"], wd)
+                    if zone is None:
+                        O.computejacobian(mode, jac, ia, ja, resd, m, l, k, gh, im, jm, coefdiag)
+                    else:
+                        O.computejacobian_withjnandcheck(jac, ia, ja, resd, m, l, k, gh, im, jm, cd, mini, n)
     keep = np.abs(jac) > mini
     a = sp.csr_matrix((jac[keep], (ia[keep], ja[keep])), shape=(5 * im * jm, 5 * im * jm))
     a.sum_duplicates()
@@ -111,8 +127,8 @@ def _reference_cyl_csr(c, coefdiag, mini=2e-16):
 @pytest.mark.parametrize("im,relaxed", [(21, True), (20, False), (22, True)])
 def test_batched_cylinder_jacobian_matches_reference_loop(im, relaxed):
     """Periodic O-mesh: joins in the tangent chain, columns wrapped in i
-    (computejacobianfromjv[_relaxed]_withjn), duplicates summed when im is not
-    a multiple of 7."""
+    (computejacobianfromjv[_relaxed]_withjn); when im is not a multiple of 7
+    the driver's two azimuthal zones of seeds."""
     from broadcast_gb300 import _lib
     from broadcast_gb300._f2py import interf4
     c = H.cyl_case(im, 10)
@@ -137,3 +153,40 @@ def test_batched_cylinder_jacobian_matches_reference_loop(im, relaxed):
     assert np.array_equal(got.indptr, ref.indptr)
     assert np.array_equal(got.indices, ref.indices)
     assert np.abs(got.data - ref.data).max() <= 1e-11 * np.abs(ref.data).max()
+
+
+def test_cylinder_jacobian_columns_at_the_periodic_join():
+    """im = 22 (not a multiple of 7): the columns of the assembled periodic
+    Jacobian next to the join, where one colour's seeds of a single zone would
+    meet across it, equal single-cell tangents (seed, tangent fills with the
+    joins, flux_num_dnc5_2d_d)."""
+    from broadcast_gb300 import _lib
+    from broadcast_gb300._f2py import interf4
+    im, jm = 22, 10
+    c = H.cyl_case(im, jm)
+    H.oracle_bcs(c, c["w"])
+    g, ph, it = c["grid"], c["phys"], c["interf"]
+    gh = g["gh"]
+    nrow = 5 * im * jm
+    cap = nrow * 245
+    indptr, indices, data = np.zeros(nrow + 1, np.int32), np.zeros(cap, np.int32), np.zeros(cap)
+    nnz = np.zeros(1, np.int64)
+    keys = ("cp", "cv", "prandtl", "gam", "rgaz", "cs", "muref", "tref", "s_suth", "k2", "k4")
+    pr = interf4
+    _lib.call("bcg_jacobian_dnc5_cyl_csr", c["w"], g["nx"], g["ny"], g["vol"], g["volf"], gh,
+              *[float(ph[k]) for k in keys], im, jm, pr(it["Jhi"]), pr(it["Jlo"]), c["wbd"], c["wbd"].shape[0],
+              pr(it["prr1"]), pr(it["prd1"]), pr(it["prr2"]), pr(it["prd2"]),
+              np.ascontiguousarray(np.asarray(it["tr"], dtype=np.int32).ravel()), None, -1.0, 0, indptr, indices,
+              data, cap, nnz)
+    n = int(nnz[0])
+    got = sp.csr_matrix((data[:n], indices[:n], indptr), shape=(nrow, nrow)).toarray()
+    for ii in (0, 1, 2, im - 3, im - 2, im - 1):
+        for jj in (0, 4):
+            for mm in (0, 3):
+                col = mm + 5 * jj + 5 * jm * ii
+                wd = np.zeros_like(c["w"])
+                wd[ii + gh, jj + gh, mm] = 1.0
+                H.oracle_bcs(c, c["w"].copy(order="F"), wd)
+                _, resd = O.jvp(g, ph, c["w"], wd)
+                dense = -H.interior(resd).reshape(-1)  # (i, j, e) C order = row numbering
+                assert np.abs(got[:, col] - dense).max() <= 1e-11 * max(1.0, np.abs(dense).max()), (ii, jj, mm)

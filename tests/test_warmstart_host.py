@@ -34,7 +34,8 @@ class FakeNewton:
         self.calls.append(dict(key=(re, mach), start=start, uniform=uniform, dist=dist))
         ok = uniform or (dist <= self.reach and (re, mach) not in self.refuse)
         it = 8 if uniform else 2 + int(np.ceil(np.log10(max(dist, 1e-12) / 1e-12)))
-        rec = dict(converged=ok, iterations=it, seconds=0.01 * it, first_norm=dist, final_norm=0.0 if ok else dist)
+        rec = dict(converged=ok, iterations=it, seconds=0.01 * it, first_norm=dist, final_norm=0.0 if ok else dist,
+                   norms=[dist], solves=[])
         if not ok:
             return None, rec
         w = np.array(w0, copy=True)
@@ -134,7 +135,7 @@ def test_compare_starts_fallbacks(patched):
 
 
 def test_sequence_levels():
-    assert WS.sequence_levels(512, 256) == [(56, 42), (112, 84), (224, 168), (512, 256)]
+    assert WS.sequence_levels(512, 256) == [(56, 42), (112, 84), (224, 168), (448, 256), (512, 256)]
     assert WS.sequence_levels(112, 84) == [(56, 42), (112, 84)]
     assert WS.sequence_levels(56, 42) == [(56, 42)]
     assert WS.sequence_levels(28, 21) == [(28, 21)]
