@@ -1013,8 +1013,9 @@ int jacobian_outputs(JacobianArgs& a, Stager& sg, int* indptr, int* indices, dou
     if (rc) return rc;
     return sg.finish();
   }
-  // host outputs: the device copy is sized to the worst case 245 entries per row
-  const long long cap = (long long)nrow * 245;
+  // host outputs: the device copy is sized to the worst case, 245 entries per
+  // row and zone
+  const long long cap = (long long)nrow * 245 * (a.nzone == 2 ? 2 : 1);
   char* ob = (char*)pool_get(POOL_STAGE_OUT, (size_t)(nrow + 1) * 4 + (size_t)cap * 12 + 512);
   if (!ob) return fail_arg("jacobian: output allocation failed"), BCG_ERR_NOMEM;
   a.indptr = (int*)ob;

@@ -176,7 +176,7 @@ def test_cylinder_jacobian_columns_at_the_periodic_join():
     _lib.call("bcg_jacobian_dnc5_cyl_csr", c["w"], g["nx"], g["ny"], g["vol"], g["volf"], gh,
               *[float(ph[k]) for k in keys], im, jm, pr(it["Jhi"]), pr(it["Jlo"]), c["wbd"], c["wbd"].shape[0],
               pr(it["prr1"]), pr(it["prd1"]), pr(it["prr2"]), pr(it["prd2"]),
-              np.ascontiguousarray(np.asarray(it["tr"], dtype=np.int32).ravel()), None, -1.0, 0, indptr, indices,
+              np.ascontiguousarray(np.asarray(it["tr"], dtype=np.int32).ravel()), None, 2e-16, 0, indptr, indices,
               data, cap, nnz)
     n = int(nnz[0])
     got = sp.csr_matrix((data[:n], indices[:n], indptr), shape=(nrow, nrow)).toarray()
