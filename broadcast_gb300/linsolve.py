@@ -61,15 +61,15 @@ class KrylovSolver:
     (bcg_band32_factor: the row-equilibrated matrix in FP32, factorised in the
     bandwidth-reducing order perm).  The factor is reused for later systems
     (the next Newton steps, neighbouring base flows) and rebuilt from the
-    current matrix when GMRES needs more than `refactor_after` iterations or
-    does not reach `rtol`.
+    current matrix when GMRES with it does not reach `rtol` within the
+    iterations one factorisation costs (at least `refactor_after`).
 
     solve(indptr, indices, data, b) takes device tensors (torch, CSR int32 /
     float64) and returns x as a device tensor."""
 
     device_csr = True
 
-    def __init__(self, perm=None, nb=1024, restart=60, maxit=240, rtol=1e-10, refactor_after=40):
+    def __init__(self, perm=None, nb=1024, restart=60, maxit=400, rtol=1e-10, refactor_after=40):
         _lib.load()
         self.perm = None if perm is None else np.ascontiguousarray(perm, dtype=np.int32)
         self.nb, self.restart, self.maxit, self.rtol = int(nb), int(restart), int(maxit), float(rtol)
@@ -107,13 +107,17 @@ class KrylovSolver:
             raise
         self.handle, self.n = int(h[0]), n
 
-    def gmres(self, indptr, indices, data, b, x):
+    def gmres(self, indptr, indices, data, b, x, maxit=None):
         it, rr = np.zeros(1, np.int32), np.zeros(1)
-        _lib.call("bcg_gmres_solve", self.handle, self.n, indptr, indices, data, b, x, self.restart, self.maxit,
-                  self.rtol, it, rr)
+        _lib.call("bcg_gmres_solve", self.handle, self.n, indptr, indices, data, b, x, self.restart,
+                  int(maxit or self.maxit), self.rtol, it, rr)
         return int(it[0]), float(rr[0])
 
     def solve(self, indptr, indices, data, b):
+        """x with ||b - A x|| <= rtol ||b||.  With a kept factor, GMRES may run
+        as many iterations as one factorisation costs (measured), at least
+        refactor_after; past that, or if it stalls, the factor is rebuilt from
+        this matrix and GMRES restarts."""
         import time
         import torch
         x = torch.empty_like(b)
@@ -122,11 +126,19 @@ class KrylovSolver:
         refactored = False
         if self.handle is None or self.n != n:
             self.factor(indptr, indices, data)
+            self._t_factor = time.perf_counter() - t0
             refactored = True
         t1 = time.perf_counter()
-        it, rr = self.gmres(indptr, indices, data, b, x)
-        if not refactored and (rr > self.rtol or it > self.refactor_after):
+        budget = self.maxit
+        if not refactored and getattr(self, "_t_iter", None):
+            budget = int(np.clip(self._t_factor / self._t_iter, self.refactor_after, self.maxit))
+        it, rr = self.gmres(indptr, indices, data, b, x, maxit=budget)
+        if it:
+            self._t_iter = (time.perf_counter() - t1) / it
+        if not refactored and rr > self.rtol:
+            tf = time.perf_counter()
             self.factor(indptr, indices, data)
+            self._t_factor = time.perf_counter() - tf
             refactored = True
             t1 = time.perf_counter()
             it2, rr = self.gmres(indptr, indices, data, b, x)
