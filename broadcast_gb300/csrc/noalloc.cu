@@ -53,6 +53,18 @@ int scratch_address(double** out) {
   return bcg::BCG_OK;
 }
 
+// the array is in device memory of the current device (managed memory is
+// reachable from every device)
+bool on_current_device(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+  if (a.type == cudaMemoryTypeManaged) return true;
+  if (a.type != cudaMemoryTypeDevice) return false;
+  int dev = -1;
+  return cudaGetDevice(&dev) == cudaSuccess && a.device == dev;
+}
+
 }  // namespace
 
 extern "C" {
@@ -66,6 +78,11 @@ int bcg_flux_num_dnc5_2d_noalloc(double* residu, const double* w, const double* 
                                  double k2, double k4, int im, int jm) {
   using namespace bcg;
   (void)x0; (void)y0; (void)xc; (void)yc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail_arg("flux_num_dnc5_2d_noalloc: no CUDA device"), BCG_ERR_NODEV;
+  }
   if (gh != 3 || im < 6 || jm < 6) return fail_arg("flux_num_dnc5_2d_noalloc: need gh == 3 and im, jm >= 6");
   const size_t need = residual_scratch_doubles(im, jm, gh, 0);
   if (need > kNoAllocScratchDoubles)
@@ -73,7 +90,8 @@ int bcg_flux_num_dnc5_2d_noalloc(double* residu, const double* w, const double* 
                     "(needs 49*(im+6)*(jm+6) + 10*(im+1)*(jm+1) <= 4194304 doubles)");
   const void* arrays[] = {residu, w, nx, ny, vol, volf};
   for (const void* a : arrays)
-    if (!is_device_ptr(a)) return fail_arg("flux_num_dnc5_2d_noalloc: every array must be a device pointer");
+    if (!on_current_device(a))
+      return fail_arg("flux_num_dnc5_2d_noalloc: every array must be a device pointer on the current device");
   double* scratch = nullptr;
   int rc = scratch_address(&scratch);
   if (rc != BCG_OK) return rc;

@@ -405,7 +405,8 @@ int bcg_batch_destroy(long long plan);
  * (a framework allocator already owning the GPU's memory, a fixed memory
  * budget, loops that cannot absorb cudaMalloc's synchronisation).  Same
  * arguments and result as bcg_flux_num_dnc5_2d, but every array must be a
- * device pointer and the working storage is a fixed 32 MiB static device
+ * device pointer on the current device (-1 otherwise; -4 without a CUDA
+ * device) and the working storage is a fixed 32 MiB static device
  * array (held by every GPU that loads the library until the process exits):
  * grids need 49*(im+6)*(jm+6) + 10*(im+1)*(jm+1) <= 4194304 doubles (256 x 256
  * and 400 x 150 fit); larger ones return -1.  All calls share that array:

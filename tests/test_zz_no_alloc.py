@@ -4,9 +4,11 @@ It exists for callers that cannot have the library allocate device memory
 during a call (a framework whose allocator already owns the GPU's memory, a
 fixed memory budget, loops that cannot absorb cudaMalloc's synchronisation).
 Its scratch is a fixed static device array shared by every call, so the test
-checks two calls in a row against the regular entry point, plus the two
-rejections it documents (too large a grid, host arrays).  This file is named
-to be collected last.
+checks two calls in a row against the regular entry point -- with a changed
+state, and after a call on another grid, so that an entry of the shared
+scratch read before this call wrote it would show -- plus the two rejections
+it documents (too large a grid, host arrays).  This file is named to be
+collected last.
 """
 import numpy as np
 import pytest
@@ -67,3 +69,27 @@ def test_noalloc_rejects_oversized_grid_and_host_arrays():
                   d["volf"], 3, *[float(ph[k]) for k in PHYS], 600, 600)
     with pytest.raises(_lib.BroadcastError, match="device pointer"):
         _call("bcg_flux_num_dnc5_2d_noalloc", c, {**d, "w": c["w"]}, out)
+
+
+def test_noalloc_after_a_different_grid_and_state():
+    """A 256 x 256 cylinder call fills the shared scratch with its own values;
+    the 40 x 30 boundary layer after it, and again with its interior state
+    scaled, must each equal the regular entry point on the same state."""
+    import torch
+    from broadcast_gb300 import _lib
+    from broadcast_gb300.operator import to_host
+    _lib.load()
+    _lib.call("bcg_set_stream", torch.cuda.current_stream().cuda_stream)
+    cc, dc = _dev_case("cyl", 256, 256)
+    _call("bcg_flux_num_dnc5_2d_noalloc", cc, dc, torch.zeros_like(dc["w"]))
+    c, d = _dev_case("bl", 40, 30)
+    for scale in (1.0, 1.0005):
+        w = d["w"].clone()
+        w[:, 3:-3, 3:-3] *= scale
+        dd = {**d, "w": w}
+        ref = torch.zeros_like(w)
+        _call("bcg_flux_num_dnc5_2d", c, dd, ref)
+        out = torch.zeros_like(w)
+        _call("bcg_flux_num_dnc5_2d_noalloc", c, dd, out)
+        torch.cuda.synchronize()
+        assert H.rel_err(to_host(out), to_host(ref), H.flux_scale(c, c["w"])) < 1e-12
