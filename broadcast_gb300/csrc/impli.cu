@@ -33,6 +33,7 @@
 //       Every cell combines the same terms in the reference's order, so the
 //       result is the reference's Gauss-Seidel iterate, not a reordering.
 //   k_impli_out  the increments into dwi (ghosts stay zero).
+#include <mutex>
 #include <cooperative_groups.h>
 #include <cstdint>
 #include "dnc5.cuh"
@@ -434,10 +435,17 @@ constexpr int kMaxRowsPerCta = 96;
 // slots (2 parities x 10 values per row, padded to 16 bytes) and the rings
 size_t sweep_smem(int rb) { return ((size_t)20 * ((rb + 1) / 2 * 2) + (size_t)rb * kRing * G_NREC) * sizeof(double); }
 
-int g_cluster = 0;  // chosen cluster size (per process; the device is fixed per process here)
+// chosen cluster size per device (the function attributes are set for the
+// device current at the first call there)
+constexpr int kMaxDev = 64;
+int g_cluster[kMaxDev] = {0};
+std::mutex g_cluster_mu;
 
 int pick_cluster() {
-  if (g_cluster) return g_cluster;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) { cudaGetLastError(); return 8; }
+  std::lock_guard<std::mutex> lk(g_cluster_mu);
+  if (g_cluster[dev]) return g_cluster[dev];
   int nc = 8;
   cudaFuncSetAttribute(k_impli_sweeps, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem(kMaxRowsPerCta));
   if (cudaFuncSetAttribute(k_impli_sweeps, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
@@ -456,7 +464,7 @@ int pick_cluster() {
     if (cudaOccupancyMaxActiveClusters(&nclusters, k_impli_sweeps, &cfg) == cudaSuccess && nclusters >= 1) nc = 16;
   }
   cudaGetLastError();  // a refused query leaves the portable size
-  g_cluster = nc;
+  g_cluster[dev] = nc;
   return nc;
 }
 

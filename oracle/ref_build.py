@@ -4,6 +4,7 @@ gcc with -ffp-contract=off).
 
 Runs only where the reference checkout is present:
     python oracle/ref_build.py [reference_root]
+The root defaults to $BROADCAST_REFERENCE_ROOT, else /root/reference.
 Outputs go to oracle/_ref/ (git-ignored): libref.c, libref.so, signatures.json.
 """
 import json
@@ -14,7 +15,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-DEFAULT_REF = "/root/reference"
+DEFAULT_REF = os.environ.get("BROADCAST_REFERENCE_ROOT", "/root/reference")
 
 # (file relative to the reference root, routines taken from it)
 ROUTINES = [
