@@ -515,6 +515,23 @@ def run_jacobian_workload(args):
     bi = torch.empty(nnz_u, dtype=torch.int32, device=dev)
     bv = torch.empty(2 * 16 * nnz_u, dtype=torch.float64, device=dev)
     t_beta, _ = timed(lambda: _lib.call("bcg_csr_spanwise_beta", *bargs, bp, bi, bv, nnz_u, nb), args.steps)
+    # the same four outputs from one pass over the seeds (bcg_jacobian_span_bl_csr)
+    one = [(torch.empty(nrow + 1, dtype=torch.int32, device=dev), torch.empty(n + 0, dtype=torch.int32, device=dev),
+            torch.empty(n + 0, dtype=torch.float64, device=dev)) for n in (nnz_j, nnz_dz, nnz_dzz)]
+    tab = [np.array([o[k].data_ptr() for o in one], np.uint64) for k in range(3)]
+    caps, nnz3 = np.array([nnz_j, nnz_dz, nnz_dzz], np.int64), np.zeros(3, np.int64)
+    op_ = torch.empty(nrow + 1, dtype=torch.int32, device=dev)
+    oi, ov = torch.empty_like(bi), torch.empty_like(bv)
+    onb = np.zeros(1, np.int64)
+
+    def one_pass():
+        _lib.call("bcg_jacobian_span_bl_csr", *geo, *[float(ph[k]) for k in keys + ("k2", "k4")], im, jm, *common,
+                  2e-16, 1, tab[0], tab[1], tab[2], caps, nnz3, 16, betas.numpy(), op_, oi, ov, nnz_u, onb)
+
+    t_one, _ = timed(one_pass, args.steps)
+    same = (list(nnz3) == [nnz_j, nnz_dz, nnz_dzz] and int(onb[0]) == nnz_u
+            and all(torch.equal(a[2], b[2][:a[2].numel()]) for a, b in zip(one, (J, Dz, Dzz)))
+            and torch.equal(ov, bv))
     # reference loop through the oracle (OpenMP), a sample of seeds
     from oracle import oracle as O
     lib = O.lib(openmp=True)
@@ -540,7 +557,9 @@ def run_jacobian_workload(args):
             "value": 245 * im * jm / t_j / 1e6, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
             "config": {"grid": "boundary layer %dx%d, Mach 0.5, Re_x0 1e5, stretch 1.03, seed 3" % (im, jm),
                        "seeds": 245, "betas": 16, "steps": args.steps},
-            "seconds": {"jacobian_csr": t_j, "dz_csr": t_dz, "dzz_csr": t_dzz, "j_beta_16": t_beta},
+            "seconds": {"jacobian_csr": t_j, "dz_csr": t_dz, "dzz_csr": t_dzz, "j_beta_16": t_beta,
+                        "separate_total": t_j + t_dz + t_dzz + t_beta, "one_pass_all_four": t_one},
+            "one_pass_bit_identical": bool(same),
             "nnz": {"J": nnz_j, "Dz": nnz_dz, "Dzz": nnz_dzz, "union": nnz_u},
             "cpu_baseline": {"seconds_245_seeds": t_cpu, "kind": "port", "cores": os.cpu_count(),
                              "sample": "%d seeds of the reference loop (testvector, linearised boundary chain, "
@@ -574,10 +593,10 @@ def _flux_scale(c):
 #       python bench.py --grids 6 --steps 1 --warmup 1 --no-extras --tile 128,128,3 --cpu-seconds 1
 # divided by the capture's cells; the full batch's figures scale with its cells.
 BATCH_NCU = {
-    "fp64_inst_per_cell": {"prim": 139.0, "sensor": 175.9, "qrows": 93.3, "vpts": 48.5, "faces": 1134.4,
+    "fp64_inst_per_cell": {"prim": 139.0, "sensor": 175.9, "qrows": 93.3, "vpts": 48.5, "faces": 924.9,
                            "balance": 30.0},
-    "dram_bytes_per_cell": {"prim": 334.2, "sensor": 161.2, "qrows": 338.5, "vpts": 232.3, "faces": 980.6,
-                            "balance": 219.7},
+    "dram_bytes_per_cell": {"prim": 334.4, "sensor": 161.2, "qrows": 338.6, "vpts": 232.0, "faces": 886.3,
+                            "balance": 219.4},
     "source": "ncu sm__inst_executed_pipe_fp64.sum x 32 lanes and dram__bytes_read.sum + dram__bytes_write.sum "
               "per k_batch launch, first 6 grids (1,344,226 cells), cold caches; per cell, scaled to this run's "
               "cells",
@@ -1017,14 +1036,16 @@ def run_newton_workload(args):
     import torch
     from broadcast_gb300 import cases
     from broadcast_gb300.newton import BLNewton, CylNewton
-    if args.case == "cyl":  # cylinder.py:841-1068 on the 256 x 256 O-mesh, Newton (cfl 1e10)
-        im, jm = args.im or 256, args.jm or 256
+    cyl = args.case == "cyl"
+    im, jm = args.im or (256 if cyl else 400), args.jm or (256 if cyl else 150)
+    # GMRES with the FP32 band-LU preconditioner above 20,000 cells unless --solver band
+    krylov = args.solver == "krylov" or (args.solver == "auto" and im * jm > 20000)
+    if cyl:  # cylinder.py:841-1068 on the 256 x 256 O-mesh, Newton (cfl 1e10)
         c = cases.cyl_case(im, jm, ops=LibOps)
-        nt = CylNewton(c, solver="krylov" if args.solver == "krylov" else None)
+        nt = CylNewton(c, solver="krylov" if krylov else None)
     else:
-        im, jm = args.im or 400, args.jm or 150
         c = cases.bl_case(im, jm, seed=0, ops=LibOps)
-        nt = BLNewton(c, solver="krylov") if args.solver == "krylov" else BLNewton(c)
+        nt = BLNewton(c, solver="krylov") if krylov else BLNewton(c)
     w = c["w"].copy(order="F")
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -1056,7 +1077,7 @@ def run_newton_workload(args):
             "seconds_per_iteration": {"total": mean("seconds"), "fills_residual_norms": mean("seconds_residual"),
                                       "jacobian_245_seeds": mean("seconds_jacobian"),
                                       "linear_solve": mean("seconds_solve")},
-            "linear_solver": ("FP64 band LU (cuSOLVER getrf panels, cuBLAS trsm/gemm)" if args.solver != "krylov" else
+            "linear_solver": ("FP64 band LU (cuSOLVER getrf panels, cuBLAS trsm/gemm)" if not krylov else
                               "FP64 GMRES, FP32 band LU preconditioner reused across iterations"),
             "krylov": getattr(nt.solver, "log", None),
             "jacobian_nnz": hist[-1]["nnz"],

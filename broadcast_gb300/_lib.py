@@ -79,6 +79,7 @@ SIGNATURES = {
     "bcg_coeffs_5p_dz2": "ppp" + "pppppppp" + "i" + "d" * 9 + "ii",
     "bcg_coeffs_5p_dz_dn": "pppi" + "pppppppp" + "i" + "d" * 9 + "ii",
     "bcg_coeffs_5p_dz2_dn": "pppi" + "pppppppp" + "i" + "d" * 9 + "ii",
+    "bcg_jacobian_span_bl_csr": "pppppi" + "d" * 11 + "ii" + "pppp" + "pipi" + "di" + "ppppp" + "ippppLp",
     "bcg_batch_create": "ipppip",
     "bcg_batch_set_arrays": "L" + "p" * 8,
     "bcg_batch_configure": "Liii",

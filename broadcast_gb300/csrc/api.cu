@@ -1118,6 +1118,91 @@ extern "C" int bcg_jacobian_dz_bl_csr(const double* w, const double* nx, const d
                          lm_field, wbd, lm_wbd, nullptr, mini, 0, indptr, indices, data, capacity, nnz);
 }
 
+// ---- J, Dz and Dzz from one pass over the seeds, J(beta) as the epilogue ------
+// (BROADCAST_npz.py:1068-1137 and 1221-1249, biglobal.py:82): the seeds and
+// their linearised boundary chain once, then the residual tangent and both
+// spanwise operators of every seeded state; device outputs only.
+extern "C" int bcg_jacobian_span_bl_csr(const double* w, const double* nx, const double* ny, const double* vol,
+                                        const double* volf, int gh, double cp, double cv, double prandtl, double gam,
+                                        double rgaz, double cs, double muref, double tref, double s_suth, double k2,
+                                        double k4, int im, int jm, const int* interf_ilo, const int* interf_jhi,
+                                        const int* interf_ihi, const int* interf_jlo, const double* field,
+                                        int lm_field, const double* wbd, int lm_wbd, double mini, int divide_by_vol,
+                                        const unsigned long long* indptr3, const unsigned long long* indices3,
+                                        const unsigned long long* data3, const long long* capacity3, long long* nnz3,
+                                        int nbeta, const double* betas, int* b_indptr, int* b_indices,
+                                        double* b_values, long long b_capacity, long long* b_nnz) {
+  if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
+  if (!dims_ok(im, jm, gh)) return fail_arg("jacobian: need gh == 3 and im, jm >= 6");
+  if (!indptr3 || !indices3 || !data3 || !capacity3 || !nnz3 || !interf_ilo || !interf_jhi || !interf_ihi ||
+      !interf_jlo)
+    return fail_arg("jacobian_span: null argument");
+  for (int k = 0; k < 3; ++k)
+    if (!is_device_ptr((const void*)indptr3[k]) || !is_device_ptr((const void*)indices3[k]) ||
+        !is_device_ptr((const void*)data3[k]))
+      return fail_arg("jacobian_span: the CSR outputs must be device arrays");
+  if (nbeta > 0 && (!betas || !b_nnz || !is_device_ptr(b_indptr) || !is_device_ptr(b_indices) ||
+                    !is_device_ptr(b_values)))
+    return fail_arg("jacobian_span: J(beta) needs host betas and device outputs");
+  const size_t np = ncell(im, jm, gh), nn = nnode(im, jm, gh);
+  cudaStream_t st = current_stream();
+  Stager sg(st);
+  const int hw = sg.in(w, np * 5 * 8), hnx = sg.in(nx, nn * 2 * 8), hny = sg.in(ny, nn * 2 * 8);
+  const int hvol = sg.in(vol, np * 8), hvolf = sg.in(volf, np * 2 * 8);
+  const int hf = sg.in(field, (size_t)lm_field * gh * 5 * 8), hb = sg.in(wbd, (size_t)lm_wbd * 5 * 8);
+  int rc = sg.commit();
+  if (rc) return rc;
+  JacobianArgs a{};
+  a.im = im; a.jm = jm; a.gh = gh;
+  a.phys = Phys{cp, cv, prandtl, gam, rgaz, cs, muref, tref, s_suth, k2, k4};
+  a.w = sg.dev<double>(hw); a.nx = sg.dev<double>(hnx); a.ny = sg.dev<double>(hny);
+  a.vol = sg.dev<double>(hvol); a.volf = sg.dev<double>(hvolf);
+  a.relaxed = 0; a.coefdiag = nullptr; a.mini = mini;
+  a.nops = 3;
+  const int ops[3] = {0, SPAN_DZ, SPAN_DZZ};
+  for (int k = 0; k < 3; ++k) {
+    a.ops[k] = ops[k];
+    a.divide_v[k] = k == 0 ? divide_by_vol : 0;
+    a.indptr_v[k] = (int*)indptr3[k]; a.indices_v[k] = (int*)indices3[k]; a.data_v[k] = (double*)data3[k];
+    a.capacity_v[k] = capacity3[k]; a.nnz_v[k] = nnz3 + k;
+  }
+  const struct { int kind; const char* loc; const int* it; const double* aux; int lm; } chain[4] = {
+      {BC_INLET, "Ilo", interf_ilo, sg.dev<double>(hf), lm_field}, {BC_NOREF, "Jhi", interf_jhi, sg.dev<double>(hb), lm_wbd},
+      {BC_EXTRAP, "Ihi", interf_ihi, nullptr, 0}, {BC_WALL, "Jlo", interf_jlo, nullptr, 0}};
+  for (const auto& c : chain) {
+    BcArgs b{};
+    b.kind = c.kind; b.im = im; b.jm = jm; b.gh = gh; b.em = 5; b.lm = c.lm; b.gam = gam; b.aux = c.aux;
+    b.nx = a.nx; b.ny = a.ny;
+    if (!make_side(c.loc, c.it, &b.side) || !side_in_bounds(b.side, im, jm, gh))
+      return fail_arg("jacobian_span: bad interface");
+    a.bcs.push_back(b);
+  }
+  a.scratch = (double*)pool_get(POOL_SCRATCH, jacobian_scratch_doubles(im, jm, gh, 1, 3) * 8);
+  a.iscratch = (int*)pool_get(POOL_AUX, jacobian_iscratch_ints(im, jm) * 4);
+  if (!a.scratch || !a.iscratch) return fail_arg("jacobian_span: scratch allocation failed"), BCG_ERR_NOMEM;
+  rc = run_jacobian(a, st);
+  if (rc) return rc;
+  if (nbeta > 0) {
+    const int nrow = 5 * im * jm;
+    CsrBetaArgs ba{};
+    ba.nrow = nrow;
+    ba.j_p = a.indptr_v[0]; ba.j_i = a.indices_v[0]; ba.j_v = a.data_v[0];
+    ba.dz_p = a.indptr_v[1]; ba.dz_i = a.indices_v[1]; ba.dz_v = a.data_v[1];
+    ba.dzz_p = a.indptr_v[2]; ba.dzz_i = a.indices_v[2]; ba.dzz_v = a.data_v[2];
+    ba.nbeta = nbeta;
+    double* dbeta = (double*)pool_get(POOL_STAGE_OUT, (size_t)nbeta * 8);
+    int* bscr = (int*)pool_get(POOL_AUX, csr_beta_iscratch_ints(nrow) * 4);
+    if (!dbeta || !bscr) return fail_arg("jacobian_span: scratch allocation failed"), BCG_ERR_NOMEM;
+    cudaError_t e = cudaMemcpyAsync(dbeta, betas, (size_t)nbeta * 8, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return fail_cuda("jacobian_span: betas", e);
+    ba.betas = dbeta; ba.indptr = b_indptr; ba.indices = b_indices; ba.values = b_values; ba.capacity = b_capacity;
+    ba.nnz = b_nnz; ba.iscratch = bscr;
+    rc = run_csr_beta(ba, st);
+    if (rc) return rc;
+  }
+  return sg.finish();
+}
+
 // ---- J(beta) = J - beta^2 Dzz + i beta Dz (biglobal.py:82) -------------------
 // Three CSR matrices of nrow rows (sorted columns) combine on the union of
 // their patterns for nbeta wavenumbers; values hold nbeta planes of nnz complex

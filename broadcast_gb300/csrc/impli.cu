@@ -188,6 +188,8 @@ __global__ void __launch_bounds__(256) k_impli_out(ImpliK k) {
 // the boundary cells, so they are formed once per sweep, in parallel.
 enum RingField { G_REC = 0, G_CARRY = 34, G_GI = 44, G_GJ = 50, G_NREC = 60 };
 enum GhostTerm { T_ROW = 6, T_COL = 10 };  // doubles per row (i-face) and per column (j-face)
+constexpr int kLanes = 8;          // threads per grid row in the sweep kernel (variables on 0..4)
+constexpr int kMaxRowsPerCta = 64; // rows per CTA: 512 threads
 constexpr int kDepth = 2;          // prefetch distance in steps
 constexpr int kRing = kDepth + 1;  // entries per thread
 
@@ -206,26 +208,20 @@ __device__ __forceinline__ int step_cell(const Ext& e, int j, int t, bool fwd) {
   return (i >= 1 && i <= e.im) ? i : 0;
 }
 
-// queue the copies of cell (i, j)'s ring entry
-__device__ __forceinline__ void prefetch(const ImpliK& k, double* ent, int i, int j, bool fwd) {
+// queue thread v's share of the copies of cell (i, j)'s ring entry (the
+// row's kLanes threads take the 16-byte chunks in turn)
+__device__ __forceinline__ void prefetch(const ImpliK& k, double* ent, int i, int j, bool fwd, int v) {
   const Ext& e = k.e;
   const double* r = k.rec + (size_t)e.cidx(i, j) * C_NREC;
 #pragma unroll
-  for (int c = 0; c < C_NREC; c += 2) cp16(ent + G_REC + c, r + c);
+  for (int c = v; c < C_NREC / 2; c += kLanes) cp16(ent + G_REC + 2 * c, r + 2 * c);
   if (i != (fwd ? 1 : e.im)) {
-    const double* cr = k.carry + (size_t)e.cidx(i, j) * K_NREC;
-#pragma unroll
-    for (int c = 0; c < K_NREC; c += 2) cp16(ent + G_CARRY + c, cr + c);
-  } else {  // i-face ghost term of the row
-    const double* g = k.gterm + (size_t)(j - 1) * T_ROW;
-#pragma unroll
-    for (int c = 0; c < T_ROW; c += 2) cp16(ent + G_GI + c, g + c);
+    if (v < K_NREC / 2) cp16(ent + G_CARRY + 2 * v, k.carry + (size_t)e.cidx(i, j) * K_NREC + 2 * v);
+  } else if (v < T_ROW / 2) {  // i-face ghost term of the row
+    cp16(ent + G_GI + 2 * v, k.gterm + (size_t)(j - 1) * T_ROW + 2 * v);
   }
-  if (j == (fwd ? 1 : e.jm)) {  // j-face ghost term of the column
-    const double* g = k.gterm + (size_t)e.jm * T_ROW + (size_t)(i - 1) * T_COL;
-#pragma unroll
-    for (int c = 0; c < T_COL; c += 2) cp16(ent + G_GJ + c, g + c);
-  }
+  if (j == (fwd ? 1 : e.jm) && v < T_COL / 2)  // j-face ghost term of the column
+    cp16(ent + G_GJ + 2 * v, k.gterm + (size_t)e.jm * T_ROW + (size_t)(i - 1) * T_COL + 2 * v);
 }
 
 // F(w + dw) - F(w), G(w + dw) - G(w) of a cell from its w, f, g (at wfg) and dw
@@ -296,32 +292,46 @@ __device__ __forceinline__ void ghost_terms(const ImpliK& k, bool fwd, double mu
 }
 
 // all lmax sweeps; launched as exactly one cluster of gridDim.x CTAs of
-// blockDim.x threads, thread (CTA c, lane t) owning row j = c*blockDim.x + t + 1.
-// Every thread runs the same sequence of cluster barrier arrives and waits
-// (no early exit); the last wait follows the last shared-memory access.
-__global__ void __launch_bounds__(96) k_impli_sweeps(ImpliK k) {
+// blockDim.x = kLanes * rb threads: the kLanes threads (r*kLanes .. r*kLanes+7)
+// of CTA c own grid row j = c*rb + r + 1, thread v < 5 of a row its variable
+// v+1.  A cell's update is per variable except F(w + dwi) and G(w + dwi),
+// which need the cell's five w + dwi: the row's threads exchange them by warp
+// shuffles (a row's threads are one 8-lane segment of a warp) and each
+// variable's thread forms the pressure and velocities, then its own flux
+// components, in the reference's operations.  Every thread runs the same
+// sequence of cluster barrier arrives and waits (no early exit); the last
+// wait follows the last shared-memory access.
+__global__ void __launch_bounds__(kLanes * kMaxRowsPerCta) k_impli_sweeps(ImpliK k) {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
   extern __shared__ __align__(16) double smem[];
   const Ext& e = k.e;
-  const int rb = (int)blockDim.x, lane = (int)threadIdx.x, rank = (int)cl.block_rank();
+  const int rb = (int)blockDim.x / kLanes, rank = (int)cl.block_rank();
   const int nc = (int)gridDim.x;
-  const int j = rank * rb + lane + 1;
+  const int r = (int)threadIdx.x / kLanes, v = (int)threadIdx.x % kLanes;
+  const bool var = v < 5;
+  const int seg = (int)threadIdx.x & 31 & ~(kLanes - 1);  // the row's first lane in its warp
+  const unsigned rowmask = 0xffu << seg;
+  // the warp's threads (the last warp of a CTA may hold 8, 16 or 24)
+  const int wbase = (int)threadIdx.x & ~31, nwarp = min(32, (int)blockDim.x - wbase);
+  const unsigned warpmask = nwarp == 32 ? 0xffffffffu : (1u << nwarp) - 1u;
+  const int j = rank * rb + r + 1;
   const bool row = j <= e.jm;
-  double* slots = smem;                                                   // [2][10][rb]
-  double* ring = smem + (size_t)20 * ((rb + 1) / 2 * 2) + (size_t)lane * kRing * G_NREC;
+  double* slots = smem;                                                // [2][10][rb]
+  double* ring = smem + (size_t)20 * ((rb + 1) / 2 * 2) + (size_t)r * kRing * G_NREC;
   auto slot = [&](double* base, int par, int c, int t) -> double* { return base + ((size_t)par * 10 + c) * rb + t; };
-  double* prev_base = lane > 0 ? slots : (rank > 0 ? cl.map_shared_rank(slots, rank - 1) : nullptr);
-  const int prev_t = lane > 0 ? lane - 1 : rb - 1;
-  double* next_base = lane < rb - 1 ? slots : (rank < nc - 1 ? cl.map_shared_rank(slots, rank + 1) : nullptr);
-  const int next_t = lane < rb - 1 ? lane + 1 : 0;
+  double* prev_base = r > 0 ? slots : (rank > 0 ? cl.map_shared_rank(slots, rank - 1) : nullptr);
+  const int prev_t = r > 0 ? r - 1 : rb - 1;
+  double* next_base = r < rb - 1 ? slots : (rank < nc - 1 ? cl.map_shared_rank(slots, rank + 1) : nullptr);
+  const int next_t = r < rb - 1 ? r + 1 : 0;
   const int nstep = e.im + e.jm - 1;
-  // dwi and carry-over of this row's last cell (the next sweep's first cell)
-  double last_dw[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, last_ss[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  // deferred store of the previous step's carry
+  const int vv = var ? v : 0;  // the variable of this thread (threads 5..7 of a row hold none)
+  // carry-over of this row's last cell of the sweep (the next sweep's first)
+  double last_ss = 0.0;
+  // deferred store of the previous step's carry (this thread's variable)
   double* pend = nullptr;
-  double pend_v[K_NREC];
-  const int tid = rank * rb + lane, nthr = nc * rb;
+  double pend_dw = 0.0, pend_ss = 0.0;
+  const int tid = rank * (int)blockDim.x + (int)threadIdx.x, nthr = nc * (int)blockDim.x;
   cluster_arrive();  // pairs with the first wait
   for (int l = 1; l <= k.lmax; ++l) {
     const bool fwd = (l & 1) != 0;
@@ -329,8 +339,8 @@ __global__ void __launch_bounds__(96) k_impli_sweeps(ImpliK k) {
     const int fo = fwd ? C_FWD : C_BWD;
     cluster_wait();  // the previous sweep's last step
     if (pend) {      // every carry of the previous sweep in memory
-#pragma unroll
-      for (int v = 0; v < K_NREC; v += 2) *reinterpret_cast<double2*>(pend + v) = make_double2(pend_v[v], pend_v[v + 1]);
+      pend[K_DWI + vv] = pend_dw;
+      pend[K_SSOR + vv] = pend_ss;
       pend = nullptr;
     }
     cluster_arrive();
@@ -342,95 +352,94 @@ __global__ void __launch_bounds__(96) k_impli_sweeps(ImpliK k) {
 #pragma unroll
     for (int t = 0; t < kDepth; ++t) {
       const int i = row ? step_cell(e, j, t, fwd) : 0;
-      if (i) prefetch(k, ring + (t % kRing) * G_NREC, i, j, fwd);
+      if (i) prefetch(k, ring + (t % kRing) * G_NREC, i, j, fwd, v);
       cp_commit();
     }
-    double ci[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // a + b of the i-face term for this row's next cell
+    double ci = 0.0;  // a + b of the i-face term of this row's next cell (this thread's variable)
     for (int t = 0; t < nstep; ++t) {
       const int par = t & 1;
       const int i = row ? step_cell(e, j, t, fwd) : 0;
-      cp_wait_depth();           // this step's entry has landed
+      cp_wait_depth();  // this thread's copies of this step's entry have landed
+      __syncwarp(warpmask);  // and the other seven threads' copies of the row's entry
       if (t > 0) cluster_wait();  // the neighbouring rows' slots of step t-1 are written
-      if (i) {
+      if (i) {  // the same for the row's kLanes threads
         const double* ent = ring + (t % kRing) * G_NREC;
-        const double* r = ent + G_REC;
+        const double* rr = ent + G_REC;
         const bool first = i == (fwd ? 1 : e.im);
-        double dwo[5], sso[5];
-#pragma unroll
-        for (int v = 0; v < 5; ++v) {
-          dwo[v] = first ? last_dw[v] : ent[G_CARRY + K_DWI + v];
-          sso[v] = first ? last_ss[v] : ent[G_CARRY + K_SSOR + v];
-        }
-        double df[5], dg[5], a[5], b[5];
-        if (first) {  // i-face term from the ghost cell
-#pragma unroll
-          for (int v = 0; v < 5; ++v) ci[v] = ent[G_GI + v];
-        }
-        double aj[5], bj[5];
-        if (j == (fwd ? 1 : e.jm)) {  // j-face term from the ghost row
-#pragma unroll
-          for (int v = 0; v < 5; ++v) { aj[v] = ent[G_GJ + v]; bj[v] = ent[G_GJ + 5 + v]; }
-        } else {
-          const double* nb = fwd ? prev_base : next_base;
-          const int nt = fwd ? prev_t : next_t;
-#pragma unroll
-          for (int v = 0; v < 5; ++v) {
-            aj[v] = *slot(const_cast<double*>(nb), par ^ 1, v, nt);
-            bj[v] = *slot(const_cast<double*>(nb), par ^ 1, 5 + v, nt);
+        // the update (lhs/impli_matrix_free.F90:199-222) of this thread's variable
+        double ssn = 0.0, dwn = 0.0, wv = 0.0;
+        if (var) {
+          const double sso = first ? last_ss : ent[G_CARRY + K_SSOR + v];
+          if (first) ci = ent[G_GI + v];  // i-face term from the ghost cell
+          double aj, bj;
+          if (j == (fwd ? 1 : e.jm)) {  // j-face term from the ghost row
+            aj = ent[G_GJ + v];
+            bj = ent[G_GJ + 5 + v];
+          } else {
+            const double* nb = fwd ? prev_base : next_base;
+            const int nt = fwd ? prev_t : next_t;
+            aj = *slot(const_cast<double*>(nb), par ^ 1, v, nt);
+            bj = *slot(const_cast<double*>(nb), par ^ 1, 5 + v, nt);
           }
+          ssn = ((ci + aj) + bj) * rr[C_TAU0];
+          dwn = (ssn + (rr[C_D1W + v] + sso)) * rr[C_CDM1];
+          wv = rr[C_W + v] + dwn;
         }
-        // the update (lhs/impli_matrix_free.F90:199-222)
-        const double tau0 = r[C_TAU0], cdiagm1 = r[C_CDM1];
-        double dwn[5], ssn[5];
+        // the cell's w + dwi on every thread of the row
+        double wi[5];
 #pragma unroll
-        for (int v = 0; v < 5; ++v) {
-          ssn[v] = ((ci[v] + aj[v]) + bj[v]) * tau0;
-          dwn[v] = (ssn[v] + (r[C_D1W + v] + sso[v])) * cdiagm1;
-        }
-        // this cell's terms for its downstream faces
-        flux_delta(k, r, dwn, df, dg);
-        if (fwd ? j < e.jm : j > 1) {
-          face_term(r + fo + 3, df, dg, dwn, multi, a, b);
-#pragma unroll
-          for (int v = 0; v < 5; ++v) {
-            *slot(slots, par, v, lane) = a[v];
-            *slot(slots, par, 5 + v, lane) = b[v];
+        for (int m = 0; m < 5; ++m) wi[m] = __shfl_sync(rowmask, wv, seg + m);
+        if (var) {
+          // this variable of F(w + dwi) - F(w), G(w + dwi) - G(w)
+          const double rhom1 = __drcp_rn(wi[0]);  // correctly rounded, as 1/wi(1)
+          const double velxi = wi[1] * rhom1, velyi = wi[2] * rhom1, velzi = wi[3] * rhom1;
+          const double pint = k.gam1 * (wi[4] - 0.5 * wi[0] * (velxi * velxi + velyi * velyi + velzi * velzi));
+          const double hp = wi[4] + pint;
+          // fi = (wi2, wi2 u + p, wi2 v, wi2 w, u (wi5 + p)), gi = (wi3, wi3 u, wi3 v + p, wi3 w, v (wi5 + p))
+          const double fa = v == 4 ? hp : wi[1], ga = v == 4 ? hp : wi[2];
+          const double fm = v == 0 ? 1.0 : (v == 1 || v == 4) ? velxi : v == 2 ? velyi : velzi;
+          const double gm = v == 0 ? 1.0 : v == 1 ? velxi : (v == 2 || v == 4) ? velyi : velzi;
+          const double fi = fa * fm + (v == 1 ? pint : 0.0), gi = ga * gm + (v == 2 ? pint : 0.0);
+          const double df = fi - rr[C_F + v], dg = gi - rr[C_G + v];
+          // this cell's terms for its downstream faces
+          // (lhs/impli_matrix_free.F90:186-190): a = multi (dF nx + dG ny), b = coef dw
+          if (fwd ? j < e.jm : j > 1) {
+            const double* fc = rr + fo + 3;
+            *slot(slots, par, v, r) = multi * (df * fc[0] + dg * fc[1]);
+            *slot(slots, par, 5 + v, r) = fc[2] * dwn;
           }
-        }
-        if (fwd ? i < e.im : i > 1) {
-          face_term(r + fo, df, dg, dwn, multi, a, b);
-#pragma unroll
-          for (int v = 0; v < 5; ++v) ci[v] = a[v] + b[v];
-        } else {  // the row's last cell of this sweep: the next sweep's first
-#pragma unroll
-          for (int v = 0; v < 5; ++v) { last_dw[v] = dwn[v]; last_ss[v] = ssn[v]; }
+          if (fwd ? i < e.im : i > 1) {
+            const double* fc = rr + fo;
+            ci = multi * (df * fc[0] + dg * fc[1]) + fc[2] * dwn;
+          } else {  // the row's last cell of this sweep: the next sweep's first
+            last_ss = ssn;
+          }
         }
         cluster_arrive();
         if (pend) {
-#pragma unroll
-          for (int v = 0; v < K_NREC; v += 2) *reinterpret_cast<double2*>(pend + v) = make_double2(pend_v[v], pend_v[v + 1]);
+          pend[K_DWI + vv] = pend_dw;
+          pend[K_SSOR + vv] = pend_ss;
         }
-        pend = k.carry + (size_t)e.cidx(i, j) * K_NREC;
-#pragma unroll
-        for (int v = 0; v < 5; ++v) { pend_v[K_DWI + v] = dwn[v]; pend_v[K_SSOR + v] = ssn[v]; }
+        pend = var ? k.carry + (size_t)e.cidx(i, j) * K_NREC : nullptr;
+        pend_dw = dwn;
+        pend_ss = ssn;
       } else {
         cluster_arrive();
       }
       // the entry of step t + kDepth
       const int in = (row && t + kDepth < nstep) ? step_cell(e, j, t + kDepth, fwd) : 0;
-      if (in) prefetch(k, ring + ((t + kDepth) % kRing) * G_NREC, in, j, fwd);
+      if (in) prefetch(k, ring + ((t + kDepth) % kRing) * G_NREC, in, j, fwd, v);
       cp_commit();
     }
   }
   if (pend) {
-#pragma unroll
-    for (int v = 0; v < K_NREC; v += 2) *reinterpret_cast<double2*>(pend + v) = make_double2(pend_v[v], pend_v[v + 1]);
+    pend[K_DWI + vv] = pend_dw;
+    pend[K_SSOR + vv] = pend_ss;
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
   cluster_wait();  // pairs with the last arrive; no CTA leaves while its slots may be read
 }
 
-constexpr int kMaxRowsPerCta = 96;
 
 // slots (2 parities x 10 values per row, padded to 16 bytes) and the rings
 size_t sweep_smem(int rb) { return ((size_t)20 * ((rb + 1) / 2 * 2) + (size_t)rb * kRing * G_NREC) * sizeof(double); }
@@ -451,7 +460,7 @@ int pick_cluster() {
   if (cudaFuncSetAttribute(k_impli_sweeps, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(16);
-    cfg.blockDim = dim3(kMaxRowsPerCta);
+    cfg.blockDim = dim3(kMaxRowsPerCta * kLanes);
     cfg.dynamicSmemBytes = sweep_smem(kMaxRowsPerCta);
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -510,7 +519,7 @@ cudaError_t run_impli(const ImpliArgs& a, cudaStream_t st) {
   if (err != cudaSuccess || a.lmax < 1) return err;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)nc);
-  cfg.blockDim = dim3((unsigned)rb);
+  cfg.blockDim = dim3((unsigned)(rb * kLanes));
   cfg.dynamicSmemBytes = sweep_smem(rb);
   cfg.stream = st;
   cudaLaunchAttribute at[1];

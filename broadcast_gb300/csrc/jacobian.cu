@@ -196,10 +196,10 @@ static int jacobian_groups(int im, int jm, int gh) {
   return (int)std::max<size_t>(1, std::min<size_t>(61, g));
 }
 
-size_t jacobian_scratch_doubles(int im, int jm, int gh, int nzone) {
+size_t jacobian_scratch_doubles(int im, int jm, int gh, int nzone, int nops) {
   const size_t np = (size_t)(im + 2 * gh) * (jm + 2 * gh);
   const size_t G = (size_t)jacobian_groups(im, jm, gh);
-  return 245 * (size_t)nzone * np * 5  // tangent outputs of every seed (per zone)
+  return 245 * (size_t)nzone * (size_t)nops * np * 5  // outputs of every seed (per zone and operator)
          + 4 * G * np * 5  // seeded tangent states of G groups
          + np * 5          // state copy written by the linearised boundary fills
          + G * residual_scratch_doubles(im, jm, gh, 4);
@@ -209,8 +209,12 @@ int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
   const int im = a.im, jm = a.jm, gh = a.gh;
   const size_t np = (size_t)(im + 2 * gh) * (jm + 2 * gh);
   const int nzone = a.nzone == 2 ? 2 : 1, nseed = 245 * nzone;
-  double* resd_all = a.scratch;
-  double* wd4 = resd_all + (size_t)nseed * np * 5;
+  const int nop = a.nops > 0 ? a.nops : 1;
+  int opv[3] = {a.op, 0, 0};
+  for (int k = 0; k < a.nops; ++k) opv[k] = a.ops[k];
+  double* resd_all = a.scratch;  // nop blocks of nseed seed outputs
+  const size_t oblk = (size_t)nseed * np * 5;
+  double* wd4 = resd_all + (size_t)nop * oblk;
   double* wcopy = wd4 + 4 * (size_t)jacobian_groups(im, jm, gh) * np * 5;
   double* rscr = wcopy + np * 5;
   int* seeds_dev = a.iscratch;                        // 2 x 245 x 4
@@ -261,43 +265,57 @@ int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
         e = launch_jn_match(jn, st);
         if (e != cudaSuccess) return fail_cuda("jacobian: periodic join", e);
       }
-    if (a.op == 0) {
-      ra.ndir = kk; ra.ngroup = ng;
-      ra.wd = wd4;
-      ra.resd = resd_all + (size_t)s0 * np * 5;
-      e = run_residual(ra, st);
-      if (e != cudaSuccess) return fail_cuda("jacobian: tangent residual", e);
-    } else {
-      for (int g = 0; g < ng; ++g) {
-        SpanArgs sa{};
-        sa.im = im; sa.jm = jm; sa.gh = gh; sa.op = a.op; sa.ndir = kk; sa.phys = a.phys; sa.w = wcopy;
-        sa.wd = wd4 + (size_t)g * kk * np * 5; sa.dstride = np * 5; sa.nx = a.nx; sa.ny = a.ny; sa.vol = a.vol;
-        sa.out = resd_all + (size_t)(s0 + g * kk) * np * 5;
-        e = run_span(sa, st);
-        if (e != cudaSuccess) return fail_cuda("jacobian: spanwise operator", e);
+    for (int k = 0; k < nop; ++k) {
+      double* outk = resd_all + (size_t)k * oblk;
+      if (opv[k] == 0) {
+        ra.ndir = kk; ra.ngroup = ng;
+        ra.wd = wd4;
+        ra.resd = outk + (size_t)s0 * np * 5;
+        e = run_residual(ra, st);
+        if (e != cudaSuccess) return fail_cuda("jacobian: tangent residual", e);
+      } else {
+        for (int g = 0; g < ng; ++g) {
+          SpanArgs sa{};
+          sa.im = im; sa.jm = jm; sa.gh = gh; sa.op = opv[k]; sa.ndir = kk; sa.phys = a.phys; sa.w = wcopy;
+          sa.wd = wd4 + (size_t)g * kk * np * 5; sa.dstride = np * 5; sa.nx = a.nx; sa.ny = a.ny; sa.vol = a.vol;
+          sa.out = outk + (size_t)(s0 + g * kk) * np * 5;
+          e = run_span(sa, st);
+          if (e != cudaSuccess) return fail_cuda("jacobian: spanwise operator", e);
+        }
       }
     }
     s0 += ns;
   }
-  // CSR: count, scan, fill
+  // CSR of each operator: count, scan, fill
   const int B = 128;
-  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(0, a.op, a.withjn, nzone, resd_all, gh, im, jm, a.relaxed, a.coefdiag,
-                                             a.mini, a.divide_by_vol ? a.vol : nullptr, count, nullptr, nullptr, nullptr);
-  k_scan_block<<<nb, kScanBlock, 0, st>>>(count, rowptr, bsum, nrow);
-  k_scan_sums<<<1, 1, 0, st>>>(bsum, nb, total);
-  k_scan_add<<<(nrow + 1 + 255) / 256, 256, 0, st>>>(rowptr, bsum, nrow, total);
-  long long nnz = 0;
-  e = cudaMemcpyAsync(&nnz, total, sizeof nnz, cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess) return fail_cuda("jacobian: nnz", e);
-  *a.nnz = nnz;
-  if (nnz > a.capacity) return fail_arg("jacobian: CSR capacity too small (see nnz)");
-  if (nnz >= (1LL << 31)) return fail_arg("jacobian: nnz exceeds 32-bit CSR indices");
-  k_ptr_to_int<<<(nrow + 1 + 255) / 256, 256, 0, st>>>(rowptr, a.indptr, nrow);
-  k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(1, a.op, a.withjn, nzone, resd_all, gh, im, jm, a.relaxed, a.coefdiag,
-                                             a.mini, a.divide_by_vol ? a.vol : nullptr, count, rowptr, a.indices, a.data);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return fail_cuda("jacobian: csr", e);
+  for (int k = 0; k < nop; ++k) {
+    const double* outk = resd_all + (size_t)k * oblk;
+    const int opk = opv[k];
+    const int relaxed = opk == 0 ? a.relaxed : 0;
+    const int divide = a.nops > 0 ? a.divide_v[k] : a.divide_by_vol;
+    int* indptr = a.nops > 0 ? a.indptr_v[k] : a.indptr;
+    int* indices = a.nops > 0 ? a.indices_v[k] : a.indices;
+    double* data = a.nops > 0 ? a.data_v[k] : a.data;
+    const long long capacity = a.nops > 0 ? a.capacity_v[k] : a.capacity;
+    long long* nnz_out = a.nops > 0 ? a.nnz_v[k] : a.nnz;
+    k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(0, opk, a.withjn, nzone, outk, gh, im, jm, relaxed, a.coefdiag,
+                                               a.mini, divide ? a.vol : nullptr, count, nullptr, nullptr, nullptr);
+    k_scan_block<<<nb, kScanBlock, 0, st>>>(count, rowptr, bsum, nrow);
+    k_scan_sums<<<1, 1, 0, st>>>(bsum, nb, total);
+    k_scan_add<<<(nrow + 1 + 255) / 256, 256, 0, st>>>(rowptr, bsum, nrow, total);
+    long long nnz = 0;
+    e = cudaMemcpyAsync(&nnz, total, sizeof nnz, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail_cuda("jacobian: nnz", e);
+    *nnz_out = nnz;
+    if (nnz > capacity) return fail_arg("jacobian: CSR capacity too small (see nnz)");
+    if (nnz >= (1LL << 31)) return fail_arg("jacobian: nnz exceeds 32-bit CSR indices");
+    k_ptr_to_int<<<(nrow + 1 + 255) / 256, 256, 0, st>>>(rowptr, indptr, nrow);
+    k_csr_rows<<<(nrow + B - 1) / B, B, 0, st>>>(1, opk, a.withjn, nzone, outk, gh, im, jm, relaxed, a.coefdiag,
+                                               a.mini, divide ? a.vol : nullptr, count, rowptr, indices, data);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail_cuda("jacobian: csr", e);
+  }
   return BCG_OK;
 }
 

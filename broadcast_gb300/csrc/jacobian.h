@@ -34,6 +34,17 @@ struct JacobianArgs {
   long long* nnz;           // host: number of stored entries
   double* scratch;          // jacobian_scratch_doubles
   int* iscratch;            // jacobian_iscratch_ints
+  // several operators from one pass over the seeds (nops > 0: op, the output
+  // fields above and divide_by_vol are replaced by these; relaxed applies to
+  // the residual tangent only)
+  int nops;
+  int ops[3];
+  int divide_v[3];
+  int* indptr_v[3];
+  int* indices_v[3];
+  double* data_v[3];
+  long long capacity_v[3];
+  long long* nnz_v[3];
 };
 
 // J(beta) = J - beta^2 Dzz + i beta Dz on the union pattern (biglobal.py:82);
@@ -55,7 +66,7 @@ struct CsrBetaArgs {
 int run_csr_beta(const CsrBetaArgs& a, cudaStream_t st);
 size_t csr_beta_iscratch_ints(int nrow);
 
-size_t jacobian_scratch_doubles(int im, int jm, int gh, int nzone = 1);
+size_t jacobian_scratch_doubles(int im, int jm, int gh, int nzone = 1, int nops = 1);
 size_t jacobian_iscratch_ints(int im, int jm);
 int run_jacobian(const JacobianArgs& a, cudaStream_t st);
 

@@ -360,6 +360,25 @@ int bcg_set_bndbl_2d(const double* w, double* field, double* wbd, int im, int jm
 /* initialisation.f90:2 */
 int bcg_initblfv(double muinf, const double* xc, const double* yc, double* w, double* field, int im, int gh, int jm);
 
+/* J (J/vol with divide_by_vol = 1), Dz and Dzz of the boundary layer from ONE
+ * pass over the 245 seeds (BROADCAST_npz.py:1068-1137 and 1221-1249: the same
+ * testvector and linearised boundary chain feed flux_num_dnc5_2d_d,
+ * coeffs_5p_dz and coeffs_5p_dz2), each filtered by |a| > mini into its CSR
+ * (computejacobianfromjv, computejacobianfromdz), then, with nbeta > 0, J(beta)
+ * = J - beta^2 Dzz + i beta Dz for the host list betas as the epilogue (as
+ * bcg_csr_spanwise_beta).  The three CSR outputs are device arrays given by
+ * tables of three device addresses (J, Dz, Dzz); capacity3 and nnz3 hold three
+ * counts each; the J(beta) outputs are device arrays too. */
+int bcg_jacobian_span_bl_csr(const double* w, const double* nx, const double* ny, const double* vol,
+                             const double* volf, int gh, double cp, double cv, double prandtl, double gam, double rgaz,
+                             double cs, double muref, double tref, double s_suth, double k2, double k4, int im, int jm,
+                             const int* interf_ilo, const int* interf_jhi, const int* interf_ihi,
+                             const int* interf_jlo, const double* field, int lm_field, const double* wbd, int lm_wbd,
+                             double mini, int divide_by_vol, const unsigned long long* indptr3,
+                             const unsigned long long* indices3, const unsigned long long* data3,
+                             const long long* capacity3, long long* nnz3, int nbeta, const double* betas,
+                             int* b_indptr, int* b_indices, double* b_values, long long b_capacity, long long* b_nnz);
+
 /* ---- uneven batch of grids (no counterpart in the reference, which runs one
  * grid per process) ---------------------------------------------------------- */
 /* A plan for ngrid independent grids (gh = 3, im, jm >= 6 each; phys holds the
@@ -422,8 +441,8 @@ int bcg_flux_num_dnc5_2d_noalloc(double* residu, const double* w, const double* 
 /* ---- learned warm start (no reference counterpart) ----------------------------- */
 /* Kernels of the conditioned MLP that gives the cylinder base-flow Newton
  * iteration (cylinder.py:841-1068) its initial state for a new (Re, Mach),
- * in place of the restart from the nearest converged neighbour
- * (cylinder.py:776-792).  BF16 operands (uint16 bit patterns), FP32
+ * in place of the restart from a converged state on the same mesh
+ * (cylinder.py:560-589).  BF16 operands (uint16 bit patterns), FP32
  * accumulation, row-major device arrays only; queued on the library stream.
  * GEMM  C[m x n] = A[m x k] B[n x k]^T (+ bias[n]), m and n multiples of 128,
  * k a multiple of 64, with the epilogue epi:

@@ -164,3 +164,51 @@ def test_spanwise_beta_operator():
         got = (cv[k, :, 0] + 1j * cv[k, :, 1])
         ref = (J - b * b * Dzz + 1j * b * Dz).toarray()[np.repeat(np.arange(nrow), np.diff(indptr)), indices[:n]]
         assert np.abs(got - ref).max() <= 1e-14 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("im,jm", [(20, 14), (64, 48)])
+def test_one_pass_jacobian_dz_dzz_and_beta(im, jm):
+    """bcg_jacobian_span_bl_csr (J/vol, Dz, Dzz from one seed loop, then J(beta))
+    gives bit for bit what the three separate assemblies and
+    bcg_csr_spanwise_beta give."""
+    import torch
+    sp = pytest.importorskip("scipy.sparse")
+    from broadcast_gb300 import _lib
+    from broadcast_gb300._f2py import interf4
+    c = H.bl_case(im, jm)
+    H.oracle_bcs(c, c["w"])
+    g, ph, it = c["grid"], c["phys"], c["interf"]
+    gh = g["gh"]
+    J, Dz, Dzz = _gpu_csr(c, "jac"), _gpu_csr(c, "dz", 1), _gpu_csr(c, "dz", 2)
+    nrow = 5 * im * jm
+    cap = nrow * 245
+    dev = torch.device("cuda", 0)
+    outs = [(torch.zeros(nrow + 1, dtype=torch.int32, device=dev), torch.zeros(cap, dtype=torch.int32, device=dev),
+             torch.zeros(cap, dtype=torch.float64, device=dev)) for _ in range(3)]
+    tab = [np.array([o[k].data_ptr() for o in outs], np.uint64) for k in range(3)]
+    caps, nnz3 = np.full(3, cap, np.int64), np.zeros(3, np.int64)
+    betas = np.array([0.0, 0.4, 1.7])
+    bcap = 3 * cap
+    bp, bi = torch.zeros(nrow + 1, dtype=torch.int32, device=dev), torch.zeros(bcap, dtype=torch.int32, device=dev)
+    bv, bn = torch.zeros(2 * len(betas) * bcap, dtype=torch.float64, device=dev), np.zeros(1, np.int64)
+    keys = SPAN + ("k2", "k4")
+    _lib.call("bcg_set_stream", torch.cuda.current_stream(dev).cuda_stream)
+    _lib.call("bcg_jacobian_span_bl_csr", c["w"], g["nx"], g["ny"], g["vol"], g["volf"], gh,
+              *[float(ph[k]) for k in keys], im, jm, interf4(it["Ilo"]), interf4(it["Jhi"]), interf4(it["Ihi"]),
+              interf4(it["Jlo"]), c["field"], c["field"].shape[0], c["wbd"], c["wbd"].shape[0], 2e-16, 1,
+              tab[0], tab[1], tab[2], caps, nnz3, len(betas), betas, bp, bi, bv, bcap, bn)
+    torch.cuda.synchronize()
+    for (p, i, v), ref, n in zip(outs, (J, Dz, Dzz), nnz3):
+        assert n == ref.nnz
+        assert np.array_equal(p.cpu().numpy(), ref.indptr)
+        assert np.array_equal(i[:n].cpu().numpy(), ref.indices)
+        assert np.array_equal(v[:n].cpu().numpy(), ref.data)
+    # the epilogue against the separate call on the three host matrices
+    rp, ri = np.zeros(nrow + 1, np.int32), np.zeros(bcap, np.int32)
+    rv, rn = np.zeros(2 * len(betas) * bcap), np.zeros(1, np.int64)
+    _lib.call("bcg_csr_spanwise_beta", nrow, J.indptr, J.indices, J.data, Dz.indptr, Dz.indices, Dz.data,
+              Dzz.indptr, Dzz.indices, Dzz.data, len(betas), betas, rp, ri, rv, bcap, rn)
+    n = int(rn[0])
+    assert int(bn[0]) == n
+    assert np.array_equal(bp.cpu().numpy(), rp) and np.array_equal(bi[:n].cpu().numpy(), ri[:n])
+    assert np.array_equal(bv[:2 * len(betas) * n].cpu().numpy(), rv[:2 * len(betas) * n])
