@@ -593,13 +593,13 @@ def _flux_scale(c):
 #       python bench.py --grids 6 --steps 1 --warmup 1 --no-extras --tile 128,128,3 --cpu-seconds 1
 # divided by the capture's cells; the full batch's figures scale with its cells.
 BATCH_NCU = {
-    "fp64_inst_per_cell": {"prim": 139.0, "sensor": 175.9, "qrows": 93.3, "vpts": 48.5, "faces": 924.9,
+    "fp64_inst_per_cell": {"prim": 141.1, "sensor": 175.9, "qrows": 93.3, "vpts": 48.5, "faces": 849.7,
                            "balance": 30.0},
-    "dram_bytes_per_cell": {"prim": 334.4, "sensor": 161.2, "qrows": 338.6, "vpts": 232.0, "faces": 886.3,
-                            "balance": 219.4},
+    "dram_bytes_per_cell": {"prim": 351.4, "sensor": 161.5, "qrows": 338.9, "vpts": 232.2, "faces": 900.5,
+                            "balance": 219.7},
     "source": "ncu sm__inst_executed_pipe_fp64.sum x 32 lanes and dram__bytes_read.sum + dram__bytes_write.sum "
               "per k_batch launch, first 6 grids (1,344,226 cells), cold caches; per cell, scaled to this run's "
-              "cells",
+              "cells; prim includes the rectilinear-grid scan (k_batch_rect) that runs with it",
 }
 BATCH_PASSES = ("prim", "sensor", "qrows", "vpts", "faces", "balance")
 
@@ -825,7 +825,7 @@ def run_batch(args):
         w_h, wd_h = [pin(c["w"]) for c in cs], [pin(wd) for wd in wds]
         geo_h = [{k: pin(c["grid"][k]) for k in ("nx", "ny", "vol", "volf")} for c in cs]
         res_h, resd_h = [pin(np.zeros_like(c["w"], order="F")) for c in cs], [pin(np.zeros_like(c["w"], order="F")) for c in cs]
-        nchunk = 8
+        nchunk = args.chunks
         for _ in range(max(args.warmup, 1)):
             gb.run_host(w_h, wd_h, res_h, resd_h, geo_h, nchunk=nchunk)
         t0 = time.perf_counter()
@@ -1190,6 +1190,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-extras", action="store_true", help="default line without the cylinder extra key")
     ap.add_argument("--lmax", type=int, default=10, help="impli workload: Gauss-Seidel sweeps per call")
+    ap.add_argument("--chunks", type=int, default=16,
+                    help="batch workload: chunks of grids whose uploads, graph replays and downloads overlap in the "
+                         "host-array (e2e) run, 1..16")
     ap.add_argument("--case", default="bl", choices=["bl", "cyl"], help="newton workload: boundary layer or cylinder")
     ap.add_argument("--solver", default="auto", choices=["auto", "band", "krylov"],
                     help="newton / warmstart workloads: FP64 band LU, or FP64 GMRES with an FP32 band LU "

@@ -151,6 +151,8 @@ int residual_call(double* residu, double* residud, const double* w, const double
   if (nd < 0) return fail_arg("flux_num_dnc5_2d_dn: negative direction count");
   const size_t np = ncell(im, jm, gh), nn = nnode(im, jm, gh);
   cudaStream_t st = current_stream();
+  // DNC5 on a rectilinear grid takes the face kernel without the zero metric products
+  const int rect = (order == 5 && nx && ny) ? (int)face_rectilinear(nx, ny, im, jm, gh, st) : 0;
   Stager sg(st);
   const int hw = sg.in(w, np * 5 * 8), hnx = sg.in(nx, nn * 2 * 8), hny = sg.in(ny, nn * 2 * 8);
   const int hvol = sg.in(vol, np * 8), hvolf = sg.in(volf, np * 2 * 8);
@@ -170,6 +172,7 @@ int residual_call(double* residu, double* residud, const double* w, const double
   a.dstride = np * 5;
   a.nowall = nowall;
   a.order = order;
+  a.rect = rect;
   double* res = hres >= 0 ? sg.dev<double>(hres) : nullptr;
   if (pipelined) {
     rc = residual_pipelined(a, res, residud, wd, nd, st);

@@ -71,13 +71,25 @@ __device__ __forceinline__ int tile_grid(const long long* __restrict__ starts, i
   return lo;
 }
 
+// per grid (blockIdx.y): the count of warps that met a nonzero i-face ny or
+// j-face nx component; zero means the grid is rectilinear
+__global__ void __launch_bounds__(256) k_batch_rect(const GridDesc* __restrict__ descs, unsigned* __restrict__ rectnz) {
+  const GridDesc& G = descs[blockIdx.y];
+  const size_t nn = G.e.nn();
+  unsigned bad = 0;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (size_t)gridDim.x * blockDim.x)
+    bad |= (G.ny[k] != 0.0) | (G.nx[nn + k] != 0.0);
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicAdd(rectnz + blockIdx.y, 1u);
+}
+
 template <class S, int PASS, int BT>
 __global__ void __launch_bounds__(BT) k_batch(const GridDesc* __restrict__ descs, const long long* __restrict__ starts,
-                                              int ngrid) {
+                                              int ngrid, const unsigned* __restrict__ rectnz) {
   const long long* st = starts + (size_t)PASS * (ngrid + 1);
   const long long T = st[ngrid];
-  __shared__ int s_g;
-  __shared__ FaceCtx<S> s_fc;
+  __shared__ int s_g, s_rect;
+  __shared__ FaceCtx<S> s_fc;           // curvilinear grids
+  __shared__ FaceCtx<S, 3, true> s_fcr;  // rectilinear grids: the face kernel without the zero metric products
   __shared__ Scratch<S> s_hn;
   for (long long t = blockIdx.x; t < T; t += gridDim.x) {
     __syncthreads();  // the previous tile is done with the shared descriptor
@@ -87,9 +99,13 @@ __global__ void __launch_bounds__(BT) k_batch(const GridDesc* __restrict__ descs
       if constexpr (PASS == P_FACES) {
         const GridDesc& G = descs[g];
         const Fields<S> f = fields_of<S>(G);
-        s_fc.e = G.e; s_fc.c = G.c; s_fc.w = state_of<S>(G);
-        s_fc.pr = f.pr; s_fc.gr = f.gr; s_fc.qr = f.qr;
-        s_fc.nx = G.nx; s_fc.ny = G.ny; s_fc.vol = G.vol; s_fc.volf = G.volf;
+        auto fill = [&](auto& fc) {
+          fc.e = G.e; fc.c = G.c; fc.w = state_of<S>(G);
+          fc.pr = f.pr; fc.gr = f.gr; fc.qr = f.qr;
+          fc.nx = G.nx; fc.ny = G.ny; fc.vol = G.vol; fc.volf = G.volf;
+        };
+        s_rect = rectnz[g] == 0;
+        if (s_rect) fill(s_fcr); else fill(s_fc);
         s_hn = f.hn;
       }
     }
@@ -97,8 +113,13 @@ __global__ void __launch_bounds__(BT) k_batch(const GridDesc* __restrict__ descs
     const int g = s_g;
     const long long el = (t - st[g]) * BT + threadIdx.x;
     if constexpr (PASS == P_FACES) {
-      const Ext& e = s_fc.e;
-      if (el < (long long)(e.im + 1) * (e.jm + 1)) face_node<S>(s_fc, s_hn, (int)el);
+      if (s_rect) {
+        const Ext& e = s_fcr.e;
+        if (el < (long long)(e.im + 1) * (e.jm + 1)) face_node<S, 3, true>(s_fcr, s_hn, (int)el);
+      } else {
+        const Ext& e = s_fc.e;
+        if (el < (long long)(e.im + 1) * (e.jm + 1)) face_node<S>(s_fc, s_hn, (int)el);
+      }
     } else {
       const GridDesc& G = descs[g];
       const Ext& e = G.e;
@@ -133,6 +154,8 @@ struct BatchPlan {
   cudaStream_t cap = nullptr;  // capture stream (the caller's may be the legacy default stream)
   cudaGraphExec_t exec = nullptr;
   bool owns_scratch = true;
+  unsigned* rectnz = nullptr;  // per grid: nonzero i-face ny / j-face nx count of the last evaluation (0: rectilinear)
+  bool owns_rectnz = true;
   // host-array runs (batch_run_host): device mirrors of every grid's arrays,
   // and the grids split into contiguous chunks, each a child plan over the
   // mirrors that shares this plan's scratch
@@ -197,6 +220,8 @@ int batch_create(int ngrid, const int* im, const int* jm, const double* phys, in
   cudaError_t e = cudaMalloc(&p->scratch, p->scratch_doubles * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&p->d, sizeof(GridDesc) * ngrid);
   if (e == cudaSuccess) e = cudaMalloc(&p->dstarts, sizeof(long long) * NPASS * (ngrid + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&p->rectnz, sizeof(unsigned) * ngrid);
+  if (e == cudaSuccess) e = cudaMemset(p->rectnz, 0xff, sizeof(unsigned) * ngrid);  // curvilinear until checked
   if (e != cudaSuccess) { batch_destroy(p); return fail_cuda("batch: device allocation", e), BCG_ERR_NOMEM; }
   for (int g = 0; g < ngrid; ++g) p->h[g].scratch = p->scratch + off[g];
   int rc = upload_starts(p);
@@ -241,7 +266,14 @@ static void launch_pass(const BatchPlan* p, int ctas, cudaStream_t st) {
   const long long T = p->ntiles[PASS];
   if (T == 0) return;
   const long long g = std::min<long long>(T, (long long)p->nsm * ctas);
-  k_batch<S, PASS, BT><<<(unsigned)g, BT, 0, st>>>(p->d, p->dstarts, p->ngrid);
+  k_batch<S, PASS, BT><<<(unsigned)g, BT, 0, st>>>(p->d, p->dstarts, p->ngrid, p->rectnz);
+}
+
+// which grids are rectilinear, from their current metrics (before the
+// primitives pass, so the face pass of the same evaluation reads the result)
+static void launch_rect(const BatchPlan* p, cudaStream_t st) {
+  cudaMemsetAsync(p->rectnz, 0, sizeof(unsigned) * p->ngrid, st);
+  k_batch_rect<<<dim3(16, (unsigned)p->ngrid), 256, 0, st>>>(p->d, p->rectnz);
 }
 
 template <class S, int BT>
@@ -259,6 +291,7 @@ static void launch_cells(const BatchPlan* p, int pass, cudaStream_t st) {
 template <class S>
 static cudaError_t launch_all(const BatchPlan* p, cudaStream_t st) {
   const int passes[5] = {P_PRIM, P_GRAD, P_QROWS, P_VPTS, -1};
+  launch_rect(p, st);
   for (int q : passes) {
     if (q < 0) break;
     if (q == P_GRAD && !p->any_grad) continue;
@@ -291,6 +324,7 @@ int batch_run_pass(BatchPlan* p, int pass, cudaStream_t st) {
       launch_cells<S, 256>(p, pass, st);
     }
   };
+  if (pass == P_PRIM) launch_rect(p, st);
   if (p->K) one(DK<1>{}); else one(0.0);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? BCG_OK : fail_cuda("batch: pass launch", e);
@@ -339,11 +373,13 @@ void batch_destroy(BatchPlan* p) {
   if (p->scratch && p->owns_scratch) cudaFree(p->scratch);
   if (p->d) cudaFree(p->d);
   if (p->dstarts) cudaFree(p->dstarts);
+  if (p->rectnz && p->owns_rectnz) cudaFree(p->rectnz);
   delete p;
 }
 
 size_t batch_device_bytes(const BatchPlan* p) {
-  size_t b = sizeof(GridDesc) * p->ngrid + sizeof(long long) * NPASS * (p->ngrid + 1);
+  size_t b = sizeof(GridDesc) * p->ngrid + sizeof(long long) * NPASS * (p->ngrid + 1) +
+             (p->owns_rectnz ? sizeof(unsigned) * p->ngrid : 0);
   if (p->owns_scratch) b += p->scratch_doubles * sizeof(double);
   if (p->mirror) b += p->moff.back() * sizeof(double);
   for (const BatchPlan* c : p->chunks) b += batch_device_bytes(c);
@@ -370,6 +406,7 @@ int make_chunk(BatchPlan* p, int g0, int g1, BatchPlan** out) {
   BatchPlan* c = new BatchPlan();
   c->ngrid = g1 - g0; c->K = p->K; c->nsm = p->nsm; c->any_grad = false;
   c->owns_scratch = false; c->scratch = p->scratch;
+  c->owns_rectnz = false; c->rectnz = p->rectnz + g0;
   c->tile_faces = p->tile_faces; c->tile_cells = p->tile_cells; c->ctas = p->ctas;
   c->h.assign(p->h.begin() + g0, p->h.begin() + g1);
   for (int g = 0; g < c->ngrid; ++g) {

@@ -10,9 +10,6 @@
 
 namespace bcg {
 
-// x is +0 or -0, tested on its bits (an integer instruction, not an FP64 one)
-BCG_HD bool zero_bits(double x) { return (__double_as_longlong(x) << 1) == 0; }
-
 // ---------------------------------------------------------------------------
 // pass 1: primitives on padded cell q (phys/Primitives.F, phys/viscosity.F)
 template <class S>
@@ -210,7 +207,14 @@ BCG_HD void sensor_cell(const Ext& e, const Coef& c, const Scratch<S>& pr, const
 
 // ---------------------------------------------------------------------------
 // pass 3: face fluxes of the DNC scheme with R point pairs (R = 3: DNC5)
-template <class S, int R = 3>
+// RECT: the grid is rectilinear, i.e. every i-face normal has ny = 0 and every
+// j-face normal nx = 0 exactly (face_rectilinear, checked per grid by the
+// caller).  The products with those zero components are then left out: the
+// centred flux's g half on i-faces and f half on j-faces, half of the viscous
+// weights, one product of the normal velocity, and the square root of |n|^2
+// (sqrt of the rounded square of x is |x| in binary floating point).  The
+// sums are the same sums of the same nonzero products (x + 0 y = x).
+template <class S, int R = 3, bool RECT = false>
 struct FaceCtx {
   // near-wall off-centred j-fluxes read the first NW cell rows
   static constexpr int NW = R == 2 ? 2 : (R == 3 ? 5 : (R == 4 ? 9 : 11));
@@ -288,11 +292,6 @@ struct FaceCtx {
   BCG_HD void visc_i(int i, int j, bool o2, double snx, double sny, S fn[4]) const {
     const double volm1 = VOLF(i, j, 1);
     const double fN = o2 ? volm1 : volm1 / 24.0, fE = o2 ? 0.25 * volm1 : c.ccross * volm1;
-    // face normals around the face: i-faces N (i+1), centre, S (i-1); j-faces E (row j+1) and O (row j)
-    const double xN = NX(i + 1, j, 1), xC = NX(i, j, 1), xS = NX(i - 1, j, 1);
-    const double xE1 = NX(i - 1, j + 1, 2), xE0 = NX(i, j + 1, 2), xO1 = NX(i - 1, j, 2), xO0 = NX(i, j, 2);
-    const double yN = NY(i + 1, j, 1), yC = NY(i, j, 1), yS = NY(i - 1, j, 1);
-    const double yE1 = NY(i - 1, j + 1, 2), yE0 = NY(i, j + 1, 2), yO1 = NY(i - 1, j, 2), yO0 = NY(i, j, 2);
     // point value of variable a (u v w T) at point p
     auto val = [&](int a, int p) -> S {
       const int f = F_U + a;  // F_U, F_V, F_W, F_T are consecutive
@@ -307,61 +306,59 @@ struct FaceCtx {
       if (p == 2) return (P(f, i, j) + P(f, i, j + 1)) + (P(f, i - 1, j) + P(f, i - 1, j + 1));
       return (P(f, i, j) + P(f, i, j - 1)) + (P(f, i - 1, j) + P(f, i - 1, j - 1));
     };
+    auto means = [&](S& uu, S& vv, S& ww, S& mmu) {
+      if (!o2) {
+        uu = 0.0625 * Q(Q_I + 0, i, j);
+        vv = 0.0625 * Q(Q_I + 1, i, j);
+        ww = 0.0625 * Q(Q_I + 2, i, j);
+        mmu = 0.0625 * Q(Q_I + 4, i, j);
+      } else {
+        uu = 0.5 * (P(F_U, i, j) + P(F_U, i - 1, j));
+        vv = 0.5 * (P(F_V, i, j) + P(F_V, i - 1, j));
+        ww = 0.5 * (P(F_W, i, j) + P(F_W, i - 1, j));
+        mmu = 0.5 * (P(F_MU, i, j) + P(F_MU, i - 1, j));
+      }
+    };
     S uu, vv, ww, mmu;
-    if (!o2) {
-      uu = 0.0625 * Q(Q_I + 0, i, j);
-      vv = 0.0625 * Q(Q_I + 1, i, j);
-      ww = 0.0625 * Q(Q_I + 2, i, j);
-      mmu = 0.0625 * Q(Q_I + 4, i, j);
-    } else {
-      uu = 0.5 * (P(F_U, i, j) + P(F_U, i - 1, j));
-      vv = 0.5 * (P(F_V, i, j) + P(F_V, i - 1, j));
-      ww = 0.5 * (P(F_W, i, j) + P(F_W, i - 1, j));
-      mmu = 0.5 * (P(F_MU, i, j) + P(F_MU, i - 1, j));
-    }
-    if (zero_bits(sny) && zero_bits(yN) && zero_bits(yC) && zero_bits(yS) && zero_bits(xE1) && zero_bits(xE0) &&
-        zero_bits(xO1) && zero_bits(xO0)) {
-      // rectilinear neighbourhood (i-faces along x, j-faces along y): ay of N
-      // and S and ax of E and O are exact zeros, so are half of the weights
-      // below (visc_normal with those zeros, the same sums of the same
-      // nonzero products)
+    if constexpr (RECT) {
+      // ay of N and S and ax of E and O are zero, and sny: of the weights of
+      // visc_normal, N and S keep c00 = e + e/3, c11 = e (e = ax snx), E and O
+      // keep c01 = -2/3 yn, c10 = yn (yn = ay snx)
       const double T3 = 1.0 / 3.0, TWOTHIRD = 2.0 / 3.0;
-      const double x0 = (0.5 * (xN + xC) * fN) * snx, x1 = (-(0.5 * (xS + xC)) * fN) * snx;
-      const double y2 = (0.5 * (yE1 + yE0) * fE) * snx, y3 = (-(0.5 * (yO1 + yO0)) * fE) * snx;
-      const S u0 = val(0, 0), u1 = val(0, 1), u2 = val(0, 2), u3 = val(0, 3);
-      const S v0 = val(1, 0), v1 = val(1, 1), v2 = val(1, 2), v3 = val(1, 3);
-      S an = (x0 + T3 * x0) * u0;
-      an = an + (x1 + T3 * x1) * u1;
-      an = an + (-(TWOTHIRD * y2)) * v2;
-      an = an + (-(TWOTHIRD * y3)) * v3;
-      S bn = x0 * v0;
-      bn = bn + x1 * v1;
-      bn = bn + y2 * u2;
-      bn = bn + y3 * u3;
+      const double x0 = (0.5 * (NX(i + 1, j, 1) + NX(i, j, 1)) * fN) * snx;
+      const double x1 = (-(0.5 * (NX(i - 1, j, 1) + NX(i, j, 1))) * fN) * snx;
+      const double y2 = (0.5 * (NY(i - 1, j + 1, 2) + NY(i, j + 1, 2)) * fE) * snx;
+      const double y3 = (-(0.5 * (NY(i - 1, j, 2) + NY(i, j, 2))) * fE) * snx;
+      means(uu, vv, ww, mmu);
+      S an = (x0 + T3 * x0) * val(0, 0);
+      an = an + (x1 + T3 * x1) * val(0, 1);
+      an = an + (-(TWOTHIRD * y2)) * val(1, 2);
+      an = an + (-(TWOTHIRD * y3)) * val(1, 3);
+      S bn = x0 * val(1, 0);
+      bn = bn + x1 * val(1, 1);
+      bn = bn + y2 * val(0, 2);
+      bn = bn + y3 * val(0, 3);
       const S wn = x0 * val(2, 0) + x1 * val(2, 1);
       const S tn = x0 * val(3, 0) + x1 * val(3, 1);
       fn[0] = mmu * an;
       fn[1] = mmu * bn;
       fn[2] = mmu * wn;
       fn[3] = (mmu * c.cpprandtl) * tn + uu * fn[0] + vv * fn[1] + ww * fn[2];
-      return;
+    } else {
+      // points N, S, O, E
+      const double ax[4] = {0.5 * (NX(i + 1, j, 1) + NX(i, j, 1)) * fN, -(0.5 * (NX(i - 1, j, 1) + NX(i, j, 1))) * fN,
+                            0.5 * (NX(i - 1, j + 1, 2) + NX(i, j + 1, 2)) * fE, -(0.5 * (NX(i - 1, j, 2) + NX(i, j, 2))) * fE};
+      const double ay[4] = {0.5 * (NY(i + 1, j, 1) + NY(i, j, 1)) * fN, -(0.5 * (NY(i - 1, j, 1) + NY(i, j, 1))) * fN,
+                            0.5 * (NY(i - 1, j + 1, 2) + NY(i, j + 1, 2)) * fE, -(0.5 * (NY(i - 1, j, 2) + NY(i, j, 2))) * fE};
+      means(uu, vv, ww, mmu);
+      visc_normal(val, ax, ay, snx, sny, mmu, uu, vv, ww, fn);
     }
-    // points N, S, O, E
-    const double ax[4] = {0.5 * (xN + xC) * fN, -(0.5 * (xS + xC)) * fN, 0.5 * (xE1 + xE0) * fE, -(0.5 * (xO1 + xO0)) * fE};
-    const double ay[4] = {0.5 * (yN + yC) * fN, -(0.5 * (yS + yC)) * fN, 0.5 * (yE1 + yE0) * fE, -(0.5 * (yO1 + yO0)) * fE};
-    visc_normal(val, ax, ay, snx, sny, mmu, uu, vv, ww, fn);
   }
 
   // Viscous flux through j-face (i,j): o4 (rhs/flux_visqueux_o4_j.F) or o2 (row 2).
   BCG_HD void visc_j(int i, int j, bool o2, double snx, double sny, S fn[4]) const {
     const double volm1 = VOLF(i, j, 2);
     const double fN = o2 ? 0.25 * volm1 : c.ccross * volm1, fE = o2 ? volm1 : volm1 / 24.0;
-    // face normals around the face: i-faces N (column i+1) and S (column i)
-    // of rows j-1 and j; j-faces E (row j+1), centre, O (row j-1)
-    const double xN1 = NX(i + 1, j - 1, 1), xN0 = NX(i + 1, j, 1), xS1 = NX(i, j - 1, 1), xS0 = NX(i, j, 1);
-    const double xE = NX(i, j + 1, 2), xC = NX(i, j, 2), xO = NX(i, j - 1, 2);
-    const double yN1 = NY(i + 1, j - 1, 1), yN0 = NY(i + 1, j, 1), yS1 = NY(i, j - 1, 1), yS0 = NY(i, j, 1);
-    const double yE = NY(i, j + 1, 2), yC = NY(i, j, 2), yO = NY(i, j - 1, 2);
     auto val = [&](int a, int p) -> S {
       const int f = F_U + a;  // F_U, F_V, F_W, F_T are consecutive
       if (!o2) {
@@ -375,53 +372,60 @@ struct FaceCtx {
       if (p == 2) return P(f, i, j);
       return P(f, i, j - 1);
     };
+    auto means = [&](S& uu, S& vv, S& ww, S& mmu) {
+      if (!o2) {
+        uu = 0.0625 * Q(Q_J + 0, i, j);
+        vv = 0.0625 * Q(Q_J + 1, i, j);
+        ww = 0.0625 * Q(Q_J + 2, i, j);
+        mmu = 0.0625 * Q(Q_J + 4, i, j);
+      } else {
+        uu = 0.5 * (P(F_U, i, j) + P(F_U, i, j - 1));
+        vv = 0.5 * (P(F_V, i, j) + P(F_V, i, j - 1));
+        ww = 0.5 * (P(F_W, i, j) + P(F_W, i, j - 1));
+        mmu = 0.5 * (P(F_MU, i, j) + P(F_MU, i, j - 1));
+      }
+    };
     S uu, vv, ww, mmu;
-    if (!o2) {
-      uu = 0.0625 * Q(Q_J + 0, i, j);
-      vv = 0.0625 * Q(Q_J + 1, i, j);
-      ww = 0.0625 * Q(Q_J + 2, i, j);
-      mmu = 0.0625 * Q(Q_J + 4, i, j);
-    } else {
-      uu = 0.5 * (P(F_U, i, j) + P(F_U, i, j - 1));
-      vv = 0.5 * (P(F_V, i, j) + P(F_V, i, j - 1));
-      ww = 0.5 * (P(F_W, i, j) + P(F_W, i, j - 1));
-      mmu = 0.5 * (P(F_MU, i, j) + P(F_MU, i, j - 1));
-    }
-    if (zero_bits(snx) && zero_bits(yN1) && zero_bits(yN0) && zero_bits(yS1) && zero_bits(yS0) && zero_bits(xE) &&
-        zero_bits(xC) && zero_bits(xO)) {
-      // rectilinear neighbourhood: ay of N and S and ax of E and O are exact
-      // zeros (see visc_i)
+    if constexpr (RECT) {
+      // ay of N and S and ax of E and O are zero, and snx: N and S keep
+      // c01 = xn, c10 = -2/3 xn (xn = ax sny), E and O keep c00 = e,
+      // c11 = e + e/3 (e = ay sny)
       const double T3 = 1.0 / 3.0, TWOTHIRD = 2.0 / 3.0;
-      const double x0 = (0.5 * (xN1 + xN0) * fN) * sny, x1 = (-(0.5 * (xS1 + xS0)) * fN) * sny;
-      const double y2 = (0.5 * (yE + yC) * fE) * sny, y3 = (-(0.5 * (yO + yC)) * fE) * sny;
-      const S u0 = val(0, 0), u1 = val(0, 1), u2 = val(0, 2), u3 = val(0, 3);
-      const S v0 = val(1, 0), v1 = val(1, 1), v2 = val(1, 2), v3 = val(1, 3);
-      S an = x0 * v0;
-      an = an + x1 * v1;
-      an = an + y2 * u2;
-      an = an + y3 * u3;
-      S bn = (-(TWOTHIRD * x0)) * u0;
-      bn = bn + (-(TWOTHIRD * x1)) * u1;
-      bn = bn + (y2 + T3 * y2) * v2;
-      bn = bn + (y3 + T3 * y3) * v3;
+      const double x0 = (0.5 * (NX(i + 1, j - 1, 1) + NX(i + 1, j, 1)) * fN) * sny;
+      const double x1 = (-(0.5 * (NX(i, j - 1, 1) + NX(i, j, 1))) * fN) * sny;
+      const double y2 = (0.5 * (NY(i, j + 1, 2) + NY(i, j, 2)) * fE) * sny;
+      const double y3 = (-(0.5 * (NY(i, j - 1, 2) + NY(i, j, 2))) * fE) * sny;
+      means(uu, vv, ww, mmu);
+      S an = x0 * val(1, 0);
+      an = an + x1 * val(1, 1);
+      an = an + y2 * val(0, 2);
+      an = an + y3 * val(0, 3);
+      S bn = (-(TWOTHIRD * x0)) * val(0, 0);
+      bn = bn + (-(TWOTHIRD * x1)) * val(0, 1);
+      bn = bn + (y2 + T3 * y2) * val(1, 2);
+      bn = bn + (y3 + T3 * y3) * val(1, 3);
       const S wn = y2 * val(2, 2) + y3 * val(2, 3);
       const S tn = y2 * val(3, 2) + y3 * val(3, 3);
       fn[0] = mmu * an;
       fn[1] = mmu * bn;
       fn[2] = mmu * wn;
       fn[3] = (mmu * c.cpprandtl) * tn + uu * fn[0] + vv * fn[1] + ww * fn[2];
-      return;
+    } else {
+      // points N, S, O, E
+      const double ax[4] = {0.5 * (NX(i + 1, j - 1, 1) + NX(i + 1, j, 1)) * fN, -(0.5 * (NX(i, j - 1, 1) + NX(i, j, 1))) * fN,
+                            0.5 * (NX(i, j + 1, 2) + NX(i, j, 2)) * fE, -(0.5 * (NX(i, j - 1, 2) + NX(i, j, 2))) * fE};
+      const double ay[4] = {0.5 * (NY(i + 1, j - 1, 1) + NY(i + 1, j, 1)) * fN, -(0.5 * (NY(i, j - 1, 1) + NY(i, j, 1))) * fN,
+                            0.5 * (NY(i, j + 1, 2) + NY(i, j, 2)) * fE, -(0.5 * (NY(i, j - 1, 2) + NY(i, j, 2))) * fE};
+      means(uu, vv, ww, mmu);
+      visc_normal(val, ax, ay, snx, sny, mmu, uu, vv, ww, fn);
     }
-    // points N, S, O, E
-    const double ax[4] = {0.5 * (xN1 + xN0) * fN, -(0.5 * (xS1 + xS0)) * fN, 0.5 * (xE + xC) * fE, -(0.5 * (xO + xC)) * fE};
-    const double ay[4] = {0.5 * (yN1 + yN0) * fN, -(0.5 * (yS1 + yS0)) * fN, 0.5 * (yE + yC) * fE, -(0.5 * (yO + yC)) * fE};
-    visc_normal(val, ax, ay, snx, sny, mmu, uu, vv, ww, fn);
   }
 
   // spectral radius, Ducros/pressure sensor and dissipation through the face
   // between cells L and R (rhs/spectralradius_i.F, ducrosfordnc_i.F,
   // dissipation_ducros_i.F); ksf: the pressure-sensor field of the face's
   // direction (S_KSI or S_KSJ).
+  template <int DIR>
   BCG_HD void dissipation(int iL, int jL, int iR, int jR, int ksf, double fnx, double fny, const S pred[5],
                           S diss[5]) const {
     // Roe average: rr = sqrt(rhoL)/(sqrt(rhoL)+sqrt(rhoR)), so
@@ -430,8 +434,9 @@ struct FaceCtx {
     const S u = (P(F_SU, iL, jL) + P(F_SU, iR, jR)) * inv, v = (P(F_SV, iL, jL) + P(F_SV, iR, jR)) * inv;
     const S c2x = (P(F_SC, iL, jL) + P(F_SC, iR, jR)) * inv;
     const double nx2 = fnx * fnx + fny * fny;
-    // a zero normal component drops its product (x + 0 y = x)
-    const S un = zero_bits(fny) ? fnx * u : (zero_bits(fnx) ? fny * v : fnx * u + fny * v);
+    S un;
+    if constexpr (RECT) un = DIR == 1 ? fnx * u : fny * v;
+    else un = fnx * u + fny * v;
     const S rspec = fabs_t(un) + sqrt_t(c2x * nx2);
     if (c.k2 == 0.0) {
       // with k2 = 0 the sensor is multiplied by zero (0 * coef = 0 for the
@@ -452,9 +457,7 @@ struct FaceCtx {
       // argument.  Arguments closer than rounding could order differently take
       // both tanh and the reference's rule (MAX keeps its first argument unless
       // it is strictly smaller).
-      // |n|; with a zero component it is the other's magnitude (sqrt of the
-      // rounded square of x is |x| in binary floating point)
-      const double nabs = zero_bits(fny) ? fabs(fnx) : (zero_bits(fnx) ? fabs(fny) : sqrt(nx2));
+      const double nabs = RECT ? (DIR == 1 ? fabs(fnx) : fabs(fny)) : sqrt(nx2);
       const S arg1 = 2.5 + SG(S_ARG, iR, jR) / (SG(S_CS, iR, jR) * nabs + 1e-15);
       const S arg2 = 2.5 + SG(S_ARG, iL, jL) / (SG(S_CS, iL, jL) * nabs + 1e-15);
       const double gap = val(arg1) - val(arg2), tol = 1e-12 * (fabs(val(arg1)) + 1.0);
@@ -486,25 +489,23 @@ struct FaceCtx {
   // Centred face flux of variable v5 along (di, dj) with the weights already
   // multiplied by the face normal (a = cc fnx, b = cc fny), once per face:
   // sum_n a_n (f(+n-1) + f(-n)) + sum_n b_n (g(+n-1) + g(-n))  (rhs/euler_o6_i.F,
-  // the o4, o8 and o10 forms for R = 2, 4, 5)
-  // A face whose normal has an exactly zero component (the axis-aligned faces
-  // of a rectilinear grid: fny = 0 on i-faces, fnx = 0 on j-faces) skips the
-  // products with that component's zero weights; the sum is the same, since
-  // x + 0 y = x.
-  BCG_HD S centred(int v5, int i, int j, int di, int dj, const double a[R], const double b[R], bool fz, bool gz) const {
-    if (fz && gz) return Planes<S>::zero();
+  // the o4, o8 and o10 forms for R = 2, 4, 5); DROP 1 leaves out the g half
+  // (b = 0), DROP 2 the f half (a = 0).
+  template <int DROP>
+  BCG_HD S centred(int v5, int i, int j, int di, int dj, const double a[R], const double b[R]) const {
     S fx;
-    if (!fz) {
+    if constexpr (DROP != 2) {
       fx = a[0] * (Fl(v5, i, j) + Fl(v5, i - di, j - dj));
 #pragma unroll
       for (int n = 2; n <= R; ++n)
         fx = fx + a[n - 1] * (Fl(v5, i + (n - 1) * di, j + (n - 1) * dj) + Fl(v5, i - n * di, j - n * dj));
     }
-    if (!gz) {
+    if constexpr (DROP != 1) {
 #pragma unroll
       for (int n = 1; n <= R; ++n) {
         const S t = Gl(v5, i + (n - 1) * di, j + (n - 1) * dj) + Gl(v5, i - n * di, j - n * dj);
-        fx = (fz && n == 1) ? b[0] * t : fx + b[n - 1] * t;
+        if constexpr (DROP == 2) fx = n == 1 ? b[0] * t : fx + b[n - 1] * t;
+        else fx = fx + b[n - 1] * t;
       }
     }
     return fx;
@@ -536,11 +537,11 @@ struct FaceCtx {
     for (int n = 0; n < R; ++n) { a[n] = c.cc[n] * fnx; b[n] = c.cc[n] * fny; }
 #pragma unroll
     for (int v5 = 1; v5 <= 5; ++v5) {
-      fx[v5 - 1] = centred(v5, i, j, 1, 0, a, b, zero_bits(fnx), zero_bits(fny));
+      fx[v5 - 1] = centred<RECT ? 1 : 0>(v5, i, j, 1, 0, a, b);
       pred[v5 - 1] = predictor(v5, i, j, 1, 0);
     }
     visc_i(i, j, ALL_O2 || (c.wall && j <= 2), fnx, fny, fn);
-    dissipation(i - 1, j, i, j, S_KSI, fnx, fny, pred, diss);
+    dissipation<1>(i - 1, j, i, j, S_KSI, fnx, fny, pred, diss);
     assemble(fx, diss, fn, h);
   }
 
@@ -554,27 +555,29 @@ struct FaceCtx {
 #pragma unroll
     for (int v5 = 1; v5 <= 5; ++v5) {
       if (j > R || !c.wall) {
-        fx[v5 - 1] = centred(v5, i, j, 0, 1, a, b, zero_bits(fnx), zero_bits(fny));
+        fx[v5 - 1] = centred<RECT ? 2 : 0>(v5, i, j, 0, 1, a, b);
       } else {
         // off-centred flux of wall row j from rows 1..NW (rhs/nearbndfluxes5demi_7p.F, 3demi, ...)
         const double* cw = c.cw[j - 2];
-        S sf = Planes<S>::zero(), sg = Planes<S>::zero();
-        if (!zero_bits(fnx)) {
-          sf = cw[0] * Fl(v5, i, 1);
-#pragma unroll
-          for (int n = 1; n < NW; ++n) sf = sf + cw[n] * Fl(v5, i, n + 1);
-        }
-        if (!zero_bits(fny)) {
-          sg = cw[0] * Gl(v5, i, 1);
+        if constexpr (RECT) {
+          S sg = cw[0] * Gl(v5, i, 1);
 #pragma unroll
           for (int n = 1; n < NW; ++n) sg = sg + cw[n] * Gl(v5, i, n + 1);
+          fx[v5 - 1] = sg * fny;
+        } else {
+          S sf = cw[0] * Fl(v5, i, 1), sg = cw[0] * Gl(v5, i, 1);
+#pragma unroll
+          for (int n = 1; n < NW; ++n) {
+            sf = sf + cw[n] * Fl(v5, i, n + 1);
+            sg = sg + cw[n] * Gl(v5, i, n + 1);
+          }
+          fx[v5 - 1] = sf * fnx + sg * fny;
         }
-        fx[v5 - 1] = zero_bits(fny) ? sf * fnx : (zero_bits(fnx) ? sg * fny : sf * fnx + sg * fny);
       }
       pred[v5 - 1] = predictor(v5, i, j, 0, 1);
     }
     visc_j(i, j, ALL_O2 || (c.wall && j == 2), fnx, fny, fn);
-    dissipation(i, j - 1, i, j, S_KSJ, fnx, fny, pred, diss);
+    dissipation<2>(i, j - 1, i, j, S_KSJ, fnx, fny, pred, diss);
     assemble(fx, diss, fn, h);
   }
 
@@ -599,8 +602,8 @@ struct FaceCtx {
 
 // node t of the (im+1) x (jm+1) node set, i fastest: the i-face (j <= jm)
 // and the j-face (i <= im) of the node into hn (5 i-face, 5 j-face fields)
-template <class S, int R = 3>
-BCG_HD void face_node(const FaceCtx<S, R>& fc, const Scratch<S>& hn, int t) {
+template <class S, int R = 3, bool RECT = false>
+BCG_HD void face_node(const FaceCtx<S, R, RECT>& fc, const Scratch<S>& hn, int t) {
   const Ext& e = fc.e;
   const int nI = e.im + 1;
   const int i = 1 + t % nI, j = 1 + t / nI;

@@ -7,9 +7,76 @@
 // cell primitive, cell gradient and face flux is computed exactly once and
 // parked in HBM scratch (L2-resident for the grid sizes of interest); the
 // memory traffic this costs is far below the bandwidth roof.
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include "residual_impl.cuh"
 
 namespace bcg {
+
+namespace {
+// count of nonzero i-face ny and j-face nx components (the planes ny(:,:,1)
+// and nx(:,:,2) of the padded node set)
+__global__ void k_rect_count(const double* __restrict__ nx, const double* __restrict__ ny, size_t nn,
+                             unsigned* __restrict__ count) {
+  unsigned bad = 0;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (size_t)gridDim.x * blockDim.x)
+    bad |= (ny[k] != 0.0) | (nx[nn + k] != 0.0);
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicAdd(count, 1u);
+}
+
+__device__ unsigned g_rect_count;  // one per device
+std::mutex g_rect_mu;
+std::map<std::tuple<int, const double*, const double*, int, int, int>, bool> g_curvilinear;  // remembered false results
+}  // namespace
+
+bool face_rectilinear_host(const double* nx, const double* ny, int im, int jm, int gh) {
+  const size_t nn = (size_t)(im + 2 * gh + 1) * (jm + 2 * gh + 1);
+  for (size_t k = 0; k < nn; ++k)
+    if (ny[k] != 0.0 || nx[nn + k] != 0.0) return false;
+  return true;
+}
+
+bool face_rectilinear_device(const double* nx, const double* ny, int im, int jm, int gh, cudaStream_t st) {
+  const size_t nn = (size_t)(im + 2 * gh + 1) * (jm + 2 * gh + 1);
+  std::lock_guard<std::mutex> lk(g_rect_mu);
+  unsigned* count = nullptr;
+  if (cudaGetSymbolAddress((void**)&count, g_rect_count) != cudaSuccess) { cudaGetLastError(); return false; }
+  unsigned h = 1;
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned), st);
+  const unsigned nb = (unsigned)std::min<size_t>((nn + 255) / 256, 1024);
+  if (e == cudaSuccess) {
+    k_rect_count<<<nb, 256, 0, st>>>(nx, ny, nn, count);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, count, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) { cudaGetLastError(); return false; }
+  return h == 0;
+}
+
+bool face_rectilinear(const double* nx, const double* ny, int im, int jm, int gh, cudaStream_t st) {
+  cudaPointerAttributes at;
+  const bool dev = cudaPointerGetAttributes(&at, nx) == cudaSuccess &&
+                   (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged);
+  cudaGetLastError();
+  if (!dev) return face_rectilinear_host(nx, ny, im, jm, gh);
+  int d = 0;
+  cudaGetDevice(&d);
+  const auto key = std::make_tuple(d, nx, ny, im, jm, gh);
+  {
+    std::lock_guard<std::mutex> lk(g_rect_mu);
+    if (g_curvilinear.count(key)) return false;
+  }
+  const bool r = face_rectilinear_device(nx, ny, im, jm, gh, st);
+  if (!r) {
+    std::lock_guard<std::mutex> lk(g_rect_mu);
+    if (g_curvilinear.size() > 4096) g_curvilinear.clear();
+    g_curvilinear[key] = true;
+  }
+  return r;
+}
 
 void launch_primal_passes(const Ext& e, const Coef& c, const double* w, double* pr, double* gr, const double* nx,
                           const double* ny, const double* vol, cudaStream_t st) {

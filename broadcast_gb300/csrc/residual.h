@@ -24,7 +24,19 @@ struct ResidualArgs {
   int ngroup;            // 0 or 1: one group; G > 1 (ndir > 0): G groups of ndir directions in one launch,
                          // group g reading wd + g*ndir*dstride and writing resd + g*ndir*dstride
   int order;             // DNC scheme order: 0 or 5 (DNC5); 3, 7 or 9 (ndir 0 or 1; gh >= (order+1)/2)
+  int rect;              // 1: the grid is rectilinear (face_rectilinear_*); DNC5 takes the face kernel
+                         // without the products with the zero metric components
 };
+
+// Whether every i-face normal of the padded node set has ny = 0 and every
+// j-face normal nx = 0 exactly (the faces the residual reads): host arrays,
+// or device arrays (queued on st and waited for; false on an error).
+bool face_rectilinear_host(const double* nx, const double* ny, int im, int jm, int gh);
+bool face_rectilinear_device(const double* nx, const double* ny, int im, int jm, int gh, cudaStream_t st);
+// the same, host or device arrays alike; device results that are false are
+// remembered per (nx, ny, im, jm, gh) so that repeated calls on a curvilinear
+// grid's resident metrics skip the check (a remembered false only costs speed)
+bool face_rectilinear(const double* nx, const double* ny, int im, int jm, int gh, cudaStream_t st);
 
 size_t residual_scratch_doubles(int im, int jm, int gh, int ndir);
 // primitives (and, when k2 != 0, gradients) of the primal state into scratch

@@ -72,18 +72,18 @@ __global__ void __launch_bounds__(256) k_sensor(Ext e, Coef c, Scratch<S> pr, Sc
   sensor_cell<S, R>(e, c, pr, sg, nx, ny, vol, t);
 }
 
-template <class S, int R = 3>
-__global__ void __launch_bounds__(128) k_faces(FaceCtx<S, R> fc0, Scratch<S> hn, GroupStride gs) {
+template <class S, int R = 3, bool RECT = false>
+__global__ void __launch_bounds__(128) k_faces(FaceCtx<S, R, RECT> fc0, Scratch<S> hn, GroupStride gs) {
   const Ext& e = fc0.e;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (e.im + 1) * (e.jm + 1)) return;
-  FaceCtx<S, R> fc = fc0;
+  FaceCtx<S, R, RECT> fc = fc0;
   shift_state(fc.w, blockIdx.y * gs.tangent);
   shift_scratch(fc.pr, blockIdx.y * gs.scratch);
   shift_scratch(fc.gr, blockIdx.y * gs.scratch);
   shift_scratch(fc.qr, blockIdx.y * gs.scratch);
   shift_scratch(hn, blockIdx.y * gs.scratch);
-  face_node<S, R>(fc, hn, t);
+  face_node<S, R, RECT>(fc, hn, t);
 }
 
 template <class S>
@@ -124,9 +124,20 @@ static cudaError_t run_residual_t(const ResidualArgs& a, cudaStream_t st) {
     k_qrows<S><<<dim3((unsigned)((e.np + B - 1) / B), ng), B, 0, st>>>(e, pr, qr, gs);
     k_vpts<S><<<dim3((unsigned)((e.np + B - 1) / B), ng), B, 0, st>>>(e, qr, gs);
   }
-  FaceCtx<S, R> fc{e, c, w, pr, gr, qr, a.nx, a.ny, a.vol, a.volf};
   const int BF = 128;
-  k_faces<S, R><<<dim3((unsigned)((nn + BF - 1) / BF), ng), BF, 0, st>>>(fc, hn, gs);
+  const dim3 gf((unsigned)((nn + BF - 1) / BF), ng);
+  if constexpr (R == 3) {  // DNC5 on a rectilinear grid: the face kernel without the zero metric products
+    if (a.rect) {
+      FaceCtx<S, R, true> fc{e, c, w, pr, gr, qr, a.nx, a.ny, a.vol, a.volf};
+      k_faces<S, R, true><<<gf, BF, 0, st>>>(fc, hn, gs);
+    } else {
+      FaceCtx<S, R> fc{e, c, w, pr, gr, qr, a.nx, a.ny, a.vol, a.volf};
+      k_faces<S, R><<<gf, BF, 0, st>>>(fc, hn, gs);
+    }
+  } else {
+    FaceCtx<S, R> fc{e, c, w, pr, gr, qr, a.nx, a.ny, a.vol, a.volf};
+    k_faces<S, R><<<gf, BF, 0, st>>>(fc, hn, gs);
+  }
   k_balance<S><<<dim3((unsigned)((a.im * a.jm + B - 1) / B), ng), B, 0, st>>>(e, hn, a.res, a.resd, a.dstride, gs);
   return cudaGetLastError();
 }

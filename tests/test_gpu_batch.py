@@ -153,3 +153,39 @@ def test_host_array_run_matches_device_run(nchunk):
             ghost = np.ones(res[g].shape, bool)
             ghost[3:-3, 3:-3] = False
             assert (res[g][ghost] == 7.0).all() and (resd[g][ghost] == -3.0).all()
+
+
+def test_rectilinear_and_curvilinear_grids_in_one_graph():
+    """Rectilinear boundary layers take the face kernel without the zero metric
+    products, a curvilinear O-mesh the general one, in the same launch; the
+    choice follows the metrics at every replay: a boundary layer whose one
+    i-face normal gets a nonzero ny on the device is curvilinear at the next
+    replay, and both grids still equal the oracle."""
+    import torch
+    from broadcast_gb300.operator import to_host
+    rng = np.random.default_rng(7)
+    cases = _cases(3, seed=9)
+    c = H.cyl_case(40, 24)
+    H.oracle_bcs(c, c["w"])
+    wd = np.zeros_like(c["w"])
+    wd[3:-3, 3:-3] = rng.standard_normal((40, 24, 5))
+    H.oracle_bcs(c, c["w"].copy(order="F"), wd)
+    cases.insert(1, (c, wd))
+    gb = _batch(cases)
+
+    def check():
+        gb.run(use_graph=True)
+        torch.cuda.synchronize()
+        for g, (cc, wdd) in enumerate(cases):
+            ref, refd = O.jvp(cc["grid"], cc["phys"], cc["w"], wdd)
+            assert H.rel_err(to_host(gb.res[g]), ref, H.flux_scale(cc, cc["w"])) < 1e-12
+            scd = np.abs(H.interior(refd)).reshape(-1, 5).max(0)
+            assert H.rel_err(to_host(gb.resd[g]), refd, scd) < 1e-11
+
+    check()
+    g = 2
+    cc = cases[g][0]
+    bump = 1e-3 * np.abs(cc["grid"]["nx"][..., 0]).max()
+    cc["grid"]["ny"][7, 6, 0] += bump      # Fortran (i, j, plane) on the host
+    gb.geo[g]["ny"][0, 6, 7] += bump        # the same entry of the device tensor (plane, j, i)
+    check()

@@ -169,7 +169,7 @@ def test_stability_jacobian_1024x512_indptr_bands_and_products():
             sel = valid & (ia >= r0) & (ia < r1)
             pr.append(ia[sel]); pc.append(ja[sel]); pv.append(jac[sel])
 
-    _seed_sweep(c, O.JAC_PLAIN, None, visit)
+    _seed_sweep(c, O.JAC_PLAIN, None, visit, stack=4)
     # structural pattern: exact in every row
     assert snnz == int(struct.sum())
     assert np.array_equal(np.diff(sptr), struct)
@@ -205,7 +205,7 @@ def test_stability_jacobian_1024x512_indptr_bands_and_products():
             for r, col, v in zip(ia[sel].tolist(), ja[sel].tolist(), jac[sel].tolist()):
                 want[r][col] = v
 
-        _seed_sweep(c, O.JAC_PLAIN, None, collect)
+        _seed_sweep(c, O.JAC_PLAIN, None, collect, stack=4)
         for r, ora in want.items():
             a, b = int(sptr[r]), int(sptr[r + 1])
             mine = dict(zip(sidx_d[a:b].cpu().numpy().tolist(), sdat_d[a:b].cpu().numpy().tolist()))
