@@ -826,6 +826,11 @@ def run_batch(args):
         geo_h = [{k: pin(c["grid"][k]) for k in ("nx", "ny", "vol", "volf")} for c in cs]
         res_h, resd_h = [pin(np.zeros_like(c["w"], order="F")) for c in cs], [pin(np.zeros_like(c["w"], order="F")) for c in cs]
         nchunk = args.chunks
+        if args.tile:
+            gb.configure_host(*[int(x) for x in args.tile.split(",")])
+            host_tune = {"config": list(gb.host_config)}
+        else:  # the chunks' own tile shapes, timed with their copies (untimed here)
+            host_tune = gb.autotune_host(w_h, wd_h, res_h, resd_h, geo_h, nchunk=nchunk)
         for _ in range(max(args.warmup, 1)):
             gb.run_host(w_h, wd_h, res_h, resd_h, geo_h, nchunk=nchunk)
         t0 = time.perf_counter()
@@ -838,6 +843,8 @@ def run_batch(args):
         d2h = 8 * 10 * cells
         e2e = {"value": cells * args.steps / el / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": el / args.steps * 1e3, "chunks": nchunk,
+               "chunk_tile": {"faces": host_tune["config"][0], "cells": host_tune["config"][1],
+                              "ctas_per_sm": host_tune["config"][2]},
                "call": "bcg_batch_run_host (GridBatch.run_host): state, direction and metrics of every grid "
                        "uploaded, residual and tangent interiors downloaded, every step"}
         # parity of this run's outputs (device run and host-array run) with the oracle

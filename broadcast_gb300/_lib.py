@@ -83,6 +83,7 @@ SIGNATURES = {
     "bcg_batch_create": "ipppip",
     "bcg_batch_set_arrays": "L" + "p" * 8,
     "bcg_batch_configure": "Liii",
+    "bcg_batch_configure_host": "Liii",
     "bcg_batch_run": "Li",
     "bcg_batch_run_pass": "Li",
     "bcg_batch_run_host": "Li" + "p" * 8,

@@ -8,6 +8,7 @@ in one set of persistent launches, optionally replayed from a CUDA graph
     gb.res[g], gb.resd[g]               # residual / tangent of grid g
     gb.run_host(ws_h, wds_h, res_h, resd_h, geo_h)  # host arrays, copies overlapped
     gb.autotune()                       # times the tile candidates, keeps the best
+    gb.autotune_host(ws_h, wds_h, res_h, resd_h, geo_h)   # the same for the host-run chunks
 
 The autotuner measures every candidate on the plan's own grids with CUDA
 events and caches the winner per batch signature in a JSON file
@@ -54,6 +55,7 @@ class GridBatch:
         self.resd = [torch.zeros(s, dtype=torch.float64, device=device) for s in shp] if self.ndir else None
         self.ws = self.wds = None
         self.config = None
+        self.host_config = None
 
     def __del__(self):
         try:
@@ -85,6 +87,29 @@ class GridBatch:
     def configure(self, tile_faces, tile_cells, ctas_per_sm):
         _lib.call("bcg_batch_configure", self.plan, int(tile_faces), int(tile_cells), int(ctas_per_sm))
         self.config = (int(tile_faces), int(tile_cells), int(ctas_per_sm))
+
+    def configure_host(self, tile_faces, tile_cells, ctas_per_sm):
+        """Tile shapes of the host-run chunks alone (bcg_batch_configure_host)."""
+        _lib.call("bcg_batch_configure_host", self.plan, int(tile_faces), int(tile_cells), int(ctas_per_sm))
+        self.host_config = (int(tile_faces), int(tile_cells), int(ctas_per_sm))
+
+    def autotune_host(self, ws, wds, res, resd, geo, nchunk=16, candidates=CANDIDATES, repeats=2):
+        """Time run_host (wall clock, copies included) with each candidate tile
+        shape for the chunks and keep the fastest; the whole batch's own shapes
+        (configure / autotune) stay as they are."""
+        import time
+        timings = []
+        for cand in candidates:
+            self.configure_host(*cand)
+            self.run_host(ws, wds, res, resd, geo, nchunk=nchunk)
+            t0 = time.perf_counter()
+            for _ in range(repeats):
+                self.run_host(ws, wds, res, resd, geo, nchunk=nchunk)
+            timings.append(((time.perf_counter() - t0) / repeats * 1e3, cand))
+        best_ms, best = min(timings)
+        self.configure_host(*best)
+        return {"config": list(best), "ms": best_ms, "nchunk": int(nchunk),
+                "timings": [[list(c), t] for t, c in timings]}
 
     def run(self, use_graph=True):
         _lib.call("bcg_batch_run", self.plan, 1 if use_graph else 0)

@@ -1323,6 +1323,12 @@ extern "C" int bcg_batch_configure(long long plan, int tile_faces, int tile_cell
   return batch_configure(p, tile_faces, tile_cells, ctas_per_sm);
 }
 
+extern "C" int bcg_batch_configure_host(long long plan, int tile_faces, int tile_cells, int ctas_per_sm) {
+  BatchPlan* p = batch_of(plan);
+  if (!p) return fail_arg("batch: unknown plan");
+  return batch_configure_host(p, tile_faces, tile_cells, ctas_per_sm);
+}
+
 extern "C" int bcg_batch_run(long long plan, int use_graph) {
   BatchPlan* p = batch_of(plan);
   if (!p) return fail_arg("batch: unknown plan");

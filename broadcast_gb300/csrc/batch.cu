@@ -149,6 +149,7 @@ struct BatchPlan {
   double* scratch = nullptr;
   size_t scratch_doubles = 0;
   int tile_faces = 128, tile_cells = 256, ctas = 2, nsm = 0;
+  int host_tile[3] = {0, 0, 0};  // tile shapes of the host-run chunk plans (0: the plan's own)
   long long ntiles[NPASS] = {0, 0, 0, 0, 0, 0};
   bool any_grad = false;
   cudaStream_t cap = nullptr;  // capture stream (the caller's may be the legacy default stream)
@@ -248,17 +249,35 @@ int batch_set_arrays(BatchPlan* p, const unsigned long long* w, const unsigned l
   return e == cudaSuccess ? BCG_OK : fail_cuda("batch: descriptors", e);
 }
 
-int batch_configure(BatchPlan* p, int tile_faces, int tile_cells, int ctas_per_sm) {
+static int check_tiles(int tile_faces, int tile_cells, int ctas_per_sm) {
   if (tile_faces != 64 && tile_faces != 128 && tile_faces != 256) return fail_arg("batch: tile_faces must be 64, 128 or 256");
   if (tile_cells != 128 && tile_cells != 256) return fail_arg("batch: tile_cells must be 128 or 256");
   if (ctas_per_sm < 1 || ctas_per_sm > 8) return fail_arg("batch: ctas_per_sm must be 1..8");
+  return BCG_OK;
+}
+
+int batch_configure(BatchPlan* p, int tile_faces, int tile_cells, int ctas_per_sm) {
+  int rc = check_tiles(tile_faces, tile_cells, ctas_per_sm);
+  if (rc) return rc;
   p->tile_faces = tile_faces; p->tile_cells = tile_cells; p->ctas = ctas_per_sm;
   if (p->exec) { cudaGraphExecDestroy(p->exec); p->exec = nullptr; }
+  if (!p->host_tile[0])  // the chunk plans follow unless they have shapes of their own
+    for (BatchPlan* c : p->chunks) {
+      rc = batch_configure(c, tile_faces, tile_cells, ctas_per_sm);
+      if (rc) return rc;
+    }
+  return upload_starts(p);
+}
+
+int batch_configure_host(BatchPlan* p, int tile_faces, int tile_cells, int ctas_per_sm) {
+  int rc = check_tiles(tile_faces, tile_cells, ctas_per_sm);
+  if (rc) return rc;
+  p->host_tile[0] = tile_faces; p->host_tile[1] = tile_cells; p->host_tile[2] = ctas_per_sm;
   for (BatchPlan* c : p->chunks) {
-    const int rc = batch_configure(c, tile_faces, tile_cells, ctas_per_sm);
+    rc = batch_configure(c, tile_faces, tile_cells, ctas_per_sm);
     if (rc) return rc;
   }
-  return upload_starts(p);
+  return BCG_OK;
 }
 
 template <class S, int PASS, int BT>
@@ -407,7 +426,10 @@ int make_chunk(BatchPlan* p, int g0, int g1, BatchPlan** out) {
   c->ngrid = g1 - g0; c->K = p->K; c->nsm = p->nsm; c->any_grad = false;
   c->owns_scratch = false; c->scratch = p->scratch;
   c->owns_rectnz = false; c->rectnz = p->rectnz + g0;
-  c->tile_faces = p->tile_faces; c->tile_cells = p->tile_cells; c->ctas = p->ctas;
+  const bool own = p->host_tile[0] != 0;
+  c->tile_faces = own ? p->host_tile[0] : p->tile_faces;
+  c->tile_cells = own ? p->host_tile[1] : p->tile_cells;
+  c->ctas = own ? p->host_tile[2] : p->ctas;
   c->h.assign(p->h.begin() + g0, p->h.begin() + g1);
   for (int g = 0; g < c->ngrid; ++g) {
     GridDesc& G = c->h[g];

@@ -20,6 +20,8 @@ int batch_set_arrays(BatchPlan* p, const unsigned long long* w, const unsigned l
 // tile (threads per CTA) of the face pass and of the cell passes, and CTAs
 // per SM of the persistent grids; drops a captured graph
 int batch_configure(BatchPlan* p, int tile_faces, int tile_cells, int ctas_per_sm);
+// tile shapes of the chunk plans of host-array runs (batch_run_host) alone
+int batch_configure_host(BatchPlan* p, int tile_faces, int tile_cells, int ctas_per_sm);
 int batch_run(BatchPlan* p, int use_graph, cudaStream_t st);
 // one pass alone (0 primitives, 1 gradients, 2 interpolation rows, 3 viscous
 // point values, 4 faces, 5 balance), for timing each kernel of a run

@@ -397,6 +397,11 @@ int bcg_batch_set_arrays(long long plan, const unsigned long long* w, const unsi
 /* Tile shapes: threads per CTA of the face pass (64, 128, 256) and of the cell
  * passes (128, 256), CTAs per SM of the face pass (1..8); drops a captured graph. */
 int bcg_batch_configure(long long plan, int tile_faces, int tile_cells, int ctas_per_sm);
+/* Tile shapes of the chunks of host-array runs (bcg_batch_run_host) alone: a
+ * chunk holds a few grids and runs beside the copies and the other chunks, so
+ * its best shapes can differ from the whole batch's; once set, later
+ * bcg_batch_configure calls no longer change them. */
+int bcg_batch_configure_host(long long plan, int tile_faces, int tile_cells, int ctas_per_sm);
 /* Queue one evaluation on the library stream; use_graph = 1 captures the
  * launches into a CUDA graph on first use and replays it afterwards. */
 int bcg_batch_run(long long plan, int use_graph);

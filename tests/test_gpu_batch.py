@@ -155,6 +155,45 @@ def test_host_array_run_matches_device_run(nchunk):
             assert (res[g][ghost] == 7.0).all() and (resd[g][ghost] == -3.0).all()
 
 
+def test_host_run_tile_shapes_of_their_own():
+    """The chunks of host-array runs take tile shapes of their own
+    (bcg_batch_configure_host, and the autotuner over them), which a later
+    configure of the whole batch leaves alone; results bit for bit those of the
+    device-array run under every shape."""
+    import torch
+    from broadcast_gb300.batch import CANDIDATES
+    from broadcast_gb300.operator import to_host
+    cases = _cases(5, seed=12)
+    gb = _batch(cases)
+    gb.configure(128, 256, 2)
+    gb.run(use_graph=True)
+    torch.cuda.synchronize()
+    ref = [(to_host(r).copy(), to_host(rd).copy()) for r, rd in zip(gb.res, gb.resd)]
+    ws, wds, geo = [c["w"] for c, _ in cases], [wd for _, wd in cases], [c["grid"] for c, _ in cases]
+    res = [np.zeros_like(c["w"]) for c, _ in cases]
+    resd = [np.zeros_like(c["w"]) for c, _ in cases]
+
+    def same():
+        for g in range(len(cases)):
+            assert np.array_equal(H.interior(res[g]), H.interior(ref[g][0]))
+            assert np.array_equal(H.interior(resd[g]), H.interior(ref[g][1]))
+
+    gb.run_host(ws, wds, res, resd, geo, nchunk=3)
+    same()
+    for cand in CANDIDATES[::5]:
+        gb.configure_host(*cand)
+        gb.run_host(ws, wds, res, resd, geo, nchunk=3)
+        same()
+    gb.configure_host(64, 128, 4)
+    gb.configure(256, 128, 1)  # the whole batch's shapes change, the chunks' stay
+    gb.run_host(ws, wds, res, resd, geo, nchunk=3)
+    same()
+    tune = gb.autotune_host(ws, wds, res, resd, geo, nchunk=3, candidates=CANDIDATES[:4], repeats=1)
+    assert tuple(tune["config"]) in CANDIDATES[:4] and gb.host_config == tuple(tune["config"])
+    gb.run_host(ws, wds, res, resd, geo, nchunk=3)
+    same()
+
+
 def test_rectilinear_and_curvilinear_grids_in_one_graph():
     """Rectilinear boundary layers take the face kernel without the zero metric
     products, a curvilinear O-mesh the general one, in the same launch; the
