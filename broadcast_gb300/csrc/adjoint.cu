@@ -18,6 +18,7 @@
 //      reverse of the primitive map give wb; residub's interior is zeroed.
 #include "dnc5.cuh"
 #include "residual.h"
+#include "residual_impl.cuh"
 #include "adjoint.h"
 
 namespace bcg {
@@ -62,6 +63,7 @@ struct AdjCtx {
   const double* __restrict__ w;
   const double* __restrict__ pr;   // primitive scratch (F_* fields, np each)
   const double* __restrict__ gr;   // gradient scratch (G_* fields, np each)
+  const double* __restrict__ qr;   // interpolation rows and point values of the forward passes (Q_*, V_* fields)
   const double* __restrict__ nx;
   const double* __restrict__ ny;
   const double* __restrict__ vol;
@@ -75,6 +77,7 @@ struct AdjCtx {
 
   BCG_HD double W(int i, int j, int v) const { return __ldg(w + (size_t)e.cidx(i, j) + (size_t)(v - 1) * e.np); }
   BCG_HD double P(int f, int i, int j) const { return __ldg(pr + (size_t)f * e.np + e.cidx(i, j)); }
+  BCG_HD double Q(int f, int i, int j) const { return __ldg(qr + (size_t)f * e.np + e.cidx(i, j)); }
   BCG_HD double Gr(int f, int i, int j) const {
     auto g = [&](int ii, int jj) { return __ldg(gr + (size_t)f * e.np + e.cidx(ii, jj)); };
     if (i == 0) return 2.0 * g(1, j) - g(2, j);
@@ -143,14 +146,14 @@ BCG_HD void visc_points_i(const AdjCtx& a, int i, int j, bool o2, ViscPts& v) {
   for (int q = 0; q < 4; ++q) {
     const int f = fl[q];
     if (!o2) {
+      // the forward passes' 3-point values (V_C: 26 P(i) - (P(i+1) + P(i-1)))
+      // and 4-point combinations of the interpolation rows (V_EI), with the
+      // stencils' constant factors
       const double T24 = 1.0 / 24.0, cc = a.c.ccross;
-      v.val[q][0] = T24 * (-a.P(f, i + 1, j) + 26.0 * a.P(f, i, j) - a.P(f, i - 1, j));
-      v.val[q][1] = T24 * (-a.P(f, i, j) + 26.0 * a.P(f, i - 1, j) - a.P(f, i - 2, j));
-      double r[5];
-      for (int k = 0; k < 5; ++k)
-        r[k] = AdjCtx::q4(a.P(f, i - 2, j - 2 + k), a.P(f, i - 1, j - 2 + k), a.P(f, i, j - 2 + k), a.P(f, i + 1, j - 2 + k));
-      v.val[q][2] = cc * (-r[0] + 7.0 * r[1] + 7.0 * r[2] - r[3]);
-      v.val[q][3] = cc * (-r[1] + 7.0 * r[2] + 7.0 * r[3] - r[4]);
+      v.val[q][0] = T24 * a.Q(V_C + q, i, j);
+      v.val[q][1] = T24 * a.Q(V_C + q, i - 1, j);
+      v.val[q][2] = cc * a.Q(V_EI + q, i, j);
+      v.val[q][3] = cc * a.Q(V_EI + q, i, j + 1);
     } else {
       v.val[q][0] = a.P(f, i, j);
       v.val[q][1] = a.P(f, i - 1, j);
@@ -158,11 +161,11 @@ BCG_HD void visc_points_i(const AdjCtx& a, int i, int j, bool o2, ViscPts& v) {
       v.val[q][3] = 0.25 * (a.P(f, i, j) + a.P(f, i, j + 1) + a.P(f, i - 1, j) + a.P(f, i - 1, j + 1));
     }
   }
-  if (!o2) {
-    v.uu = 0.0625 * AdjCtx::q4(a.P(F_U, i - 2, j), a.P(F_U, i - 1, j), a.P(F_U, i, j), a.P(F_U, i + 1, j));
-    v.vv = 0.0625 * AdjCtx::q4(a.P(F_V, i - 2, j), a.P(F_V, i - 1, j), a.P(F_V, i, j), a.P(F_V, i + 1, j));
-    v.ww = 0.0625 * AdjCtx::q4(a.P(F_W, i - 2, j), a.P(F_W, i - 1, j), a.P(F_W, i, j), a.P(F_W, i + 1, j));
-    v.mmu = 0.0625 * AdjCtx::q4(a.P(F_MU, i - 2, j), a.P(F_MU, i - 1, j), a.P(F_MU, i, j), a.P(F_MU, i + 1, j));
+  if (!o2) {  // the interpolation rows QI at the face
+    v.uu = 0.0625 * a.Q(Q_I + 0, i, j);
+    v.vv = 0.0625 * a.Q(Q_I + 1, i, j);
+    v.ww = 0.0625 * a.Q(Q_I + 2, i, j);
+    v.mmu = 0.0625 * a.Q(Q_I + 4, i, j);
   } else {
     v.uu = 0.5 * (a.P(F_U, i, j) + a.P(F_U, i - 1, j));
     v.vv = 0.5 * (a.P(F_V, i, j) + a.P(F_V, i - 1, j));
@@ -183,15 +186,12 @@ BCG_HD void visc_points_j(const AdjCtx& a, int i, int j, bool o2, ViscPts& v) {
   const int fl[4] = {F_U, F_V, F_W, F_T};
   for (int q = 0; q < 4; ++q) {
     const int f = fl[q];
-    if (!o2) {
+    if (!o2) {  // V_NJ: 4-point combinations of the rows QJ; V_D: 3-point values along j
       const double T24 = 1.0 / 24.0, cc = a.c.ccross;
-      double k[5];
-      for (int m = 0; m < 5; ++m)
-        k[m] = AdjCtx::q4(a.P(f, i - 2 + m, j - 2), a.P(f, i - 2 + m, j - 1), a.P(f, i - 2 + m, j), a.P(f, i - 2 + m, j + 1));
-      v.val[q][0] = cc * (-k[1] + 7.0 * k[2] + 7.0 * k[3] - k[4]);
-      v.val[q][1] = cc * (-k[0] + 7.0 * k[1] + 7.0 * k[2] - k[3]);
-      v.val[q][2] = T24 * (-a.P(f, i, j) + 26.0 * a.P(f, i, j - 1) - a.P(f, i, j - 2));
-      v.val[q][3] = T24 * (-a.P(f, i, j + 1) + 26.0 * a.P(f, i, j) - a.P(f, i, j - 1));
+      v.val[q][0] = cc * a.Q(V_NJ + q, i + 1, j);
+      v.val[q][1] = cc * a.Q(V_NJ + q, i, j);
+      v.val[q][2] = T24 * a.Q(V_D + q, i, j - 1);
+      v.val[q][3] = T24 * a.Q(V_D + q, i, j);
     } else {
       v.val[q][0] = 0.25 * (a.P(f, i, j) + a.P(f, i + 1, j) + a.P(f, i, j - 1) + a.P(f, i + 1, j - 1));
       v.val[q][1] = 0.25 * (a.P(f, i, j) + a.P(f, i - 1, j) + a.P(f, i, j - 1) + a.P(f, i - 1, j - 1));
@@ -199,11 +199,11 @@ BCG_HD void visc_points_j(const AdjCtx& a, int i, int j, bool o2, ViscPts& v) {
       v.val[q][3] = a.P(f, i, j);
     }
   }
-  if (!o2) {
-    v.uu = 0.0625 * AdjCtx::q4(a.P(F_U, i, j - 2), a.P(F_U, i, j - 1), a.P(F_U, i, j), a.P(F_U, i, j + 1));
-    v.vv = 0.0625 * AdjCtx::q4(a.P(F_V, i, j - 2), a.P(F_V, i, j - 1), a.P(F_V, i, j), a.P(F_V, i, j + 1));
-    v.ww = 0.0625 * AdjCtx::q4(a.P(F_W, i, j - 2), a.P(F_W, i, j - 1), a.P(F_W, i, j), a.P(F_W, i, j + 1));
-    v.mmu = 0.0625 * AdjCtx::q4(a.P(F_MU, i, j - 2), a.P(F_MU, i, j - 1), a.P(F_MU, i, j), a.P(F_MU, i, j + 1));
+  if (!o2) {  // the interpolation rows QJ at the face
+    v.uu = 0.0625 * a.Q(Q_J + 0, i, j);
+    v.vv = 0.0625 * a.Q(Q_J + 1, i, j);
+    v.ww = 0.0625 * a.Q(Q_J + 2, i, j);
+    v.mmu = 0.0625 * a.Q(Q_J + 4, i, j);
   } else {
     v.uu = 0.5 * (a.P(F_U, i, j) + a.P(F_U, i, j - 1));
     v.vv = 0.5 * (a.P(F_V, i, j) + a.P(F_V, i, j - 1));
@@ -352,12 +352,15 @@ BCG_HD void face_rev(const AdjCtx& a, int dir, int i, int j, double* __restrict_
     rrb -= omrrb;
     const double rb_ = -rr * rr * rrb;
     const double qb = (qrat == 0.0) ? 0.0 : rb_ / (2.0 * r);
-    rhoRb += qb / rhoml;
-    rhoLb -= qb * qrat / rhoml;
-    ruRb += urb / rhomr; rhoRb -= urb * ur / rhomr;
-    rvRb += vrb / rhomr; rhoRb -= vrb * vr / rhomr;
-    ruLb += ulb / rhoml; rhoLb -= ulb * ul / rhoml;
-    rvLb += vlb / rhoml; rhoLb -= vlb * vl / rhoml;
+    // the reverse divides by the two densities through their reciprocals
+    // (derivative values only: the forward quantities above keep the divisions)
+    const double irl = 1.0 / rhoml, irr = 1.0 / rhomr;
+    rhoRb += qb * irl;
+    rhoLb -= qb * qrat * irl;
+    ruRb += urb * irr; rhoRb -= urb * ur * irr;
+    rvRb += vrb * irr; rhoRb -= vrb * vr * irr;
+    ruLb += ulb * irl; rhoLb -= ulb * ul * irl;
+    rvLb += vlb * irl; rhoLb -= vlb * vl * irl;
     TRb += a.c.c2fac * c2rb;
     TLb += a.c.c2fac * c2lb;
   }
@@ -374,9 +377,9 @@ BCG_HD void face_rev(const AdjCtx& a, int dir, int i, int j, double* __restrict_
     g8[2 * q] = vp.val[q][0] * vp.ax[0] + vp.val[q][1] * vp.ax[1] + vp.val[q][3] * vp.ax[3] + vp.val[q][2] * vp.ax[2];
     g8[2 * q + 1] = vp.val[q][0] * vp.ay[0] + vp.val[q][1] * vp.ay[1] + vp.val[q][3] * vp.ay[3] + vp.val[q][2] * vp.ay[2];
   }
-  const double sn = sqrt(nx2), invsn = 1.0 / sn, nxl = fnx * invsn, nyl = fny * invsn;
+  // (fv nx/|n| + gv ny/|n|) |n| = fv nx + gv ny (rhs/fluxnumassembly_i.F), as in the forward faces
   double fvb[4], gvb[4];
-  for (int q = 0; q < 4; ++q) { fvb[q] = -hb[q + 1] * sn * nxl; gvb[q] = -hb[q + 1] * sn * nyl; }
+  for (int q = 0; q < 4; ++q) { fvb[q] = -hb[q + 1] * fnx; gvb[q] = -hb[q + 1] * fny; }
   double mmub = 0, lambdab = 0, uub = 0, vvb = 0, wwb = 0, gb[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   visc_fluxes_rev(vp.mmu, vp.lambda, vp.uu, vp.vv, vp.ww, g8, fvb, gvb, mmub, lambdab, uub, vvb, wwb, gb);
   mmub += a.c.cpprandtl * lambdab;
@@ -462,6 +465,100 @@ BCG_HD double w_row(int s) {  // -1 7 7 -1 over offsets 0..3 from the first row
   switch (s) { case 0: return -1.0; case 1: return 7.0; case 2: return 7.0; case 3: return -1.0; default: return 0.0; }
 }
 
+// The viscous point adjoints of one face record (R_VS, R_VM) that reach a cell
+// at offset (di, dj) = (cell - face) from the face, through the transposed
+// point stencils: N and S are the face's own-direction 3-point values
+// (T24 (-1, 26, -1)), E and O the cross points (ccross x the 4-point column
+// (-1, 9, 9, -1) x the 4-point row (-1, 7, 7, -1)), uu..mmu the 4-point means
+// (0.0625 (-1, 9, 9, -1)); the o2 rows (the wall's first rows) use 2-point
+// and 4-cell averages.  Called from fully unrolled window loops, so di, dj
+// and the zero pattern of the weights are constants and the zero terms drop
+// out; the nonzero terms are summed in the order N, S, E, O.
+template <bool IFACE, bool O2, class RF>
+BCG_HD void gather_visc(double cc, int di, int dj, const RF& Rf, int i, int j, double ub[4], double& mub) {
+  const double T24 = 1.0 / 24.0;
+  double cN = 0.0, cS = 0.0, cE = 0.0, cO = 0.0, cu = 0.0;  // integer stencil factors (0 = no term)
+  bool xN = false, xS = false, xE = false, xO = false;      // factors that take ccross
+  if constexpr (IFACE) {
+    if constexpr (!O2) {
+      cN = (dj == 0) ? (di == 1 ? -1.0 : di == 0 ? 26.0 : di == -1 ? -1.0 : 0.0) : 0.0;
+      cS = (dj == 0) ? (di == 0 ? -1.0 : di == -1 ? 26.0 : di == -2 ? -1.0 : 0.0) : 0.0;
+      const double col = w_q4(di);
+      cE = col; cO = col;
+      xE = w_row(dj + 2) != 0.0; xO = w_row(dj + 1) != 0.0;
+      cu = (dj == 0) ? col : 0.0;
+    } else {
+      cN = (dj == 0 && di == 0) ? 1.0 : 0.0;
+      cS = (dj == 0 && di == -1) ? 1.0 : 0.0;
+      const bool col = (di == 0 || di == -1);
+      cE = (col && (dj == 0 || dj == -1)) ? 1.0 : 0.0;
+      cO = (col && (dj == 0 || dj == 1)) ? 1.0 : 0.0;
+      cu = (col && dj == 0) ? 1.0 : 0.0;
+    }
+  } else {
+    if constexpr (!O2) {
+      const double row = w_q4(dj);
+      cN = row; cS = row;
+      xN = w_row(di + 1) != 0.0; xS = w_row(di + 2) != 0.0;
+      cE = (di == 0) ? (dj == 0 ? -1.0 : dj == -1 ? 26.0 : dj == -2 ? -1.0 : 0.0) : 0.0;
+      cO = (di == 0) ? (dj == 1 ? -1.0 : dj == 0 ? 26.0 : dj == -1 ? -1.0 : 0.0) : 0.0;
+      cu = (di == 0) ? row : 0.0;
+    } else {
+      const bool rowok = (dj == 0 || dj == -1);
+      cN = (rowok && (di == 0 || di == 1)) ? 1.0 : 0.0;
+      cS = (rowok && (di == 0 || di == -1)) ? 1.0 : 0.0;
+      cO = (di == 0 && dj == 0) ? 1.0 : 0.0;
+      cE = (di == 0 && dj == -1) ? 1.0 : 0.0;
+      cu = (di == 0 && rowok) ? 1.0 : 0.0;
+    }
+  }
+  // the weights, in the forms (and roundings) of the point stencils
+  double wN, wS, wE, wO, wuu;
+  if constexpr (IFACE) {
+    if constexpr (!O2) {
+      wN = T24 * cN; wS = T24 * cS;
+      wE = cc * cE * w_row(dj + 2); wO = cc * cO * w_row(dj + 1);
+      wuu = 0.0625 * cu;
+    } else {
+      wN = cN; wS = cS; wE = 0.25 * cE; wO = 0.25 * cO; wuu = 0.5 * cu;
+    }
+  } else {
+    if constexpr (!O2) {
+      wN = cc * cN * w_row(di + 1); wS = cc * cS * w_row(di + 2);
+      wE = T24 * cE; wO = T24 * cO;
+      wuu = 0.0625 * cu;
+    } else {
+      wN = 0.25 * cN; wS = 0.25 * cS; wE = cE; wO = cO; wuu = 0.5 * cu;
+    }
+  }
+  const bool hN = cN != 0.0 && (IFACE || O2 || xN), hS = cS != 0.0 && (IFACE || O2 || xS);
+  const bool hE = cE != 0.0 && (!IFACE || O2 || xE), hO = cO != 0.0 && (!IFACE || O2 || xO);
+  const bool hu = cu != 0.0;
+  if (!(hN || hS || hE || hO || hu)) return;
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    double acc = 0.0;
+    bool any = false;
+    auto add = [&](bool has, double wt, int f) {
+      if (!has) return;
+      const double x = wt * Rf(f, i, j);
+      acc = any ? acc + x : x;
+      any = true;
+    };
+    add(hN, wN, R_VS + 4 * v + 0);
+    add(hS, wS, R_VS + 4 * v + 1);
+    add(hE, wE, R_VS + 4 * v + 2);
+    add(hO, wO, R_VS + 4 * v + 3);
+    if (any) ub[v] += acc;
+  }
+  if (hu) {
+    ub[0] += wuu * Rf(R_VM + 0, i, j);
+    ub[1] += wuu * Rf(R_VM + 1, i, j);
+    ub[2] += wuu * Rf(R_VM + 2, i, j);
+    mub += wuu * Rf(R_VM + 3, i, j);
+  }
+}
+
 __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
   // this cotangent's records
   const double* __restrict__ rec1 = g.rec1 + ycot() * g.kstride;
@@ -476,7 +573,7 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
   double fb[5] = {0, 0, 0, 0, 0}, gb[5] = {0, 0, 0, 0, 0}, wb[5] = {0, 0, 0, 0, 0};
   double ub[4] = {0, 0, 0, 0};  // u, v, w, T
   double pb = 0.0, mub = 0.0;
-  const double T24 = 1.0 / 24.0, cc = c.ccross;
+  const double cc = c.ccross;
   // ---- i-faces -------------------------------------------------------------
   // Euler and predictor on row cj: faces i = ci - s, s in [-3, 2]
   for (int s = -3; s <= 2; ++s) {
@@ -507,35 +604,14 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
     }
   }
   // viscous: i-faces (i, j) with i - ci in [-1, 2] and j - cj in [-2, 2]
-  for (int j = cj - 2; j <= cj + 2; ++j)
-    for (int i = ci - 1; i <= ci + 2; ++i) {
+#pragma unroll
+  for (int jj = -2; jj <= 2; ++jj)
+#pragma unroll
+    for (int ii = -1; ii <= 2; ++ii) {
+      const int i = ci + ii, j = cj + jj;
       if (!g.ifx(i, j)) continue;
-      const bool o2 = c.wall && j <= 2;
-      const int di = ci - i, dj = cj - j;  // cell offset from the face
-      double wN, wS, wE, wO, wuu;
-      if (!o2) {
-        wN = (dj == 0) ? T24 * (di == 1 ? -1.0 : di == 0 ? 26.0 : di == -1 ? -1.0 : 0.0) : 0.0;
-        wS = (dj == 0) ? T24 * (di == 0 ? -1.0 : di == -1 ? 26.0 : di == -2 ? -1.0 : 0.0) : 0.0;
-        const double col = w_q4(di);
-        wE = cc * col * w_row(dj + 2);
-        wO = cc * col * w_row(dj + 1);
-        wuu = (dj == 0) ? 0.0625 * col : 0.0;
-      } else {
-        wN = (dj == 0 && di == 0) ? 1.0 : 0.0;
-        wS = (dj == 0 && di == -1) ? 1.0 : 0.0;
-        const bool col = (di == 0 || di == -1);
-        wE = (col && (dj == 0 || dj == -1)) ? 0.25 : 0.0;
-        wO = (col && (dj == 0 || dj == 1)) ? 0.25 : 0.0;
-        wuu = (col && dj == 0) ? 0.5 : 0.0;
-      }
-      if (wN == 0.0 && wS == 0.0 && wE == 0.0 && wO == 0.0 && wuu == 0.0) continue;
-      for (int v = 0; v < 4; ++v)
-        ub[v] += wN * R1(R_VS + 4 * v + 0, i, j) + wS * R1(R_VS + 4 * v + 1, i, j) +
-                 wE * R1(R_VS + 4 * v + 2, i, j) + wO * R1(R_VS + 4 * v + 3, i, j);
-      ub[0] += wuu * R1(R_VM + 0, i, j);
-      ub[1] += wuu * R1(R_VM + 1, i, j);
-      ub[2] += wuu * R1(R_VM + 2, i, j);
-      mub += wuu * R1(R_VM + 3, i, j);
+      if (c.wall && j <= 2) gather_visc<true, true>(cc, -ii, -jj, R1, i, j, ub, mub);
+      else gather_visc<true, false>(cc, -ii, -jj, R1, i, j, ub, mub);
     }
   // ---- j-faces -------------------------------------------------------------
   // Euler: generic faces j >= 4 over rows j-3..j+2; near-wall faces 2, 3 over
@@ -588,36 +664,14 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
     }
   }
   // viscous j-faces (i, j) with i - ci in [-2, 2] and j - cj in [-1, 2]
-  for (int j = cj - 1; j <= cj + 2; ++j)
-    for (int i = ci - 2; i <= ci + 2; ++i) {
+#pragma unroll
+  for (int jj = -1; jj <= 2; ++jj)
+#pragma unroll
+    for (int ii = -2; ii <= 2; ++ii) {
+      const int i = ci + ii, j = cj + jj;
       if (j < jfirst || !g.jfx(i, j)) continue;
-      const bool o2 = c.wall && (j == 2);
-      const int di = ci - i, dj = cj - j;
-      double wN, wS, wE, wO, wuu;
-      if (!o2) {
-        // N uses columns i-1..i+2 (rows j-2..j+1), S columns i-2..i+1
-        const double row = w_q4(dj);
-        wN = cc * row * w_row(di + 1);
-        wS = cc * row * w_row(di + 2);
-        wE = (di == 0) ? T24 * (dj == 0 ? -1.0 : dj == -1 ? 26.0 : dj == -2 ? -1.0 : 0.0) : 0.0;
-        wO = (di == 0) ? T24 * (dj == 1 ? -1.0 : dj == 0 ? 26.0 : dj == -1 ? -1.0 : 0.0) : 0.0;
-        wuu = (di == 0) ? 0.0625 * row : 0.0;
-      } else {
-        const bool rowok = (dj == 0 || dj == -1);
-        wN = (rowok && (di == 0 || di == 1)) ? 0.25 : 0.0;
-        wS = (rowok && (di == 0 || di == -1)) ? 0.25 : 0.0;
-        wO = (di == 0 && dj == 0) ? 1.0 : 0.0;
-        wE = (di == 0 && dj == -1) ? 1.0 : 0.0;
-        wuu = (di == 0 && rowok) ? 0.5 : 0.0;
-      }
-      if (wN == 0.0 && wS == 0.0 && wE == 0.0 && wO == 0.0 && wuu == 0.0) continue;
-      for (int v = 0; v < 4; ++v)
-        ub[v] += wN * R2(R_VS + 4 * v + 0, i, j) + wS * R2(R_VS + 4 * v + 1, i, j) +
-                 wE * R2(R_VS + 4 * v + 2, i, j) + wO * R2(R_VS + 4 * v + 3, i, j);
-      ub[0] += wuu * R2(R_VM + 0, i, j);
-      ub[1] += wuu * R2(R_VM + 1, i, j);
-      ub[2] += wuu * R2(R_VM + 2, i, j);
-      mub += wuu * R2(R_VM + 3, i, j);
+      if (c.wall && j == 2) gather_visc<false, true>(cc, -ii, -jj, R2, i, j, ub, mub);
+      else gather_visc<false, false>(cc, -ii, -jj, R2, i, j, ub, mub);
     }
   // ---- gradient adjoints (interior cells, sensor only) ----------------------
   double gsb[4] = {0, 0, 0, 0};  // ux, uy, vx, vy
@@ -744,7 +798,8 @@ size_t adjoint_cotangent_doubles(int im, int jm, int gh) {
 
 size_t adjoint_scratch_doubles(int im, int jm, int gh, int ncot) {
   const Ext e = make_ext(im, jm, gh);
-  return (size_t)(F_NPRIM + G_NGRAD) * e.np + (size_t)(ncot > 1 ? ncot : 1) * adjoint_cotangent_doubles(im, jm, gh);
+  return (size_t)(F_NPRIM + G_NGRAD + Q_NQ) * e.np +
+         (size_t)(ncot > 1 ? ncot : 1) * adjoint_cotangent_doubles(im, jm, gh);
 }
 
 cudaError_t run_adjoint(const AdjointArgs& a, cudaStream_t st) {
@@ -754,7 +809,8 @@ cudaError_t run_adjoint(const AdjointArgs& a, cudaStream_t st) {
   const size_t nn = (size_t)(a.im + 1) * (a.jm + 1);
   double* pr = a.scratch;
   double* gr = pr + (size_t)F_NPRIM * e.np;
-  double* cadj = gr + (size_t)G_NGRAD * e.np;
+  double* qr = gr + (size_t)G_NGRAD * e.np;
+  double* cadj = qr + (size_t)Q_NQ * e.np;
   double* rec1 = cadj + (size_t)NCADJ * e.np;
   double* rec2 = rec1 + (size_t)NREC * nn;
   const int B = 256;
@@ -762,7 +818,14 @@ cudaError_t run_adjoint(const AdjointArgs& a, cudaStream_t st) {
   const size_t cstride = a.cstride ? a.cstride : (size_t)5 * e.np;
   const size_t kstride = adjoint_cotangent_doubles(a.im, a.jm, a.gh);
   launch_primal_passes(e, c, a.w, pr, gr, a.nx, a.ny, a.vol, st);  // shared by the cotangents
-  AdjCtx ac{e, c, a.w, pr, gr, a.nx, a.ny, a.vol, a.volf, a.rb, rec1, rec2, nn, cstride, kstride};
+  // the viscous point values of the 4th-order rows, as the forward residual forms them
+  {
+    const GroupStride gs{0, 0};
+    const unsigned gq = (unsigned)((e.np + B - 1) / B);
+    k_qrows<double><<<gq, B, 0, st>>>(e, Scratch<double>{pr, e.np}, Scratch<double>{qr, e.np}, gs);
+    k_vpts<double><<<gq, B, 0, st>>>(e, Scratch<double>{qr, e.np}, gs);
+  }
+  AdjCtx ac{e, c, a.w, pr, gr, qr, a.nx, a.ny, a.vol, a.volf, a.rb, rec1, rec2, nn, cstride, kstride};
   const int BF = 128;
   k_adj_faces<<<dim3((unsigned)((nn + BF - 1) / BF), ncot), BF, 0, st>>>(ac);
   GatherCtx gc{e, c, rec1, rec2, nn, a.nx, a.ny, a.vol, cadj, kstride};
