@@ -236,8 +236,9 @@ BCG_HD void face_rev(const AdjCtx& a, int dir, int i, int j, double* __restrict_
   }
   // forward spectral radius (Roe average of L and R)
   const double rhomr = a.W(i, j, 1), rhoml = a.W(iL, jL, 1);
-  const double ur = a.W(i, j, 2) / rhomr, vr = a.W(i, j, 3) / rhomr;
-  const double ul = a.W(iL, jL, 2) / rhoml, vl = a.W(iL, jL, 3) / rhoml;
+  // velocities of L and R from the primitives pass (rho u times the reciprocal of rho)
+  const double ur = a.P(F_U, i, j), vr = a.P(F_V, i, j);
+  const double ul = a.P(F_U, iL, jL), vl = a.P(F_V, iL, jL);
   const double c2r = a.c.c2fac * a.P(F_T, i, j), c2l = a.c.c2fac * a.P(F_T, iL, jL);
   const double qrat = rhomr / rhoml;
   const double r = sqrt(qrat);
@@ -353,7 +354,6 @@ BCG_HD void face_rev(const AdjCtx& a, int dir, int i, int j, double* __restrict_
     const double rb_ = -rr * rr * rrb;
     const double qb = (qrat == 0.0) ? 0.0 : rb_ / (2.0 * r);
     // the reverse divides by the two densities through their reciprocals
-    // (derivative values only: the forward quantities above keep the divisions)
     const double irl = 1.0 / rhoml, irr = 1.0 / rhomr;
     rhoRb += qb * irl;
     rhoLb -= qb * qrat * irl;
@@ -445,6 +445,8 @@ struct GatherCtx {
   const double* __restrict__ vol;
   double* __restrict__ cadj;  // NCADJ x np
   size_t kstride;             // doubles between the scratch blocks of consecutive cotangents
+  // cross-point weights (ccross * (-1, 9, 9, -1)[a]) * (-1, 7, 7, -1)[b], formed once on the host
+  double wt[4][4];
   BCG_HD bool ifx(int i, int j) const { return i >= 1 && i <= e.im + 1 && j >= 1 && j <= e.jm; }
   BCG_HD bool jfx(int i, int j) const { return i >= 1 && i <= e.im && j >= 1 && j <= e.jm + 1; }
 };
@@ -475,7 +477,8 @@ BCG_HD double w_row(int s) {  // -1 7 7 -1 over offsets 0..3 from the first row
 // and the zero pattern of the weights are constants and the zero terms drop
 // out; the nonzero terms are summed in the order N, S, E, O.
 template <bool IFACE, bool O2, class RF>
-BCG_HD void gather_visc(double cc, int di, int dj, const RF& Rf, int i, int j, double ub[4], double& mub) {
+BCG_HD void gather_visc(const double (&wt)[4][4], int di, int dj, const RF& Rf, int i, int j, double ub[4],
+                        double& mub) {
   const double T24 = 1.0 / 24.0;
   double cN = 0.0, cS = 0.0, cE = 0.0, cO = 0.0, cu = 0.0;  // integer stencil factors (0 = no term)
   bool xN = false, xS = false, xE = false, xO = false;      // factors that take ccross
@@ -517,14 +520,14 @@ BCG_HD void gather_visc(double cc, int di, int dj, const RF& Rf, int i, int j, d
   if constexpr (IFACE) {
     if constexpr (!O2) {
       wN = T24 * cN; wS = T24 * cS;
-      wE = cc * cE * w_row(dj + 2); wO = cc * cO * w_row(dj + 1);
+      wE = 0.0; wO = 0.0;  // from the table below
       wuu = 0.0625 * cu;
     } else {
       wN = cN; wS = cS; wE = 0.25 * cE; wO = 0.25 * cO; wuu = 0.5 * cu;
     }
   } else {
     if constexpr (!O2) {
-      wN = cc * cN * w_row(di + 1); wS = cc * cS * w_row(di + 2);
+      wN = 0.0; wS = 0.0;  // from the table below
       wE = T24 * cE; wO = T24 * cO;
       wuu = 0.0625 * cu;
     } else {
@@ -533,6 +536,16 @@ BCG_HD void gather_visc(double cc, int di, int dj, const RF& Rf, int i, int j, d
   }
   const bool hN = cN != 0.0 && (IFACE || O2 || xN), hS = cS != 0.0 && (IFACE || O2 || xS);
   const bool hE = cE != 0.0 && (!IFACE || O2 || xE), hO = cO != 0.0 && (!IFACE || O2 || xO);
+  // the cross-point weights from the table (the same products, formed once)
+  if constexpr (!O2) {
+    if constexpr (IFACE) {
+      if (hE) wE = wt[di + 2][dj + 2];
+      if (hO) wO = wt[di + 2][dj + 1];
+    } else {
+      if (hN) wN = wt[dj + 2][di + 1];
+      if (hS) wS = wt[dj + 2][di + 2];
+    }
+  }
   const bool hu = cu != 0.0;
   if (!(hN || hS || hE || hO || hu)) return;
 #pragma unroll
@@ -573,7 +586,6 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
   double fb[5] = {0, 0, 0, 0, 0}, gb[5] = {0, 0, 0, 0, 0}, wb[5] = {0, 0, 0, 0, 0};
   double ub[4] = {0, 0, 0, 0};  // u, v, w, T
   double pb = 0.0, mub = 0.0;
-  const double cc = c.ccross;
   // ---- i-faces -------------------------------------------------------------
   // Euler and predictor on row cj: faces i = ci - s, s in [-3, 2]
   for (int s = -3; s <= 2; ++s) {
@@ -610,8 +622,8 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
     for (int ii = -1; ii <= 2; ++ii) {
       const int i = ci + ii, j = cj + jj;
       if (!g.ifx(i, j)) continue;
-      if (c.wall && j <= 2) gather_visc<true, true>(cc, -ii, -jj, R1, i, j, ub, mub);
-      else gather_visc<true, false>(cc, -ii, -jj, R1, i, j, ub, mub);
+      if (c.wall && j <= 2) gather_visc<true, true>(g.wt, -ii, -jj, R1, i, j, ub, mub);
+      else gather_visc<true, false>(g.wt, -ii, -jj, R1, i, j, ub, mub);
     }
   // ---- j-faces -------------------------------------------------------------
   // Euler: generic faces j >= 4 over rows j-3..j+2; near-wall faces 2, 3 over
@@ -670,8 +682,8 @@ __global__ void __launch_bounds__(128) k_adj_gather(GatherCtx g) {
     for (int ii = -2; ii <= 2; ++ii) {
       const int i = ci + ii, j = cj + jj;
       if (j < jfirst || !g.jfx(i, j)) continue;
-      if (c.wall && j == 2) gather_visc<false, true>(cc, -ii, -jj, R2, i, j, ub, mub);
-      else gather_visc<false, false>(cc, -ii, -jj, R2, i, j, ub, mub);
+      if (c.wall && j == 2) gather_visc<false, true>(g.wt, -ii, -jj, R2, i, j, ub, mub);
+      else gather_visc<false, false>(g.wt, -ii, -jj, R2, i, j, ub, mub);
     }
   // ---- gradient adjoints (interior cells, sensor only) ----------------------
   double gsb[4] = {0, 0, 0, 0};  // ux, uy, vx, vy
@@ -828,7 +840,10 @@ cudaError_t run_adjoint(const AdjointArgs& a, cudaStream_t st) {
   AdjCtx ac{e, c, a.w, pr, gr, qr, a.nx, a.ny, a.vol, a.volf, a.rb, rec1, rec2, nn, cstride, kstride};
   const int BF = 128;
   k_adj_faces<<<dim3((unsigned)((nn + BF - 1) / BF), ncot), BF, 0, st>>>(ac);
-  GatherCtx gc{e, c, rec1, rec2, nn, a.nx, a.ny, a.vol, cadj, kstride};
+  GatherCtx gc{e, c, rec1, rec2, nn, a.nx, a.ny, a.vol, cadj, kstride, {}};
+  const double q4w[4] = {-1.0, 9.0, 9.0, -1.0}, roww[4] = {-1.0, 7.0, 7.0, -1.0};
+  for (int x = 0; x < 4; ++x)
+    for (int y = 0; y < 4; ++y) gc.wt[x][y] = c.ccross * q4w[x] * roww[y];
   k_adj_gather<<<dim3((unsigned)((e.np + BF - 1) / BF), ncot), BF, 0, st>>>(gc);
   k_adj_final<<<dim3((unsigned)((e.np + B - 1) / B), ncot), B, 0, st>>>(e, c, a.w, cadj, a.wb, a.rb, cstride, kstride);
   return cudaGetLastError();
