@@ -881,7 +881,7 @@ def run_batch(args):
             "inputs_sha": inputs_digest(cs, wds),
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "gpu_launches": 6 * args.steps,
+            "gpu_launches": 7 * args.steps,  # per graph replay: the rectilinear scan and the six passes
             "clocks": clocks,
         }
     if not args.no_extras and rank == 0:

@@ -93,7 +93,7 @@ class GridBatch:
         _lib.call("bcg_batch_configure_host", self.plan, int(tile_faces), int(tile_cells), int(ctas_per_sm))
         self.host_config = (int(tile_faces), int(tile_cells), int(ctas_per_sm))
 
-    def autotune_host(self, ws, wds, res, resd, geo, nchunk=16, candidates=CANDIDATES, repeats=2):
+    def autotune_host(self, ws, wds, res, resd, geo, nchunk=16, candidates=CANDIDATES, repeats=3):
         """Time run_host (wall clock, copies included) with each candidate tile
         shape for the chunks and keep the fastest; the whole batch's own shapes
         (configure / autotune) stay as they are."""
