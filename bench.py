@@ -593,10 +593,10 @@ def _flux_scale(c):
 #       python bench.py --grids 6 --steps 1 --warmup 1 --no-extras --tile 128,128,3 --cpu-seconds 1
 # divided by the capture's cells; the full batch's figures scale with its cells.
 BATCH_NCU = {
-    "fp64_inst_per_cell": {"prim": 141.1, "sensor": 175.9, "qrows": 93.3, "vpts": 48.5, "faces": 849.7,
+    "fp64_inst_per_cell": {"prim": 135.9, "sensor": 175.9, "qrows": 93.3, "vpts": 48.5, "faces": 833.7,
                            "balance": 30.0},
-    "dram_bytes_per_cell": {"prim": 351.4, "sensor": 161.5, "qrows": 338.9, "vpts": 232.2, "faces": 900.5,
-                            "balance": 219.7},
+    "dram_bytes_per_cell": {"prim": 351.3, "sensor": 161.2, "qrows": 338.9, "vpts": 231.9, "faces": 900.7,
+                            "balance": 219.4},
     "source": "ncu sm__inst_executed_pipe_fp64.sum x 32 lanes and dram__bytes_read.sum + dram__bytes_write.sum "
               "per k_batch launch, first 6 grids (1,344,226 cells), cold caches; per cell, scaled to this run's "
               "cells; prim includes the rectilinear-grid scan (k_batch_rect) that runs with it",

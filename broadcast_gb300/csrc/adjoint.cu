@@ -241,13 +241,15 @@ BCG_HD void face_rev(const AdjCtx& a, int dir, int i, int j, double* __restrict_
   const double ul = a.P(F_U, iL, jL), vl = a.P(F_V, iL, jL);
   const double c2r = a.c.c2fac * a.P(F_T, i, j), c2l = a.c.c2fac * a.P(F_T, iL, jL);
   const double qrat = rhomr / rhoml;
-  const double r = sqrt(qrat);
+  const double rsq = (qrat == 0.0) ? 0.0 : rsqrt(qrat);  // r = sqrt(qrat) through rsqrt, reused by the reverse
+  const double r = qrat * rsq;
   const double rr = 1.0 / (1.0 + r), omrr = 1.0 - rr;
   const double u = ul * rr + ur * omrr, v = vl * rr + vr * omrr;
   const double c2x = c2l * rr + c2r * omrr;
   const double nx2 = fnx * fnx + fny * fny;
   const double X = fnx * u + fny * v;
-  const double sq = sqrt(c2x * nx2);
+  const double c2n = c2x * nx2, rsc = (c2n == 0.0) ? 0.0 : rsqrt(c2n);
+  const double sq = c2n * rsc;  // sqrt(c2x nx2) through rsqrt, reused by the reverse
   const double rspec = fabs(X) + sq;
   // forward sensor
   double eps2 = 0.0, eps4 = 0.0 < a.c.k4 ? a.c.k4 : 0.0;
@@ -344,7 +346,7 @@ BCG_HD void face_rev(const AdjCtx& a, int dir, int i, int j, double* __restrict_
   // reverse of rspec = |X| + sqrt(c2x nx2) with the Roe average
   {
     const double Xb = X >= 0.0 ? rspecb : -rspecb;
-    const double c2xb = (c2x * nx2 == 0.0) ? 0.0 : rspecb * nx2 / (2.0 * sq);
+    const double c2xb = rspecb * nx2 * (0.5 * rsc);
     const double ub = fnx * Xb, vb = fny * Xb;
     double rrb = ul * ub + vl * vb + c2l * c2xb;
     const double omrrb = ur * ub + vr * vb + c2r * c2xb;
@@ -352,7 +354,7 @@ BCG_HD void face_rev(const AdjCtx& a, int dir, int i, int j, double* __restrict_
     const double c2lb = rr * c2xb, c2rb = omrr * c2xb;
     rrb -= omrrb;
     const double rb_ = -rr * rr * rrb;
-    const double qb = (qrat == 0.0) ? 0.0 : rb_ / (2.0 * r);
+    const double qb = rb_ * (0.5 * rsq);
     // the reverse divides by the two densities through their reciprocals
     const double irl = 1.0 / rhoml, irr = 1.0 / rhomr;
     rhoRb += qb * irl;

@@ -87,6 +87,16 @@ template <int K> BCG_HD DK<K> sqrt_t(const DK<K>& a) { DK<K> r; r.v = sqrt(a.v);
 #pragma unroll
   for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * s; return r; }
 BCG_HD double sqrt_t(double a) { return sqrt(a); }
+// sqrt through one reciprocal square root: x rsqrt(x), derivative 0.5 rsqrt(x)
+// (within 2 ulp of the correctly rounded sqrt; for the magnitudes that feed
+// no branch: spectral radius, sqrt(rho), the Sutherland term)
+template <int K> BCG_HD DK<K> sqrt_r(const DK<K>& a) { DK<K> r;
+  const double rs = (a.v == 0.0) ? 0.0 : rsqrt(a.v);
+  r.v = a.v * rs;
+  const double s = 0.5 * rs;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * s; return r; }
+BCG_HD double sqrt_r(double a) { return (a == 0.0) ? 0.0 : a * rsqrt(a); }
 template <int K> BCG_HD DK<K> fabs_t(const DK<K>& a) { return (a.v >= 0.0) ? a : -a; }
 BCG_HD double fabs_t(double a) { return fabs(a); }
 template <int K> BCG_HD DK<K> tanh_t(const DK<K>& a) { DK<K> r; r.v = tanh(a.v); const double s = 1.0 - r.v * r.v;

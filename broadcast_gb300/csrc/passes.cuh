@@ -28,9 +28,9 @@ BCG_HD void prim_cell(const Ext& e, const Coef& c, const State<S>& w, const Scra
   pr.st(F_U, q, u); pr.st(F_V, q, v); pr.st(F_W, q, ww); pr.st(F_T, q, t); pr.st(F_P, q, p);
   pr.st(F_F2, q, ru * u + p); pr.st(F_F3, q, ru * v); pr.st(F_F4, q, ru * ww); pr.st(F_F5, q, ru * htot);
   pr.st(F_G2, q, rv * u); pr.st(F_G3, q, rv * v + p); pr.st(F_G4, q, rv * ww); pr.st(F_G5, q, rv * htot);
-  pr.st(F_MU, q, c.betas / (t + c.s_suth) * sqrt_t(t) * t);
+  pr.st(F_MU, q, c.betas / (t + c.s_suth) * sqrt_r(t) * t);
   // Roe-average ingredients: sqrt(rho), and sqrt(rho) times u, v and c^2
-  const S sr = sqrt_t(ro);
+  const S sr = sqrt_r(ro);
   pr.st(F_SR, q, sr);
   pr.st(F_SU, q, sr * u);
   pr.st(F_SV, q, sr * v);
@@ -437,7 +437,7 @@ struct FaceCtx {
     S un;
     if constexpr (RECT) un = DIR == 1 ? fnx * u : fny * v;
     else un = fnx * u + fny * v;
-    const S rspec = fabs_t(un) + sqrt_t(c2x * nx2);
+    const S rspec = fabs_t(un) + sqrt_r(c2x * nx2);
     if (c.k2 == 0.0) {
       // with k2 = 0 the sensor is multiplied by zero (0 * coef = 0 for the
       // finite coef of a physical state, and so is its tangent): eps2 = 0,
