@@ -238,7 +238,7 @@ int run_jacobian(const JacobianArgs& a, cudaStream_t st) {
   ResidualArgs ra{};
   ra.im = im; ra.jm = jm; ra.gh = gh; ra.phys = a.phys; ra.w = wcopy; ra.nx = a.nx; ra.ny = a.ny;
   ra.vol = a.vol; ra.volf = a.volf; ra.dstride = np * 5; ra.scratch = rscr; ra.res = nullptr;
-  ra.rect = face_rectilinear_device(a.nx, a.ny, im, jm, gh, st) ? 1 : 0;
+  ra.rect = face_rectilinear(a.nx, a.ny, im, jm, gh, st) ? 1 : 0;
   // chunks of G groups of 4 seeds: seed, linearised boundary chain per group,
   // then one tangent launch per pass over the whole chunk (blockIdx.y = group);
   // the last seeds (245 = 61 * 4 + 1, 490 = 122 * 4 + 2) run as 1-direction chunks

@@ -62,6 +62,10 @@ bool face_rectilinear(const double* nx, const double* ny, int im, int jm, int gh
                    (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged);
   cudaGetLastError();
   if (!dev) return face_rectilinear_host(nx, ny, im, jm, gh);
+  // a stream being captured into a graph cannot wait for the check: the general kernel
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) { cudaGetLastError(); return false; }
+  if (cap != cudaStreamCaptureStatusNone) return false;
   int d = 0;
   cudaGetDevice(&d);
   const auto key = std::make_tuple(d, nx, ny, im, jm, gh);

@@ -35,7 +35,8 @@ bool face_rectilinear_host(const double* nx, const double* ny, int im, int jm, i
 bool face_rectilinear_device(const double* nx, const double* ny, int im, int jm, int gh, cudaStream_t st);
 // the same, host or device arrays alike; device results that are false are
 // remembered per (nx, ny, im, jm, gh) so that repeated calls on a curvilinear
-// grid's resident metrics skip the check (a remembered false only costs speed)
+// grid's resident metrics skip the check (a remembered false only costs speed),
+// and a stream that is being captured into a graph gets false (no wait)
 bool face_rectilinear(const double* nx, const double* ny, int im, int jm, int gh, cudaStream_t st);
 
 size_t residual_scratch_doubles(int im, int jm, int gh, int ndir);
