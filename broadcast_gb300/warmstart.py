@@ -376,11 +376,15 @@ def solve_baseflows(params, im, jm, ratio=None, tol=1e-10, maxit=12, log=None, s
 
 
 def compare_starts(model, train_params, train_states, held_params, im, jm, ratio=None, tol=1e-10, maxit=12,
-                   log=None, solver=None):
+                   log=None, solver=None, solver_learned=None):
     """Time to tol for every held-out (Re, Mach): from the nearest training
     base flow (plain continuation) and from the network's guess (with the
-    plain start as fallback), both with the same linear `solver`.  Returns
-    per-point records."""
+    plain start as fallback).  Each arm solves with its own linear solver
+    (`solver` for the plain arm, `solver_learned` for the learned one; the same
+    object when that is None), so that a solver that keeps state between solves
+    (the Krylov solver's preconditioner factor) gives neither arm the other's
+    work: give two solvers in the same state.  Returns per-point records."""
+    solver_learned = solver if solver_learned is None else solver_learned
     ratio = radial_ratio(jm) if ratio is None else ratio
     ok = [i for i, s in enumerate(train_states) if s is not None]
     ta, tb = normalise(train_params[ok, 0], train_params[ok, 1])
@@ -402,15 +406,15 @@ def compare_starts(model, train_params, train_states, held_params, im, jm, ratio
         t0 = time.perf_counter()
         guess = decode(model.predict(theta, rho, re, mach), case["phys"], im, jm)
         t_guess = time.perf_counter() - t0
-        _, learned = newton_to_tol(case, _full_state(case, guess), tol=tol, maxit=maxit, solver=solver)
+        _, learned = newton_to_tol(case, _full_state(case, guess), tol=tol, maxit=maxit, solver=solver_learned)
         learned["seconds"] += t_guess
         learned["guess_seconds"] = t_guess
         learned["fallback"] = False
         if not learned["converged"]:  # the plain start as fallback
             if plain["iterations"] and not plain["fallback"]:
-                _, fb = newton_to_tol(case, w_plain0, tol=tol, maxit=maxit, solver=solver)
+                _, fb = newton_to_tol(case, w_plain0, tol=tol, maxit=maxit, solver=solver_learned)
             else:
-                _, fb = sequenced_baseflow(re, mach, im, jm, tol=tol, maxit=maxit, solver=solver)
+                _, fb = sequenced_baseflow(re, mach, im, jm, tol=tol, maxit=maxit, solver=solver_learned)
             learned.update(fallback=True, converged=fb["converged"], seconds=learned["seconds"] + fb["seconds"],
                            iterations=learned["iterations"] + fb["iterations"])
         rec = dict(re=float(re), mach=float(mach), plain=plain, learned=learned)
