@@ -28,9 +28,11 @@ void jvp_k(double* res, double* resd, const double* w, const double* wd, int nd,
            int order = 5) {
   const size_t n = np_(im, jm, gh) * 5;
   std::vector<Dual<K>> wdual(n), rdual(n);
+  // wd holds nd <= K directions: the dual slots past nd stay zero (they are
+  // never written back), so nothing past the caller's nd planes is read
   for (size_t q = 0; q < n; ++q) {
     wdual[q].v = w[q];
-    for (int k = 0; k < K; ++k) wdual[q].d[k] = wd[(size_t)k * n + q];
+    for (int k = 0; k < K; ++k) wdual[q].d[k] = k < nd ? wd[(size_t)k * n + q] : 0.0;
   }
   flux_num_dnc5_2d<Dual<K>>(rdual.data(), wdual.data(), nx, ny, vol, volf, gh, c, im, jm, wall, order);
   FArr<Dual<K>> r(rdual.data(), im + 2 * gh, jm + 2 * gh, 1 - gh);
