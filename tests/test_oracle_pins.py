@@ -8,9 +8,9 @@ kernels match to rounding in the GPU parity tests.
 - The reference's own finite-difference recipe for the tangent
   (BROADCAST_npz.py:1091-1125), executed against the linearised boundary chain
   plus the tangent of flux_num_dnc5_2d_d.
-- The colored 245-seed Jacobian assembly (misc/ComputeJacobian.f90:292-1204,
-  the loops of BROADCAST_npz.py:1068-1137 and cylinder.py:889-960) against the
-  dense Jacobian built column by column from unit directions.
+- The colored 245-seed Jacobian and Dz / Dzz assemblies (misc/ComputeJacobian.f90:292-1204,
+  the loops of BROADCAST_npz.py:1068-1137, 1221-1249 and cylinder.py:889-960)
+  against the dense operators built column by column from unit directions.
 """
 import numpy as np
 import pytest
@@ -248,5 +248,43 @@ def test_colored_assembly_equals_dense_columns(kind):
     keep = (ia >= 0) & (ia < n) & (np.abs(jac) > mini)
     A = sp.csr_matrix((jac[keep], (ia[keep], ja[keep])), shape=(n, n)).toarray()
     D = _dense_jacobian(c, w)
+    D[np.abs(D) <= mini] = 0.0
+    assert np.array_equal(A, D), np.abs(A - D).max()
+
+
+@pytest.mark.parametrize("which", ["dz", "dzz"])
+def test_spanwise_assembly_equals_dense_columns(which):
+    """The Dz / Dzz assembly of BROADCAST_npz.py:1221-1249 (testvector, the
+    linearised boundary chain, coeffs_5p_dz / coeffs_5p_dz2,
+    computejacobianfromdz, the 2e-16 filter) is the dense operator built from
+    unit columns bit for bit."""
+    op = O.dz if which == "dz" else O.dzz
+    c = H.bl_case(14, 14, seed=1)
+    g, ph = c["grid"], c["phys"]
+    im, jm, gh = g["im"], g["jm"], g["gh"]
+    w = c["w"].copy(order="F")
+    H.oracle_bcs(c, w)
+    n, nb, mini = 5 * im * jm, im * jm * 49 * 25, 2e-16
+    jac, ia, ja = np.zeros(nb), np.zeros(nb, np.int32), np.zeros(nb, np.int32)
+    for m in range(5):
+        for l in range(7):
+            for k in range(7):
+                wd = O.testvector(m, l, k, gh, im, jm)
+                H.oracle_bcs(c, w.copy(order="F"), wd)
+                O.computejacobian(O.JAC_DZ, jac, ia, ja, op(g, ph, w, wd), m, l, k, gh, im, jm, None)
+    keep = (ia >= 0) & (ia < n) & (np.abs(jac) > mini)
+    A = sp.csr_matrix((jac[keep], (ia[keep], ja[keep])), shape=(n, n)).toarray()
+    D = np.zeros((n, n))
+    for i in range(im):
+        for j in range(jm):
+            wds = []
+            for v in range(5):
+                wd = np.zeros_like(w, order="F")
+                wd[i + gh, j + gh, v] = 1.0
+                H.oracle_bcs(c, w.copy(order="F"), wd)
+                wds.append(wd)
+            out = op(g, ph, w, np.stack(wds))
+            for v in range(5):
+                D[:, v + 5 * j + 5 * jm * i] = H.interior(out[v]).reshape(-1)
     D[np.abs(D) <= mini] = 0.0
     assert np.array_equal(A, D), np.abs(A - D).max()
