@@ -380,6 +380,7 @@ int bcg_abi_version(void) { return 1; }
 int bcg_set_stream(void* stream) { set_stream((cudaStream_t)stream); return BCG_OK; }
 void* bcg_get_stream(void) { return (void*)current_stream(); }
 int bcg_synchronize(void) {
+  if (!has_device()) return fail_arg("no CUDA device"), BCG_ERR_NODEV;
   cudaError_t e = cudaStreamSynchronize(current_stream());
   return e == cudaSuccess ? BCG_OK : fail_cuda("bcg_synchronize", e);
 }

@@ -17,6 +17,11 @@ __global__ void k_fp64_fma(double* out, int iters, double a, double b) {
 
 extern "C" int bcg_fp64_peak_tflops(double* tflops) {
   using namespace bcg;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail_arg("fp64 peak: no CUDA device"), BCG_ERR_NODEV;
+  }
   int dev = 0, sms = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
