@@ -288,3 +288,43 @@ def test_spanwise_assembly_equals_dense_columns(which):
                 D[:, v + 5 * j + 5 * jm * i] = H.interior(out[v]).reshape(-1)
     D[np.abs(D) <= mini] = 0.0
     assert np.array_equal(A, D), np.abs(A - D).max()
+
+
+# ---- adjoint dot-product identity through the boundary chain -----------------------
+def test_adjoint_chain_dot_product():
+    """<T x, u> = <x, T^T u> for T = (interior of) the residual tangent after
+    the boundary-layer chain of tangent fills (inlet, no-reflexion,
+    extrapolation, wall; BROADCAST_npz.py:1079-1085), and T^T = the residual
+    adjoint (flux_num_dnc5_b.f90) followed by the fill adjoints in reverse
+    order (bc_*_b.f90), with x and u random on the interior; to 1e-12."""
+    c = H.bl_case(24, 18, seed=2)
+    g, ph, it = c["grid"], c["phys"], c["interf"]
+    im, jm, gh = g["im"], g["jm"], g["gh"]
+    w = c["w"].copy(order="F")
+    H.oracle_bcs(c, w)
+    rng = np.random.default_rng(31)
+    x = np.zeros_like(w, order="F")
+    x[gh:-gh, gh:-gh] = rng.standard_normal((im, jm, 5))
+    u = np.zeros_like(w, order="F")
+    u[gh:-gh, gh:-gh] = rng.standard_normal((im, jm, 5))
+    steps = [("inlet", "Ilo"), ("noref", "Jhi"), ("extrap", "Ihi"), ("wall", "Jlo")]
+    states, ws, tx = [], w.copy(order="F"), x.copy(order="F")
+    for kind, loc in steps:
+        states.append(ws.copy(order="F"))
+        if kind == "inlet":
+            O.bc_inlet(ws, loc, it[loc], c["field"], g["nx"], g["ny"], ph["gam"], im, jm, gh, wd=tx)
+        elif kind == "noref":
+            O.bc_noref(ws, c["wbd"], loc, it[loc], g["nx"], g["ny"], ph["gam"], gh, im, jm, wd=tx)
+        elif kind == "extrap":
+            O.bc_extrap(ws, loc, it[loc], im, jm, gh, wd=tx)
+        else:
+            O.bc_wall(ws, loc, ph["gam"], it[loc], gh, im, jm, wd=tx)
+    _, jx = O.jvp(g, ph, ws, tx)
+    lhs = float(np.sum(H.interior(jx) * H.interior(u)))
+    wb = O.vjp(g, ph, ws, u)
+    for (kind, loc), st in zip(reversed(steps), reversed(states)):
+        aux = {"inlet": c["field"], "noref": c["wbd"]}.get(kind)
+        O.bc_adjoint(kind, st, wb, loc, it[loc], gh, im, jm, gam=ph["gam"], aux=aux, nx=g["nx"], ny=g["ny"])
+    rhs = float(np.sum(x * wb))
+    scale = float(np.sum(np.abs(H.interior(jx) * H.interior(u))))
+    assert abs(lhs - rhs) <= 1e-12 * scale, (lhs, rhs)
