@@ -51,3 +51,47 @@ def test_lists_from_csr_rebuild_the_matrix():
     perm = rng.permutation(len(v))  # the reference's lists come in seed-slot order
     b = sp.csr_matrix((v[perm], (ia[perm], ja[perm])), shape=a.shape)  # createMatPetscCSR's conversion
     assert (a != b).nnz == 0
+
+
+def _reference_inputs():
+    """The inputs tests/golden/make_npz.py gave the reference's writer."""
+    import importlib.util
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "make_npz.py")
+    spec = importlib.util.spec_from_file_location("make_npz", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.inputs(), mod.OUT
+
+
+def test_reads_the_file_the_reference_writes():
+    """tests/golden/npz_tree_bl_10x8.npz was written by the reference's own
+    writeNPZ, fillNPZ and fillNPZ_3D (BROADCAST_npz.py:247-333); readNPZtree
+    returns what they were given, the end-of-run state and residual first."""
+    (args, fill, _), fn = _reference_inputs()
+    t = npz.readNPZtree(fn)
+    assert len(t) == 36
+    assert (int(t[0]), int(t[1]), int(t[2])) == args[:3]
+    assert np.array_equal(t[3], fill[0]) and np.array_equal(t[14], fill[1])
+    for q in range(4, 14):
+        assert np.array_equal(t[q], args[q]), q
+    assert t[15] == "dnc5" and t[22] == args[22]
+    for q in (18, 19, 20, 21):
+        assert np.array_equal(t[q], args[q]), q
+
+
+def test_writes_what_the_reference_writes(tmp_path):
+    """The same calls through this package give the same file: the same keys,
+    and under each key the same dtype, shape, memory order and values."""
+    (args, fill, fill3), ref_fn = _reference_inputs()
+    fn = str(tmp_path / "tree")
+    npz.writeNPZ(fn, *args, pinf=1.0)
+    npz.fillNPZ(fn, *fill)
+    npz.fillNPZ_3D(fn, *fill3)
+    mine, ref = np.load(fn + ".npz"), np.load(ref_fn + ".npz")
+    assert set(mine.files) == set(ref.files)
+    for k in ref.files:
+        a, b = mine[k], ref[k]
+        assert a.dtype == b.dtype and a.shape == b.shape, k
+        assert a.flags.f_contiguous == b.flags.f_contiguous and a.flags.c_contiguous == b.flags.c_contiguous, k
+        assert np.array_equal(a, b), k
