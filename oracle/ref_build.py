@@ -50,6 +50,8 @@ ROUTINES = [
     ("srcfv/adjoint/bc_supandsubinlet_b.f90", ["bc_supandsubinlet_2d_b"]),
     ("srcfv/adjoint/bc_extrapolateo2_b.f90", ["bc_extrapolate_o2_2d_b"]),
     ("srcfv/adjoint/jn_match_2d_b.f90", ["jn_match_2d_b"]),
+    ("srcfv/prepro/jn_match.f90", ["jn_match_2d"]),
+    ("srcfv/prepro/jn_match_geom.f90", ["jn_match_geom_2d"]),
     ("misc/ComputeJacobian.f90", ["testvector", "testvector_partial", "computejacobianfromjv",
                                   "computejacobianfromjv_relaxed", "computejacobianfromjv_relaxed_withjn",
                                   "computejacobianfromjv_withjn", "computejacobianfromjv_relaxed_withjnandcheck",

@@ -303,6 +303,7 @@ def _number(txt):
 class Var:
     def __init__(self, name, typ, dims=None, arg=False):
         self.name, self.typ, self.dims, self.arg = name, typ, dims, arg
+        self.ptr = False  # a scalar POINTER local: held as a C pointer, read through it
 
 
 class Sub:
@@ -321,7 +322,7 @@ class Sub:
             if args is None:
                 if v.dims:
                     return Expr("ARRAY:" + name, "array")
-                code = ("(*%s)" % name) if (v.arg and v.typ != "char") else name
+                code = ("(*%s)" % name) if ((v.arg or v.ptr) and v.typ != "char") else name
                 return Expr(code, v.typ if v.typ != "char" else "str")
             if not v.dims:
                 if v.typ == "char":
@@ -450,7 +451,15 @@ class Translator:
                 continue
             m = DECL.match(s)
             if m and "::" in s:
-                self._decl(sub, m.group(1), s.split("::", 1)[0][len(m.group(1)):], s.split("::", 1)[1])
+                attrs = s.split("::", 1)[0][len(m.group(1)):]
+                names = s.split("::", 1)[1]
+                self._decl(sub, m.group(1), attrs, names)
+                if re.search(r"\bpointer\b", attrs, re.I):
+                    for n in _split_top(names):
+                        v = sub.vars[n.strip().lower()]
+                        if v.dims:
+                            raise TranslateError("array pointer %s not supported" % v.name)
+                        v.ptr = True
                 continue
             body.append(s)
         for a in args:
@@ -506,6 +515,9 @@ class Translator:
         # scalar locals first (array extents may use them? only args)
         for v in sub.vars.values():
             if v.arg or v.dims:
+                continue
+            if v.ptr:
+                lines.append("  %s* %s = 0;" % (self._ctype(v), v.name))
                 continue
             if v.typ == "char":
                 lines.append("  char %s[64] = {0};" % v.name)
@@ -627,7 +639,13 @@ class Translator:
                 i += 1
                 continue
             if "=>" in s:
-                raise TranslateError("pointer assignment not supported: %s" % s)
+                m = re.match(r"^(\w+)\s*=>\s*(\w+)$", s)
+                p, q = (sub.vars.get(m.group(1).lower()), sub.vars.get(m.group(2).lower())) if m else (None, None)
+                if p is None or q is None or not p.ptr or q.dims or q.typ != p.typ:
+                    raise TranslateError("pointer assignment not supported: %s" % s)
+                lines.append("%s%s = %s%s;" % (pad, p.name, "" if (q.arg or q.ptr) else "&", q.name))
+                i += 1
+                continue
             self._assign(sub, s, lines, pad)
             i += 1
 
@@ -653,7 +671,7 @@ class Translator:
             a = a.strip()
             if re.match(r"^\w+$", a) and a.lower() in sub.vars:
                 v = sub.vars[a.lower()]
-                if v.dims or v.typ == "char" or v.arg:
+                if v.dims or v.typ == "char" or v.arg or v.ptr:
                     actual.append(v.name)
                 else:
                     actual.append("&" + v.name)

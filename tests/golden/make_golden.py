@@ -68,10 +68,12 @@ def ref_bcs(c, w, wd=None):
             ref.call("bc_no_reflexion_2d_d", w, wd, wbd, "Jhi", fi(it["Jhi"]), g["nx"], g["ny"], gam, gh, im, jm,
                      wbd.shape[0])
             ref.call("bc_wall_viscous_adia_2d_d", w, wd, "Jlo", gam, fi(it["Jlo"]), gh, im, jm)
-        # periodic joins (borders/jn_match.F90): block copies of gh columns
+        # periodic joins through the reference's jn_match_2d (borders/jn_match.F90), the
+        # drivers' ranges (cylinder.py:481-486), each array its own donor
         for a in ([w] if wd is None else [wd, w]):
-            a[gh + im:gh + im + gh] = a[gh:2 * gh]
-            a[0:gh] = a[im:im + gh]
+            for prr, prd in ((it["prr1"], it["prd2"]), (it["prr2"], it["prd1"])):
+                ref.call("jn_match_2d", a, fi(prr), gh, gh, gh, gh, im, jm, a, fi(prd), gh, gh, gh, gh, im, jm,
+                         fi(it["tr"]), 5)
 
 
 def residual_args(c):

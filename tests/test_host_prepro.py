@@ -101,3 +101,18 @@ def test_jn_match_geom_against_oracle_join():
         f_bnd.jn_match_geom_2d(x, it["prr1"], gh, gh, gh, gh, im, jm, x, it["prd2"], gh, gh, gh, gh, im, jm, it["tr"])
         f_bnd.jn_match_geom_2d(x, it["prr2"], gh, gh, gh, gh, im, jm, x, it["prd1"], gh, gh, gh, gh, im, jm, it["tr"])
         assert np.array_equal(x, g[key]), key
+
+
+@pytest.mark.parametrize("im,jm", [(14, 8), (15, 10)])
+@pytest.mark.parametrize("build", ["library", "oracle"])
+def test_omesh_metrics_against_the_reference_driver(im, jm, build):
+    """The O-mesh metrics with their periodic joins (cases.cyl_grid, through
+    the library's host routines or the oracle) against the reference driver's
+    own statements (cylinder.py:478-525: computegeom_2d, jn_match_geom_2d on
+    xc, yc, vol, jn_match_2d on the face normals, volf), executed on the same
+    nodes by tests/golden/make_omesh.py: bit for bit, ghosts included."""
+    import os
+    fix = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "omesh_metrics.npz"))
+    g = cases.cyl_grid(im, jm, ops=None if build == "library" else H.OracleOps)
+    for k in ("nx", "ny", "xc", "yc", "vol", "volf"):
+        assert np.array_equal(g[k], fix["%s_%dx%d" % (k, im, jm)]), k
