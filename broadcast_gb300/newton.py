@@ -39,6 +39,12 @@ class BLNewton:
     cfl = 1e10 is the boundary-layer card's setting (card_bl2d_fv_npz.py:56):
     the relaxation vanishes and the iteration is Newton's."""
 
+    # the boundary-layer driver forms dt once, before its Newton loop
+    # (BROADCAST_npz.py:1009): halving the CFL number after a failed update
+    # leaves dt as it was; the cylinder driver forms dt from the CFL number at
+    # every iteration (cylinder.py:842), so there dt halves with it
+    dt_follows_cfl = False
+
     def __init__(self, case, cfl=1.0e10, mach=None, solver=band_lu_solve):
         from ._f2py import interf4
         _lib.load()
@@ -128,7 +134,8 @@ class BLNewton:
             self.norm0m1 = 1.0 / np.maximum(norm, 1e-15)
             self.ninf0m1 = 1.0 / np.maximum(ninf, 1e-15)
         r = np.max(np.concatenate([norm[:3] * self.norm0m1[:3], ninf[:3] * self.ninf0m1[:3]]))
-        cflm1 = r / self.dt
+        dtm1 = 1.0 / self.dt
+        cflm1 = r * dtm1  # BROADCAST_npz.py:1010,1063; cylinder.py:843,890
         gh = self.gh
         coefdiag = cflm1 * self.c["grid"]["vol"][gh:-gh, gh:-gh]
         rhs = np.ravel(res[gh:-gh, gh:-gh, :])
@@ -154,12 +161,13 @@ class BLNewton:
             w[gh:-gh, gh:-gh, :] += dw
             self.dw_old = dw
         else:
-            # step back and halve the CFL number (:1167-1172); here the time
-            # step follows the CFL number
+            # step back and halve the CFL number (BROADCAST_npz.py:1170-1175,
+            # cylinder.py:1026-1031)
             if hasattr(self, "dw_old"):
                 w[gh:-gh, gh:-gh, :] -= self.dw_old
             self.cfl /= 2.0
-            self.dt /= 2.0
+            if self.dt_follows_cfl:
+                self.dt /= 2.0
         t3 = time.perf_counter()
         self.history.append(dict(norm=norm.tolist(), cflm1=float(cflm1), nnz=nnz, seconds=t3 - t0,
                                  seconds_residual=t1 - t0, seconds_jacobian=t2 - t1, seconds_solve=t3 - t2))
@@ -185,6 +193,8 @@ class CylNewton(BLNewton):
     GPU; the linear solve by the GPU band LU in the folded azimuthal order,
     which makes the periodic Jacobian banded (kl ~ 15 im + 35).  The cylinder
     card runs cfl 0.9 (card_cyl2d.py:57); cfl 1e10 gives Newton's iteration."""
+
+    dt_follows_cfl = True
 
     def __init__(self, case, cfl=1.0e10, mach=None, solver=None):
         g = case["grid"]

@@ -34,7 +34,7 @@ def test_first_update_matches_reference_loop():
     n2, ninf = O.norml2inf(res, im, jm, gh)
     n2, ninf = np.asarray(n2), np.asarray(ninf)
     r = np.max(np.concatenate([n2[:3] / np.maximum(n2[:3], 1e-15), ninf[:3] / np.maximum(ninf[:3], 1e-15)]))
-    coef = np.asfortranarray(r / nt.dt * g["vol"][gh:-gh, gh:-gh])
+    coef = np.asfortranarray(r * (1.0 / nt.dt) * g["vol"][gh:-gh, gh:-gh])
     nb = im * jm * 49 * 25
     jac, ia, ja = np.zeros(nb), np.zeros(nb, np.int32), np.zeros(nb, np.int32)
     for m in range(5):
